@@ -1,0 +1,160 @@
+/*
+ * et_array_interface.h -- C-ABI of lib_et_array_interface.so, the GB300
+ * (sm_103a) implementation of NiftyRec's rotation-based SPECT emission path.
+ *
+ * Every entry point of the reference's emission array interface on this path
+ * keeps its name, argument list, argument meaning and status codes; each
+ * declaration names the reference declaration it replaces.  Buffers are
+ * caller-owned host float32 arrays in nifti order (size[0] fastest); outputs
+ * are written in place; calls are synchronous.  The computation always runs on
+ * the GPU: the "Gpu"/"GPU"/"use_gpu" flags are accepted and ignored.
+ *
+ * Status codes (emission-lib/_et_common.h:40-48): 0 success, 1 unspecified,
+ * 2 parameters, 3 kernel, 4 allocgpu, 5 alloccpu, 6 transfergpu,
+ * 7 nogpubuilt, 8 nogpuinstalled; 9 (new) a bounded device-side wait expired.
+ */
+#ifndef NIFTYREC_GB300_ET_ARRAY_INTERFACE_H
+#define NIFTYREC_GB300_ET_ARRAY_INTERFACE_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#if defined(__GNUC__)
+#pragma GCC visibility push(default)
+#endif
+
+/* SimpleWrap status helpers -- emission-lib/_et_array_interface.h:22-27. */
+int status_success(int *status);
+int status_io_error(int *status);
+int status_initialisation_error(int *status);
+int status_parameter_error(int *status);
+int status_unhandled_error(int *status);
+int echo(int *in, int *out);
+
+/* Message of a status code -- emission-lib/_et_common.h:56. */
+char *niftyrec_error_msg(int status);
+
+/* Devices -- emission-lib/_et_array_interface.h:36-41. */
+int et_array_list_gpus(int *gpu_count, int *gpus_info_array);
+int et_array_set_gpu(int id);
+int et_array_set_gpu_pointer(int *id);
+int et_array_isinstalled(void);
+int et_array_reset_gpu(void);
+unsigned short et_array_is_block_multiple(unsigned short size);
+unsigned short et_array_get_block_size(void);
+
+/* Projection -- emission-lib/_et_array_interface.h:44 (scalars by pointer). */
+int SPECT_project_parallelholes(float *activity, int *activity_size, float *sinogram, int *sinogram_size,
+                                float *cameras, int *cameras_size, float *psf, int *psf_size, float *attenuation,
+                                int *attenuation_size, float *Background, float *Background_attenuation, int *Gpu,
+                                int *Truncate_negative_values);
+
+/* Backprojection -- emission-lib/_et_array_interface.h:45. */
+int SPECT_backproject_parallelholes(float *sino, int *sino_size, float *bkpr, int *bkpr_size, float *cameras,
+                                    int *cameras_size, float *psf, int *psf_size, float *attenuation,
+                                    int *attenuation_size, float *Background, float *Background_attenuation,
+                                    int *Gpu, int *Truncate_negative_values);
+
+/* By-value spellings bound by Python/NiftyRec/NiftyRec/NiftyRec.py:83-84 and
+ * :145-146 (absent from the reference library itself). */
+int et_array_project(float *activity, int *activity_size, float *sinogram, int *sinogram_size, float *cameras,
+                     int *cameras_size, float *psf, int *psf_size, float *attenuation, int *attenuation_size,
+                     float background, float background_attenuation, int gpu, int truncate_negative_values);
+int et_array_backproject(float *sino, int *sino_size, float *bkpr, int *bkpr_size, float *cameras,
+                         int *cameras_size, float *psf, int *psf_size, float *attenuation, int *attenuation_size,
+                         float background, float background_attenuation, int gpu, int truncate_negative_values);
+
+/* Attenuation gradient -- emission-lib/_et_array_interface.h:48 (the GPU
+ * semantics of emission-lib/_et.cpp:1679-1924); et_array_attenuation_gradient
+ * is the same function under the spelling of the project description. */
+int et_array_gradient_attenuation(float *sino, int *sino_size, float *activity, int *activity_size,
+                                  float *gradient, int *gradient_size, float *cameras, int *cameras_size, float *psf,
+                                  int *psf_size, float *attenuation, int *attenuation_size, float background,
+                                  float background_attenuation, int GPU, int truncate_negative_values);
+int et_array_attenuation_gradient(float *sino, int *sino_size, float *activity, int *activity_size,
+                                  float *gradient, int *gradient_size, float *cameras, int *cameras_size, float *psf,
+                                  int *psf_size, float *attenuation, int *attenuation_size, float background,
+                                  float background_attenuation, int GPU, int truncate_negative_values);
+
+/* PSF / camera helpers -- emission-lib/_et_array_interface.h:53-55. */
+int et_array_calculate_size_psf(unsigned int *psf_size_x, unsigned int *psf_size_y, float fwhm_pixels_dist0,
+                                float sensitivity0, float dist0, float fwhm_pixels_dist1, float sensitivity1,
+                                float dist1);
+int et_array_make_psf(float *psf_data, unsigned int psf_size_x, unsigned int psf_size_y, float fwhm_pixels_dist0,
+                      float sensitivity0, float dist0, float fwhm_pixels_dist1, float sensitivity1, float dist1,
+                      unsigned int N_psf_planes);
+int et_array_make_cameras(float *cameras_data, float firstcamera_deg, float lastcamera_deg, unsigned int n_cameras,
+                          unsigned int rotation_axis);
+
+/* Rotation of a volume -- emission-lib/_et_array_interface.h:32. */
+int et_array_rotate(float *image, int *size, float *rotated_image, float *angles, float *centers, float background,
+                    int axis_order, int GPU);
+
+/* OSEM / MLEM -- emission-lib/_et_array_interface.h:56-59. */
+int et_array_osem(float *activity_data, unsigned int size_x, unsigned int size_y, unsigned int subset_order,
+                  float *sinogram_data, int n_cameras, float firstcamera, float lastcamera,
+                  unsigned int rotation_axis, int iterations, int use_attenuation, float *attenuation_data,
+                  int use_psf, float *psf_data, unsigned int psf_size_x, unsigned int psf_size_y, float background,
+                  float background_attenuation, float epsilon, int use_gpu);
+int et_array_osem_step(float *activity_data, int size_x, int size_y, unsigned int subset_order,
+                       float *sinogram_data, int n_cameras, float *cameras_data, int use_attenuation,
+                       float *attenuation_data, int use_psf, float *psf_data, unsigned int psf_size_x,
+                       unsigned int psf_size_y, float background, float background_attenuation, float epsilon,
+                       int use_gpu);
+int et_array_mlem(float *activity_data, unsigned int size_x, unsigned int size_y, float *sinogram_data,
+                  int n_cameras, float firstcamera, float lastcamera, unsigned int rotation_axis, int iterations,
+                  int use_attenuation, float *attenuation_data, int use_psf, float *psf_data,
+                  unsigned int psf_size_x, unsigned int psf_size_y, float background, float background_attenuation,
+                  float epsilon, int use_gpu);
+int et_array_mlem_step(float *activity_data, int size_x, int size_y, float *sinogram_data, int n_cameras,
+                       float *cameras_data, int use_attenuation, float *attenuation_data, int use_psf,
+                       float *psf_data, unsigned int psf_size_x, unsigned int psf_size_y, float background,
+                       float background_attenuation, float epsilon, int use_gpu);
+
+/* Deterministic OSEM step over explicit camera indexes.  Replaces the random
+ * subset draw of et_array_osem_step (emission-lib/_et_array_interface.cpp:1001-1009,
+ * unseeded rand()) so that results are reproducible. */
+int et_array_osem_step_subset(float *activity_data, int size_x, int size_y, float *sinogram_data, int n_cameras,
+                              float *cameras_data, const int *camera_indexes, int n_subset, int use_attenuation,
+                              float *attenuation_data, int use_psf, float *psf_data, unsigned int psf_size_x,
+                              unsigned int psf_size_y, float background, float background_attenuation,
+                              float epsilon);
+
+/* Device-pointer entry points (additions; the reference's GPU path has no
+ * equivalent -- it copies host buffers in and out on every call,
+ * emission-lib/_et.cpp:917-1137).  Buffers are device float32 in nifti order;
+ * cameras and PSF are host arrays; work is enqueued on `stream` (a
+ * cudaStream_t) and the call returns without waiting.  size = {nx, ny, nz}.
+ * For the backprojection the centre of rotation is (size0, size1, size0),
+ * as in SPECT_backproject_parallelholes; mode 0 is the reference backprojector. */
+int nrgb_project_device(const float *d_activity, const float *d_attenuation, const int *size, float *d_sinogram,
+                        const float *cameras, const int *cameras_size, const float *psf, const int *psf_size,
+                        float background, float background_attenuation, int truncate, void *stream);
+int nrgb_backproject_device(const float *d_sinogram, const float *d_attenuation, const int *size, float *d_out,
+                            const float *cameras, const int *cameras_size, const float *psf, const int *psf_size,
+                            float background, float background_attenuation, int truncate, int mode, void *stream);
+
+/* Diagnostics: 1 if the calling thread's last call ran the fused y-gantry
+ * kernels, 2 if it ran the general-orientation kernels, 0 before any call. */
+int nrgb_last_path(void);
+
+/* Instrumentation (no counterpart in the reference).  nrgb_launch_count: CUDA
+ * kernels this library launched since it was loaded.  nrgb_profile_enable(1)
+ * brackets every launch with CUDA events on its stream (0 turns it off; both
+ * clear the record); nrgb_profile_summary writes one "name launches total_ms"
+ * line per kernel into buf, waiting for the recorded events, and returns the
+ * size it needs. */
+long long nrgb_launch_count(void);
+int nrgb_profile_enable(int on);
+int nrgb_profile_summary(char *buf, int len);
+
+#if defined(__GNUC__)
+#pragma GCC visibility pop
+#endif
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif

@@ -1,0 +1,633 @@
+// The C-ABI: the entry points of NiftyRec's emission array interface
+// (emission-lib/_et_array_interface.h), with the reference's argument meaning,
+// size rules and status codes, implemented on the GB300 engine; plus
+// device-pointer entry points for callers that keep data on the GPU.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <vector>
+
+#include "et_array_interface.h"
+#include "et_engine.h"
+#include "et_kernels.h"
+
+using namespace nrgb;
+
+namespace {
+
+bool all_zero3(const int* s) { return s[0] == 0 && s[1] == 0 && s[2] == 0; }
+
+// Diagnostics: which path the last call of this thread took.
+thread_local int g_last_path = 0;  // 1 = fused y-gantry kernels, 2 = general path
+
+size_t fbytes(size_t n) { return n * sizeof(float); }
+
+int finish(DeviceState& ds, int status) {
+  cudaEventRecord(ds.last_use, ds.stream);
+  const cudaError_t e = cudaStreamSynchronize(ds.stream);
+  if (status != kOk) return status;
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    return kErrKernel;
+  }
+  return kOk;
+}
+
+int h2d(float* d, const float* h, size_t n, cudaStream_t st) {
+  return cudaMemcpyAsync(d, h, fbytes(n), cudaMemcpyHostToDevice, st) == cudaSuccess ? kOk : kErrTransferGpu;
+}
+
+int d2h(float* h, const float* d, size_t n, cudaStream_t st) {
+  return cudaMemcpyAsync(h, d, fbytes(n), cudaMemcpyDeviceToHost, st) == cudaSuccess ? kOk : kErrTransferGpu;
+}
+
+// Project with host buffers (activity and/or attenuation may be null).
+int project_host(const Problem& pb, const float* act, const float* att, float* sino) {
+  int s;
+  DeviceState& ds = current_device_state(&s);
+  if (s != kOk) return s;
+  std::lock_guard<std::mutex> lk(ds.mu);
+  const size_t nvox = static_cast<size_t>(pb.nx) * pb.ny * pb.nz;
+  const size_t nsino = static_cast<size_t>(pb.nx) * pb.ny * pb.cams.n;
+  const size_t ws = project_workspace(pb, act != nullptr, att != nullptr);
+  if ((s = ensure_arena(ds, fbytes(2 * nvox + nsino) + 4 * 256 + ws)) != kOk) return s;
+  Carver cv(ds.arena, ds.arena_bytes);
+  float* d_act = act ? cv.take<float>(nvox) : nullptr;
+  float* d_att = att ? cv.take<float>(nvox) : nullptr;
+  float* d_sino = cv.take<float>(nsino);
+  char* w = cv.take<char>(ws);
+  cudaStream_t st = ds.stream;
+  if (act && (s = h2d(d_act, act, nvox, st)) != kOk) return finish(ds, s);
+  if (att && (s = h2d(d_att, att, nvox, st)) != kOk) return finish(ds, s);
+  g_last_path = (use_fused(pb) && act) ? 1 : 2;
+  s = project_device(pb, d_act, d_att, d_sino, w, ws, st);
+  if (s == kOk) s = d2h(sino, d_sino, nsino, st);
+  return finish(ds, s);
+}
+
+int backproject_host(const Problem& pb, const float* sino, const float* att, float* out) {
+  int s;
+  DeviceState& ds = current_device_state(&s);
+  if (s != kOk) return s;
+  std::lock_guard<std::mutex> lk(ds.mu);
+  const size_t nvox = static_cast<size_t>(pb.nx) * pb.ny * pb.nz;
+  const size_t nsino = static_cast<size_t>(pb.nx) * pb.ny * pb.cams.n;
+  const size_t ws = backproject_workspace(pb, att != nullptr);
+  if ((s = ensure_arena(ds, fbytes(2 * nvox + nsino) + 4 * 256 + ws)) != kOk) return s;
+  Carver cv(ds.arena, ds.arena_bytes);
+  float* d_sino = cv.take<float>(nsino);
+  float* d_att = att ? cv.take<float>(nvox) : nullptr;
+  float* d_out = cv.take<float>(nvox);
+  char* w = cv.take<char>(ws);
+  cudaStream_t st = ds.stream;
+  if ((s = h2d(d_sino, sino, nsino, st)) != kOk) return finish(ds, s);
+  if (att && (s = h2d(d_att, att, nvox, st)) != kOk) return finish(ds, s);
+  g_last_path = use_fused(pb) ? 1 : 2;
+  s = backproject_device(pb, d_sino, d_att, d_out, w, ws, st);
+  if (s == kOk) s = d2h(out, d_out, nvox, st);
+  return finish(ds, s);
+}
+
+int gradient_host(const Problem& pb, const float* sino, const float* act, const float* att, float* out) {
+  int s;
+  DeviceState& ds = current_device_state(&s);
+  if (s != kOk) return s;
+  std::lock_guard<std::mutex> lk(ds.mu);
+  const size_t nvox = static_cast<size_t>(pb.nx) * pb.ny * pb.nz;
+  const size_t nsino = static_cast<size_t>(pb.nx) * pb.ny * pb.cams.n;
+  const size_t ws = gradient_workspace(pb);
+  if ((s = ensure_arena(ds, fbytes(3 * nvox + nsino) + 5 * 256 + ws)) != kOk) return s;
+  Carver cv(ds.arena, ds.arena_bytes);
+  float* d_sino = cv.take<float>(nsino);
+  float* d_act = cv.take<float>(nvox);
+  float* d_att = cv.take<float>(nvox);
+  float* d_out = cv.take<float>(nvox);
+  char* w = cv.take<char>(ws);
+  cudaStream_t st = ds.stream;
+  if ((s = h2d(d_sino, sino, nsino, st)) != kOk) return finish(ds, s);
+  if ((s = h2d(d_act, act, nvox, st)) != kOk) return finish(ds, s);
+  if ((s = h2d(d_att, att, nvox, st)) != kOk) return finish(ds, s);
+  g_last_path = 2;
+  s = gradient_device(pb, d_sino, d_act, d_att, d_out, w, ws, st);
+  if (s == kOk) s = d2h(out, d_out, nvox, st);
+  return finish(ds, s);
+}
+
+// One OSEM step over the given camera subset on the device:
+// project (truncate) -> ratio -> backproject ratio and ones (truncate) -> update,
+// emission-lib/_et_array_interface.cpp:1017-1044.
+int osem_step_host(const Problem& pb, float* act, const float* ysub, const float* att, float eps) {
+  int s;
+  DeviceState& ds = current_device_state(&s);
+  if (s != kOk) return s;
+  std::lock_guard<std::mutex> lk(ds.mu);
+  const size_t nvox = static_cast<size_t>(pb.nx) * pb.ny * pb.nz;
+  const size_t nsino = static_cast<size_t>(pb.nx) * pb.ny * pb.cams.n;
+  const size_t ws = std::max(project_workspace(pb, true, att != nullptr), backproject_workspace(pb, att != nullptr));
+  if ((s = ensure_arena(ds, fbytes(4 * nvox + 3 * nsino) + 8 * 256 + ws)) != kOk) return s;
+  Carver cv(ds.arena, ds.arena_bytes);
+  float* d_act = cv.take<float>(nvox);
+  float* d_att = att ? cv.take<float>(nvox) : nullptr;
+  float* d_num = cv.take<float>(nvox);
+  float* d_den = cv.take<float>(nvox);
+  float* d_y = cv.take<float>(nsino);
+  float* d_p = cv.take<float>(nsino);
+  float* d_ones = cv.take<float>(nsino);
+  char* w = cv.take<char>(ws);
+  cudaStream_t st = ds.stream;
+  if ((s = h2d(d_act, act, nvox, st)) != kOk) return finish(ds, s);
+  if (att && (s = h2d(d_att, att, nvox, st)) != kOk) return finish(ds, s);
+  if ((s = h2d(d_y, ysub, nsino, st)) != kOk) return finish(ds, s);
+  Problem p1 = pb;
+  p1.truncate = 1;
+  g_last_path = use_fused(p1) ? 1 : 2;
+  if ((s = project_device(p1, d_act, d_att, d_p, w, ws, st)) != kOk) return finish(ds, s);
+  if ((s = osem_ratio(d_y, d_p, nsino, eps, st)) != kOk) return finish(ds, s);
+  if ((s = backproject_device(p1, d_p, d_att, d_num, w, ws, st)) != kOk) return finish(ds, s);
+  if ((s = fill(d_ones, nsino, 1.0f, st)) != kOk) return finish(ds, s);
+  if ((s = backproject_device(p1, d_ones, d_att, d_den, w, ws, st)) != kOk) return finish(ds, s);
+  if ((s = osem_update(d_act, d_num, d_den, nvox, eps, st)) != kOk) return finish(ds, s);
+  s = d2h(act, d_act, nvox, st);
+  return finish(ds, s);
+}
+
+// random_0_1 of emission-lib/_et_array_interface.cpp:961-967 (two rand() draws).
+float random_0_1() {
+  const float scale = RAND_MAX + 1.;
+  const float base = rand() / scale;
+  const float fine = rand() / scale;
+  return base + fine / scale;
+}
+
+int subset_step(float* activity_data, int size_x, int size_y, const float* sinogram_data, int n_cameras,
+                const float* cameras_data, const std::vector<int>& idx, int use_attenuation,
+                const float* attenuation_data, int use_psf, const float* psf_data, unsigned psf_size_x,
+                unsigned psf_size_y, float background, float background_attenuation, float epsilon) {
+  const int nsub = static_cast<int>(idx.size());
+  if (size_x <= 0 || size_y <= 0 || n_cameras <= 0 || nsub <= 0) return kErrParameters;
+  for (int i : idx)
+    if (i < 0 || i >= n_cameras) return kErrParameters;
+  std::vector<float> cams(3 * static_cast<size_t>(nsub));
+  for (int c = 0; c < nsub; ++c)
+    for (int a = 0; a < 3; ++a) cams[a * nsub + c] = cameras_data[idx[c] + a * static_cast<size_t>(n_cameras)];
+  const size_t nxy = static_cast<size_t>(size_x) * size_y;
+  std::vector<float> ysub(nxy * nsub);
+  for (int c = 0; c < nsub; ++c) std::memcpy(&ysub[nxy * c], sinogram_data + nxy * idx[c], fbytes(nxy));
+  const int vsize[3] = {size_x, size_y, size_x};
+  Cameras cc;
+  int s = expand_cameras(cams.data(), nsub, 3, vsize, &cc);
+  if (s != kOk) return s;
+  const int psz[3] = {static_cast<int>(psf_size_x), static_cast<int>(psf_size_y), size_x};
+  Problem pb;
+  s = make_problem(size_x, size_y, size_x, cc, use_psf ? psf_data : nullptr, psz, background, background_attenuation,
+                   1, &pb);
+  if (s != kOk) return s;
+  return osem_step_host(pb, activity_data, ysub.data(), use_attenuation ? attenuation_data : nullptr, epsilon);
+}
+
+int spect_project(float* activity, int* activity_size, float* sinogram, int* sinogram_size, float* cameras,
+                  int* cameras_size, float* psf, int* psf_size, float* attenuation, int* attenuation_size,
+                  float background, float background_attenuation, int truncate) {
+  if (!activity_size || !cameras_size || !psf_size || !attenuation_size) return kErrParameters;
+  int asz[3] = {activity_size[0], activity_size[1], activity_size[2]};
+  const bool no_act = all_zero3(asz);
+  const bool no_psf = all_zero3(psf_size);
+  const bool no_att = all_zero3(attenuation_size);
+  if (no_act && no_att) return kErrParameters;
+  if (no_act) std::memcpy(asz, attenuation_size, sizeof(asz));
+  if (!no_act && !no_att &&
+      (attenuation_size[0] != asz[0] || attenuation_size[1] != asz[1] || attenuation_size[2] != asz[2]))
+    return kErrParameters;
+  const int ncam = cameras_size[0], ncols = cameras_size[1];
+  if (!(ncols == 1 || ncols == 3 || ncols == 6)) return kErrParameters;
+  if (!no_psf && (psf_size[0] % 2 != 1 || psf_size[1] % 2 != 1 || psf_size[2] != asz[0])) return kErrParameters;
+  if (sinogram_size &&
+      static_cast<long long>(sinogram_size[0]) * sinogram_size[1] * sinogram_size[2] <
+          static_cast<long long>(asz[0]) * asz[1] * ncam)
+    return kErrParameters;
+  Cameras cc;
+  int s = expand_cameras(cameras, ncam, ncols, asz, &cc);
+  if (s != kOk) return s;
+  Problem pb;
+  s = make_problem(asz[0], asz[1], asz[2], cc, no_psf ? nullptr : psf, psf_size, background, background_attenuation,
+                   truncate, &pb);
+  if (s != kOk) return s;
+  return project_host(pb, no_act ? nullptr : activity, no_att ? nullptr : attenuation, sinogram);
+}
+
+int spect_backproject(float* sino, int* sino_size, float* bkpr, int* bkpr_size, float* cameras, int* cameras_size,
+                      float* psf, int* psf_size, float* attenuation, int* attenuation_size, float background,
+                      float background_attenuation, int truncate) {
+  if (!sino_size || !bkpr_size || !cameras_size || !psf_size || !attenuation_size) return kErrParameters;
+  const bool no_psf = all_zero3(psf_size);
+  const bool no_att = all_zero3(attenuation_size);
+  const int ncam = cameras_size[0], ncols = cameras_size[1];
+  if (!(ncols == 1 || ncols == 3 || ncols == 6)) return kErrParameters;
+  if (sino_size[2] != ncam) return kErrParameters;
+  if (!no_psf && (psf_size[0] % 2 != 1 || psf_size[1] % 2 != 1 || psf_size[2] != sino_size[0])) return kErrParameters;
+  // The spread writes sinogram plane (x, y) into the volume grid, so they must agree.
+  if (bkpr_size[0] != sino_size[0] || bkpr_size[1] != sino_size[1]) return kErrParameters;
+  if (!no_att && (attenuation_size[0] != bkpr_size[0] || attenuation_size[1] != bkpr_size[1] ||
+                  attenuation_size[2] != bkpr_size[2]))
+    return kErrParameters;
+  // Centre of rotation from (sino0, sino1, sino0), emission-lib/_et_array_interface.cpp:598-630.
+  const int csz[3] = {sino_size[0], sino_size[1], sino_size[0]};
+  Cameras cc;
+  int s = expand_cameras(cameras, ncam, ncols, csz, &cc);
+  if (s != kOk) return s;
+  Problem pb;
+  s = make_problem(bkpr_size[0], bkpr_size[1], bkpr_size[2], cc, no_psf ? nullptr : psf, psf_size, background,
+                   background_attenuation, truncate, &pb);
+  if (s != kOk) return s;
+  return backproject_host(pb, sino, no_att ? nullptr : attenuation, bkpr);
+}
+
+const char* kMessages[] = {
+    "niftyrec: success",
+    "niftyrec: unspecified error",
+    "niftyrec: wrong parameters",
+    "niftyrec: CUDA kernel failed",
+    "niftyrec: GPU memory allocation failed",
+    "niftyrec: host memory allocation failed",
+    "niftyrec: host/GPU transfer failed",
+    "niftyrec: built without GPU support",
+    "niftyrec: no GPU installed",
+    "niftyrec: a bounded device-side wait expired",
+};
+
+}  // namespace
+
+extern "C" {
+
+// ---------------------------------------------------------------- status
+// emission-lib/_et_array_interface.cpp:21-52
+int status_success(int* status) { *status = 0; return 0; }
+int status_io_error(int* status) { *status = 101; return 0; }
+int status_initialisation_error(int* status) { *status = 103; return 0; }
+int status_parameter_error(int* status) { *status = 104; return 0; }
+int status_unhandled_error(int* status) { *status = 105; return 0; }
+int echo(int* in, int* out) { *out = *in; return 0; }
+
+// emission-lib/_et_common.cpp:269-306
+char* niftyrec_error_msg(int status) {
+  if (status >= 0 && status <= kErrTimeout) return const_cast<char*>(kMessages[status]);
+  return const_cast<char*>("niftyrec: unknown status");
+}
+
+// --------------------------------------------------------------- devices
+// emission-lib/_et_array_interface.cpp:269-272 returns 0; here 1 when a GPU is usable.
+int et_array_isinstalled() {
+  int n = 0;
+  if (cudaGetDeviceCount(&n) != cudaSuccess) {
+    cudaGetLastError();
+    return 0;
+  }
+  return n > 0 ? 1 : 0;
+}
+
+// emission-lib/_et.cpp:1988-2022: five ints per device
+// {id, SMs * clock_kHz, SMs, clock_kHz, global memory in MB}.
+int et_array_list_gpus(int* gpu_count, int* gpus_info_array) {
+  int n = 0;
+  if (cudaGetDeviceCount(&n) != cudaSuccess) {
+    cudaGetLastError();
+    gpu_count[0] = 0;
+    return kErrNoGpuInstalled;
+  }
+  const int nmax = std::min(n, 16);
+  for (int d = 0; d < nmax; ++d) {
+    int sms = 0, clk = 0;
+    size_t mem = 0;
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, d);
+    cudaDeviceGetAttribute(&clk, cudaDevAttrClockRate, d);
+    cudaDeviceProp prop;
+    if (cudaGetDeviceProperties(&prop, d) == cudaSuccess) mem = prop.totalGlobalMem;
+    gpus_info_array[5 * d + 0] = d;
+    gpus_info_array[5 * d + 1] = sms * clk;
+    gpus_info_array[5 * d + 2] = sms;
+    gpus_info_array[5 * d + 3] = clk;
+    gpus_info_array[5 * d + 4] = static_cast<int>(std::floor(mem / 1000000.0));
+  }
+  gpu_count[0] = n;
+  return kOk;
+}
+
+// emission-lib/_et.cpp:2029-2044
+int et_array_set_gpu(int id) {
+  int n = 0;
+  if (cudaGetDeviceCount(&n) != cudaSuccess || id < 0 || id >= n) {
+    cudaGetLastError();
+    return kErrUnspecified;
+  }
+  return cudaSetDevice(id) == cudaSuccess ? kOk : kErrUnspecified;
+}
+
+int et_array_set_gpu_pointer(int* id) { return et_array_set_gpu(id[0]); }
+
+// emission-lib/_et.cpp:2445-2451.  Frees this library's work space on the
+// current device; the CUDA context itself is left to its other users.
+int et_array_reset_gpu() {
+  int s;
+  DeviceState& ds = current_device_state(&s);
+  if (s != kOk) return s;
+  std::lock_guard<std::mutex> lk(ds.mu);
+  cudaStreamSynchronize(ds.stream);
+  if (ds.arena) cudaFree(ds.arena);
+  ds.arena = nullptr;
+  ds.arena_bytes = 0;
+  return kOk;
+}
+
+// emission-lib/_et.cpp:27-36.  The fused kernels take any size: every size is
+// a "block multiple" and the block size is 1.
+unsigned short et_array_is_block_multiple(unsigned short size) { return size > 0 ? 1 : 0; }
+unsigned short et_array_get_block_size(void) { return 1; }
+
+// ------------------------------------------------------------ projection
+// emission-lib/_et_array_interface.h:44 (scalars by pointer), impl .cpp:337-541.
+int SPECT_project_parallelholes(float* activity, int* activity_size, float* sinogram, int* sinogram_size,
+                                float* cameras, int* cameras_size, float* psf, int* psf_size, float* attenuation,
+                                int* attenuation_size, float* Background, float* Background_attenuation, int* Gpu,
+                                int* Truncate_negative_values) {
+  (void)Gpu;
+  return spect_project(activity, activity_size, sinogram, sinogram_size, cameras, cameras_size, psf, psf_size,
+                       attenuation, attenuation_size, *Background, *Background_attenuation,
+                       *Truncate_negative_values);
+}
+
+// The by-value spelling bound by Python/NiftyRec/NiftyRec/NiftyRec.py:83-84.
+int et_array_project(float* activity, int* activity_size, float* sinogram, int* sinogram_size, float* cameras,
+                     int* cameras_size, float* psf, int* psf_size, float* attenuation, int* attenuation_size,
+                     float background, float background_attenuation, int gpu, int truncate_negative_values) {
+  (void)gpu;
+  return spect_project(activity, activity_size, sinogram, sinogram_size, cameras, cameras_size, psf, psf_size,
+                       attenuation, attenuation_size, background, background_attenuation, truncate_negative_values);
+}
+
+// --------------------------------------------------------- backprojection
+// emission-lib/_et_array_interface.h:45, impl .cpp:547-710.
+int SPECT_backproject_parallelholes(float* sino, int* sino_size, float* bkpr, int* bkpr_size, float* cameras,
+                                    int* cameras_size, float* psf, int* psf_size, float* attenuation,
+                                    int* attenuation_size, float* Background, float* Background_attenuation,
+                                    int* Gpu, int* Truncate_negative_values) {
+  (void)Gpu;
+  return spect_backproject(sino, sino_size, bkpr, bkpr_size, cameras, cameras_size, psf, psf_size, attenuation,
+                           attenuation_size, *Background, *Background_attenuation, *Truncate_negative_values);
+}
+
+// By-value spelling bound by Python/NiftyRec/NiftyRec/NiftyRec.py:145-146.
+int et_array_backproject(float* sino, int* sino_size, float* bkpr, int* bkpr_size, float* cameras, int* cameras_size,
+                         float* psf, int* psf_size, float* attenuation, int* attenuation_size, float background,
+                         float background_attenuation, int gpu, int truncate_negative_values) {
+  (void)gpu;
+  return spect_backproject(sino, sino_size, bkpr, bkpr_size, cameras, cameras_size, psf, psf_size, attenuation,
+                           attenuation_size, background, background_attenuation, truncate_negative_values);
+}
+
+// ---------------------------------------------------- attenuation gradient
+// emission-lib/_et_array_interface.h:48, impl .cpp:714-892 (3-D sinograms),
+// computed as et_gradient_attenuation_gpu, emission-lib/_et.cpp:1679-1924.
+int et_array_gradient_attenuation(float* sino, int* sino_size, float* activity, int* activity_size, float* gradient,
+                                  int* gradient_size, float* cameras, int* cameras_size, float* psf, int* psf_size,
+                                  float* attenuation, int* attenuation_size, float background,
+                                  float background_attenuation, int GPU, int truncate_negative_values) {
+  (void)GPU;
+  (void)attenuation_size;
+  if (!sino_size || !activity_size || !gradient_size || !cameras_size || !psf_size) return kErrParameters;
+  const bool no_psf = all_zero3(psf_size);
+  const int ncam = cameras_size[0], ncols = cameras_size[1];
+  if (!(ncols == 1 || ncols == 3 || ncols == 6)) return kErrParameters;
+  if (sino_size[2] != ncam) return kErrParameters;
+  if (!no_psf && (psf_size[0] % 2 != 1 || psf_size[1] % 2 != 1 || psf_size[2] != sino_size[0])) return kErrParameters;
+  if (gradient_size[0] != sino_size[0] || gradient_size[1] != sino_size[1]) return kErrParameters;
+  if (!activity || !attenuation || !gradient) return kErrParameters;
+  Cameras cc;
+  int s = expand_cameras(cameras, ncam, ncols, activity_size, &cc);
+  if (s != kOk) return s;
+  Problem pb;
+  s = make_problem(gradient_size[0], gradient_size[1], gradient_size[2], cc, no_psf ? nullptr : psf, psf_size,
+                   background, background_attenuation, truncate_negative_values, &pb);
+  if (s != kOk) return s;
+  return gradient_host(pb, sino, activity, attenuation, gradient);
+}
+
+// The spelling used in the project's spec description.
+int et_array_attenuation_gradient(float* sino, int* sino_size, float* activity, int* activity_size, float* gradient,
+                                  int* gradient_size, float* cameras, int* cameras_size, float* psf, int* psf_size,
+                                  float* attenuation, int* attenuation_size, float background,
+                                  float background_attenuation, int GPU, int truncate_negative_values) {
+  return et_array_gradient_attenuation(sino, sino_size, activity, activity_size, gradient, gradient_size, cameras,
+                                       cameras_size, psf, psf_size, attenuation, attenuation_size, background,
+                                       background_attenuation, GPU, truncate_negative_values);
+}
+
+// ------------------------------------------------------------ utilities
+// emission-lib/_et_array_interface.cpp:896-920: the reference's PSF builder is a
+// fixed 5 x 5 stub filled with ones; kept as is for drop-in behaviour.
+int et_array_calculate_size_psf(unsigned int* psf_size_x, unsigned int* psf_size_y, float, float, float, float,
+                                float, float) {
+  *psf_size_x = 5;
+  *psf_size_y = 5;
+  return 0;
+}
+
+int et_array_make_psf(float* psf_data, unsigned int psf_size_x, unsigned int psf_size_y, float, float, float, float,
+                      float, float, unsigned int N_psf_planes) {
+  if (psf_size_x != 5 || psf_size_y != 5) {
+    std::fprintf(stderr, "et_array_make_psf: PSF size mismatch. \n");
+    return 1;
+  }
+  for (unsigned i = 0; i < psf_size_x * psf_size_y * N_psf_planes; ++i) psf_data[i] = 1.0f;
+  return 0;
+}
+
+// emission-lib/_et_array_interface.cpp:923-937, same float arithmetic; a single
+// camera gets the first angle (the reference divides by n-1 = 0 there).
+int et_array_make_cameras(float* cameras_data, float firstcamera_deg, float lastcamera_deg, unsigned int n_cameras,
+                          unsigned int rotation_axis) {
+  const float kPi = 3.141592653589793f;
+  for (unsigned cam = 0; cam < n_cameras; ++cam) {
+    float angle;
+    if (n_cameras > 1)
+      angle = (firstcamera_deg + (lastcamera_deg - firstcamera_deg) * static_cast<int>(cam) /
+                                     static_cast<float>(n_cameras - 1)) /
+              180.0f * kPi;
+    else
+      angle = firstcamera_deg / 180.0f * kPi;
+    for (unsigned axis = 0; axis < 3; ++axis)
+      cameras_data[cam + axis * n_cameras] = (axis == rotation_axis) ? angle : 0.0f;
+  }
+  return 0;
+}
+
+// emission-lib/_et_array_interface.cpp:112-156: rotate a volume about a centre.
+int et_array_rotate(float* image, int* size, float* rotated_image, float* angles, float* centers, float background,
+                    int axis_order, int GPU) {
+  (void)GPU;
+  if (!size || size[0] <= 0 || size[1] <= 0 || size[2] <= 0) return kErrParameters;
+  int s;
+  DeviceState& ds = current_device_state(&s);
+  if (s != kOk) return s;
+  std::lock_guard<std::mutex> lk(ds.mu);
+  const size_t nvox = static_cast<size_t>(size[0]) * size[1] * size[2];
+  if ((s = ensure_arena(ds, fbytes(2 * nvox) + 512)) != kOk) return s;
+  Carver cv(ds.arena, ds.arena_bytes);
+  float* d_in = cv.take<float>(nvox);
+  float* d_out = cv.take<float>(nvox);
+  float M[16];
+  rotation_matrix(M, angles[0], angles[1], angles[2], centers[0], centers[1], centers[2], axis_order);
+  if ((s = h2d(d_in, image, nvox, ds.stream)) != kOk) return finish(ds, s);
+  s = general_rotate(d_in, d_out, size[0], size[1], size[2], M, background, ds.stream);
+  if (s == kOk) s = d2h(rotated_image, d_out, nvox, ds.stream);
+  return finish(ds, s);
+}
+
+// ---------------------------------------------------------- OSEM / MLEM
+// emission-lib/_et_array_interface.cpp:972-1054.  Subset of n_cameras /
+// subset_order cameras drawn with rand() as the reference does; an index that
+// rounds up to n_cameras is clamped to n_cameras - 1 (the reference reads one
+// past the end there, :1006).
+int et_array_osem_step(float* activity_data, int size_x, int size_y, unsigned int subset_order, float* sinogram_data,
+                       int n_cameras, float* cameras_data, int use_attenuation, float* attenuation_data, int use_psf,
+                       float* psf_data, unsigned int psf_size_x, unsigned int psf_size_y, float background,
+                       float background_attenuation, float epsilon, int use_gpu) {
+  (void)use_gpu;
+  if (subset_order == 0 || n_cameras <= 0) return kErrParameters;
+  const int nsub = n_cameras / static_cast<int>(subset_order);
+  if (nsub <= 0) return kErrParameters;
+  std::vector<int> idx(nsub);
+  for (int c = 0; c < nsub; ++c) {
+    const float R = random_0_1();
+    unsigned v = static_cast<unsigned>(n_cameras * R);
+    if (v >= static_cast<unsigned>(n_cameras)) v = n_cameras - 1;
+    idx[c] = static_cast<int>(v);
+  }
+  return subset_step(activity_data, size_x, size_y, sinogram_data, n_cameras, cameras_data, idx, use_attenuation,
+                     attenuation_data, use_psf, psf_data, psf_size_x, psf_size_y, background, background_attenuation,
+                     epsilon);
+}
+
+// Deterministic variant of et_array_osem_step: the subset is given as camera
+// indexes (the reference draws it from unseeded rand()).
+int et_array_osem_step_subset(float* activity_data, int size_x, int size_y, float* sinogram_data, int n_cameras,
+                              float* cameras_data, const int* camera_indexes, int n_subset, int use_attenuation,
+                              float* attenuation_data, int use_psf, float* psf_data, unsigned int psf_size_x,
+                              unsigned int psf_size_y, float background, float background_attenuation, float epsilon) {
+  if (!camera_indexes || n_subset <= 0) return kErrParameters;
+  std::vector<int> idx(camera_indexes, camera_indexes + n_subset);
+  return subset_step(activity_data, size_x, size_y, sinogram_data, n_cameras, cameras_data, idx, use_attenuation,
+                     attenuation_data, use_psf, psf_data, psf_size_x, psf_size_y, background, background_attenuation,
+                     epsilon);
+}
+
+// emission-lib/_et_array_interface.cpp:1080-1131.
+int et_array_mlem_step(float* activity_data, int size_x, int size_y, float* sinogram_data, int n_cameras,
+                       float* cameras_data, int use_attenuation, float* attenuation_data, int use_psf,
+                       float* psf_data, unsigned int psf_size_x, unsigned int psf_size_y, float background,
+                       float background_attenuation, float epsilon, int use_gpu) {
+  (void)use_gpu;
+  if (n_cameras <= 0) return kErrParameters;
+  std::vector<int> idx(n_cameras);
+  for (int c = 0; c < n_cameras; ++c) idx[c] = c;
+  return subset_step(activity_data, size_x, size_y, sinogram_data, n_cameras, cameras_data, idx, use_attenuation,
+                     attenuation_data, use_psf, psf_data, psf_size_x, psf_size_y, background, background_attenuation,
+                     epsilon);
+}
+
+// emission-lib/_et_array_interface.cpp:940-957.
+int et_array_osem(float* activity_data, unsigned int size_x, unsigned int size_y, unsigned int subset_order,
+                  float* sinogram_data, int n_cameras, float firstcamera, float lastcamera, unsigned int rotation_axis,
+                  int iterations, int use_attenuation, float* attenuation_data, int use_psf, float* psf_data,
+                  unsigned int psf_size_x, unsigned int psf_size_y, float background, float background_attenuation,
+                  float epsilon, int use_gpu) {
+  const size_t n = static_cast<size_t>(size_x) * size_y * size_x;
+  for (size_t i = 0; i < n; ++i) activity_data[i] = 1.0f;
+  std::vector<float> cams(3 * static_cast<size_t>(n_cameras));
+  int status = et_array_make_cameras(cams.data(), firstcamera, lastcamera, n_cameras, rotation_axis);
+  for (int it = 0; it < iterations; ++it)
+    status += et_array_osem_step(activity_data, size_x, size_y, subset_order, sinogram_data, n_cameras, cams.data(),
+                                 use_attenuation, attenuation_data, use_psf, psf_data, psf_size_x, psf_size_y,
+                                 background, background_attenuation, epsilon, use_gpu);
+  return status;
+}
+
+// emission-lib/_et_array_interface.cpp:1058-1076.
+int et_array_mlem(float* activity_data, unsigned int size_x, unsigned int size_y, float* sinogram_data, int n_cameras,
+                  float firstcamera, float lastcamera, unsigned int rotation_axis, int iterations, int use_attenuation,
+                  float* attenuation_data, int use_psf, float* psf_data, unsigned int psf_size_x,
+                  unsigned int psf_size_y, float background, float background_attenuation, float epsilon,
+                  int use_gpu) {
+  const size_t n = static_cast<size_t>(size_x) * size_y * size_x;
+  for (size_t i = 0; i < n; ++i) activity_data[i] = 1.0f;
+  std::vector<float> cams(3 * static_cast<size_t>(n_cameras));
+  int status = et_array_make_cameras(cams.data(), firstcamera, lastcamera, n_cameras, rotation_axis);
+  for (int it = 0; it < iterations; ++it)
+    status += et_array_mlem_step(activity_data, size_x, size_y, sinogram_data, n_cameras, cams.data(),
+                                 use_attenuation, attenuation_data, use_psf, psf_data, psf_size_x, psf_size_y,
+                                 background, background_attenuation, epsilon, use_gpu);
+  return status;
+}
+
+// ------------------------------------------------ device-pointer additions
+// Same operations on device buffers (nifti layout) on the caller's stream;
+// cameras and PSF stay host arrays.  The call returns once the work is
+// enqueued.  No counterpart in the reference (its GPU path copies host
+// buffers in and out on every call).
+int nrgb_project_device(const float* d_activity, const float* d_attenuation, const int* size, float* d_sinogram,
+                        const float* cameras, const int* cameras_size, const float* psf, const int* psf_size,
+                        float background, float background_attenuation, int truncate, void* stream) {
+  if (!size || !cameras || !cameras_size || (!d_activity && !d_attenuation) || !d_sinogram) return kErrParameters;
+  Cameras cc;
+  int s = expand_cameras(cameras, cameras_size[0], cameras_size[1], size, &cc);
+  if (s != kOk) return s;
+  Problem pb;
+  s = make_problem(size[0], size[1], size[2], cc, psf, psf_size, background, background_attenuation, truncate, &pb);
+  if (s != kOk) return s;
+  DeviceState& ds = current_device_state(&s);
+  if (s != kOk) return s;
+  std::lock_guard<std::mutex> lk(ds.mu);
+  const size_t ws = project_workspace(pb, d_activity != nullptr, d_attenuation != nullptr);
+  if ((s = ensure_arena(ds, ws)) != kOk) return s;
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  cudaStreamWaitEvent(st, ds.last_use, 0);
+  g_last_path = (use_fused(pb) && d_activity) ? 1 : 2;
+  s = project_device(pb, d_activity, d_attenuation, d_sinogram, ds.arena, ds.arena_bytes, st);
+  cudaEventRecord(ds.last_use, st);
+  return s;
+}
+
+// mode: 0 = the reference's inverse-rotation backprojector.
+int nrgb_backproject_device(const float* d_sinogram, const float* d_attenuation, const int* size, float* d_out,
+                            const float* cameras, const int* cameras_size, const float* psf, const int* psf_size,
+                            float background, float background_attenuation, int truncate, int mode, void* stream) {
+  if (!size || !cameras || !cameras_size || !d_sinogram || !d_out || mode != kBackReference) return kErrParameters;
+  Cameras cc;
+  const int csz[3] = {size[0], size[1], size[0]};
+  int s = expand_cameras(cameras, cameras_size[0], cameras_size[1], csz, &cc);
+  if (s != kOk) return s;
+  Problem pb;
+  s = make_problem(size[0], size[1], size[2], cc, psf, psf_size, background, background_attenuation, truncate, &pb);
+  if (s != kOk) return s;
+  pb.back_mode = mode;
+  DeviceState& ds = current_device_state(&s);
+  if (s != kOk) return s;
+  std::lock_guard<std::mutex> lk(ds.mu);
+  const size_t ws = backproject_workspace(pb, d_attenuation != nullptr);
+  if ((s = ensure_arena(ds, ws)) != kOk) return s;
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  cudaStreamWaitEvent(st, ds.last_use, 0);
+  g_last_path = use_fused(pb) ? 1 : 2;
+  s = backproject_device(pb, d_sinogram, d_attenuation, d_out, ds.arena, ds.arena_bytes, st);
+  cudaEventRecord(ds.last_use, st);
+  return s;
+}
+
+// 1 when the last call of this thread ran the fused y-gantry kernels, 2 when
+// it ran the general-orientation path, 0 before any call.
+int nrgb_last_path(void) { return g_last_path; }
+
+}  // extern "C"

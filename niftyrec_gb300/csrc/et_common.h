@@ -1,0 +1,54 @@
+// Shared definitions of the GB300 SPECT projector library: status codes,
+// per-camera geometry, problem description and device layouts.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstddef>
+#include <cstdint>
+
+namespace nrgb {
+
+// Status codes.  0..8 keep the values of the reference
+// (emission-lib/_et_common.h:40-48); 9 is new: a bounded device-side wait
+// expired and the kernel returned early.
+enum Status : int {
+  kOk = 0,
+  kErrUnspecified = 1,
+  kErrParameters = 2,
+  kErrKernel = 3,
+  kErrAllocGpu = 4,
+  kErrAllocCpu = 5,
+  kErrTransferGpu = 6,
+  kErrNoGpuBuilt = 7,
+  kErrNoGpuInstalled = 8,
+  kErrTimeout = 9,
+};
+
+// Memory layouts of device volumes and sinograms.
+//  kLayoutNifti : x fastest, then y, then z (cameras for sinograms) -- the
+//                 reference's nifti order.
+//  kLayoutColumn: y fastest ("columns" along the gantry axis), then x, then z;
+//                 each column padded to cy = round_up(ny, 4) floats with zero
+//                 pads.  Native layout of the fused y-gantry kernels.
+enum Layout : int { kLayoutNifti = 0, kLayoutColumn = 1 };
+
+// Affine rows of one camera.  fwd: the projector's resampling matrix (XYZ
+// order, +theta, about the centre); bwd: the backprojector's inverse
+// resampling matrix (ZYX order, -theta).  Row-major 3x4: p_i = m[4i+0]*x +
+// m[4i+1]*y + m[4i+2]*z + m[4i+3].
+struct CamGeom {
+  float fwd[12];
+  float bwd[12];
+};
+
+// Backprojector variants.
+//  kBackReference: the reference's inverse-rotation gather
+//                  (emission-lib/_et.cpp:474-494).
+//  kBackAdjoint  : exact transpose of the projector (transposed PSF and
+//                  transposed trilinear interpolation); not in the reference.
+enum BackMode : int { kBackReference = 0, kBackAdjoint = 1 };
+
+inline int round_up(int v, int m) { return (v + m - 1) / m * m; }
+
+}  // namespace nrgb

@@ -1,0 +1,285 @@
+// Engine implementation: dispatch between the fused y-gantry kernels and the
+// general-orientation path, work-space layout, per-device state.
+#include "et_engine.h"
+
+#include <algorithm>
+#include <cstring>
+#include <map>
+#include <memory>
+
+#include "et_kernels.h"
+
+namespace nrgb {
+
+int make_problem(int nx, int ny, int nz, const Cameras& cams, const float* psf, const int* psf_size, float bg,
+                 float bg_att, int truncate, Problem* out) {
+  if (nx <= 0 || ny <= 0 || nz <= 0 || cams.n <= 0) return kErrParameters;
+  Problem pb;
+  pb.nx = nx;
+  pb.ny = ny;
+  pb.nz = nz;
+  pb.cams = cams;
+  pb.geom = camera_geometry(cams);
+  pb.ygantry = is_y_gantry(cams);
+  pb.bg = bg;
+  pb.bg_att = bg_att;
+  pb.truncate = truncate;
+  if (psf) {
+    const int kx = psf_size[0], ky = psf_size[1], planes = psf_size[2];
+    // The reference separates the PSF assuming kx == ky (emission-lib/_et.cpp:199-213
+    // indexes both kernels with psf_size[0]) and reads plane z for every depth z.
+    if (kx % 2 != 1 || ky % 2 != 1 || kx != ky || planes < nz) return kErrParameters;
+    pb.psf_k = kx;
+    pb.psf_sep = separate_psf(psf, kx, nz);
+  }
+  *out = std::move(pb);
+  return kOk;
+}
+
+bool use_fused(const Problem& pb) {
+  return pb.ygantry && pb.bg == 0.0f && pb.bg_att == 0.0f && yg_supported(pb.nx, pb.ny, pb.nz, pb.psf_k);
+}
+
+namespace {
+
+size_t vol_n(const Problem& pb) { return static_cast<size_t>(pb.nx) * pb.ny * pb.nz; }
+size_t col_n(const Problem& pb) { return static_cast<size_t>(pb.nx) * round_up(pb.ny, 4) * pb.nz; }
+size_t sino_col_n(const Problem& pb) { return static_cast<size_t>(pb.nx) * round_up(pb.ny, 4) * pb.cams.n; }
+constexpr size_t kSlack = 8 * 256;
+
+size_t common_bytes(const Problem& pb) {
+  return sizeof(CamGeom) * pb.cams.n + sizeof(float) * pb.psf_sep.size() + kSlack;
+}
+
+int upload_common(const Problem& pb, Carver& cv, CamGeom** d_geom, float** d_psf, cudaStream_t st) {
+  *d_geom = cv.take<CamGeom>(pb.cams.n);
+  *d_psf = nullptr;
+  if (!*d_geom) return kErrAllocGpu;
+  if (cudaMemcpyAsync(*d_geom, pb.geom.data(), sizeof(CamGeom) * pb.cams.n, cudaMemcpyHostToDevice, st) != cudaSuccess)
+    return kErrTransferGpu;
+  if (pb.psf_k) {
+    *d_psf = cv.take<float>(pb.psf_sep.size());
+    if (!*d_psf) return kErrAllocGpu;
+    if (cudaMemcpyAsync(*d_psf, pb.psf_sep.data(), sizeof(float) * pb.psf_sep.size(), cudaMemcpyHostToDevice, st) !=
+        cudaSuccess)
+      return kErrTransferGpu;
+  }
+  return kOk;
+}
+
+int check(int status) {
+  if (status != kOk) return status;
+  return cudaGetLastError() == cudaSuccess ? kOk : kErrKernel;
+}
+
+}  // namespace
+
+size_t project_workspace(const Problem& pb, bool has_act, bool has_att) {
+  size_t b = common_bytes(pb);
+  if (use_fused(pb) && has_act)
+    b += sizeof(float) * (col_n(pb) * (has_att ? 2 : 1) + sino_col_n(pb));
+  else
+    b += sizeof(float) * vol_n(pb) * 3;
+  return b;
+}
+
+size_t backproject_workspace(const Problem& pb, bool has_att) {
+  size_t b = common_bytes(pb);
+  if (use_fused(pb))
+    b += sizeof(float) * (col_n(pb) * (has_att ? 2 : 1) + sino_col_n(pb)) +
+         yg_backproject_workspace(pb.nx, pb.ny, pb.nz, pb.cams.n, pb.group) + kSlack;
+  else
+    b += sizeof(float) * vol_n(pb) * 3;
+  return b;
+}
+
+size_t gradient_workspace(const Problem& pb) { return common_bytes(pb) + sizeof(float) * vol_n(pb) * 3; }
+
+int project_device(const Problem& pb, const float* d_act, const float* d_att, float* d_sino, char* ws,
+                   size_t ws_bytes, cudaStream_t st) {
+  Carver cv(ws, ws_bytes);
+  CamGeom* d_geom;
+  float* d_psf;
+  int s = upload_common(pb, cv, &d_geom, &d_psf, st);
+  if (s != kOk) return s;
+  if (use_fused(pb) && d_act) {
+    const int cy = round_up(pb.ny, 4);
+    float* act_c = cv.take<float>(col_n(pb));
+    float* mu_c = d_att ? cv.take<float>(col_n(pb)) : nullptr;
+    float* sino_c = cv.take<float>(sino_col_n(pb));
+    if (!act_c || !sino_c || (d_att && !mu_c)) return kErrAllocGpu;
+    if ((s = to_column(d_act, act_c, pb.nx, pb.ny, cy, pb.nz, st)) != kOk) return s;
+    if (d_att && (s = to_column(d_att, mu_c, pb.nx, pb.ny, cy, pb.nz, st)) != kOk) return s;
+    YgArgs a;
+    a.nx = pb.nx;
+    a.ny = pb.ny;
+    a.nz = pb.nz;
+    a.cy = cy;
+    a.ncam = pb.cams.n;
+    a.geom = d_geom;
+    a.act = act_c;
+    a.mu = mu_c;
+    a.out = sino_c;
+    a.psf = d_psf;
+    a.psf_k = pb.psf_k;
+    a.truncate = pb.truncate;
+    if ((s = yg_project(a, st)) != kOk) return s;
+    return check(from_column(sino_c, d_sino, pb.nx, pb.ny, cy, pb.cams.n, 0, st));
+  }
+  GeneralArgs g;
+  g.nx = pb.nx;
+  g.ny = pb.ny;
+  g.nz = pb.nz;
+  g.ncam = pb.cams.n;
+  g.geom_host = pb.geom.data();
+  g.act = d_act;
+  g.att = d_att;
+  g.out = d_sino;
+  g.psf_sep = d_psf;
+  g.psf_k = pb.psf_k;
+  g.bg = pb.bg;
+  g.bg_att = pb.bg_att;
+  g.truncate = pb.truncate;
+  g.ws_act = cv.take<float>(vol_n(pb));
+  g.ws_att = cv.take<float>(vol_n(pb));
+  g.ws_tmp = cv.take<float>(vol_n(pb));
+  if (!g.ws_act || !g.ws_att || !g.ws_tmp) return kErrAllocGpu;
+  return check(general_project(g, st));
+}
+
+int backproject_device(const Problem& pb, const float* d_sino, const float* d_att, float* d_out, char* ws,
+                       size_t ws_bytes, cudaStream_t st) {
+  Carver cv(ws, ws_bytes);
+  CamGeom* d_geom;
+  float* d_psf;
+  int s = upload_common(pb, cv, &d_geom, &d_psf, st);
+  if (s != kOk) return s;
+  if (use_fused(pb)) {
+    const int cy = round_up(pb.ny, 4);
+    float* sino_c = cv.take<float>(sino_col_n(pb));
+    float* mu_c = d_att ? cv.take<float>(col_n(pb)) : nullptr;
+    float* out_c = cv.take<float>(col_n(pb));
+    const int group = std::max(1, std::min(pb.group, pb.cams.n));
+    float* slab = cv.take<float>(yg_backproject_workspace(pb.nx, pb.ny, pb.nz, pb.cams.n, group) / sizeof(float));
+    if (!sino_c || !out_c || !slab || (d_att && !mu_c)) return kErrAllocGpu;
+    if ((s = to_column(d_sino, sino_c, pb.nx, pb.ny, cy, pb.cams.n, st)) != kOk) return s;
+    if (d_att && (s = to_column(d_att, mu_c, pb.nx, pb.ny, cy, pb.nz, st)) != kOk) return s;
+    YgArgs a;
+    a.nx = pb.nx;
+    a.ny = pb.ny;
+    a.nz = pb.nz;
+    a.cy = cy;
+    a.ncam = pb.cams.n;
+    a.geom = d_geom;
+    a.mu = mu_c;
+    a.sino = sino_c;
+    a.out = out_c;
+    a.psf = d_psf;
+    a.psf_k = pb.psf_k;
+    a.truncate = pb.truncate;
+    a.back_mode = pb.back_mode;
+    a.group = group;
+    a.work = slab;
+    if ((s = yg_backproject(a, st)) != kOk) return s;
+    return check(from_column(out_c, d_out, pb.nx, pb.ny, cy, pb.nz, pb.truncate, st));
+  }
+  GeneralArgs g;
+  g.nx = pb.nx;
+  g.ny = pb.ny;
+  g.nz = pb.nz;
+  g.ncam = pb.cams.n;
+  g.geom_host = pb.geom.data();
+  g.att = d_att;
+  g.sino = d_sino;
+  g.out = d_out;
+  g.psf_sep = d_psf;
+  g.psf_k = pb.psf_k;
+  g.bg = pb.bg;
+  g.bg_att = pb.bg_att;
+  g.truncate = pb.truncate;
+  g.ws_act = cv.take<float>(vol_n(pb));
+  g.ws_att = cv.take<float>(vol_n(pb));
+  g.ws_tmp = cv.take<float>(vol_n(pb));
+  if (!g.ws_act || !g.ws_att || !g.ws_tmp) return kErrAllocGpu;
+  return check(general_backproject(g, st));
+}
+
+int gradient_device(const Problem& pb, const float* d_sino, const float* d_act, const float* d_att, float* d_out,
+                    char* ws, size_t ws_bytes, cudaStream_t st) {
+  Carver cv(ws, ws_bytes);
+  CamGeom* d_geom;
+  float* d_psf;
+  int s = upload_common(pb, cv, &d_geom, &d_psf, st);
+  if (s != kOk) return s;
+  GeneralArgs g;
+  g.nx = pb.nx;
+  g.ny = pb.ny;
+  g.nz = pb.nz;
+  g.ncam = pb.cams.n;
+  g.geom_host = pb.geom.data();
+  g.act = d_act;
+  g.att = d_att;
+  g.sino = d_sino;
+  g.out = d_out;
+  g.psf_sep = d_psf;
+  g.psf_k = pb.psf_k;
+  g.bg = pb.bg;
+  g.bg_att = pb.bg_att;
+  g.truncate = pb.truncate;
+  g.ws_act = cv.take<float>(vol_n(pb));
+  g.ws_att = cv.take<float>(vol_n(pb));
+  g.ws_tmp = cv.take<float>(vol_n(pb));
+  if (!g.ws_act || !g.ws_att || !g.ws_tmp) return kErrAllocGpu;
+  return check(general_gradient(g, st));
+}
+
+// ------------------------------------------------------------ device state
+namespace {
+std::mutex g_states_mu;
+std::map<int, std::unique_ptr<DeviceState>> g_states;
+}  // namespace
+
+DeviceState& current_device_state(int* status) {
+  int dev = 0;
+  *status = kOk;
+  int count = 0;
+  if (cudaGetDeviceCount(&count) != cudaSuccess || count == 0) {
+    cudaGetLastError();
+    *status = kErrNoGpuInstalled;
+  }
+  cudaGetDevice(&dev);
+  std::lock_guard<std::mutex> lk(g_states_mu);
+  auto& p = g_states[dev];
+  if (!p) {
+    p.reset(new DeviceState());
+    p->device = dev;
+    if (*status == kOk) {
+      if (cudaStreamCreateWithFlags(&p->stream, cudaStreamNonBlocking) != cudaSuccess ||
+          cudaEventCreateWithFlags(&p->last_use, cudaEventDisableTiming) != cudaSuccess)
+        *status = kErrUnspecified;
+    }
+  }
+  return *p;
+}
+
+int ensure_arena(DeviceState& ds, size_t bytes) {
+  if (ds.arena_bytes >= bytes) return kOk;
+  if (ds.arena) {
+    cudaStreamSynchronize(ds.stream);
+    cudaDeviceSynchronize();
+    cudaFree(ds.arena);
+    ds.arena = nullptr;
+    ds.arena_bytes = 0;
+  }
+  // grow geometrically so repeated slightly-larger calls do not reallocate
+  const size_t want = std::max(bytes, static_cast<size_t>(64) << 20);
+  if (cudaMalloc(&ds.arena, want) != cudaSuccess) {
+    cudaGetLastError();
+    ds.arena = nullptr;
+    return kErrAllocGpu;
+  }
+  ds.arena_bytes = want;
+  return kOk;
+}
+
+}  // namespace nrgb

@@ -1,0 +1,86 @@
+// Engine: problem description, per-device work space and the device-pointer
+// implementations behind the C-ABI.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <mutex>
+#include <vector>
+
+#include "et_common.h"
+#include "et_geometry.h"
+
+namespace nrgb {
+
+// One projection / backprojection problem: grid, cameras, PSF, backgrounds.
+struct Problem {
+  int nx = 0, ny = 0, nz = 0;
+  Cameras cams;
+  std::vector<CamGeom> geom;
+  bool ygantry = false;
+  int psf_k = 0;               // 0: no PSF
+  std::vector<float> psf_sep;  // [nz][2k]
+  float bg = 0.0f, bg_att = 0.0f;
+  int truncate = 0;
+  int back_mode = kBackReference;
+  int group = 8;  // cameras per backprojection scratch group
+};
+
+// Build a Problem; psf may be null.  psf_size = {kx, ky, planes}.  Returns
+// kErrParameters for shapes the engine does not support (non-square or even
+// PSF, fewer PSF planes than nz).
+int make_problem(int nx, int ny, int nz, const Cameras& cams, const float* psf, const int* psf_size, float bg,
+                 float bg_att, int truncate, Problem* out);
+
+// Whether the fused y-gantry kernels handle this problem.
+bool use_fused(const Problem& pb);
+
+// Per-device state: a library-owned stream, a growing device arena and an
+// event that orders successive users of the arena on any stream.
+struct DeviceState {
+  std::mutex mu;
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  char* arena = nullptr;
+  size_t arena_bytes = 0;
+  cudaEvent_t last_use = nullptr;
+};
+
+// Lock the current device's state (created on first use) for the caller.
+DeviceState& current_device_state(int* status);
+
+// Carves 256-byte aligned pieces out of the arena.
+class Carver {
+ public:
+  Carver(char* base, size_t cap) : base_(base), cap_(cap) {}
+  template <class T>
+  T* take(size_t count) {
+    const size_t bytes = (count * sizeof(T) + 255) / 256 * 256;
+    if (off_ + bytes > cap_) return nullptr;
+    T* p = reinterpret_cast<T*>(base_ + off_);
+    off_ += bytes;
+    return p;
+  }
+  size_t used() const { return off_; }
+
+ private:
+  char* base_;
+  size_t cap_;
+  size_t off_ = 0;
+};
+
+// Ensure the arena holds at least `bytes`.
+int ensure_arena(DeviceState& ds, size_t bytes);
+
+// Device-pointer operations (nifti layout in and out, stream-ordered).
+size_t project_workspace(const Problem& pb, bool has_act, bool has_att);
+size_t backproject_workspace(const Problem& pb, bool has_att);
+size_t gradient_workspace(const Problem& pb);
+int project_device(const Problem& pb, const float* d_act, const float* d_att, float* d_sino, char* ws, size_t ws_bytes,
+                   cudaStream_t st);
+int backproject_device(const Problem& pb, const float* d_sino, const float* d_att, float* d_out, char* ws,
+                       size_t ws_bytes, cudaStream_t st);
+int gradient_device(const Problem& pb, const float* d_sino, const float* d_act, const float* d_att, float* d_out,
+                    char* ws, size_t ws_bytes, cudaStream_t st);
+
+}  // namespace nrgb

@@ -1,0 +1,274 @@
+// General-orientation path: cameras with any (theta_x, theta_y, theta_z),
+// any background values, any grid.  Volumes in nifti layout.  Each stage is a
+// separate kernel following the reference's float operation order (products
+// and sums rounded separately), so this path reproduces the reference CPU
+// path up to the last bit of expf.  The fused kernels of et_ygantry.cu cover
+// the common gantry case; this path covers everything else.
+#include "et_kernels.h"
+#include "et_profile.h"
+
+namespace nrgb {
+
+namespace {
+
+struct Affine34 {
+  float m[12];
+};
+
+__device__ __forceinline__ float fm(float a, float b) { return __fmul_rn(a, b); }
+__device__ __forceinline__ float fa(float a, float b) { return __fadd_rn(a, b); }
+
+// Trilinear resampling of one voxel, reg-lib/_reg_resampling.cpp:334-450
+// (positions from reg-lib/_reg_affineTransformation.cpp:116-132 with an
+// identity voxel-to-world matrix).  With bg != 0 every neighbour outside the
+// grid adds bg * xBasis[.] to a separate background weight, as the reference
+// does (:366-396).
+__device__ __forceinline__ float trilinear_ref(const float* __restrict__ src, int nx, int ny, int nz,
+                                               const Affine34& A, int x, int y, int z, float bg) {
+  const float fx = static_cast<float>(x), fy = static_cast<float>(y), fz = static_cast<float>(z);
+  float pos[3];
+#pragma unroll
+  for (int i = 0; i < 3; ++i)
+    pos[i] = fa(fa(fa(fm(A.m[4 * i + 0], fx), fm(A.m[4 * i + 1], fy)), fm(A.m[4 * i + 2], fz)), A.m[4 * i + 3]);
+  int prev[3];
+  float b0[3], b1[3];
+#pragma unroll
+  for (int i = 0; i < 3; ++i) {
+    prev[i] = static_cast<int>(floorf(pos[i]));
+    float rel = __fsub_rn(pos[i], static_cast<float>(prev[i]));
+    if (rel < 0.0f) rel = 0.0f;
+    b0[i] = __fsub_rn(1.0f, rel);
+    b1[i] = rel;
+  }
+  const float bx[2] = {b0[0], b1[0]};
+  const float by[2] = {b0[1], b1[1]};
+  const float bz[2] = {b0[2], b1[2]};
+  float val = 0.0f, bgw = 0.0f;
+  const bool use_bg = (bg != 0.0f);
+#pragma unroll
+  for (int c = 0; c < 2; ++c) {
+    const int Z = prev[2] + c;
+    if (Z >= 0 && Z < nz) {
+      float ysum = 0.0f;
+#pragma unroll
+      for (int b = 0; b < 2; ++b) {
+        const int Y = prev[1] + b;
+        if (Y >= 0 && Y < ny) {
+          const float* row = src + (static_cast<size_t>(Z) * ny + Y) * nx;
+          float xsum = 0.0f;
+#pragma unroll
+          for (int a = 0; a < 2; ++a) {
+            const int X = prev[0] + a;
+            if (X >= 0 && X < nx)
+              xsum = fa(xsum, fm(__ldg(row + X), bx[a]));
+            else if (use_bg)
+              bgw = fa(bgw, fm(bg, bx[a]));
+          }
+          ysum = fa(ysum, fm(xsum, by[b]));
+        } else if (use_bg) {
+          bgw = fa(bgw, fm(bg, bx[b]));
+        }
+      }
+      val = fa(val, fm(ysum, bz[c]));
+    } else if (use_bg) {
+      bgw = fa(bgw, fm(bg, bx[c]));
+    }
+  }
+  if (use_bg) val = fa(val, bgw);
+  return val;
+}
+
+template <bool ACCUM>
+__global__ void k_resample(const float* __restrict__ src, float* __restrict__ dst, int nx, int ny, int nz,
+                           Affine34 A, float bg) {
+  const size_t nvox = static_cast<size_t>(nx) * ny * nz;
+  for (size_t i = blockIdx.x * static_cast<size_t>(blockDim.x) + threadIdx.x; i < nvox;
+       i += static_cast<size_t>(gridDim.x) * blockDim.x) {
+    const int x = static_cast<int>(i % nx);
+    const int y = static_cast<int>((i / nx) % ny);
+    const int z = static_cast<int>(i / (static_cast<size_t>(nx) * ny));
+    const float v = trilinear_ref(src, nx, ny, nz, A, x, y, z, bg);
+    if (ACCUM)
+      dst[i] = fa(dst[i], v);
+    else
+      dst[i] = v;
+  }
+}
+
+// Row (x) then column (y) pass of emission-lib/_et_convolveSeparable2D.cpp:13-40:
+// true convolution (kernel index R-k), zero outside the plane, plane z uses
+// kernel plane z.  sep layout [plane][row k | column k].
+template <bool ROWS>
+__global__ void k_conv(const float* __restrict__ in, float* __restrict__ out, int nx, int ny, int nz,
+                       const float* __restrict__ sep, int k) {
+  const size_t nvox = static_cast<size_t>(nx) * ny * nz;
+  const int R = (k - 1) / 2;
+  for (size_t i = blockIdx.x * static_cast<size_t>(blockDim.x) + threadIdx.x; i < nvox;
+       i += static_cast<size_t>(gridDim.x) * blockDim.x) {
+    const int x = static_cast<int>(i % nx);
+    const int y = static_cast<int>((i / nx) % ny);
+    const int z = static_cast<int>(i / (static_cast<size_t>(nx) * ny));
+    const float* K = sep + static_cast<size_t>(2 * k) * z + (ROWS ? 0 : k);
+    float s = 0.0f;
+    for (int kk = -R; kk <= R; ++kk) {
+      if (ROWS) {
+        const int d = x + kk;
+        if (d >= 0 && d < nx) s = fa(s, fm(__ldg(in + i + kk), __ldg(K + R - kk)));
+      } else {
+        const int d = y + kk;
+        if (d >= 0 && d < ny) s = fa(s, fm(__ldg(in + i + static_cast<ptrdiff_t>(kk) * nx), __ldg(K + R - kk)));
+      }
+    }
+    out[i] = s;
+  }
+}
+
+// Attenuated line integral along z, emission-lib/_et_line_integral_attenuated.cpp:14-68.
+__global__ void k_line_integral(const float* __restrict__ act, const float* __restrict__ att,
+                                float* __restrict__ out, int nx, int ny, int nz, float bg) {
+  const int nxy = nx * ny;
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= nxy) return;
+  float p = 0.0f, T = 0.0f;
+  if (act && att) {
+    for (int z = 0; z < nz; ++z) {
+      T = fa(T, __ldg(att + static_cast<size_t>(z) * nxy + i));
+      p = fa(p, fm(__ldg(act + static_cast<size_t>(z) * nxy + i), expf(-T)));
+    }
+    p = fa(p, fm(bg, expf(-T)));
+  } else if (act) {
+    for (int z = 0; z < nz; ++z) p = fa(p, __ldg(act + static_cast<size_t>(z) * nxy + i));
+    p = fa(p, bg);
+  } else {
+    for (int z = 0; z < nz; ++z) T = fa(T, __ldg(att + static_cast<size_t>(z) * nxy + i));
+    p = fm(bg, expf(-T));
+  }
+  out[i] = p;
+}
+
+// Spread along z, emission-lib/_et_line_backproject_attenuated.cpp:17-36 and
+// emission-lib/_et_line_backproject.cpp:17-30.
+__global__ void k_spread(const float* __restrict__ plane, const float* __restrict__ att, float* __restrict__ vol,
+                         int nx, int ny, int nz) {
+  const int nxy = nx * ny;
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= nxy) return;
+  const float s = __ldg(plane + i);
+  float T = 0.0f;
+  for (int z = 0; z < nz; ++z) {
+    const size_t j = static_cast<size_t>(z) * nxy + i;
+    if (att) {
+      T = fa(T, __ldg(att + j));
+      vol[j] = fm(s, expf(-T));
+    } else {
+      vol[j] = s;
+    }
+  }
+}
+
+// Attenuation-gradient scan, emission-lib_gpu/_et_attenuation_gradient_gpu_kernels.cu:24-39:
+// pass 1 stores the inclusive prefix T_z, pass 2 (far to near) accumulates
+// a_z * exp(-T_z) and stores s * acc.
+__global__ void k_grad_scan(const float* __restrict__ act, const float* __restrict__ att,
+                            const float* __restrict__ plane, float* __restrict__ vol, int nx, int ny, int nz) {
+  const int nxy = nx * ny;
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= nxy) return;
+  float T = 0.0f;
+  for (int z = 0; z < nz; ++z) {
+    const size_t j = static_cast<size_t>(z) * nxy + i;
+    T = fa(T, __ldg(att + j));
+    vol[j] = T;
+  }
+  const float s = __ldg(plane + i);
+  float acc = 0.0f;
+  for (int z = nz - 1; z >= 0; --z) {
+    const size_t j = static_cast<size_t>(z) * nxy + i;
+    acc = fa(acc, fm(__ldg(act + j), expf(-vol[j])));
+    vol[j] = fm(s, acc);
+  }
+}
+
+int grid_for(size_t n, int block) {
+  const size_t g = (n + block - 1) / block;
+  return static_cast<int>(g < 152 * 64 ? g : 152 * 64);
+}
+
+Affine34 affine_of(const float* m12) {
+  Affine34 a;
+  for (int i = 0; i < 12; ++i) a.m[i] = m12[i];
+  return a;
+}
+
+}  // namespace
+
+int general_project(const GeneralArgs& a, cudaStream_t st) {
+  const int nx = a.nx, ny = a.ny, nz = a.nz;
+  const size_t nvox = static_cast<size_t>(nx) * ny * nz, nxy = static_cast<size_t>(nx) * ny;
+  const int B = 256;
+  for (int cam = 0; cam < a.ncam; ++cam) {
+    const Affine34 F = affine_of(a.geom_host[cam].fwd);
+    if (a.act) { NRGB_LAUNCH_SCOPE("k_resample", st); k_resample<false><<<grid_for(nvox, B), B, 0, st>>>(a.act, a.ws_act, nx, ny, nz, F, a.bg); }
+    if (a.att) { NRGB_LAUNCH_SCOPE("k_resample", st); k_resample<false><<<grid_for(nvox, B), B, 0, st>>>(a.att, a.ws_att, nx, ny, nz, F, a.bg_att); }
+    if (a.psf_sep && a.act) {
+      { NRGB_LAUNCH_SCOPE("k_conv", st); k_conv<true><<<grid_for(nvox, B), B, 0, st>>>(a.ws_act, a.ws_tmp, nx, ny, nz, a.psf_sep, a.psf_k); }
+      { NRGB_LAUNCH_SCOPE("k_conv", st); k_conv<false><<<grid_for(nvox, B), B, 0, st>>>(a.ws_tmp, a.ws_act, nx, ny, nz, a.psf_sep, a.psf_k); }
+    }
+    { NRGB_LAUNCH_SCOPE("k_line_integral", st); k_line_integral<<<static_cast<int>((nxy + B - 1) / B), B, 0, st>>>(a.act ? a.ws_act : nullptr,
+                                                                      a.att ? a.ws_att : nullptr,
+                                                                      a.out + nxy * cam, nx, ny, nz, a.bg); }
+  }
+  if (a.truncate) launch_truncate(a.out, nxy * a.ncam, st);
+  return cudaGetLastError() == cudaSuccess ? kOk : kErrKernel;
+}
+
+int general_backproject(const GeneralArgs& a, cudaStream_t st) {
+  const int nx = a.nx, ny = a.ny, nz = a.nz;
+  const size_t nvox = static_cast<size_t>(nx) * ny * nz, nxy = static_cast<size_t>(nx) * ny;
+  const int B = 256;
+  cudaMemsetAsync(a.out, 0, nvox * sizeof(float), st);
+  for (int cam = 0; cam < a.ncam; ++cam) {
+    const Affine34 F = affine_of(a.geom_host[cam].fwd);
+    const Affine34 Bk = affine_of(a.geom_host[cam].bwd);
+    if (a.att) { NRGB_LAUNCH_SCOPE("k_resample", st); k_resample<false><<<grid_for(nvox, B), B, 0, st>>>(a.att, a.ws_att, nx, ny, nz, F, a.bg_att); }
+    { NRGB_LAUNCH_SCOPE("k_spread", st); k_spread<<<static_cast<int>((nxy + B - 1) / B), B, 0, st>>>(a.sino + nxy * cam, a.att ? a.ws_att : nullptr,
+                                                               a.ws_act, nx, ny, nz); }
+    if (a.psf_sep) {
+      { NRGB_LAUNCH_SCOPE("k_conv", st); k_conv<true><<<grid_for(nvox, B), B, 0, st>>>(a.ws_act, a.ws_tmp, nx, ny, nz, a.psf_sep, a.psf_k); }
+      { NRGB_LAUNCH_SCOPE("k_conv", st); k_conv<false><<<grid_for(nvox, B), B, 0, st>>>(a.ws_tmp, a.ws_act, nx, ny, nz, a.psf_sep, a.psf_k); }
+    }
+    { NRGB_LAUNCH_SCOPE("k_resample", st); k_resample<true><<<grid_for(nvox, B), B, 0, st>>>(a.ws_act, a.out, nx, ny, nz, Bk, a.bg); }
+  }
+  if (a.truncate) launch_truncate(a.out, nvox, st);
+  return cudaGetLastError() == cudaSuccess ? kOk : kErrKernel;
+}
+
+int general_gradient(const GeneralArgs& a, cudaStream_t st) {
+  const int nx = a.nx, ny = a.ny, nz = a.nz;
+  const size_t nvox = static_cast<size_t>(nx) * ny * nz, nxy = static_cast<size_t>(nx) * ny;
+  const int B = 256;
+  cudaMemsetAsync(a.out, 0, nvox * sizeof(float), st);
+  for (int cam = 0; cam < a.ncam; ++cam) {
+    const Affine34 F = affine_of(a.geom_host[cam].fwd);
+    const Affine34 Bk = affine_of(a.geom_host[cam].bwd);
+    { NRGB_LAUNCH_SCOPE("k_resample", st); k_resample<false><<<grid_for(nvox, B), B, 0, st>>>(a.att, a.ws_att, nx, ny, nz, F, a.bg_att); }
+    { NRGB_LAUNCH_SCOPE("k_resample", st); k_resample<false><<<grid_for(nvox, B), B, 0, st>>>(a.act, a.ws_act, nx, ny, nz, F, a.bg); }
+    { NRGB_LAUNCH_SCOPE("k_grad_scan", st); k_grad_scan<<<static_cast<int>((nxy + B - 1) / B), B, 0, st>>>(a.ws_act, a.ws_att, a.sino + nxy * cam,
+                                                                  a.ws_tmp, nx, ny, nz); }
+    if (a.psf_sep) {
+      { NRGB_LAUNCH_SCOPE("k_conv", st); k_conv<true><<<grid_for(nvox, B), B, 0, st>>>(a.ws_tmp, a.ws_act, nx, ny, nz, a.psf_sep, a.psf_k); }
+      { NRGB_LAUNCH_SCOPE("k_conv", st); k_conv<false><<<grid_for(nvox, B), B, 0, st>>>(a.ws_act, a.ws_tmp, nx, ny, nz, a.psf_sep, a.psf_k); }
+    }
+    { NRGB_LAUNCH_SCOPE("k_resample", st); k_resample<true><<<grid_for(nvox, B), B, 0, st>>>(a.ws_tmp, a.out, nx, ny, nz, Bk, a.bg); }
+  }
+  if (a.truncate) launch_truncate(a.out, nvox, st);
+  return cudaGetLastError() == cudaSuccess ? kOk : kErrKernel;
+}
+
+int general_rotate(const float* src, float* dst, int nx, int ny, int nz, const float* m12, float bg, cudaStream_t st) {
+  const size_t nvox = static_cast<size_t>(nx) * ny * nz;
+  { NRGB_LAUNCH_SCOPE("k_resample", st); k_resample<false><<<grid_for(nvox, 256), 256, 0, st>>>(src, dst, nx, ny, nz, affine_of(m12), bg); }
+  return cudaGetLastError() == cudaSuccess ? kOk : kErrKernel;
+}
+
+}  // namespace nrgb

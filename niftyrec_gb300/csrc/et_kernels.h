@@ -1,0 +1,74 @@
+// Launch-side declarations of the CUDA kernels (device code in et_general.cu,
+// et_ygantry.cu, et_update.cu).
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include "et_common.h"
+
+namespace nrgb {
+
+// ---- general-orientation path (nifti layout) ----
+struct GeneralArgs {
+  int nx = 0, ny = 0, nz = 0, ncam = 0;
+  const CamGeom* geom_host = nullptr;  // host array; matrices go to kernels by value
+  const float* act = nullptr;          // device volume or null
+  const float* att = nullptr;          // device volume or null
+  const float* sino = nullptr;         // device sinogram input (backprojection, gradient)
+  float* out = nullptr;                // device output
+  const float* psf_sep = nullptr;      // device [nz][2k] or null
+  int psf_k = 0;
+  float bg = 0.0f, bg_att = 0.0f;
+  int truncate = 0;
+  float* ws_act = nullptr;  // three nvox work volumes
+  float* ws_att = nullptr;
+  float* ws_tmp = nullptr;
+};
+int general_project(const GeneralArgs& a, cudaStream_t st);
+int general_backproject(const GeneralArgs& a, cudaStream_t st);
+int general_gradient(const GeneralArgs& a, cudaStream_t st);
+int general_rotate(const float* src, float* dst, int nx, int ny, int nz, const float* m12, float bg, cudaStream_t st);
+
+// ---- y-gantry fused path (column layout) ----
+struct YgArgs {
+  int nx = 0, ny = 0, nz = 0, cy = 0, ncam = 0;
+  const CamGeom* geom = nullptr;  // device [ncam]
+  const float* act = nullptr;     // [nz][nx][cy]
+  const float* mu = nullptr;      // [nz][nx][cy] or null
+  const float* sino = nullptr;    // [ncam][nx][cy] (backprojection input)
+  float* out = nullptr;           // projector: [ncam][nx][cy]; backprojector: [nz][nx][cy]
+  const float* psf = nullptr;     // device [nz][2k] or null
+  int psf_k = 0;
+  int truncate = 0;
+  int back_mode = kBackReference;
+  // backprojector work space (yg_backproject_workspace bytes); the kernels
+  // see it as slab sums [ncam][slabs][nx][cy] then scratch [group][nz][nx][cy]
+  float* work = nullptr;
+  float* slab_T = nullptr;
+  float* temp = nullptr;
+  int group = 8;
+};
+// True when the fused kernels support this grid / PSF size.
+bool yg_supported(int nx, int ny, int nz, int psf_k);
+// Bytes of work space yg_backproject needs (slab sums + camera-group scratch).
+size_t yg_backproject_workspace(int nx, int ny, int nz, int ncam, int group);
+int yg_project(const YgArgs& a, cudaStream_t st);
+int yg_backproject(const YgArgs& a, cudaStream_t st);
+
+// ---- layout conversion and elementwise helpers ----
+// planes x [ny][nx] (nifti) <-> planes x [nx][cy] (column), zero pads.
+int to_column(const float* src, float* dst, int nx, int ny, int cy, int planes, cudaStream_t st);
+int from_column(const float* src, float* dst, int nx, int ny, int cy, int planes, int truncate, cudaStream_t st);
+void launch_truncate(float* buf, size_t n, cudaStream_t st);
+
+// ---- OSEM / MLEM update kernels ----
+// ratio[i] = y[i] / (p[i] < eps ? eps : p[i])   (emission-lib/_et_array_interface.cpp:1022-1028)
+int osem_ratio(const float* y, float* p_to_ratio, size_t n, float eps, cudaStream_t st);
+// x[i] *= num[i] / max(den[i], eps)            (:1036-1044)
+int osem_update(float* x, const float* num, const float* den, size_t n, float eps, cudaStream_t st);
+// FP64 totals: out[0] = sum(a), out[1] = sum(b) (b may be null), device doubles.
+int sum_fp64(const float* a, const float* b, size_t n, double* out, cudaStream_t st);
+// out[i] = value
+int fill(float* out, size_t n, float value, cudaStream_t st);
+
+}  // namespace nrgb

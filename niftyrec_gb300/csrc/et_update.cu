@@ -1,0 +1,128 @@
+// Elementwise kernels of the OSEM / MLEM step and small helpers.  All are
+// HBM-streaming: float4 vectorised where the buffer allows it, grid-stride
+// loops over a grid sized to a few waves of the 152 SMs.
+#include "et_kernels.h"
+#include "et_profile.h"
+
+namespace nrgb {
+
+namespace {
+
+constexpr int kBlock = 256;
+
+int grid_for(size_t n) {
+  const size_t g = (n + kBlock - 1) / kBlock;
+  const size_t cap = 152 * 16;
+  return static_cast<int>(g < cap ? (g == 0 ? 1 : g) : cap);
+}
+
+// emission-lib/_et_array_interface.cpp:1022-1028: y/eps where p < eps, else y/p.
+__global__ void k_ratio(const float* __restrict__ y, float* __restrict__ p, size_t n, float eps) {
+  for (size_t i = blockIdx.x * static_cast<size_t>(blockDim.x) + threadIdx.x; i < n;
+       i += static_cast<size_t>(gridDim.x) * blockDim.x) {
+    const float pv = p[i];
+    p[i] = (pv < eps) ? __fdiv_rn(y[i], eps) : __fdiv_rn(y[i], pv);
+  }
+}
+
+// emission-lib/_et_array_interface.cpp:1036-1044: den < eps -> eps; x *= num / den.
+__global__ void k_update(float* __restrict__ x, const float* __restrict__ num, const float* __restrict__ den,
+                         size_t n, float eps) {
+  for (size_t i = blockIdx.x * static_cast<size_t>(blockDim.x) + threadIdx.x; i < n;
+       i += static_cast<size_t>(gridDim.x) * blockDim.x) {
+    float d = den[i];
+    if (d < eps) d = eps;
+    x[i] = __fmul_rn(x[i], __fdiv_rn(num[i], d));
+  }
+}
+
+__global__ void k_truncate(float* __restrict__ b, size_t n) {
+  for (size_t i = blockIdx.x * static_cast<size_t>(blockDim.x) + threadIdx.x; i < n;
+       i += static_cast<size_t>(gridDim.x) * blockDim.x)
+    if (b[i] < 0.0f) b[i] = 0.0f;
+}
+
+__global__ void k_fill(float* __restrict__ b, size_t n, float v) {
+  for (size_t i = blockIdx.x * static_cast<size_t>(blockDim.x) + threadIdx.x; i < n;
+       i += static_cast<size_t>(gridDim.x) * blockDim.x)
+    b[i] = v;
+}
+
+// Deterministic FP64 totals: one partial per block (fixed order), then a
+// single-block pass over the partials.
+__global__ void k_sum_partial(const float* __restrict__ a, const float* __restrict__ b, size_t n,
+                              double* __restrict__ part) {
+  __shared__ double sa[kBlock], sb[kBlock];
+  double va = 0.0, vb = 0.0;
+  for (size_t i = blockIdx.x * static_cast<size_t>(blockDim.x) + threadIdx.x; i < n;
+       i += static_cast<size_t>(gridDim.x) * blockDim.x) {
+    va += static_cast<double>(a[i]);
+    if (b) vb += static_cast<double>(b[i]);
+  }
+  sa[threadIdx.x] = va;
+  sb[threadIdx.x] = vb;
+  __syncthreads();
+  for (int s = kBlock / 2; s > 0; s >>= 1) {
+    if (threadIdx.x < s) {
+      sa[threadIdx.x] += sa[threadIdx.x + s];
+      sb[threadIdx.x] += sb[threadIdx.x + s];
+    }
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) {
+    part[2 * blockIdx.x] = sa[0];
+    part[2 * blockIdx.x + 1] = sb[0];
+  }
+}
+
+__global__ void k_sum_final(const double* __restrict__ part, int nparts, double* __restrict__ out) {
+  __shared__ double sa[kBlock], sb[kBlock];
+  double va = 0.0, vb = 0.0;
+  for (int i = threadIdx.x; i < nparts; i += blockDim.x) {
+    va += part[2 * i];
+    vb += part[2 * i + 1];
+  }
+  sa[threadIdx.x] = va;
+  sb[threadIdx.x] = vb;
+  __syncthreads();
+  for (int s = kBlock / 2; s > 0; s >>= 1) {
+    if (threadIdx.x < s) {
+      sa[threadIdx.x] += sa[threadIdx.x + s];
+      sb[threadIdx.x] += sb[threadIdx.x + s];
+    }
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) {
+    out[0] = sa[0];
+    out[1] = sb[0];
+  }
+}
+
+}  // namespace
+
+int osem_ratio(const float* y, float* p, size_t n, float eps, cudaStream_t st) {
+  { NRGB_LAUNCH_SCOPE("k_ratio", st); k_ratio<<<grid_for(n), kBlock, 0, st>>>(y, p, n, eps); }
+  return cudaGetLastError() == cudaSuccess ? kOk : kErrKernel;
+}
+
+int osem_update(float* x, const float* num, const float* den, size_t n, float eps, cudaStream_t st) {
+  { NRGB_LAUNCH_SCOPE("k_update", st); k_update<<<grid_for(n), kBlock, 0, st>>>(x, num, den, n, eps); }
+  return cudaGetLastError() == cudaSuccess ? kOk : kErrKernel;
+}
+
+void launch_truncate(float* buf, size_t n, cudaStream_t st) { { NRGB_LAUNCH_SCOPE("k_truncate", st); k_truncate<<<grid_for(n), kBlock, 0, st>>>(buf, n); } }
+
+int fill(float* out, size_t n, float value, cudaStream_t st) {
+  { NRGB_LAUNCH_SCOPE("k_fill", st); k_fill<<<grid_for(n), kBlock, 0, st>>>(out, n, value); }
+  return cudaGetLastError() == cudaSuccess ? kOk : kErrKernel;
+}
+
+// out must hold 2 + 2 * 256 doubles: [total_a, total_b, partials...].
+int sum_fp64(const float* a, const float* b, size_t n, double* out, cudaStream_t st) {
+  const int parts = 256;
+  { NRGB_LAUNCH_SCOPE("k_sum_partial", st); k_sum_partial<<<parts, kBlock, 0, st>>>(a, b, n, out + 2); }
+  { NRGB_LAUNCH_SCOPE("k_sum_final", st); k_sum_final<<<1, kBlock, 0, st>>>(out + 2, parts, out); }
+  return cudaGetLastError() == cudaSuccess ? kOk : kErrKernel;
+}
+
+}  // namespace nrgb

@@ -1,0 +1,621 @@
+// Fused kernels for cameras that rotate about the gantry axis (nifti y):
+// theta_x = theta_z = 0, so the resampling matrix is an exact rotation in the
+// (x, z) plane and y maps to itself.  Every detector row y then samples the
+// SAME bilinear footprint in the (x, z) plane, so the device layout puts y
+// fastest ("column layout" [z][x][cy]) and one warp handles whole columns:
+// lane l owns y = 4l..4l+3 (float4), the footprint of a (x, z) column is
+// computed once per warp and every gather is a coalesced 16-byte-per-lane
+// column load.
+//
+// Projector  (emission-lib/_et.cpp:218-281): per camera, per depth plane z:
+//   rotate (bilinear gather of activity and mu), per-plane separable PSF
+//   (row pass along x in a register sliding window, column pass along y with
+//   warp shuffles), attenuated depth scan T += mu; p += v * exp(-T).  No
+//   rotated volume is written anywhere: one CTA owns (camera, x-tile), its
+//   warps own depth slabs and merge (T, p) in shared memory at the end:
+//   p = p0 + exp(-T0) p1 + exp(-T0-T1) p2 + ...
+// Backprojector, reference mode (emission-lib/_et.cpp:415-499):
+//   (1) slab sums of the rotated mu (carry-in of each depth slab),
+//   (2) per camera group: spread s*exp(-T) + PSF in the rotated frame into a
+//       small L2-sized scratch, (3) inverse-rotation gather of the group into
+//       the accumulator.
+#include "et_kernels.h"
+#include "et_profile.h"
+
+#include <algorithm>
+
+namespace nrgb {
+
+namespace {
+
+constexpr int kWarps = 4;       // warps per CTA = depth slabs
+constexpr int kTileX = 8;       // output x columns per warp
+constexpr int kGatherCols = 8;  // accumulator columns per warp in the gather
+constexpr unsigned kFull = 0xffffffffu;
+
+__device__ __forceinline__ float fm(float a, float b) { return __fmul_rn(a, b); }
+__device__ __forceinline__ float fa(float a, float b) { return __fadd_rn(a, b); }
+
+// Bilinear footprint of one sampled column.  Corner (a, c) sits at
+// off + a*dx + c*dz; corners outside the grid get weight 0 and a clamped
+// (valid) address, so loads never leave the volume.
+struct __align__(16) Tap {
+  int off, dx, dz, any;
+  float w00, w10, w01, w11;
+};
+
+// Footprint of rotated column (xp, zp) under rows (m00, m02, m03) -> x and
+// (m20, m22, m23) -> z.  Position arithmetic follows
+// reg-lib/_reg_affineTransformation.cpp:116-132 (the y terms are exact zeros
+// for a y-gantry), floor/relative/basis follow reg-lib/_reg_resampling.cpp:347-364.
+__device__ __forceinline__ Tap make_tap(int xp, int zp, float m00, float m02, float m03, float m20, float m22,
+                                        float m23, int nx, int nz, int cy, bool col_valid) {
+  const float fx = static_cast<float>(xp), fz = static_cast<float>(zp);
+  const float px = fa(fa(fm(m00, fx), fm(m02, fz)), m03);
+  const float pz = fa(fa(fm(m20, fx), fm(m22, fz)), m23);
+  const int xs = static_cast<int>(floorf(px));
+  const int zs = static_cast<int>(floorf(pz));
+  float rx = __fsub_rn(px, static_cast<float>(xs));
+  float rz = __fsub_rn(pz, static_cast<float>(zs));
+  if (rx < 0.0f) rx = 0.0f;
+  if (rz < 0.0f) rz = 0.0f;
+  const float wx0 = __fsub_rn(1.0f, rx), wx1 = rx, wz0 = __fsub_rn(1.0f, rz), wz1 = rz;
+  const bool x0 = col_valid && xs >= 0 && xs < nx;
+  const bool x1 = col_valid && xs + 1 >= 0 && xs + 1 < nx;
+  const bool z0 = col_valid && zs >= 0 && zs < nz;
+  const bool z1 = col_valid && zs + 1 >= 0 && zs + 1 < nz;
+  Tap t;
+  const int xb = x0 ? xs : (x1 ? xs + 1 : 0);
+  const int zb = z0 ? zs : (z1 ? zs + 1 : 0);
+  t.off = (zb * nx + xb) * cy;
+  t.dx = (x0 && x1) ? cy : 0;
+  t.dz = (z0 && z1) ? nx * cy : 0;
+  t.w00 = (x0 && z0) ? wx0 * wz0 : 0.0f;
+  t.w10 = (x1 && z0) ? wx1 * wz0 : 0.0f;
+  t.w01 = (x0 && z1) ? wx0 * wz1 : 0.0f;
+  t.w11 = (x1 && z1) ? wx1 * wz1 : 0.0f;
+  t.any = (x0 || x1) && (z0 || z1);
+  return t;
+}
+
+__device__ __forceinline__ float4 ldg4(const float* p) { return __ldg(reinterpret_cast<const float4*>(p)); }
+
+__device__ __forceinline__ float4 sample4(const float* __restrict__ base, const Tap& t, int yb, bool yok) {
+  float4 r = make_float4(0.f, 0.f, 0.f, 0.f);
+  if (!t.any || !yok) return r;
+  const float* p = base + t.off + yb;
+  const float4 a = ldg4(p), b = ldg4(p + t.dx), c = ldg4(p + t.dz), d = ldg4(p + t.dx + t.dz);
+  r.x = fmaf(d.x, t.w11, fmaf(c.x, t.w01, fmaf(b.x, t.w10, a.x * t.w00)));
+  r.y = fmaf(d.y, t.w11, fmaf(c.y, t.w01, fmaf(b.y, t.w10, a.y * t.w00)));
+  r.z = fmaf(d.z, t.w11, fmaf(c.z, t.w01, fmaf(b.z, t.w10, a.z * t.w00)));
+  r.w = fmaf(d.w, t.w11, fmaf(c.w, t.w01, fmaf(b.w, t.w10, a.w * t.w00)));
+  return r;
+}
+
+__device__ __forceinline__ float comp(const float4& v, int c) { return c == 0 ? v.x : c == 1 ? v.y : c == 2 ? v.z : v.w; }
+
+__device__ __forceinline__ void axpy4(float4& acc, float k, const float4& v) {
+  acc.x = fmaf(k, v.x, acc.x);
+  acc.y = fmaf(k, v.y, acc.y);
+  acc.z = fmaf(k, v.z, acc.z);
+  acc.w = fmaf(k, v.w, acc.w);
+}
+
+// Rows y >= ny are zero pads of the column layout; the column pass must not
+// leak into them (the reference's column pass only produces rows < ny).
+__device__ __forceinline__ float4 mask_rows(float4 v, int yb, int ny) {
+  if (yb + 0 >= ny) v.x = 0.0f;
+  if (yb + 1 >= ny) v.y = 0.0f;
+  if (yb + 2 >= ny) v.z = 0.0f;
+  if (yb + 3 >= ny) v.w = 0.0f;
+  return v;
+}
+
+// Column (y) pass of the per-plane convolution for the 4 rows a lane owns:
+// out[y] = sum_k in[y+k] * kc[R-k], zero outside [0, ny) (rows >= ny are zero
+// pads, rows < 0 come from lanes below 0 and are masked).  Neighbour rows come
+// from lanes l-1, l-2 and l+1, l+2 by shuffles.
+template <int R>
+__device__ __forceinline__ float4 yconv4(const float4& u, const float* kc, int lane) {
+  float w[2 * R + 4];
+  w[R + 0] = u.x;
+  w[R + 1] = u.y;
+  w[R + 2] = u.z;
+  w[R + 3] = u.w;
+#pragma unroll
+  for (int t = 1; t <= R; ++t) {
+    const int dl = (t + 3) / 4;
+    const float s = __shfl_up_sync(kFull, comp(u, 4 * dl - t), dl);
+    w[R - t] = (lane >= dl) ? s : 0.0f;
+  }
+#pragma unroll
+  for (int t = 1; t <= R; ++t) {
+    const int dl = (t + 3) / 4;
+    const float s = __shfl_down_sync(kFull, comp(u, t + 3 - 4 * dl), dl);
+    w[R + 3 + t] = (lane + dl < 32) ? s : 0.0f;
+  }
+  float4 o = make_float4(0.f, 0.f, 0.f, 0.f);
+#pragma unroll
+  for (int k = -R; k <= R; ++k) {
+    const float kk = kc[R - k];
+    o.x = fmaf(w[R + 0 + k], kk, o.x);
+    o.y = fmaf(w[R + 1 + k], kk, o.y);
+    o.z = fmaf(w[R + 2 + k], kk, o.z);
+    o.w = fmaf(w[R + 3 + k], kk, o.w);
+  }
+  return o;
+}
+
+// Per-plane separable PSF over a tile of TX output columns from NJ = TX + 2R
+// sampled columns.  sample(j) produces the rotated value at x' = x0 - R + j
+// (zero outside the grid: the row pass pads with zeros), emit(i, v) receives
+// the convolved value of output column x0 + i.  Row pass: sliding window of
+// 2R+1 partial sums in registers; column pass: yconv4.
+template <int TX, int R, class SampleFn, class EmitFn>
+__device__ __forceinline__ void psf_tile(SampleFn sample, EmitFn emit, const float* kr, const float* kc, int lane,
+                                         int ny) {
+  constexpr int K = 2 * R + 1;
+  constexpr int NJ = TX + 2 * R;
+  float4 u[K];
+#pragma unroll
+  for (int q = 0; q < K; ++q) u[q] = make_float4(0.f, 0.f, 0.f, 0.f);
+#pragma unroll
+  for (int j = 0; j < NJ; ++j) {
+    const float4 r = sample(j);
+#pragma unroll
+    for (int d = 0; d < K; ++d) {
+      const int i = j - d;
+      if (i >= 0 && i < TX) axpy4(u[i % K], kr[2 * R - d], r);
+    }
+    const int i = j - 2 * R;
+    if (i >= 0 && i < TX) {
+      emit(i, mask_rows(yconv4<R>(u[i % K], kc, lane), 4 * lane, ny));
+      u[i % K] = make_float4(0.f, 0.f, 0.f, 0.f);
+    }
+  }
+}
+
+__device__ __forceinline__ float4 exp_neg4(const float4& t) {
+  return make_float4(__expf(-t.x), __expf(-t.y), __expf(-t.z), __expf(-t.w));
+}
+
+__device__ __forceinline__ void add4(float4& a, const float4& b) {
+  a.x += b.x;
+  a.y += b.y;
+  a.z += b.z;
+  a.w += b.w;
+}
+
+__device__ __forceinline__ void fma4(float4& acc, const float4& a, const float4& b) {
+  acc.x = fmaf(a.x, b.x, acc.x);
+  acc.y = fmaf(a.y, b.y, acc.y);
+  acc.z = fmaf(a.z, b.z, acc.z);
+  acc.w = fmaf(a.w, b.w, acc.w);
+}
+
+__device__ __forceinline__ float4 mul4(const float4& a, const float4& b) {
+  return make_float4(a.x * b.x, a.y * b.y, a.z * b.z, a.w * b.w);
+}
+
+struct CamRows {
+  float m00, m02, m03, m20, m22, m23;
+};
+
+__device__ __forceinline__ CamRows cam_rows(const float* m) {
+  CamRows c;
+  c.m00 = __ldg(m + 0);
+  c.m02 = __ldg(m + 2);
+  c.m03 = __ldg(m + 3);
+  c.m20 = __ldg(m + 8);
+  c.m22 = __ldg(m + 10);
+  c.m23 = __ldg(m + 11);
+  return c;
+}
+
+// ---------------------------------------------------------------- projector
+template <int TX, int R, bool PSF, bool ATT>
+__global__ void __launch_bounds__(32 * kWarps) k_project_yg(const YgArgs a) {
+  constexpr int NJ = TX + 2 * R;
+  constexpr int K = 2 * R + 1;
+  __shared__ Tap s_tap[kWarps][NJ];
+  __shared__ float4 s_T[kWarps][TX][32];
+  __shared__ float4 s_P[kWarps][TX][32];
+  extern __shared__ float s_psf[];
+
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int ntile = (a.nx + TX - 1) / TX;
+  const int cam = blockIdx.x / ntile;
+  const int x0 = (blockIdx.x % ntile) * TX;
+  const int yb = lane * 4;
+  const bool yok = yb < a.cy;
+
+  if (PSF) {
+    for (int i = threadIdx.x; i < a.nz * 2 * K; i += blockDim.x) s_psf[i] = __ldg(a.psf + i);
+    __syncthreads();
+  }
+  const CamRows cr = cam_rows(a.geom[cam].fwd);
+  const int zper = (a.nz + kWarps - 1) / kWarps;
+  const int zbeg = warp * zper, zend = min(a.nz, zbeg + zper);
+
+  float4 T[TX], P[TX];
+#pragma unroll
+  for (int i = 0; i < TX; ++i) {
+    T[i] = make_float4(0.f, 0.f, 0.f, 0.f);
+    P[i] = make_float4(0.f, 0.f, 0.f, 0.f);
+  }
+
+  for (int z = zbeg; z < zend; ++z) {
+    for (int j = lane; j < NJ; j += 32) {
+      const int xp = x0 - R + j;
+      s_tap[warp][j] = make_tap(xp, z, cr.m00, cr.m02, cr.m03, cr.m20, cr.m22, cr.m23, a.nx, a.nz, a.cy,
+                                xp >= 0 && xp < a.nx);
+    }
+    __syncwarp();
+    auto emit = [&](int i, const float4& v) {
+      if (ATT) {
+        const float4 m = sample4(a.mu, s_tap[warp][i + R], yb, yok);
+        add4(T[i], m);
+        fma4(P[i], v, exp_neg4(T[i]));
+      } else {
+        add4(P[i], v);
+      }
+    };
+    if (PSF) {
+      const float* kr = s_psf + z * 2 * K;
+      auto sample = [&](int j) { return sample4(a.act, s_tap[warp][j], yb, yok); };
+      psf_tile<TX, R>(sample, emit, kr, kr + K, lane, a.ny);
+    } else {
+#pragma unroll
+      for (int i = 0; i < TX; ++i) emit(i, sample4(a.act, s_tap[warp][i], yb, yok));
+    }
+    __syncwarp();
+  }
+
+#pragma unroll
+  for (int i = 0; i < TX; ++i) {
+    s_T[warp][i][lane] = T[i];
+    s_P[warp][i][lane] = P[i];
+  }
+  __syncthreads();
+  for (int i = warp; i < TX; i += kWarps) {
+    const int x = x0 + i;
+    if (x >= a.nx || !yok) continue;
+    float4 Pt = make_float4(0.f, 0.f, 0.f, 0.f), Tt = make_float4(0.f, 0.f, 0.f, 0.f);
+    for (int s = 0; s < kWarps; ++s) {
+      if (ATT) {
+        fma4(Pt, exp_neg4(Tt), s_P[s][i][lane]);
+        add4(Tt, s_T[s][i][lane]);
+      } else {
+        add4(Pt, s_P[s][i][lane]);
+      }
+    }
+    if (a.truncate) {
+      Pt.x = fmaxf(Pt.x, 0.f);
+      Pt.y = fmaxf(Pt.y, 0.f);
+      Pt.z = fmaxf(Pt.z, 0.f);
+      Pt.w = fmaxf(Pt.w, 0.f);
+    }
+    *reinterpret_cast<float4*>(a.out + (static_cast<size_t>(cam) * a.nx + x) * a.cy + yb) = Pt;
+  }
+}
+
+// ------------------------------------------------ backprojector: slab sums
+// slab_T[cam][s][x][y] = sum over z in depth slab s of the rotated mu.
+__global__ void __launch_bounds__(32 * kWarps) k_mu_slabsum_yg(const YgArgs a) {
+  constexpr int C = kTileX;
+  __shared__ Tap s_tap[kWarps][C];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int nchunk = (a.nx + C - 1) / C;
+  const int cam = blockIdx.x / nchunk;
+  const int x0 = (blockIdx.x % nchunk) * C;
+  const int yb = lane * 4;
+  const bool yok = yb < a.cy;
+  const CamRows cr = cam_rows(a.geom[cam].fwd);
+  const int zper = (a.nz + kWarps - 1) / kWarps;
+  const int zbeg = warp * zper, zend = min(a.nz, zbeg + zper);
+  float4 S[C];
+#pragma unroll
+  for (int i = 0; i < C; ++i) S[i] = make_float4(0.f, 0.f, 0.f, 0.f);
+  for (int z = zbeg; z < zend; ++z) {
+    if (lane < C) {
+      const int xp = x0 + lane;
+      s_tap[warp][lane] = make_tap(xp, z, cr.m00, cr.m02, cr.m03, cr.m20, cr.m22, cr.m23, a.nx, a.nz, a.cy, xp < a.nx);
+    }
+    __syncwarp();
+#pragma unroll
+    for (int i = 0; i < C; ++i) add4(S[i], sample4(a.mu, s_tap[warp][i], yb, yok));
+    __syncwarp();
+  }
+  if (!yok) return;
+#pragma unroll
+  for (int i = 0; i < C; ++i) {
+    const int x = x0 + i;
+    if (x < a.nx)
+      *reinterpret_cast<float4*>(a.slab_T + ((static_cast<size_t>(cam) * kWarps + warp) * a.nx + x) * a.cy + yb) = S[i];
+  }
+}
+
+// ---------------------------------------- backprojector: spread + PSF
+// temp[g][z][x][y] = PSF_z( s(x', y) * exp(-T_z(x', y)) ) for camera c0+g,
+// T inclusive (emission-lib/_et_line_backproject_attenuated.cpp:24-34), PSF
+// as in the projector.  Warp w owns depth slab w; its carry-in is the sum of
+// the slab sums of the slabs before it.
+template <int TX, int R, bool PSF, bool ATT>
+__global__ void __launch_bounds__(32 * kWarps) k_spread_yg(const YgArgs a, int c0) {
+  constexpr int NJ = TX + 2 * R;
+  constexpr int K = 2 * R + 1;
+  __shared__ Tap s_tap[kWarps][NJ];
+  extern __shared__ float s_psf[];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int ntile = (a.nx + TX - 1) / TX;
+  const int g = blockIdx.x / ntile;
+  const int cam = c0 + g;
+  const int x0 = (blockIdx.x % ntile) * TX;
+  const int yb = lane * 4;
+  const bool yok = yb < a.cy;
+  if (PSF) {
+    for (int i = threadIdx.x; i < a.nz * 2 * K; i += blockDim.x) s_psf[i] = __ldg(a.psf + i);
+    __syncthreads();
+  }
+  const CamRows cr = cam_rows(a.geom[cam].fwd);
+  const int zper = (a.nz + kWarps - 1) / kWarps;
+  const int zbeg = warp * zper, zend = min(a.nz, zbeg + zper);
+  const size_t vol = static_cast<size_t>(a.nz) * a.nx * a.cy;
+  float* __restrict__ tmp = a.temp + vol * g;
+  const float* __restrict__ srow = a.sino + static_cast<size_t>(cam) * a.nx * a.cy;
+
+  float4 Tc[NJ];
+#pragma unroll
+  for (int j = 0; j < NJ; ++j) {
+    Tc[j] = make_float4(0.f, 0.f, 0.f, 0.f);
+    const int xp = x0 - R + j;
+    if (ATT && yok && xp >= 0 && xp < a.nx)
+      for (int s = 0; s < warp; ++s)
+        add4(Tc[j], ldg4(a.slab_T + ((static_cast<size_t>(cam) * kWarps + s) * a.nx + xp) * a.cy + yb));
+  }
+
+  for (int z = zbeg; z < zend; ++z) {
+    for (int j = lane; j < NJ; j += 32) {
+      const int xp = x0 - R + j;
+      s_tap[warp][j] = make_tap(xp, z, cr.m00, cr.m02, cr.m03, cr.m20, cr.m22, cr.m23, a.nx, a.nz, a.cy,
+                                xp >= 0 && xp < a.nx);
+    }
+    __syncwarp();
+    auto spread = [&](int j) {
+      const int xp = x0 - R + j;
+      float4 s = make_float4(0.f, 0.f, 0.f, 0.f);
+      if (xp >= 0 && xp < a.nx && yok) s = ldg4(srow + static_cast<size_t>(xp) * a.cy + yb);
+      if (ATT) {
+        add4(Tc[j], sample4(a.mu, s_tap[warp][j], yb, yok));
+        s = mul4(s, exp_neg4(Tc[j]));
+      }
+      return s;
+    };
+    auto emit = [&](int i, const float4& v) {
+      const int x = x0 + i;
+      if (x < a.nx && yok) *reinterpret_cast<float4*>(tmp + (static_cast<size_t>(z) * a.nx + x) * a.cy + yb) = v;
+    };
+    if (PSF) {
+      const float* kr = s_psf + z * 2 * K;
+      psf_tile<TX, R>(spread, emit, kr, kr + K, lane, a.ny);
+    } else {
+#pragma unroll
+      for (int i = 0; i < TX; ++i) emit(i, spread(i));
+    }
+    __syncwarp();
+  }
+}
+
+// ------------------------------------ backprojector: inverse-rotation gather
+// out[Z][X][y] (+)= sum_g bilinear(temp[g], B_g * (X, y, Z)) with B_g the
+// camera's inverse matrix (ZYX order, -theta), emission-lib/_et.cpp:474-497.
+__global__ void __launch_bounds__(32 * kWarps) k_gather_yg(const YgArgs a, int c0, int gcount, int first) {
+  constexpr int C = kGatherCols;
+  extern __shared__ Tap s_gtap[];  // [kWarps][C * group]
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int nchunk = (a.nx + C - 1) / C;
+  const int item = blockIdx.x * kWarps + warp;
+  if (item >= nchunk * a.nz) return;
+  const int Z = item / nchunk;
+  const int X0 = (item % nchunk) * C;
+  const int yb = lane * 4;
+  const bool yok = yb < a.cy;
+  Tap* tap = s_gtap + warp * C * a.group;
+  for (int e = lane; e < C * gcount; e += 32) {
+    const int g = e / C, X = X0 + e % C;
+    const CamRows cr = cam_rows(a.geom[c0 + g].bwd);
+    tap[e] = make_tap(X, Z, cr.m00, cr.m02, cr.m03, cr.m20, cr.m22, cr.m23, a.nx, a.nz, a.cy, X < a.nx);
+  }
+  __syncwarp();
+  if (!yok) return;
+  const size_t vol = static_cast<size_t>(a.nz) * a.nx * a.cy;
+  for (int i = 0; i < C; ++i) {
+    const int X = X0 + i;
+    if (X >= a.nx) break;
+    float4 acc = make_float4(0.f, 0.f, 0.f, 0.f);
+    for (int g = 0; g < gcount; ++g) add4(acc, sample4(a.temp + vol * g, tap[g * C + i], yb, true));
+    float4* dst = reinterpret_cast<float4*>(a.out + (static_cast<size_t>(Z) * a.nx + X) * a.cy + yb);
+    if (!first) add4(acc, *dst);
+    *dst = acc;
+  }
+}
+
+// --------------------------------------------------------------- layouts
+__global__ void k_to_col(const float* __restrict__ src, float* __restrict__ dst, int nx, int ny, int cy) {
+  __shared__ float tile[32][33];
+  const int p = blockIdx.z;
+  const int xb = blockIdx.x * 32, yb = blockIdx.y * 32;
+  const int tx = threadIdx.x;
+  for (int dy = threadIdx.y; dy < 32; dy += blockDim.y) {
+    const int y = yb + dy, x = xb + tx;
+    tile[dy][tx] = (y < ny && x < nx) ? src[(static_cast<size_t>(p) * ny + y) * nx + x] : 0.0f;
+  }
+  __syncthreads();
+  for (int dx = threadIdx.y; dx < 32; dx += blockDim.y) {
+    const int x = xb + dx, y = yb + tx;
+    if (x < nx && y < cy) dst[(static_cast<size_t>(p) * nx + x) * cy + y] = tile[tx][dx];
+  }
+}
+
+__global__ void k_from_col(const float* __restrict__ src, float* __restrict__ dst, int nx, int ny, int cy,
+                           int truncate) {
+  __shared__ float tile[32][33];
+  const int p = blockIdx.z;
+  const int xb = blockIdx.x * 32, yb = blockIdx.y * 32;
+  const int tx = threadIdx.x;
+  for (int dx = threadIdx.y; dx < 32; dx += blockDim.y) {
+    const int x = xb + dx, y = yb + tx;
+    tile[dx][tx] = (x < nx && y < ny) ? src[(static_cast<size_t>(p) * nx + x) * cy + y] : 0.0f;
+  }
+  __syncthreads();
+  for (int dy = threadIdx.y; dy < 32; dy += blockDim.y) {
+    const int y = yb + dy, x = xb + tx;
+    if (x < nx && y < ny) {
+      float v = tile[tx][dy];
+      if (truncate && v < 0.0f) v = 0.0f;
+      dst[(static_cast<size_t>(p) * ny + y) * nx + x] = v;
+    }
+  }
+}
+
+// ------------------------------------------------------------- dispatch
+template <int R>
+int launch_project_R(const YgArgs& a, cudaStream_t st) {
+  const int ntile = (a.nx + kTileX - 1) / kTileX;
+  const dim3 grid(a.ncam * ntile), block(32 * kWarps);
+  const bool psf = a.psf != nullptr;
+  const size_t smem = psf ? sizeof(float) * a.nz * 2 * (2 * R + 1) : 0;
+  if (psf) {
+    if (a.mu) {
+      auto k = k_project_yg<kTileX, R, true, true>;
+      cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
+      { NRGB_LAUNCH_SCOPE("k_project_yg", st); k<<<grid, block, smem, st>>>(a); }
+    } else {
+      auto k = k_project_yg<kTileX, R, true, false>;
+      cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
+      { NRGB_LAUNCH_SCOPE("k_project_yg", st); k<<<grid, block, smem, st>>>(a); }
+    }
+  } else {
+    if (a.mu)
+      { NRGB_LAUNCH_SCOPE("k_project_yg", st); k_project_yg<kTileX, 0, false, true><<<grid, block, 0, st>>>(a); }
+    else
+      { NRGB_LAUNCH_SCOPE("k_project_yg", st); k_project_yg<kTileX, 0, false, false><<<grid, block, 0, st>>>(a); }
+  }
+  return cudaGetLastError() == cudaSuccess ? kOk : kErrKernel;
+}
+
+template <int R>
+int launch_spread_R(const YgArgs& a, int c0, int gcount, cudaStream_t st) {
+  const int ntile = (a.nx + kTileX - 1) / kTileX;
+  const dim3 grid(gcount * ntile), block(32 * kWarps);
+  const bool psf = a.psf != nullptr;
+  const size_t smem = psf ? sizeof(float) * a.nz * 2 * (2 * R + 1) : 0;
+  if (psf) {
+    if (a.mu) {
+      auto k = k_spread_yg<kTileX, R, true, true>;
+      cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
+      { NRGB_LAUNCH_SCOPE("k_spread_yg", st); k<<<grid, block, smem, st>>>(a, c0); }
+    } else {
+      auto k = k_spread_yg<kTileX, R, true, false>;
+      cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
+      { NRGB_LAUNCH_SCOPE("k_spread_yg", st); k<<<grid, block, smem, st>>>(a, c0); }
+    }
+  } else {
+    if (a.mu)
+      { NRGB_LAUNCH_SCOPE("k_spread_yg", st); k_spread_yg<kTileX, 0, false, true><<<grid, block, 0, st>>>(a, c0); }
+    else
+      { NRGB_LAUNCH_SCOPE("k_spread_yg", st); k_spread_yg<kTileX, 0, false, false><<<grid, block, 0, st>>>(a, c0); }
+  }
+  return cudaGetLastError() == cudaSuccess ? kOk : kErrKernel;
+}
+
+int project_by_radius(int R, const YgArgs& a, cudaStream_t st) {
+  switch (R) {
+    case 0: return launch_project_R<0>(a, st);
+    case 1: return launch_project_R<1>(a, st);
+    case 2: return launch_project_R<2>(a, st);
+    case 3: return launch_project_R<3>(a, st);
+    case 4: return launch_project_R<4>(a, st);
+    case 5: return launch_project_R<5>(a, st);
+    case 6: return launch_project_R<6>(a, st);
+    case 7: return launch_project_R<7>(a, st);
+    default: return kErrParameters;
+  }
+}
+
+int spread_by_radius(int R, const YgArgs& a, int c0, int gcount, cudaStream_t st) {
+  switch (R) {
+    case 0: return launch_spread_R<0>(a, c0, gcount, st);
+    case 1: return launch_spread_R<1>(a, c0, gcount, st);
+    case 2: return launch_spread_R<2>(a, c0, gcount, st);
+    case 3: return launch_spread_R<3>(a, c0, gcount, st);
+    case 4: return launch_spread_R<4>(a, c0, gcount, st);
+    case 5: return launch_spread_R<5>(a, c0, gcount, st);
+    case 6: return launch_spread_R<6>(a, c0, gcount, st);
+    case 7: return launch_spread_R<7>(a, c0, gcount, st);
+    default: return kErrParameters;
+  }
+}
+
+}  // namespace
+
+bool yg_supported(int nx, int ny, int nz, int psf_k) {
+  const int cy = round_up(ny, 4);
+  if (nx < 1 || ny < 1 || nz < 1) return false;
+  if (cy > 128) return false;
+  if (psf_k != 0 && (psf_k % 2 != 1 || psf_k > 15)) return false;
+  // 32-bit element offsets inside one volume / scratch slot
+  if (static_cast<size_t>(nz) * nx * cy >= (1u << 31)) return false;
+  return true;
+}
+
+size_t yg_backproject_workspace(int nx, int ny, int nz, int ncam, int group) {
+  const size_t cy = round_up(ny, 4);
+  const size_t vol = static_cast<size_t>(nz) * nx * cy;
+  const size_t slabs = static_cast<size_t>(ncam) * kWarps * nx * cy;
+  return sizeof(float) * (slabs + vol * std::max(1, std::min(group, ncam)));
+}
+
+int yg_project(const YgArgs& a, cudaStream_t st) {
+  const int R = a.psf ? (a.psf_k - 1) / 2 : 0;
+  return project_by_radius(R, a, st);
+}
+
+int yg_backproject(const YgArgs& a_in, cudaStream_t st) {
+  YgArgs a = a_in;
+  const int R = a.psf ? (a.psf_k - 1) / 2 : 0;
+  const int group = std::max(1, std::min(a.group, a.ncam));
+  // work space: slab sums first, then the camera-group scratch
+  a.slab_T = a.work;
+  a.temp = a.work + static_cast<size_t>(a.ncam) * kWarps * a.nx * a.cy;
+  a.group = group;
+  if (a.mu) {
+    const int nchunk = (a.nx + kTileX - 1) / kTileX;
+    { NRGB_LAUNCH_SCOPE("k_mu_slabsum_yg", st); k_mu_slabsum_yg<<<a.ncam * nchunk, 32 * kWarps, 0, st>>>(a); }
+  }
+  const int nchunk = (a.nx + kGatherCols - 1) / kGatherCols;
+  const int gblocks = (nchunk * a.nz + kWarps - 1) / kWarps;
+  const size_t gsmem = sizeof(Tap) * kWarps * kGatherCols * group;
+  cudaFuncSetAttribute(k_gather_yg, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(gsmem));
+  for (int c0 = 0; c0 < a.ncam; c0 += group) {
+    const int gcount = std::min(group, a.ncam - c0);
+    int st_ = spread_by_radius(R, a, c0, gcount, st);
+    if (st_ != kOk) return st_;
+    { NRGB_LAUNCH_SCOPE("k_gather_yg", st); k_gather_yg<<<gblocks, 32 * kWarps, gsmem, st>>>(a, c0, gcount, c0 == 0 ? 1 : 0); }
+  }
+  return cudaGetLastError() == cudaSuccess ? kOk : kErrKernel;
+}
+
+int to_column(const float* src, float* dst, int nx, int ny, int cy, int planes, cudaStream_t st) {
+  const dim3 grid((nx + 31) / 32, (cy + 31) / 32, planes), block(32, 8);
+  { NRGB_LAUNCH_SCOPE("k_to_col", st); k_to_col<<<grid, block, 0, st>>>(src, dst, nx, ny, cy); }
+  return cudaGetLastError() == cudaSuccess ? kOk : kErrKernel;
+}
+
+int from_column(const float* src, float* dst, int nx, int ny, int cy, int planes, int truncate, cudaStream_t st) {
+  const dim3 grid((nx + 31) / 32, (ny + 31) / 32, planes), block(32, 8);
+  { NRGB_LAUNCH_SCOPE("k_from_col", st); k_from_col<<<grid, block, 0, st>>>(src, dst, nx, ny, cy, truncate); }
+  return cudaGetLastError() == cudaSuccess ? kOk : kErrKernel;
+}
+
+}  // namespace nrgb

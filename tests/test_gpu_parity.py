@@ -1,0 +1,153 @@
+"""Parity of the CUDA path, called through the C-ABI, with the reference's own
+outputs (golden fixtures from the compiled reference CPU path) and with the
+oracle's C restatement on fresh seeded inputs.
+
+Tolerance: relative L2 error <= 1e-5 per projection plane and per
+backprojected volume (float32 arithmetic in a different order and CUDA's
+__expf against the reference's expf)."""
+import numpy as np
+import pytest
+
+from conftest import rel_l2
+from niftyrec_gb300 import array_api as A
+from niftyrec_gb300 import synthetic as S
+from oracle.oracle import Restated
+
+pytestmark = pytest.mark.gpu
+
+RTOL = 1e-5
+FUSED, GENERAL = 1, 2
+
+
+def per_plane_rel(a, b):
+    return max(rel_l2(a[i], b[i]) for i in range(b.shape[0]))
+
+
+@pytest.fixture(scope="module")
+def o32():
+    return Restated("f32")
+
+
+def test_golden_ygantry_psf_att(golden):
+    g = golden("ygantry_psf_att_24")
+    s = A.project(g["act"], g["cameras"], g["psf"], g["mu"])
+    assert A.last_path() == FUSED
+    assert per_plane_rel(s, g["sino"]) < RTOL
+    b = A.backproject(g["counts"], g["cameras"], g["psf"], g["mu"])
+    assert A.last_path() == FUSED
+    assert rel_l2(b, g["bkpr"]) < RTOL
+
+
+def test_golden_plain(golden):
+    g = golden("ygantry_plain_20")
+    for cams in (g["cameras"], g["cameras3"]):
+        s = A.project(g["act"], cams)
+        assert A.last_path() == FUSED
+        assert per_plane_rel(s, g["sino"]) < RTOL
+        b = A.backproject(g["sino"], cams)
+        assert rel_l2(b, g["bkpr"]) < RTOL
+
+
+def test_golden_noncubic(golden):
+    g = golden("noncubic_24x20x16")
+    s = A.project(g["act"], g["cameras"], g["psf"], g["mu"])
+    assert A.last_path() == FUSED
+    assert per_plane_rel(s, g["sino"]) < RTOL
+    b = A.backproject(g["sino"], g["cameras"], g["psf"], g["mu"], nz=16)
+    assert A.last_path() == FUSED
+    assert rel_l2(b, g["bkpr"]) < RTOL
+
+
+def test_golden_general_cameras(golden):
+    g = golden("general_cams_18")
+    bg, bga = float(g["bg"]), float(g["bg_att"])
+    s = A.project(g["act"], g["cameras6"], None, g["mu"], bg, bga)
+    assert A.last_path() == GENERAL
+    assert per_plane_rel(s, g["sino_bg"]) < RTOL
+    b = A.backproject(g["sino_bg"], g["cameras6"], None, g["mu"], bg, bga)
+    assert rel_l2(b, g["bkpr_bg"]) < RTOL
+    s = A.project(g["act"], g["cameras3"], None, g["mu"])
+    assert A.last_path() == GENERAL
+    assert per_plane_rel(s, g["sino"]) < RTOL
+    b = A.backproject(g["sino"], g["cameras3"], None, g["mu"])
+    assert rel_l2(b, g["bkpr"]) < RTOL
+
+
+def test_golden_mlem_steps(golden):
+    g = golden("mlem_16")
+    x1 = A.mlem_step(np.ones_like(g["mu"]), g["counts"], g["cameras3"], g["mu"], g["psf"])
+    assert A.last_path() == FUSED
+    assert rel_l2(x1, g["x1"]) < RTOL
+    x2 = A.mlem_step(x1, g["counts"], g["cameras3"], g["mu"], g["psf"])
+    assert rel_l2(x2, g["x2"]) < 2 * RTOL
+
+
+def test_golden_rotate(golden):
+    g = golden("rotate_16x14x12")
+    r = A.rotate(g["vol"], [0.3, -0.7, 0.2], [7.5, 6.5, 5.5], 0.0, 0)
+    assert rel_l2(r, g["rot_xyz"]) < 1e-6
+    r = A.rotate(g["vol"], [-0.3, 0.7, -0.2], [7.5, 6.5, 5.5], 0.0, 5)
+    assert rel_l2(r, g["rot_zyx"]) < 1e-6
+
+
+# (nz, ny, nx): the PSF has nx planes (the reference's rule) and plane z serves
+# depth z, so nz <= nx.
+@pytest.mark.parametrize("shape,k,ncam", [((64, 64, 64), 11, 12), ((36, 52, 40), 7, 9), ((30, 18, 32), 15, 5),
+                                          ((48, 128, 48), 3, 4), ((30, 30, 30), 1, 3)])
+def test_oracle_fresh_inputs(o32, shape, k, ncam):
+    act = S.ellipsoid_phantom(shape, seed=sum(shape))
+    mu = S.mu_map(shape, seed=sum(shape))
+    psf = S.gaussian_psf(k, shape[2], 0.5, 0.05)
+    cams = S.cameras_about_y(ncam, 1.5)
+    s = A.project(act, cams, psf, mu)
+    assert A.last_path() == FUSED
+    so = o32.project(act, cams, psf, mu)
+    assert per_plane_rel(s, so) < RTOL
+    b = A.backproject(so, cams, psf, mu, nz=shape[0])
+    assert A.last_path() == FUSED
+    bo = o32.backproject(so, cams, psf, mu, nz=shape[0])
+    assert rel_l2(b, bo) < RTOL
+
+
+def test_general_path_large_ny(o32):
+    """ny > 128 runs on the general-orientation kernels."""
+    shape = (20, 132, 20)  # ny = 132 > 128
+    act = S.ellipsoid_phantom(shape, seed=4)
+    mu = S.mu_map(shape, seed=4)
+    psf = S.gaussian_psf(5, 20)
+    cams = S.cameras_about_y(3, 10.0)
+    s = A.project(act, cams, psf, mu)
+    assert A.last_path() == GENERAL
+    assert per_plane_rel(s, o32.project(act, cams, psf, mu)) < RTOL
+
+
+def test_gradient_attenuation_matches_restated_reference(o32):
+    shape = (24, 24, 24)
+    act = S.ellipsoid_phantom(shape, seed=21)
+    mu = S.mu_map(shape, seed=21)
+    psf = S.gaussian_psf(5, 24)
+    cams = S.cameras_about_y(6, 2.0)
+    y = S.poisson_counts(o32.project(act, cams, psf, mu), 50)
+    g = A.gradient_attenuation(y, act, mu, cams, psf)
+    go = o32.gradient_attenuation(y, act, mu, cams, psf)
+    assert rel_l2(g, go) < RTOL
+
+
+def test_known_answer_angle0_is_depth_sum():
+    vol = S.ellipsoid_phantom((32, 32, 32), seed=8)
+    s = A.project(vol, np.zeros(1, np.float32))
+    np.testing.assert_allclose(s[0], vol.sum(axis=0), rtol=1e-5, atol=1e-5)
+
+
+def test_parameter_errors():
+    act = np.ones((8, 8, 8), np.float32)
+    cams = np.zeros(2, np.float32)
+    with pytest.raises(Exception) as e:
+        A.project(act, cams, np.ones((8, 4, 4), np.float32))  # even PSF
+    assert getattr(e.value, "status", None) == 2
+    with pytest.raises(Exception) as e:
+        A.project(act, cams, np.ones((8, 3, 5), np.float32))  # non-square PSF
+    assert getattr(e.value, "status", None) == 2
+    with pytest.raises(Exception) as e:
+        A.backproject(np.ones((3, 8, 8), np.float32), cams)  # n_cameras mismatch
+    assert getattr(e.value, "status", None) == 2
