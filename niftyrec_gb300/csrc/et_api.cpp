@@ -64,7 +64,7 @@ int project_host(const Problem& pb, const float* act, const float* att, float* s
   if (act && (s = h2d(d_act, act, nvox, st)) != kOk) return finish(ds, s);
   if (att && (s = h2d(d_att, att, nvox, st)) != kOk) return finish(ds, s);
   g_last_path = (use_fused(pb) && act) ? 1 : 2;
-  s = project_device(pb, d_act, d_att, d_sino, w, ws, st);
+  s = project_device(pb, d_act, d_att, d_sino, w, ws, &ds.staging, st);
   if (s == kOk) s = d2h(sino, d_sino, nsino, st);
   return finish(ds, s);
 }
@@ -87,7 +87,7 @@ int backproject_host(const Problem& pb, const float* sino, const float* att, flo
   if ((s = h2d(d_sino, sino, nsino, st)) != kOk) return finish(ds, s);
   if (att && (s = h2d(d_att, att, nvox, st)) != kOk) return finish(ds, s);
   g_last_path = use_fused(pb) ? 1 : 2;
-  s = backproject_device(pb, d_sino, d_att, d_out, w, ws, st);
+  s = backproject_device(pb, d_sino, d_att, d_out, w, ws, &ds.staging, st);
   if (s == kOk) s = d2h(out, d_out, nvox, st);
   return finish(ds, s);
 }
@@ -112,7 +112,7 @@ int gradient_host(const Problem& pb, const float* sino, const float* act, const 
   if ((s = h2d(d_act, act, nvox, st)) != kOk) return finish(ds, s);
   if ((s = h2d(d_att, att, nvox, st)) != kOk) return finish(ds, s);
   g_last_path = 2;
-  s = gradient_device(pb, d_sino, d_act, d_att, d_out, w, ws, st);
+  s = gradient_device(pb, d_sino, d_act, d_att, d_out, w, ws, &ds.staging, st);
   if (s == kOk) s = d2h(out, d_out, nvox, st);
   return finish(ds, s);
 }
@@ -145,11 +145,11 @@ int osem_step_host(const Problem& pb, float* act, const float* ysub, const float
   Problem p1 = pb;
   p1.truncate = 1;
   g_last_path = use_fused(p1) ? 1 : 2;
-  if ((s = project_device(p1, d_act, d_att, d_p, w, ws, st)) != kOk) return finish(ds, s);
+  if ((s = project_device(p1, d_act, d_att, d_p, w, ws, &ds.staging, st)) != kOk) return finish(ds, s);
   if ((s = osem_ratio(d_y, d_p, nsino, eps, st)) != kOk) return finish(ds, s);
-  if ((s = backproject_device(p1, d_p, d_att, d_num, w, ws, st)) != kOk) return finish(ds, s);
+  if ((s = backproject_device(p1, d_p, d_att, d_num, w, ws, &ds.staging, st)) != kOk) return finish(ds, s);
   if ((s = fill(d_ones, nsino, 1.0f, st)) != kOk) return finish(ds, s);
-  if ((s = backproject_device(p1, d_ones, d_att, d_den, w, ws, st)) != kOk) return finish(ds, s);
+  if ((s = backproject_device(p1, d_ones, d_att, d_den, w, ws, &ds.staging, st)) != kOk) return finish(ds, s);
   if ((s = osem_update(d_act, d_num, d_den, nvox, eps, st)) != kOk) return finish(ds, s);
   s = d2h(act, d_act, nvox, st);
   return finish(ds, s);
@@ -595,7 +595,7 @@ int nrgb_project_device(const float* d_activity, const float* d_attenuation, con
   cudaStream_t st = static_cast<cudaStream_t>(stream);
   cudaStreamWaitEvent(st, ds.last_use, 0);
   g_last_path = (use_fused(pb) && d_activity) ? 1 : 2;
-  s = project_device(pb, d_activity, d_attenuation, d_sinogram, ds.arena, ds.arena_bytes, st);
+  s = project_device(pb, d_activity, d_attenuation, d_sinogram, ds.arena, ds.arena_bytes, &ds.staging, st);
   cudaEventRecord(ds.last_use, st);
   return s;
 }
@@ -621,7 +621,7 @@ int nrgb_backproject_device(const float* d_sinogram, const float* d_attenuation,
   cudaStream_t st = static_cast<cudaStream_t>(stream);
   cudaStreamWaitEvent(st, ds.last_use, 0);
   g_last_path = use_fused(pb) ? 1 : 2;
-  s = backproject_device(pb, d_sinogram, d_attenuation, d_out, ds.arena, ds.arena_bytes, st);
+  s = backproject_device(pb, d_sinogram, d_attenuation, d_out, ds.arena, ds.arena_bytes, &ds.staging, st);
   cudaEventRecord(ds.last_use, st);
   return s;
 }

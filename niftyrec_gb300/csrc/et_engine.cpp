@@ -51,19 +51,43 @@ size_t common_bytes(const Problem& pb) {
   return sizeof(CamGeom) * pb.cams.n + sizeof(float) * pb.psf_sep.size() + kSlack;
 }
 
-int upload_common(const Problem& pb, Carver& cv, CamGeom** d_geom, float** d_psf, cudaStream_t st) {
+// Uploads camera matrices and the separated PSF through the pinned staging
+// slot that is not in flight (waiting for its previous copy if needed).
+int upload_common(const Problem& pb, Carver& cv, CamGeom** d_geom, float** d_psf, Staging* stg, cudaStream_t st) {
   *d_geom = cv.take<CamGeom>(pb.cams.n);
   *d_psf = nullptr;
   if (!*d_geom) return kErrAllocGpu;
-  if (cudaMemcpyAsync(*d_geom, pb.geom.data(), sizeof(CamGeom) * pb.cams.n, cudaMemcpyHostToDevice, st) != cudaSuccess)
-    return kErrTransferGpu;
   if (pb.psf_k) {
     *d_psf = cv.take<float>(pb.psf_sep.size());
     if (!*d_psf) return kErrAllocGpu;
-    if (cudaMemcpyAsync(*d_psf, pb.psf_sep.data(), sizeof(float) * pb.psf_sep.size(), cudaMemcpyHostToDevice, st) !=
-        cudaSuccess)
-      return kErrTransferGpu;
   }
+  const size_t gbytes = sizeof(CamGeom) * pb.cams.n;
+  const size_t pbytes = sizeof(float) * pb.psf_sep.size();
+  const int slot = stg->slot;
+  stg->slot ^= 1;
+  if (stg->done[slot]) {
+    cudaEventSynchronize(stg->done[slot]);
+  } else if (cudaEventCreateWithFlags(&stg->done[slot], cudaEventDisableTiming) != cudaSuccess) {
+    return kErrUnspecified;
+  }
+  if (stg->bytes[slot] < gbytes + pbytes) {
+    if (stg->pinned[slot]) cudaFreeHost(stg->pinned[slot]);
+    stg->pinned[slot] = nullptr;
+    stg->bytes[slot] = 0;
+    const size_t want = std::max(gbytes + pbytes, static_cast<size_t>(1) << 20);
+    if (cudaMallocHost(&stg->pinned[slot], want) != cudaSuccess) {
+      cudaGetLastError();
+      return kErrAllocCpu;
+    }
+    stg->bytes[slot] = want;
+  }
+  char* h = stg->pinned[slot];
+  std::memcpy(h, pb.geom.data(), gbytes);
+  if (pbytes) std::memcpy(h + gbytes, pb.psf_sep.data(), pbytes);
+  if (cudaMemcpyAsync(*d_geom, h, gbytes, cudaMemcpyHostToDevice, st) != cudaSuccess) return kErrTransferGpu;
+  if (pbytes && cudaMemcpyAsync(*d_psf, h + gbytes, pbytes, cudaMemcpyHostToDevice, st) != cudaSuccess)
+    return kErrTransferGpu;
+  cudaEventRecord(stg->done[slot], st);
   return kOk;
 }
 
@@ -96,11 +120,11 @@ size_t backproject_workspace(const Problem& pb, bool has_att) {
 size_t gradient_workspace(const Problem& pb) { return common_bytes(pb) + sizeof(float) * vol_n(pb) * 3; }
 
 int project_device(const Problem& pb, const float* d_act, const float* d_att, float* d_sino, char* ws,
-                   size_t ws_bytes, cudaStream_t st) {
+                   size_t ws_bytes, Staging* stg, cudaStream_t st) {
   Carver cv(ws, ws_bytes);
   CamGeom* d_geom;
   float* d_psf;
-  int s = upload_common(pb, cv, &d_geom, &d_psf, st);
+  int s = upload_common(pb, cv, &d_geom, &d_psf, stg, st);
   if (s != kOk) return s;
   if (use_fused(pb) && d_act) {
     const int cy = round_up(pb.ny, 4);
@@ -148,11 +172,11 @@ int project_device(const Problem& pb, const float* d_act, const float* d_att, fl
 }
 
 int backproject_device(const Problem& pb, const float* d_sino, const float* d_att, float* d_out, char* ws,
-                       size_t ws_bytes, cudaStream_t st) {
+                       size_t ws_bytes, Staging* stg, cudaStream_t st) {
   Carver cv(ws, ws_bytes);
   CamGeom* d_geom;
   float* d_psf;
-  int s = upload_common(pb, cv, &d_geom, &d_psf, st);
+  int s = upload_common(pb, cv, &d_geom, &d_psf, stg, st);
   if (s != kOk) return s;
   if (use_fused(pb)) {
     const int cy = round_up(pb.ny, 4);
@@ -205,11 +229,11 @@ int backproject_device(const Problem& pb, const float* d_sino, const float* d_at
 }
 
 int gradient_device(const Problem& pb, const float* d_sino, const float* d_act, const float* d_att, float* d_out,
-                    char* ws, size_t ws_bytes, cudaStream_t st) {
+                    char* ws, size_t ws_bytes, Staging* stg, cudaStream_t st) {
   Carver cv(ws, ws_bytes);
   CamGeom* d_geom;
   float* d_psf;
-  int s = upload_common(pb, cv, &d_geom, &d_psf, st);
+  int s = upload_common(pb, cv, &d_geom, &d_psf, stg, st);
   if (s != kOk) return s;
   GeneralArgs g;
   g.nx = pb.nx;

@@ -35,8 +35,18 @@ int make_problem(int nx, int ny, int nz, const Cameras& cams, const float* psf, 
 // Whether the fused y-gantry kernels handle this problem.
 bool use_fused(const Problem& pb);
 
-// Per-device state: a library-owned stream, a growing device arena and an
-// event that orders successive users of the arena on any stream.
+// Pinned, double-buffered staging of the per-call parameters (camera
+// matrices, separated PSF): copies from pinned memory stay asynchronous,
+// where a copy from pageable memory would synchronise the stream.
+struct Staging {
+  char* pinned[2] = {nullptr, nullptr};
+  size_t bytes[2] = {0, 0};
+  cudaEvent_t done[2] = {nullptr, nullptr};
+  int slot = 0;
+};
+
+// Per-device state: a library-owned stream, a growing device arena, an event
+// that orders successive users of the arena on any stream, and the staging.
 struct DeviceState {
   std::mutex mu;
   int device = 0;
@@ -44,6 +54,7 @@ struct DeviceState {
   char* arena = nullptr;
   size_t arena_bytes = 0;
   cudaEvent_t last_use = nullptr;
+  Staging staging;
 };
 
 // Lock the current device's state (created on first use) for the caller.
@@ -77,10 +88,10 @@ size_t project_workspace(const Problem& pb, bool has_act, bool has_att);
 size_t backproject_workspace(const Problem& pb, bool has_att);
 size_t gradient_workspace(const Problem& pb);
 int project_device(const Problem& pb, const float* d_act, const float* d_att, float* d_sino, char* ws, size_t ws_bytes,
-                   cudaStream_t st);
+                   Staging* stg, cudaStream_t st);
 int backproject_device(const Problem& pb, const float* d_sino, const float* d_att, float* d_out, char* ws,
-                       size_t ws_bytes, cudaStream_t st);
+                       size_t ws_bytes, Staging* stg, cudaStream_t st);
 int gradient_device(const Problem& pb, const float* d_sino, const float* d_act, const float* d_att, float* d_out,
-                    char* ws, size_t ws_bytes, cudaStream_t st);
+                    char* ws, size_t ws_bytes, Staging* stg, cudaStream_t st);
 
 }  // namespace nrgb

@@ -3,24 +3,24 @@
 // (x, z) plane and y maps to itself.  Every detector row y then samples the
 // SAME bilinear footprint in the (x, z) plane, so the device layout puts y
 // fastest ("column layout" [z][x][cy]) and one warp handles whole columns:
-// lane l owns y = 4l..4l+3 (float4), the footprint of a (x, z) column is
-// computed once per warp and every gather is a coalesced 16-byte-per-lane
-// column load.
+// lane l owns y = 4l..4l+3 (float4), the footprint of an (x, z) column is
+// computed once and every gather is a coalesced 16-byte-per-lane column load.
 //
-// Projector  (emission-lib/_et.cpp:218-281): per camera, per depth plane z:
+// Projector (emission-lib/_et.cpp:218-281): per camera and depth plane z,
 //   rotate (bilinear gather of activity and mu), per-plane separable PSF
-//   (row pass along x in a register sliding window, column pass along y with
-//   warp shuffles), attenuated depth scan T += mu; p += v * exp(-T).  No
-//   rotated volume is written anywhere: one CTA owns (camera, x-tile), its
-//   warps own depth slabs and merge (T, p) in shared memory at the end:
-//   p = p0 + exp(-T0) p1 + exp(-T0-T1) p2 + ...
+//   (row pass along x in a register sliding window over a shared tile, column
+//   pass along y with warp shuffles), attenuated depth scan T += mu;
+//   p += v * exp(-T).  No rotated volume is written anywhere: a thread-block
+//   cluster owns (camera, 32-column x-tile), its CTAs own depth slabs and
+//   merge (T, p) through distributed shared memory.
 // Backprojector, reference mode (emission-lib/_et.cpp:415-499):
-//   (1) slab sums of the rotated mu (carry-in of each depth slab),
-//   (2) per camera group: spread s*exp(-T) + PSF in the rotated frame into a
-//       small L2-sized scratch, (3) inverse-rotation gather of the group into
-//       the accumulator.
+//   (1) per-slab transmission carries of the rotated mu, (2) per camera
+//   group: spread s*exp(-T) + PSF in the rotated frame into an L2-sized
+//   scratch, (3) inverse-rotation gather of the group into the accumulator.
 #include "et_kernels.h"
 #include "et_profile.h"
+
+#include <cooperative_groups.h>
 
 #include <algorithm>
 
@@ -28,9 +28,15 @@ namespace nrgb {
 
 namespace {
 
-constexpr int kWarps = 4;       // warps per CTA = depth slabs
-constexpr int kTileX = 8;       // output x columns per warp
-constexpr int kGatherCols = 8;  // accumulator columns per warp in the gather
+namespace cg = cooperative_groups;
+
+constexpr int kW = 8;             // warps per CTA of the tile engine
+constexpr int kTXW = 4;           // output columns per warp
+constexpr int kTXC = kW * kTXW;   // output columns per CTA
+constexpr int kSlabsP = 4;        // projector depth slabs = cluster size
+constexpr int kSlabsB = 8;        // backprojector depth slabs
+constexpr int kGatherWarps = 4;   // warps per CTA of the inverse-rotation gather
+constexpr int kGatherCols = 8;    // accumulator columns per warp in the gather
 constexpr unsigned kFull = 0xffffffffu;
 
 __device__ __forceinline__ float fm(float a, float b) { return __fmul_rn(a, b); }
@@ -146,35 +152,6 @@ __device__ __forceinline__ float4 yconv4(const float4& u, const float* kc, int l
   return o;
 }
 
-// Per-plane separable PSF over a tile of TX output columns from NJ = TX + 2R
-// sampled columns.  sample(j) produces the rotated value at x' = x0 - R + j
-// (zero outside the grid: the row pass pads with zeros), emit(i, v) receives
-// the convolved value of output column x0 + i.  Row pass: sliding window of
-// 2R+1 partial sums in registers; column pass: yconv4.
-template <int TX, int R, class SampleFn, class EmitFn>
-__device__ __forceinline__ void psf_tile(SampleFn sample, EmitFn emit, const float* kr, const float* kc, int lane,
-                                         int ny) {
-  constexpr int K = 2 * R + 1;
-  constexpr int NJ = TX + 2 * R;
-  float4 u[K];
-#pragma unroll
-  for (int q = 0; q < K; ++q) u[q] = make_float4(0.f, 0.f, 0.f, 0.f);
-#pragma unroll
-  for (int j = 0; j < NJ; ++j) {
-    const float4 r = sample(j);
-#pragma unroll
-    for (int d = 0; d < K; ++d) {
-      const int i = j - d;
-      if (i >= 0 && i < TX) axpy4(u[i % K], kr[2 * R - d], r);
-    }
-    const int i = j - 2 * R;
-    if (i >= 0 && i < TX) {
-      emit(i, mask_rows(yconv4<R>(u[i % K], kc, lane), 4 * lane, ny));
-      u[i % K] = make_float4(0.f, 0.f, 0.f, 0.f);
-    }
-  }
-}
-
 __device__ __forceinline__ float4 exp_neg4(const float4& t) {
   return make_float4(__expf(-t.x), __expf(-t.y), __expf(-t.z), __expf(-t.w));
 }
@@ -212,48 +189,116 @@ __device__ __forceinline__ CamRows cam_rows(const float* m) {
   return c;
 }
 
-// ---------------------------------------------------------------- projector
-template <int TX, int R, bool PSF, bool ATT>
-__global__ void __launch_bounds__(32 * kWarps) k_project_yg(const YgArgs a) {
-  constexpr int NJ = TX + 2 * R;
-  constexpr int K = 2 * R + 1;
-  __shared__ Tap s_tap[kWarps][NJ];
-  __shared__ float4 s_T[kWarps][TX][32];
-  __shared__ float4 s_P[kWarps][TX][32];
-  extern __shared__ float s_psf[];
+// ------------------------------------------------------------ tile engine
+// A CTA of kW warps owns kTXC = kW * kTXW consecutive output columns of one
+// camera and walks one depth slab.  At every depth step the NS = kTXC + 2R
+// sampled columns (outputs plus the PSF row halo) are produced once per CTA
+// -- column c by warp c % kW -- into a double-buffered shared tile; after one
+// barrier each warp runs the row pass (register sliding window over its
+// kTXW + 2R tile columns), the column pass and its consumer for its kTXW
+// outputs.  Writes of step z+1 go to the other buffer, so one barrier per
+// step suffices.
+template <int R>
+struct TileShape {
+  static constexpr int NS = kTXC + 2 * R;            // sampled columns per CTA
+  static constexpr int kOwn = (NS + kW - 1) / kW;    // sampled columns per warp (max)
+  static constexpr size_t kSbBytes = sizeof(float4) * 2 * NS * 32;
+  static constexpr size_t kTapBytes = sizeof(Tap) * 2 * NS;
+};
 
+template <int R>
+__host__ __device__ constexpr size_t tile_smem_bytes(int nz) {
+  return TileShape<R>::kSbBytes + TileShape<R>::kTapBytes + sizeof(float) * static_cast<size_t>(nz) * 2 * (2 * R + 1);
+}
+
+// Row pass from the shared tile: outputs i = 0..kTXW-1 of this warp use tile
+// columns base + i .. base + i + 2R (base = warp * kTXW).
+template <int R, class EmitFn>
+__device__ __forceinline__ void rowpass_from_tile(const float4* __restrict__ sbuf, int base, EmitFn emit,
+                                                  const float* kr, const float* kc, int lane, int ny) {
+  constexpr int K = 2 * R + 1;
+  constexpr int NJ = kTXW + 2 * R;
+  float4 u[K];
+#pragma unroll
+  for (int q = 0; q < K; ++q) u[q] = make_float4(0.f, 0.f, 0.f, 0.f);
+#pragma unroll
+  for (int j = 0; j < NJ; ++j) {
+    const float4 r = sbuf[(base + j) * 32 + lane];
+#pragma unroll
+    for (int d = 0; d < K; ++d) {
+      const int i = j - d;
+      if (i >= 0 && i < kTXW) axpy4(u[i % K], kr[2 * R - d], r);
+    }
+    const int i = j - 2 * R;
+    if (i >= 0 && i < kTXW) {
+      emit(i, mask_rows(yconv4<R>(u[i % K], kc, lane), 4 * lane, ny));
+      u[i % K] = make_float4(0.f, 0.f, 0.f, 0.f);
+    }
+  }
+}
+
+// ---------------------------------------------------------------- projector
+// Cluster of kSlabsP CTAs = the depth slabs of one (camera, x-tile).  Each
+// CTA accumulates (T, p) over its slab; the cluster merges through
+// distributed shared memory: p = p0 + exp(-T0) p1 + exp(-T0-T1) p2 + ...
+template <int R, bool PSF, bool ATT>
+__global__ void __cluster_dims__(kSlabsP, 1, 1) __launch_bounds__(32 * kW, 2) k_project_yg(const YgArgs a) {
+  using TS = TileShape<R>;
+  constexpr int NS = TS::NS;
+  constexpr int K = 2 * R + 1;
+  extern __shared__ __align__(16) unsigned char smem[];
+  float4* sb = reinterpret_cast<float4*>(smem);                       // [2][NS][32]
+  Tap* taps = reinterpret_cast<Tap*>(smem + TS::kSbBytes);             // [2][NS]
+  float* s_psf = reinterpret_cast<float*>(smem + TS::kSbBytes + TS::kTapBytes);  // [nz][2K]
+
+  cg::cluster_group cluster = cg::this_cluster();
+  const int slab = static_cast<int>(cluster.block_rank());
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int ntile = (a.nx + TX - 1) / TX;
-  const int cam = blockIdx.x / ntile;
-  const int x0 = (blockIdx.x % ntile) * TX;
+  const int ntile = (a.nx + kTXC - 1) / kTXC;
+  const int item = blockIdx.x / kSlabsP;
+  const int cam = item / ntile;
+  const int x0 = (item % ntile) * kTXC;
   const int yb = lane * 4;
   const bool yok = yb < a.cy;
 
   if (PSF) {
     for (int i = threadIdx.x; i < a.nz * 2 * K; i += blockDim.x) s_psf[i] = __ldg(a.psf + i);
-    __syncthreads();
   }
   const CamRows cr = cam_rows(a.geom[cam].fwd);
-  const int zper = (a.nz + kWarps - 1) / kWarps;
-  const int zbeg = warp * zper, zend = min(a.nz, zbeg + zper);
+  const int zper = (a.nz + kSlabsP - 1) / kSlabsP;
+  const int zbeg = slab * zper, zend = min(a.nz, zbeg + zper);
 
-  float4 T[TX], P[TX];
+  float4 T[kTXW], P[kTXW];
 #pragma unroll
-  for (int i = 0; i < TX; ++i) {
+  for (int i = 0; i < kTXW; ++i) {
     T[i] = make_float4(0.f, 0.f, 0.f, 0.f);
     P[i] = make_float4(0.f, 0.f, 0.f, 0.f);
   }
+  __syncthreads();
 
   for (int z = zbeg; z < zend; ++z) {
-    for (int j = lane; j < NJ; j += 32) {
-      const int xp = x0 - R + j;
-      s_tap[warp][j] = make_tap(xp, z, cr.m00, cr.m02, cr.m03, cr.m20, cr.m22, cr.m23, a.nx, a.nz, a.cy,
-                                xp >= 0 && xp < a.nx);
+    const int b = z & 1;
+    float4* sbuf = sb + b * NS * 32;
+    Tap* tb = taps + b * NS;
+    // footprints of the columns this warp samples (c = warp + kW * k)
+    if (lane < TS::kOwn) {
+      const int c = warp + kW * lane;
+      if (c < NS) {
+        const int xp = x0 - R + c;
+        tb[c] = make_tap(xp, z, cr.m00, cr.m02, cr.m03, cr.m20, cr.m22, cr.m23, a.nx, a.nz, a.cy,
+                         xp >= 0 && xp < a.nx);
+      }
     }
     __syncwarp();
+#pragma unroll
+    for (int k = 0; k < TS::kOwn; ++k) {
+      const int c = warp + kW * k;
+      if (c < NS) sbuf[c * 32 + lane] = sample4(a.act, tb[c], yb, yok);
+    }
+    __syncthreads();
     auto emit = [&](int i, const float4& v) {
       if (ATT) {
-        const float4 m = sample4(a.mu, s_tap[warp][i + R], yb, yok);
+        const float4 m = sample4(a.mu, tb[warp * kTXW + i + R], yb, yok);
         add4(T[i], m);
         fma4(P[i], v, exp_neg4(T[i]));
       } else {
@@ -262,31 +307,39 @@ __global__ void __launch_bounds__(32 * kWarps) k_project_yg(const YgArgs a) {
     };
     if (PSF) {
       const float* kr = s_psf + z * 2 * K;
-      auto sample = [&](int j) { return sample4(a.act, s_tap[warp][j], yb, yok); };
-      psf_tile<TX, R>(sample, emit, kr, kr + K, lane, a.ny);
+      rowpass_from_tile<R>(sbuf, warp * kTXW, emit, kr, kr + K, lane, a.ny);
     } else {
 #pragma unroll
-      for (int i = 0; i < TX; ++i) emit(i, sample4(a.act, s_tap[warp][i], yb, yok));
+      for (int i = 0; i < kTXW; ++i) emit(i, sbuf[(warp * kTXW + i) * 32 + lane]);
     }
-    __syncwarp();
   }
 
-#pragma unroll
-  for (int i = 0; i < TX; ++i) {
-    s_T[warp][i][lane] = T[i];
-    s_P[warp][i][lane] = P[i];
-  }
+  // cluster merge of the depth slabs (the shared tile is free after this barrier)
   __syncthreads();
-  for (int i = warp; i < TX; i += kWarps) {
-    const int x = x0 + i;
-    if (x >= a.nx || !yok) continue;
+  float4* sT = sb;                // [kTXC][32]
+  float4* sP = sb + kTXC * 32;    // [kTXC][32]
+#pragma unroll
+  for (int i = 0; i < kTXW; ++i) {
+    sT[(warp * kTXW + i) * 32 + lane] = T[i];
+    sP[(warp * kTXW + i) * 32 + lane] = P[i];
+  }
+  cluster.sync();
+  constexpr int kPerRank = kTXC / kSlabsP;  // outputs merged by each CTA of the cluster
+#pragma unroll
+  for (int i = 0; i < kTXW; ++i) {
+    const int o = warp * kTXW + i;
+    const int x = x0 + o;
+    if (o / kPerRank != slab || x >= a.nx || !yok) continue;
     float4 Pt = make_float4(0.f, 0.f, 0.f, 0.f), Tt = make_float4(0.f, 0.f, 0.f, 0.f);
-    for (int s = 0; s < kWarps; ++s) {
+    for (int s = 0; s < kSlabsP; ++s) {
+      const float4* rT = cluster.map_shared_rank(sT, s);
+      const float4* rP = cluster.map_shared_rank(sP, s);
+      const float4 ps = rP[o * 32 + lane];
       if (ATT) {
-        fma4(Pt, exp_neg4(Tt), s_P[s][i][lane]);
-        add4(Tt, s_T[s][i][lane]);
+        fma4(Pt, exp_neg4(Tt), ps);
+        add4(Tt, rT[o * 32 + lane]);
       } else {
-        add4(Pt, s_P[s][i][lane]);
+        add4(Pt, ps);
       }
     }
     if (a.truncate) {
@@ -297,13 +350,16 @@ __global__ void __launch_bounds__(32 * kWarps) k_project_yg(const YgArgs a) {
     }
     *reinterpret_cast<float4*>(a.out + (static_cast<size_t>(cam) * a.nx + x) * a.cy + yb) = Pt;
   }
+  cluster.sync();  // keep this CTA's shared memory alive until the others have read it
 }
 
-// ------------------------------------------------ backprojector: slab sums
-// slab_T[cam][s][x][y] = sum over z in depth slab s of the rotated mu.
-__global__ void __launch_bounds__(32 * kWarps) k_mu_slabsum_yg(const YgArgs a) {
-  constexpr int C = kTileX;
-  __shared__ Tap s_tap[kWarps][C];
+// ------------------------------------------------ backprojector: slab carry
+// carry[cam][s][x][y] = sum of the rotated mu over the depth slabs before s
+// (exclusive prefix): the transmission a depth slab starts from.
+__global__ void __launch_bounds__(32 * kSlabsB) k_mu_carry_yg(const YgArgs a) {
+  constexpr int C = 8;
+  __shared__ Tap s_tap[kSlabsB][C];
+  __shared__ float4 s_sum[kSlabsB][C][32];
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int nchunk = (a.nx + C - 1) / C;
   const int cam = blockIdx.x / nchunk;
@@ -311,7 +367,7 @@ __global__ void __launch_bounds__(32 * kWarps) k_mu_slabsum_yg(const YgArgs a) {
   const int yb = lane * 4;
   const bool yok = yb < a.cy;
   const CamRows cr = cam_rows(a.geom[cam].fwd);
-  const int zper = (a.nz + kWarps - 1) / kWarps;
+  const int zper = (a.nz + kSlabsB - 1) / kSlabsB;
   const int zbeg = warp * zper, zend = min(a.nz, zbeg + zper);
   float4 S[C];
 #pragma unroll
@@ -326,95 +382,116 @@ __global__ void __launch_bounds__(32 * kWarps) k_mu_slabsum_yg(const YgArgs a) {
     for (int i = 0; i < C; ++i) add4(S[i], sample4(a.mu, s_tap[warp][i], yb, yok));
     __syncwarp();
   }
+#pragma unroll
+  for (int i = 0; i < C; ++i) s_sum[warp][i][lane] = S[i];
+  __syncthreads();
   if (!yok) return;
 #pragma unroll
   for (int i = 0; i < C; ++i) {
     const int x = x0 + i;
-    if (x < a.nx)
-      *reinterpret_cast<float4*>(a.slab_T + ((static_cast<size_t>(cam) * kWarps + warp) * a.nx + x) * a.cy + yb) = S[i];
+    if (x >= a.nx) continue;
+    float4 pre = make_float4(0.f, 0.f, 0.f, 0.f);
+    for (int s = 0; s < warp; ++s) add4(pre, s_sum[s][i][lane]);
+    *reinterpret_cast<float4*>(a.slab_T + ((static_cast<size_t>(cam) * kSlabsB + warp) * a.nx + x) * a.cy + yb) = pre;
   }
 }
 
 // ---------------------------------------- backprojector: spread + PSF
 // temp[g][z][x][y] = PSF_z( s(x', y) * exp(-T_z(x', y)) ) for camera c0+g,
 // T inclusive (emission-lib/_et_line_backproject_attenuated.cpp:24-34), PSF
-// as in the projector.  Warp w owns depth slab w; its carry-in is the sum of
-// the slab sums of the slabs before it.
-template <int TX, int R, bool PSF, bool ATT>
-__global__ void __launch_bounds__(32 * kWarps) k_spread_yg(const YgArgs a, int c0) {
-  constexpr int NJ = TX + 2 * R;
+// as in the projector.  CTA = (camera, x-tile, depth slab); every sampled
+// column starts its transmission from the slab carry.
+template <int R, bool PSF, bool ATT>
+__global__ void __launch_bounds__(32 * kW, 2) k_spread_yg(const YgArgs a, int c0) {
+  using TS = TileShape<R>;
+  constexpr int NS = TS::NS;
   constexpr int K = 2 * R + 1;
-  __shared__ Tap s_tap[kWarps][NJ];
-  extern __shared__ float s_psf[];
+  extern __shared__ __align__(16) unsigned char smem[];
+  float4* sb = reinterpret_cast<float4*>(smem);
+  Tap* taps = reinterpret_cast<Tap*>(smem + TS::kSbBytes);
+  float* s_psf = reinterpret_cast<float*>(smem + TS::kSbBytes + TS::kTapBytes);
+
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int ntile = (a.nx + TX - 1) / TX;
-  const int g = blockIdx.x / ntile;
+  const int ntile = (a.nx + kTXC - 1) / kTXC;
+  const int slab = blockIdx.x % kSlabsB;
+  const int item = blockIdx.x / kSlabsB;
+  const int g = item / ntile;
   const int cam = c0 + g;
-  const int x0 = (blockIdx.x % ntile) * TX;
+  const int x0 = (item % ntile) * kTXC;
   const int yb = lane * 4;
   const bool yok = yb < a.cy;
+  const int zper = (a.nz + kSlabsB - 1) / kSlabsB;
+  const int zbeg = slab * zper, zend = min(a.nz, zbeg + zper);
+  if (zbeg >= zend) return;  // uniform over the CTA
   if (PSF) {
     for (int i = threadIdx.x; i < a.nz * 2 * K; i += blockDim.x) s_psf[i] = __ldg(a.psf + i);
-    __syncthreads();
   }
   const CamRows cr = cam_rows(a.geom[cam].fwd);
-  const int zper = (a.nz + kWarps - 1) / kWarps;
-  const int zbeg = warp * zper, zend = min(a.nz, zbeg + zper);
   const size_t vol = static_cast<size_t>(a.nz) * a.nx * a.cy;
   float* __restrict__ tmp = a.temp + vol * g;
   const float* __restrict__ srow = a.sino + static_cast<size_t>(cam) * a.nx * a.cy;
 
-  float4 Tc[NJ];
+  float4 Tc[TS::kOwn];
 #pragma unroll
-  for (int j = 0; j < NJ; ++j) {
-    Tc[j] = make_float4(0.f, 0.f, 0.f, 0.f);
-    const int xp = x0 - R + j;
-    if (ATT && yok && xp >= 0 && xp < a.nx)
-      for (int s = 0; s < warp; ++s)
-        add4(Tc[j], ldg4(a.slab_T + ((static_cast<size_t>(cam) * kWarps + s) * a.nx + xp) * a.cy + yb));
+  for (int k = 0; k < TS::kOwn; ++k) {
+    Tc[k] = make_float4(0.f, 0.f, 0.f, 0.f);
+    const int xp = x0 - R + warp + kW * k;
+    if (ATT && warp + kW * k < NS && xp >= 0 && xp < a.nx && yok)
+      Tc[k] = ldg4(a.slab_T + ((static_cast<size_t>(cam) * kSlabsB + slab) * a.nx + xp) * a.cy + yb);
   }
+  __syncthreads();
 
   for (int z = zbeg; z < zend; ++z) {
-    for (int j = lane; j < NJ; j += 32) {
-      const int xp = x0 - R + j;
-      s_tap[warp][j] = make_tap(xp, z, cr.m00, cr.m02, cr.m03, cr.m20, cr.m22, cr.m23, a.nx, a.nz, a.cy,
-                                xp >= 0 && xp < a.nx);
+    const int b = z & 1;
+    float4* sbuf = sb + b * NS * 32;
+    Tap* tb = taps + b * NS;
+    if (ATT && lane < TS::kOwn) {
+      const int c = warp + kW * lane;
+      if (c < NS) {
+        const int xp = x0 - R + c;
+        tb[c] = make_tap(xp, z, cr.m00, cr.m02, cr.m03, cr.m20, cr.m22, cr.m23, a.nx, a.nz, a.cy,
+                         xp >= 0 && xp < a.nx);
+      }
     }
     __syncwarp();
-    auto spread = [&](int j) {
-      const int xp = x0 - R + j;
-      float4 s = make_float4(0.f, 0.f, 0.f, 0.f);
-      if (xp >= 0 && xp < a.nx && yok) s = ldg4(srow + static_cast<size_t>(xp) * a.cy + yb);
-      if (ATT) {
-        add4(Tc[j], sample4(a.mu, s_tap[warp][j], yb, yok));
-        s = mul4(s, exp_neg4(Tc[j]));
+#pragma unroll
+    for (int k = 0; k < TS::kOwn; ++k) {
+      const int c = warp + kW * k;
+      if (c < NS) {
+        const int xp = x0 - R + c;
+        float4 s = make_float4(0.f, 0.f, 0.f, 0.f);
+        if (xp >= 0 && xp < a.nx && yok) s = ldg4(srow + static_cast<size_t>(xp) * a.cy + yb);
+        if (ATT) {
+          add4(Tc[k], sample4(a.mu, tb[c], yb, yok));
+          s = mul4(s, exp_neg4(Tc[k]));
+        }
+        sbuf[c * 32 + lane] = s;
       }
-      return s;
-    };
+    }
+    __syncthreads();
     auto emit = [&](int i, const float4& v) {
-      const int x = x0 + i;
+      const int x = x0 + warp * kTXW + i;
       if (x < a.nx && yok) *reinterpret_cast<float4*>(tmp + (static_cast<size_t>(z) * a.nx + x) * a.cy + yb) = v;
     };
     if (PSF) {
       const float* kr = s_psf + z * 2 * K;
-      psf_tile<TX, R>(spread, emit, kr, kr + K, lane, a.ny);
+      rowpass_from_tile<R>(sbuf, warp * kTXW, emit, kr, kr + K, lane, a.ny);
     } else {
 #pragma unroll
-      for (int i = 0; i < TX; ++i) emit(i, spread(i));
+      for (int i = 0; i < kTXW; ++i) emit(i, sbuf[(warp * kTXW + i) * 32 + lane]);
     }
-    __syncwarp();
   }
 }
 
 // ------------------------------------ backprojector: inverse-rotation gather
 // out[Z][X][y] (+)= sum_g bilinear(temp[g], B_g * (X, y, Z)) with B_g the
 // camera's inverse matrix (ZYX order, -theta), emission-lib/_et.cpp:474-497.
-__global__ void __launch_bounds__(32 * kWarps) k_gather_yg(const YgArgs a, int c0, int gcount, int first) {
+__global__ void __launch_bounds__(32 * kGatherWarps) k_gather_yg(const YgArgs a, int c0, int gcount, int first) {
   constexpr int C = kGatherCols;
-  extern __shared__ Tap s_gtap[];  // [kWarps][C * group]
+  extern __shared__ Tap s_gtap[];  // [kGatherWarps][C * group]
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int nchunk = (a.nx + C - 1) / C;
-  const int item = blockIdx.x * kWarps + warp;
+  const int item = blockIdx.x * kGatherWarps + warp;
   if (item >= nchunk * a.nz) return;
   const int Z = item / nchunk;
   const int X0 = (item % nchunk) * C;
@@ -481,50 +558,42 @@ __global__ void k_from_col(const float* __restrict__ src, float* __restrict__ ds
 // ------------------------------------------------------------- dispatch
 template <int R>
 int launch_project_R(const YgArgs& a, cudaStream_t st) {
-  const int ntile = (a.nx + kTileX - 1) / kTileX;
-  const dim3 grid(a.ncam * ntile), block(32 * kWarps);
+  const int ntile = (a.nx + kTXC - 1) / kTXC;
+  const dim3 grid(a.ncam * ntile * kSlabsP), block(32 * kW);
   const bool psf = a.psf != nullptr;
-  const size_t smem = psf ? sizeof(float) * a.nz * 2 * (2 * R + 1) : 0;
+  const size_t smem = tile_smem_bytes<R>(psf ? a.nz : 0);
+  auto go = [&](auto k) {
+    cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
+    NRGB_LAUNCH_SCOPE("k_project_yg", st);
+    k<<<grid, block, smem, st>>>(a);
+  };
   if (psf) {
-    if (a.mu) {
-      auto k = k_project_yg<kTileX, R, true, true>;
-      cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
-      { NRGB_LAUNCH_SCOPE("k_project_yg", st); k<<<grid, block, smem, st>>>(a); }
-    } else {
-      auto k = k_project_yg<kTileX, R, true, false>;
-      cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
-      { NRGB_LAUNCH_SCOPE("k_project_yg", st); k<<<grid, block, smem, st>>>(a); }
-    }
+    if (a.mu) go(k_project_yg<R, true, true>);
+    else go(k_project_yg<R, true, false>);
   } else {
-    if (a.mu)
-      { NRGB_LAUNCH_SCOPE("k_project_yg", st); k_project_yg<kTileX, 0, false, true><<<grid, block, 0, st>>>(a); }
-    else
-      { NRGB_LAUNCH_SCOPE("k_project_yg", st); k_project_yg<kTileX, 0, false, false><<<grid, block, 0, st>>>(a); }
+    if (a.mu) go(k_project_yg<0, false, true>);
+    else go(k_project_yg<0, false, false>);
   }
   return cudaGetLastError() == cudaSuccess ? kOk : kErrKernel;
 }
 
 template <int R>
 int launch_spread_R(const YgArgs& a, int c0, int gcount, cudaStream_t st) {
-  const int ntile = (a.nx + kTileX - 1) / kTileX;
-  const dim3 grid(gcount * ntile), block(32 * kWarps);
+  const int ntile = (a.nx + kTXC - 1) / kTXC;
+  const dim3 grid(gcount * ntile * kSlabsB), block(32 * kW);
   const bool psf = a.psf != nullptr;
-  const size_t smem = psf ? sizeof(float) * a.nz * 2 * (2 * R + 1) : 0;
+  const size_t smem = tile_smem_bytes<R>(psf ? a.nz : 0);
+  auto go = [&](auto k) {
+    cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
+    NRGB_LAUNCH_SCOPE("k_spread_yg", st);
+    k<<<grid, block, smem, st>>>(a, c0);
+  };
   if (psf) {
-    if (a.mu) {
-      auto k = k_spread_yg<kTileX, R, true, true>;
-      cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
-      { NRGB_LAUNCH_SCOPE("k_spread_yg", st); k<<<grid, block, smem, st>>>(a, c0); }
-    } else {
-      auto k = k_spread_yg<kTileX, R, true, false>;
-      cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
-      { NRGB_LAUNCH_SCOPE("k_spread_yg", st); k<<<grid, block, smem, st>>>(a, c0); }
-    }
+    if (a.mu) go(k_spread_yg<R, true, true>);
+    else go(k_spread_yg<R, true, false>);
   } else {
-    if (a.mu)
-      { NRGB_LAUNCH_SCOPE("k_spread_yg", st); k_spread_yg<kTileX, 0, false, true><<<grid, block, 0, st>>>(a, c0); }
-    else
-      { NRGB_LAUNCH_SCOPE("k_spread_yg", st); k_spread_yg<kTileX, 0, false, false><<<grid, block, 0, st>>>(a, c0); }
+    if (a.mu) go(k_spread_yg<0, false, true>);
+    else go(k_spread_yg<0, false, false>);
   }
   return cudaGetLastError() == cudaSuccess ? kOk : kErrKernel;
 }
@@ -564,6 +633,8 @@ bool yg_supported(int nx, int ny, int nz, int psf_k) {
   if (nx < 1 || ny < 1 || nz < 1) return false;
   if (cy > 128) return false;
   if (psf_k != 0 && (psf_k % 2 != 1 || psf_k > 15)) return false;
+  // the PSF table of one CTA lives in shared memory next to the tile
+  if (psf_k != 0 && tile_smem_bytes<7>(nz) > 110 * 1024) return false;
   // 32-bit element offsets inside one volume / scratch slot
   if (static_cast<size_t>(nz) * nx * cy >= (1u << 31)) return false;
   return true;
@@ -572,7 +643,7 @@ bool yg_supported(int nx, int ny, int nz, int psf_k) {
 size_t yg_backproject_workspace(int nx, int ny, int nz, int ncam, int group) {
   const size_t cy = round_up(ny, 4);
   const size_t vol = static_cast<size_t>(nz) * nx * cy;
-  const size_t slabs = static_cast<size_t>(ncam) * kWarps * nx * cy;
+  const size_t slabs = static_cast<size_t>(ncam) * kSlabsB * nx * cy;
   return sizeof(float) * (slabs + vol * std::max(1, std::min(group, ncam)));
 }
 
@@ -585,23 +656,24 @@ int yg_backproject(const YgArgs& a_in, cudaStream_t st) {
   YgArgs a = a_in;
   const int R = a.psf ? (a.psf_k - 1) / 2 : 0;
   const int group = std::max(1, std::min(a.group, a.ncam));
-  // work space: slab sums first, then the camera-group scratch
+  // work space: slab carries first, then the camera-group scratch
   a.slab_T = a.work;
-  a.temp = a.work + static_cast<size_t>(a.ncam) * kWarps * a.nx * a.cy;
+  a.temp = a.work + static_cast<size_t>(a.ncam) * kSlabsB * a.nx * a.cy;
   a.group = group;
   if (a.mu) {
-    const int nchunk = (a.nx + kTileX - 1) / kTileX;
-    { NRGB_LAUNCH_SCOPE("k_mu_slabsum_yg", st); k_mu_slabsum_yg<<<a.ncam * nchunk, 32 * kWarps, 0, st>>>(a); }
+    const int nchunk = (a.nx + 7) / 8;
+    NRGB_LAUNCH_SCOPE("k_mu_carry_yg", st);
+    k_mu_carry_yg<<<a.ncam * nchunk, 32 * kSlabsB, 0, st>>>(a);
   }
   const int nchunk = (a.nx + kGatherCols - 1) / kGatherCols;
-  const int gblocks = (nchunk * a.nz + kWarps - 1) / kWarps;
-  const size_t gsmem = sizeof(Tap) * kWarps * kGatherCols * group;
+  const int gblocks = (nchunk * a.nz + kGatherWarps - 1) / kGatherWarps;
+  const size_t gsmem = sizeof(Tap) * kGatherWarps * kGatherCols * group;
   cudaFuncSetAttribute(k_gather_yg, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(gsmem));
   for (int c0 = 0; c0 < a.ncam; c0 += group) {
     const int gcount = std::min(group, a.ncam - c0);
     int st_ = spread_by_radius(R, a, c0, gcount, st);
     if (st_ != kOk) return st_;
-    { NRGB_LAUNCH_SCOPE("k_gather_yg", st); k_gather_yg<<<gblocks, 32 * kWarps, gsmem, st>>>(a, c0, gcount, c0 == 0 ? 1 : 0); }
+    { NRGB_LAUNCH_SCOPE("k_gather_yg", st); k_gather_yg<<<gblocks, 32 * kGatherWarps, gsmem, st>>>(a, c0, gcount, c0 == 0 ? 1 : 0); }
   }
   return cudaGetLastError() == cudaSuccess ? kOk : kErrKernel;
 }

@@ -1,0 +1,78 @@
+"""Named workloads of the projector/backprojector, runnable from the command
+line (e.g. under a profiler) through the device-pointer C-ABI:
+
+    python -m niftyrec_gb300.workloads pair --n 128 --ncam 120 --psf 11 --reps 2
+    python -m niftyrec_gb300.workloads project --n 64 --ncam 60 --psf 0 --no-att
+
+Inputs are the seeded synthetic phantom, mu map and depth-dependent Gaussian
+PSF of niftyrec_gb300.synthetic; cameras rotate about the gantry axis in
+360/ncam degree steps.  Prints the mean device time per repetition.
+"""
+from __future__ import annotations
+
+import argparse
+import ctypes
+
+import numpy as np
+
+
+def main(argv=None):
+    import torch
+
+    from . import _lib
+    from . import synthetic as S
+
+    ap = argparse.ArgumentParser()
+    ap.add_argument("op", choices=["project", "backproject", "pair"])
+    ap.add_argument("--n", type=int, default=128)
+    ap.add_argument("--ncam", type=int, default=120)
+    ap.add_argument("--psf", type=int, default=11, help="PSF width (0: none)")
+    ap.add_argument("--no-att", action="store_true")
+    ap.add_argument("--reps", type=int, default=2)
+    a = ap.parse_args(argv)
+
+    L = _lib.load()
+    n = a.n
+    act = S.ellipsoid_phantom((n, n, n), seed=0)
+    mu = S.mu_map((n, n, n), seed=0)
+    psf = S.gaussian_psf(a.psf, n, 0.5, 0.02) if a.psf else None
+    cams = S.cameras_about_y(a.ncam)[1].copy()
+    dev = torch.device("cuda", 0)
+    t_act = torch.from_numpy(act).to(dev)
+    t_mu = None if a.no_att else torch.from_numpy(mu).to(dev)
+    t_sino = torch.zeros((a.ncam, n, n), dtype=torch.float32, device=dev)
+    t_bk = torch.zeros((n, n, n), dtype=torch.float32, device=dev)
+    vp = ctypes.c_void_p
+    size = (ctypes.c_int * 3)(n, n, n)
+    csize = (ctypes.c_int * 2)(a.ncam, 1)
+    psize = (ctypes.c_int * 3)(a.psf, a.psf, n) if a.psf else (ctypes.c_int * 3)(0, 0, 0)
+    psf_p = psf.ctypes.data_as(vp) if psf is not None else None
+    mu_p = vp(t_mu.data_ptr()) if t_mu is not None else None
+    stream = torch.cuda.current_stream(dev)
+
+    def run():
+        sp = vp(stream.cuda_stream)
+        if a.op in ("project", "pair"):
+            st = L.nrgb_project_device(vp(t_act.data_ptr()), mu_p, size, vp(t_sino.data_ptr()),
+                                       cams.ctypes.data_as(vp), csize, psf_p, psize, 0.0, 0.0, 1, sp)
+            assert st == 0, st
+        if a.op in ("backproject", "pair"):
+            st = L.nrgb_backproject_device(vp(t_sino.data_ptr()), mu_p, size, vp(t_bk.data_ptr()),
+                                           cams.ctypes.data_as(vp), csize, psf_p, psize, 0.0, 0.0, 1, 0, sp)
+            assert st == 0, st
+
+    run()
+    torch.cuda.synchronize()
+    ev = [torch.cuda.Event(enable_timing=True) for _ in range(2)]
+    ev[0].record(stream)
+    for _ in range(a.reps):
+        run()
+    ev[1].record(stream)
+    torch.cuda.synchronize()
+    print(f"{a.op} n={n} ncam={a.ncam} psf={a.psf} att={not a.no_att}: "
+          f"{ev[0].elapsed_time(ev[1]) / a.reps:.3f} ms per repetition")
+    return 0
+
+
+if __name__ == "__main__":
+    raise SystemExit(main())
