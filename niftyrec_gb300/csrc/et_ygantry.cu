@@ -23,6 +23,8 @@
 #include <cooperative_groups.h>
 
 #include <algorithm>
+#include <map>
+#include <mutex>
 
 namespace nrgb {
 
@@ -506,14 +508,23 @@ __global__ void __launch_bounds__(32 * kGatherWarps) k_gather_yg(const YgArgs a,
   __syncwarp();
   if (!yok) return;
   const size_t vol = static_cast<size_t>(a.nz) * a.nx * a.cy;
+  // camera outer, columns inner: neighbouring accumulator columns of one
+  // camera share footprint columns, which then hit in L1
+  float4 acc[C];
+#pragma unroll
+  for (int i = 0; i < C; ++i) acc[i] = make_float4(0.f, 0.f, 0.f, 0.f);
+  for (int g = 0; g < gcount; ++g) {
+    const float* src = a.temp + vol * g;
+#pragma unroll
+    for (int i = 0; i < C; ++i) add4(acc[i], sample4(src, tap[g * C + i], yb, true));
+  }
+#pragma unroll
   for (int i = 0; i < C; ++i) {
     const int X = X0 + i;
-    if (X >= a.nx) break;
-    float4 acc = make_float4(0.f, 0.f, 0.f, 0.f);
-    for (int g = 0; g < gcount; ++g) add4(acc, sample4(a.temp + vol * g, tap[g * C + i], yb, true));
+    if (X >= a.nx) continue;
     float4* dst = reinterpret_cast<float4*>(a.out + (static_cast<size_t>(Z) * a.nx + X) * a.cy + yb);
-    if (!first) add4(acc, *dst);
-    *dst = acc;
+    if (!first) add4(acc[i], *dst);
+    *dst = acc[i];
   }
 }
 
@@ -644,7 +655,8 @@ size_t yg_backproject_workspace(int nx, int ny, int nz, int ncam, int group) {
   const size_t cy = round_up(ny, 4);
   const size_t vol = static_cast<size_t>(nz) * nx * cy;
   const size_t slabs = static_cast<size_t>(ncam) * kSlabsB * nx * cy;
-  return sizeof(float) * (slabs + vol * std::max(1, std::min(group, ncam)));
+  // two scratch slots: the spread of group g+1 overlaps the gather of group g
+  return sizeof(float) * (slabs + 2 * vol * std::max(1, std::min(group, ncam)));
 }
 
 int yg_project(const YgArgs& a, cudaStream_t st) {
@@ -652,13 +664,47 @@ int yg_project(const YgArgs& a, cudaStream_t st) {
   return project_by_radius(R, a, st);
 }
 
+namespace {
+
+// Second stream and events of the backprojection pipeline, one set per device.
+struct Pipe {
+  cudaStream_t aux = nullptr;
+  cudaEvent_t fork = nullptr, join = nullptr, spread_done[2] = {nullptr, nullptr},
+              gather_done[2] = {nullptr, nullptr};
+};
+
+Pipe* pipe_for_current_device() {
+  static std::mutex mu;
+  static std::map<int, Pipe> pipes;
+  int dev = 0;
+  cudaGetDevice(&dev);
+  std::lock_guard<std::mutex> lk(mu);
+  Pipe& p = pipes[dev];
+  if (!p.aux) {
+    if (cudaStreamCreateWithFlags(&p.aux, cudaStreamNonBlocking) != cudaSuccess) return nullptr;
+    cudaEvent_t* evs[] = {&p.fork, &p.join, &p.spread_done[0], &p.spread_done[1], &p.gather_done[0],
+                          &p.gather_done[1]};
+    for (cudaEvent_t* e : evs)
+      if (cudaEventCreateWithFlags(e, cudaEventDisableTiming) != cudaSuccess) return nullptr;
+  }
+  return &p;
+}
+
+}  // namespace
+
+// Spreads run on the caller's stream, gathers on a second stream; group g
+// uses scratch slot g % 2, so the spread of group g+1 runs while the gather of
+// group g reads the other slot.
 int yg_backproject(const YgArgs& a_in, cudaStream_t st) {
   YgArgs a = a_in;
   const int R = a.psf ? (a.psf_k - 1) / 2 : 0;
   const int group = std::max(1, std::min(a.group, a.ncam));
-  // work space: slab carries first, then the camera-group scratch
+  Pipe* pp = pipe_for_current_device();
+  if (!pp) return kErrUnspecified;
+  // work space: slab carries first, then two camera-group scratch slots
+  const size_t vol = static_cast<size_t>(a.nz) * a.nx * a.cy;
   a.slab_T = a.work;
-  a.temp = a.work + static_cast<size_t>(a.ncam) * kSlabsB * a.nx * a.cy;
+  float* slot0 = a.work + static_cast<size_t>(a.ncam) * kSlabsB * a.nx * a.cy;
   a.group = group;
   if (a.mu) {
     const int nchunk = (a.nx + 7) / 8;
@@ -669,12 +715,26 @@ int yg_backproject(const YgArgs& a_in, cudaStream_t st) {
   const int gblocks = (nchunk * a.nz + kGatherWarps - 1) / kGatherWarps;
   const size_t gsmem = sizeof(Tap) * kGatherWarps * kGatherCols * group;
   cudaFuncSetAttribute(k_gather_yg, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(gsmem));
-  for (int c0 = 0; c0 < a.ncam; c0 += group) {
+  cudaEventRecord(pp->fork, st);
+  cudaStreamWaitEvent(pp->aux, pp->fork, 0);
+  int gi = 0;
+  for (int c0 = 0; c0 < a.ncam; c0 += group, ++gi) {
     const int gcount = std::min(group, a.ncam - c0);
+    const int slot = gi & 1;
+    a.temp = slot0 + vol * group * slot;
+    if (gi >= 2) cudaStreamWaitEvent(st, pp->gather_done[slot], 0);
     int st_ = spread_by_radius(R, a, c0, gcount, st);
     if (st_ != kOk) return st_;
-    { NRGB_LAUNCH_SCOPE("k_gather_yg", st); k_gather_yg<<<gblocks, 32 * kGatherWarps, gsmem, st>>>(a, c0, gcount, c0 == 0 ? 1 : 0); }
+    cudaEventRecord(pp->spread_done[slot], st);
+    cudaStreamWaitEvent(pp->aux, pp->spread_done[slot], 0);
+    {
+      NRGB_LAUNCH_SCOPE("k_gather_yg", pp->aux);
+      k_gather_yg<<<gblocks, 32 * kGatherWarps, gsmem, pp->aux>>>(a, c0, gcount, c0 == 0 ? 1 : 0);
+    }
+    cudaEventRecord(pp->gather_done[slot], pp->aux);
   }
+  cudaEventRecord(pp->join, pp->aux);
+  cudaStreamWaitEvent(st, pp->join, 0);
   return cudaGetLastError() == cudaSuccess ? kOk : kErrKernel;
 }
 
