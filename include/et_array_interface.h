@@ -135,6 +135,26 @@ int nrgb_backproject_device(const float *d_sinogram, const float *d_attenuation,
                             const float *cameras, const int *cameras_size, const float *psf, const int *psf_size,
                             float background, float background_attenuation, int truncate, int mode, void *stream);
 
+/* Backprojection that allocates nothing.  No counterpart in the reference.
+ * For callers that cannot call cudaMalloc: code inside a CUDA-graph capture,
+ * processes whose device memory is held by a framework's allocator, real-time
+ * loops that must not enter the driver's allocator.  Same arguments and result
+ * as nrgb_backproject_device with mode 0; every temporary lives in a fixed
+ * 64 MiB __device__ array of this library (held by every GPU that loads it,
+ * until the process exits), camera matrices and PSF are built in fixed host
+ * arrays.  Problems whose work space does not fit (e.g. 128^3 x 120 cameras)
+ * return status 10; use nrgb_backproject_device for those.  The first call on
+ * a device looks up the array's device address (cudaGetSymbolAddress): make
+ * that first call before any stream capture.  All calls share the array and
+ * it keeps the last call's contents; calls that overlap on the GPU (two
+ * streams, two threads) race on it, so serialise them.  No cudaMalloc,
+ * cudaFree or allocating library routine is called (with the launch profiler
+ * off, its default). */
+int nrgb_backproject_device_noalloc(const float *d_sinogram, const float *d_attenuation, const int *size,
+                                    float *d_out, const float *cameras, const int *cameras_size, const float *psf,
+                                    const int *psf_size, float background, float background_attenuation,
+                                    int truncate, void *stream);
+
 /* Diagnostics: 1 if the calling thread's last call ran the fused y-gantry
  * kernels, 2 if it ran the general-orientation kernels, 0 before any call. */
 int nrgb_last_path(void);

@@ -53,6 +53,7 @@ PROTOTYPES = {
     "et_array_mlem": (_I, [_P, _U, _U, _P, _I, _F, _F, _U, _I, _I, _P, _I, _P, _U, _U, _F, _F, _F, _I]),
     "nrgb_project_device": (_I, [_P, _P, _PI, _P, _P, _PI, _P, _PI, _F, _F, _I, _P]),
     "nrgb_backproject_device": (_I, [_P, _P, _PI, _P, _P, _PI, _P, _PI, _F, _F, _I, _I, _P]),
+    "nrgb_backproject_device_noalloc": (_I, [_P, _P, _PI, _P, _P, _PI, _P, _PI, _F, _F, _I, _P]),
     "nrgb_last_path": (_I, []),
     "nrgb_launch_count": (ctypes.c_longlong, []),
     "nrgb_profile_enable": (_I, [_I]),
@@ -82,7 +83,7 @@ def load() -> ctypes.CDLL:
 
 
 STATUS = {
-    0: "success", 1: "unspecified", 2: "parameters", 3: "kernel", 4: "allocgpu", 5: "alloccpu",
+    0: "success", 1: "unspecified", 2: "parameters", 3: "kernel", 4: "allocgpu", 5: "alloccpu", 10: "scratch",
     6: "transfergpu", 7: "nogpubuilt", 8: "nogpuinstalled", 9: "timeout",
 }
 

@@ -257,6 +257,8 @@ const char* kMessages[] = {
     "niftyrec: built without GPU support",
     "niftyrec: no GPU installed",
     "niftyrec: a bounded device-side wait expired",
+    "niftyrec: the problem needs more work space than the 64 MiB fixed scratch of "
+    "nrgb_backproject_device_noalloc (use nrgb_backproject_device, or fewer cameras / a smaller grid)",
 };
 
 }  // namespace
@@ -274,7 +276,7 @@ int echo(int* in, int* out) { *out = *in; return 0; }
 
 // emission-lib/_et_common.cpp:269-306
 char* niftyrec_error_msg(int status) {
-  if (status >= 0 && status <= kErrTimeout) return const_cast<char*>(kMessages[status]);
+  if (status >= 0 && status <= kErrScratchTooSmall) return const_cast<char*>(kMessages[status]);
   return const_cast<char*>("niftyrec: unknown status");
 }
 

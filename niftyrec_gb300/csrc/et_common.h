@@ -10,8 +10,9 @@
 namespace nrgb {
 
 // Status codes.  0..8 keep the values of the reference
-// (emission-lib/_et_common.h:40-48); 9 is new: a bounded device-side wait
-// expired and the kernel returned early.
+// (emission-lib/_et_common.h:40-48); 9 and 10 are new: 9 a bounded
+// device-side wait expired and the kernel returned early; 10 the problem does
+// not fit the fixed scratch of the no-allocation backprojection entry point.
 enum Status : int {
   kOk = 0,
   kErrUnspecified = 1,
@@ -23,6 +24,7 @@ enum Status : int {
   kErrNoGpuBuilt = 7,
   kErrNoGpuInstalled = 8,
   kErrTimeout = 9,
+  kErrScratchTooSmall = 10,
 };
 
 // Memory layouts of device volumes and sinograms.

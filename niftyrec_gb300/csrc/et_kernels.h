@@ -47,11 +47,16 @@ struct YgArgs {
   float* slab_T = nullptr;
   float* temp = nullptr;
   int group = 8;
+  // 1: spread on the caller's stream, gather on a second stream, two scratch
+  // slots; 0: both on the caller's stream with one slot (creates no stream
+  // or event).
+  int pipelined = 1;
 };
 // True when the fused kernels support this grid / PSF size.
 bool yg_supported(int nx, int ny, int nz, int psf_k);
-// Bytes of work space yg_backproject needs (slab sums + camera-group scratch).
-size_t yg_backproject_workspace(int nx, int ny, int nz, int ncam, int group);
+// Bytes of work space yg_backproject needs (slab carries + `slots` camera-group
+// scratch volumes of `group` cameras each).
+size_t yg_backproject_workspace(int nx, int ny, int nz, int ncam, int group, int slots = 2);
 int yg_project(const YgArgs& a, cudaStream_t st);
 int yg_backproject(const YgArgs& a, cudaStream_t st);
 

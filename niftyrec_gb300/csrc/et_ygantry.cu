@@ -651,12 +651,12 @@ bool yg_supported(int nx, int ny, int nz, int psf_k) {
   return true;
 }
 
-size_t yg_backproject_workspace(int nx, int ny, int nz, int ncam, int group) {
+size_t yg_backproject_workspace(int nx, int ny, int nz, int ncam, int group, int slots) {
   const size_t cy = round_up(ny, 4);
   const size_t vol = static_cast<size_t>(nz) * nx * cy;
   const size_t slabs = static_cast<size_t>(ncam) * kSlabsB * nx * cy;
-  // two scratch slots: the spread of group g+1 overlaps the gather of group g
-  return sizeof(float) * (slabs + 2 * vol * std::max(1, std::min(group, ncam)));
+  // with two slots the spread of group g+1 overlaps the gather of group g
+  return sizeof(float) * (slabs + static_cast<size_t>(slots) * vol * std::max(1, std::min(group, ncam)));
 }
 
 int yg_project(const YgArgs& a, cudaStream_t st) {
@@ -699,9 +699,7 @@ int yg_backproject(const YgArgs& a_in, cudaStream_t st) {
   YgArgs a = a_in;
   const int R = a.psf ? (a.psf_k - 1) / 2 : 0;
   const int group = std::max(1, std::min(a.group, a.ncam));
-  Pipe* pp = pipe_for_current_device();
-  if (!pp) return kErrUnspecified;
-  // work space: slab carries first, then two camera-group scratch slots
+  // work space: slab carries first, then the camera-group scratch slot(s)
   const size_t vol = static_cast<size_t>(a.nz) * a.nx * a.cy;
   a.slab_T = a.work;
   float* slot0 = a.work + static_cast<size_t>(a.ncam) * kSlabsB * a.nx * a.cy;
@@ -715,6 +713,19 @@ int yg_backproject(const YgArgs& a_in, cudaStream_t st) {
   const int gblocks = (nchunk * a.nz + kGatherWarps - 1) / kGatherWarps;
   const size_t gsmem = sizeof(Tap) * kGatherWarps * kGatherCols * group;
   cudaFuncSetAttribute(k_gather_yg, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(gsmem));
+  if (!a.pipelined) {
+    a.temp = slot0;
+    for (int c0 = 0; c0 < a.ncam; c0 += group) {
+      const int gcount = std::min(group, a.ncam - c0);
+      int st_ = spread_by_radius(R, a, c0, gcount, st);
+      if (st_ != kOk) return st_;
+      NRGB_LAUNCH_SCOPE("k_gather_yg", st);
+      k_gather_yg<<<gblocks, 32 * kGatherWarps, gsmem, st>>>(a, c0, gcount, c0 == 0 ? 1 : 0);
+    }
+    return cudaGetLastError() == cudaSuccess ? kOk : kErrKernel;
+  }
+  Pipe* pp = pipe_for_current_device();
+  if (!pp) return kErrUnspecified;
   cudaEventRecord(pp->fork, st);
   cudaStreamWaitEvent(pp->aux, pp->fork, 0);
   int gi = 0;
