@@ -159,6 +159,43 @@ int nrgb_backproject_device_noalloc(const float *d_sinogram, const float *d_atte
  * kernels, 2 if it ran the general-orientation kernels, 0 before any call. */
 int nrgb_last_path(void);
 
+/* Plans (no counterpart in the reference, whose OSEM step re-uploads and
+ * recomputes everything per call, emission-lib/_et_array_interface.cpp:972-1131).
+ * A plan holds device state for one grid, camera set, PSF and attenuation map:
+ * camera matrices, mu in column layout, the transmission carries of every
+ * camera and, after nrgb_plan_osem_prepare, the per-subset sensitivity images.
+ * nrgb_plan_create allocates (and computes) everything; the execute calls
+ * (project, backproject, osem_step) allocate nothing and copy nothing from the
+ * host, so a sequence of them can be captured in a CUDA graph.  layout: 0 =
+ * nifti order, 1 = column layout [planes][nx][round_up(ny,4)] with zero pads
+ * (fused plans only; convert with nrgb_layout_convert).  Sinograms of a subset
+ * hold its cameras in nrgb_plan_subset_cameras order.  The projection uses the
+ * centre rule of SPECT_project_parallelholes, the backprojection the rule of
+ * SPECT_backproject_parallelholes. */
+int nrgb_plan_create(void **out_plan, const int *size, const float *cameras, const int *cameras_size,
+                     const float *psf, const int *psf_size, const float *d_attenuation, float background,
+                     float background_attenuation, const int *subset_of_camera, int n_subsets, void *stream);
+int nrgb_plan_destroy(void *plan);
+int nrgb_plan_shape(void *plan, int *out);
+int nrgb_plan_subset_cameras(void *plan, int subset, int *idx_out);
+int nrgb_plan_project(void *plan, int subset, const float *d_activity, float *d_sinogram, int layout,
+                      int truncate, void *stream);
+int nrgb_plan_backproject(void *plan, int subset, const float *d_sinogram, float *d_out, int layout,
+                          int truncate, void *stream);
+int nrgb_plan_osem_prepare(void *plan, int layout, void *stream);
+int nrgb_plan_osem_step(void *plan, int subset, float *d_activity, const float *d_counts, float epsilon,
+                        void *stream);
+int nrgb_layout_convert(const float *src, float *dst, int nx, int ny, int planes, int direction, int truncate,
+                        void *stream);
+
+/* Tuning table of the fused backprojector (no counterpart in the reference):
+ * cameras per L2-resident scratch group for a problem shape (nx, ny, nz,
+ * n_cameras); an all-zero shape sets the default for shapes without an entry
+ * (8 initially).  niftyrec_gb300.autotune measures candidates and records the
+ * fastest. */
+int nrgb_set_backproject_group(int nx, int ny, int nz, int ncam, int group);
+int nrgb_get_backproject_group(int nx, int ny, int nz, int ncam);
+
 /* Instrumentation (no counterpart in the reference).  nrgb_launch_count: CUDA
  * kernels this library launched since it was loaded.  nrgb_profile_enable(1)
  * brackets every launch with CUDA events on its stream (0 turns it off; both

@@ -54,6 +54,17 @@ PROTOTYPES = {
     "nrgb_project_device": (_I, [_P, _P, _PI, _P, _P, _PI, _P, _PI, _F, _F, _I, _P]),
     "nrgb_backproject_device": (_I, [_P, _P, _PI, _P, _P, _PI, _P, _PI, _F, _F, _I, _I, _P]),
     "nrgb_backproject_device_noalloc": (_I, [_P, _P, _PI, _P, _P, _PI, _P, _PI, _F, _F, _I, _P]),
+    "nrgb_plan_create": (_I, [ctypes.POINTER(_P), _PI, _P, _PI, _P, _PI, _P, _F, _F, _PI, _I, _P]),
+    "nrgb_plan_destroy": (_I, [_P]),
+    "nrgb_plan_shape": (_I, [_P, _PI]),
+    "nrgb_plan_subset_cameras": (_I, [_P, _I, _PI]),
+    "nrgb_plan_project": (_I, [_P, _I, _P, _P, _I, _I, _P]),
+    "nrgb_plan_backproject": (_I, [_P, _I, _P, _P, _I, _I, _P]),
+    "nrgb_plan_osem_prepare": (_I, [_P, _I, _P]),
+    "nrgb_plan_osem_step": (_I, [_P, _I, _P, _P, _F, _P]),
+    "nrgb_layout_convert": (_I, [_P, _P, _I, _I, _I, _I, _I, _P]),
+    "nrgb_set_backproject_group": (_I, [_I, _I, _I, _I, _I]),
+    "nrgb_get_backproject_group": (_I, [_I, _I, _I, _I]),
     "nrgb_last_path": (_I, []),
     "nrgb_launch_count": (ctypes.c_longlong, []),
     "nrgb_profile_enable": (_I, [_I]),

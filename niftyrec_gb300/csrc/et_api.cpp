@@ -628,6 +628,16 @@ int nrgb_backproject_device(const float* d_sinogram, const float* d_attenuation,
   return s;
 }
 
+// Tuning table of the fused backprojector: cameras per scratch group for the
+// shape (nx, ny, nz, n_cameras); an all-zero shape sets the default.
+int nrgb_set_backproject_group(int nx, int ny, int nz, int ncam, int group) {
+  if (group < 1 || group > 64) return kErrParameters;
+  set_tuned_group(nx, ny, nz, ncam, group);
+  return kOk;
+}
+
+int nrgb_get_backproject_group(int nx, int ny, int nz, int ncam) { return tuned_group(nx, ny, nz, ncam); }
+
 // 1 when the last call of this thread ran the fused y-gantry kernels, 2 when
 // it ran the general-orientation path, 0 before any call.
 int nrgb_last_path(void) { return g_last_path; }

@@ -6,10 +6,33 @@
 #include <cstring>
 #include <map>
 #include <memory>
+#include <tuple>
 
 #include "et_kernels.h"
 
 namespace nrgb {
+
+// ------------------------------------------------------------ tuning table
+// Cameras per backprojection scratch group, keyed by (nx, ny, nz, ncam); a
+// key of zeros is the default.  Filled by nrgb_tune_set (the autotuner in
+// niftyrec_gb300/autotune.py measures candidates and records the fastest).
+namespace {
+std::mutex g_tune_mu;
+std::map<std::tuple<int, int, int, int>, int> g_tune_group;
+}  // namespace
+
+int tuned_group(int nx, int ny, int nz, int ncam) {
+  std::lock_guard<std::mutex> lk(g_tune_mu);
+  auto it = g_tune_group.find(std::make_tuple(nx, ny, nz, ncam));
+  if (it != g_tune_group.end()) return it->second;
+  it = g_tune_group.find(std::make_tuple(0, 0, 0, 0));
+  return it != g_tune_group.end() ? it->second : 8;
+}
+
+void set_tuned_group(int nx, int ny, int nz, int ncam, int group) {
+  std::lock_guard<std::mutex> lk(g_tune_mu);
+  g_tune_group[std::make_tuple(nx, ny, nz, ncam)] = group;
+}
 
 int make_problem(int nx, int ny, int nz, const Cameras& cams, const float* psf, const int* psf_size, float bg,
                  float bg_att, int truncate, Problem* out) {
@@ -24,6 +47,7 @@ int make_problem(int nx, int ny, int nz, const Cameras& cams, const float* psf, 
   pb.bg = bg;
   pb.bg_att = bg_att;
   pb.truncate = truncate;
+  pb.group = tuned_group(nx, ny, nz, cams.n);
   if (psf) {
     const int kx = psf_size[0], ky = psf_size[1], planes = psf_size[2];
     // The reference separates the PSF assuming kx == ky (emission-lib/_et.cpp:199-213

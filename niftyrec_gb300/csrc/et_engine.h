@@ -35,6 +35,11 @@ int make_problem(int nx, int ny, int nz, const Cameras& cams, const float* psf, 
 // Whether the fused y-gantry kernels handle this problem.
 bool use_fused(const Problem& pb);
 
+// Cameras per backprojection scratch group for a problem shape (tuning table;
+// all-zero shape = default for shapes without an entry).
+int tuned_group(int nx, int ny, int nz, int ncam);
+void set_tuned_group(int nx, int ny, int nz, int ncam, int group);
+
 // Pinned, double-buffered staging of the per-call parameters (camera
 // matrices, separated PSF): copies from pinned memory stay asynchronous,
 // where a copy from pageable memory would synchronise the stream.

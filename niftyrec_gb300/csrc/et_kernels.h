@@ -51,7 +51,16 @@ struct YgArgs {
   // slots; 0: both on the caller's stream with one slot (creates no stream
   // or event).
   int pipelined = 1;
+  // Non-null: transmission carries [ncam][slabs][nx][cy] computed beforehand
+  // (yg_mu_carry) for exactly these cameras; the backprojector then skips
+  // that pass and the work space holds only the scratch slot(s).
+  const float* carry = nullptr;
 };
+// Slab count of the backprojector's transmission carries.
+int yg_carry_slabs();
+// Transmission carries of the rotated mu for a.ncam cameras into out
+// ([ncam][slabs][nx][cy]).
+int yg_mu_carry(const YgArgs& a, float* out, cudaStream_t st);
 // True when the fused kernels support this grid / PSF size.
 bool yg_supported(int nx, int ny, int nz, int psf_k);
 // Bytes of work space yg_backproject needs (slab carries + `slots` camera-group

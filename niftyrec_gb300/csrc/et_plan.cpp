@@ -1,0 +1,441 @@
+// Plans: device state precomputed once for repeated projections and
+// backprojections with the same grid, cameras, PSF and attenuation map -- the
+// OSEM pattern of emission-lib/_et_array_interface.cpp:972-1131, where every
+// subset step projects and backprojects with unchanged mu.  A plan owns its
+// device memory (allocated at creation), keeps mu in column layout, holds the
+// transmission carries of every camera and the per-subset sensitivity images,
+// so its execute calls allocate nothing, copy nothing from the host and can be
+// captured in CUDA graphs.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cstring>
+#include <new>
+#include <vector>
+
+#include "et_array_interface.h"
+#include "et_engine.h"
+#include "et_kernels.h"
+
+namespace nrgb {
+namespace {
+
+struct Plan {
+  int device = 0;
+  Problem proj;  // cameras in subset order, centres of SPECT_project_parallelholes
+  Problem back;  // same cameras, centres of SPECT_backproject_parallelholes
+  bool fused = false;
+  bool has_att = false;
+  int cy = 0;
+  int n_subsets = 1;
+  std::vector<int> sub_begin;  // n_subsets + 1 offsets into the reordered cameras
+  std::vector<int> order;      // reordered position -> original camera index
+  char* mem = nullptr;
+  size_t bytes = 0;
+  CamGeom* geom_p = nullptr;
+  CamGeom* geom_b = nullptr;
+  float* psf = nullptr;
+  float* mu = nullptr;     // column layout (fused) or nifti copy (general)
+  float* carry = nullptr;  // [ncam][slabs][nx][cy] (fused with attenuation)
+  float* act_c = nullptr;  // column staging for nifti-layout calls (fused)
+  float* sino_c = nullptr;
+  float* out_c = nullptr;
+  float* work = nullptr;
+  size_t work_bytes = 0;
+  // OSEM state
+  int osem_layout = -1;
+  float* osem_p = nullptr;
+  float* osem_num = nullptr;
+  float* sens = nullptr;  // [n_subsets][volume]
+  size_t vol_elems = 0, plane_elems = 0;  // per layout of the OSEM buffers
+};
+
+size_t al(size_t b) { return (b + 255) / 256 * 256; }
+
+int check() { return cudaGetLastError() == cudaSuccess ? kOk : kErrKernel; }
+
+void range(const Plan& p, int subset, int* b, int* e) {
+  if (subset < 0) {
+    *b = 0;
+    *e = p.proj.cams.n;
+  } else {
+    *b = p.sub_begin[subset];
+    *e = p.sub_begin[subset + 1];
+  }
+}
+
+int plan_project(Plan& p, int subset, const float* d_act, float* d_sino, int layout, int truncate, cudaStream_t st) {
+  int b, e;
+  range(p, subset, &b, &e);
+  const int n = e - b;
+  if (n <= 0) return kOk;
+  const Problem& pb = p.proj;
+  if (p.fused) {
+    const float* act = d_act;
+    if (layout == kLayoutNifti) {
+      int s = to_column(d_act, p.act_c, pb.nx, pb.ny, p.cy, pb.nz, st);
+      if (s != kOk) return s;
+      act = p.act_c;
+    }
+    YgArgs a;
+    a.nx = pb.nx;
+    a.ny = pb.ny;
+    a.nz = pb.nz;
+    a.cy = p.cy;
+    a.ncam = n;
+    a.geom = p.geom_p + b;
+    a.act = act;
+    a.mu = p.has_att ? p.mu : nullptr;
+    a.out = layout == kLayoutNifti ? p.sino_c : d_sino;
+    a.psf = p.psf;
+    a.psf_k = pb.psf_k;
+    a.truncate = truncate;
+    int s = yg_project(a, st);
+    if (s != kOk) return s;
+    if (layout == kLayoutNifti) return from_column(p.sino_c, d_sino, pb.nx, pb.ny, p.cy, n, 0, st);
+    return kOk;
+  }
+  if (layout != kLayoutNifti) return kErrParameters;
+  GeneralArgs g;
+  g.nx = pb.nx;
+  g.ny = pb.ny;
+  g.nz = pb.nz;
+  g.ncam = n;
+  g.geom_host = pb.geom.data() + b;
+  g.act = d_act;
+  g.att = p.has_att ? p.mu : nullptr;
+  g.out = d_sino;
+  g.psf_sep = p.psf;
+  g.psf_k = pb.psf_k;
+  g.bg = pb.bg;
+  g.bg_att = pb.bg_att;
+  g.truncate = truncate;
+  const size_t nv = static_cast<size_t>(pb.nx) * pb.ny * pb.nz;
+  g.ws_act = p.work;
+  g.ws_att = p.work + nv;
+  g.ws_tmp = p.work + 2 * nv;
+  int s = general_project(g, st);
+  return s != kOk ? s : check();
+}
+
+int plan_backproject(Plan& p, int subset, const float* d_sino, float* d_out, int layout, int truncate,
+                     cudaStream_t st) {
+  int b, e;
+  range(p, subset, &b, &e);
+  const int n = e - b;
+  if (n <= 0) return kErrParameters;
+  const Problem& pb = p.back;
+  if (p.fused) {
+    const float* sino = d_sino;
+    if (layout == kLayoutNifti) {
+      int s = to_column(d_sino, p.sino_c, pb.nx, pb.ny, p.cy, n, st);
+      if (s != kOk) return s;
+      sino = p.sino_c;
+    }
+    float* out = layout == kLayoutNifti ? p.out_c : d_out;
+    YgArgs a;
+    a.nx = pb.nx;
+    a.ny = pb.ny;
+    a.nz = pb.nz;
+    a.cy = p.cy;
+    a.ncam = n;
+    a.geom = p.geom_b + b;
+    a.mu = p.has_att ? p.mu : nullptr;
+    a.sino = sino;
+    a.out = out;
+    a.psf = p.psf;
+    a.psf_k = pb.psf_k;
+    a.truncate = truncate;
+    a.group = pb.group;
+    a.work = p.work;
+    a.carry = p.carry ? p.carry + static_cast<size_t>(b) * yg_carry_slabs() * pb.nx * p.cy : nullptr;
+    int s = yg_backproject(a, st);
+    if (s != kOk) return s;
+    if (layout == kLayoutNifti) return from_column(p.out_c, d_out, pb.nx, pb.ny, p.cy, pb.nz, truncate, st);
+    if (truncate) launch_truncate(d_out, static_cast<size_t>(pb.nz) * pb.nx * p.cy, st);
+    return check();
+  }
+  if (layout != kLayoutNifti) return kErrParameters;
+  GeneralArgs g;
+  g.nx = pb.nx;
+  g.ny = pb.ny;
+  g.nz = pb.nz;
+  g.ncam = n;
+  g.geom_host = pb.geom.data() + b;
+  g.att = p.has_att ? p.mu : nullptr;
+  g.sino = d_sino;
+  g.out = d_out;
+  g.psf_sep = p.psf;
+  g.psf_k = pb.psf_k;
+  g.bg = pb.bg;
+  g.bg_att = pb.bg_att;
+  g.truncate = truncate;
+  const size_t nv = static_cast<size_t>(pb.nx) * pb.ny * pb.nz;
+  g.ws_act = p.work;
+  g.ws_att = p.work + nv;
+  g.ws_tmp = p.work + 2 * nv;
+  int s = general_backproject(g, st);
+  return s != kOk ? s : check();
+}
+
+}  // namespace
+}  // namespace nrgb
+
+using namespace nrgb;
+
+extern "C" {
+
+// Create a plan.  size = {nx, ny, nz}; cameras as for SPECT_project_parallelholes
+// ([n x 1|3|6], axis-major); psf host [k, k, >= nz] or null; d_attenuation a
+// device volume (nifti order) or null; subset_of_camera: per camera its subset
+// in [0, n_subsets), or null for a single subset.
+int nrgb_plan_create(void** out_plan, const int* size, const float* cameras, const int* cameras_size,
+                     const float* psf, const int* psf_size, const float* d_attenuation, float background,
+                     float background_attenuation, const int* subset_of_camera, int n_subsets, void* stream) {
+  if (!out_plan || !size || !cameras || !cameras_size || n_subsets < 1) return kErrParameters;
+  *out_plan = nullptr;
+  const int nx = size[0], ny = size[1], nz = size[2], ncam = cameras_size[0], ncols = cameras_size[1];
+  if (nx <= 0 || ny <= 0 || nz <= 0 || ncam <= 0) return kErrParameters;
+  // subset order: cameras of subset 0, then subset 1, ...; stable inside a subset
+  std::vector<int> order;
+  std::vector<int> begin(n_subsets + 1, 0);
+  for (int s = 0; s < n_subsets; ++s) {
+    begin[s] = static_cast<int>(order.size());
+    for (int c = 0; c < ncam; ++c) {
+      const int sc = subset_of_camera ? subset_of_camera[c] : 0;
+      if (sc < 0 || sc >= n_subsets) return kErrParameters;
+      if (sc == s) order.push_back(c);
+    }
+  }
+  begin[n_subsets] = ncam;
+  // reorder the camera table (all 6 columns' meaning kept)
+  Cameras cp, cb;
+  const int psz[3] = {size[0], size[1], size[2]};
+  const int bsz[3] = {size[0], size[1], size[0]};
+  int s = expand_cameras(cameras, ncam, ncols, psz, &cp);
+  if (s != kOk) return s;
+  s = expand_cameras(cameras, ncam, ncols, bsz, &cb);
+  if (s != kOk) return s;
+  auto reorder = [&](Cameras& c) {
+    Cameras r = c;
+    for (int i = 0; i < ncam; ++i)
+      for (int a = 0; a < 3; ++a) {
+        r.angles[a * ncam + i] = c.angles[a * ncam + order[i]];
+        r.centers[a * ncam + i] = c.centers[a * ncam + order[i]];
+      }
+    c = r;
+  };
+  reorder(cp);
+  reorder(cb);
+  Plan* p = new (std::nothrow) Plan();
+  if (!p) return kErrAllocCpu;
+  cudaGetDevice(&p->device);
+  s = make_problem(nx, ny, nz, cp, psf, psf_size, background, background_attenuation, 0, &p->proj);
+  if (s == kOk) s = make_problem(nx, ny, nz, cb, psf, psf_size, background, background_attenuation, 0, &p->back);
+  if (s != kOk) {
+    delete p;
+    return s;
+  }
+  p->fused = use_fused(p->proj);
+  p->has_att = d_attenuation != nullptr;
+  p->cy = round_up(ny, 4);
+  p->n_subsets = n_subsets;
+  p->sub_begin = begin;
+  p->order = order;
+  int max_sub = 0;
+  for (int i = 0; i < n_subsets; ++i) max_sub = std::max(max_sub, begin[i + 1] - begin[i]);
+
+  const size_t nv = static_cast<size_t>(nx) * ny * nz;
+  const size_t ncv = static_cast<size_t>(nx) * p->cy * nz;
+  const size_t nsc = static_cast<size_t>(nx) * p->cy * ncam;
+  size_t bytes = al(sizeof(CamGeom) * ncam) * 2 + al(sizeof(float) * p->proj.psf_sep.size());
+  if (p->fused) {
+    bytes += al(sizeof(float) * ncv) * (p->has_att ? 4 : 3) + al(sizeof(float) * nsc);
+    if (p->has_att) bytes += al(sizeof(float) * static_cast<size_t>(ncam) * yg_carry_slabs() * nx * p->cy);
+    p->work_bytes = yg_backproject_workspace(nx, ny, nz, ncam, p->back.group, 2) -
+                    sizeof(float) * static_cast<size_t>(ncam) * yg_carry_slabs() * nx * p->cy;
+  } else {
+    bytes += al(sizeof(float) * nv) * (p->has_att ? 1 : 0);
+    p->work_bytes = sizeof(float) * nv * 3;
+  }
+  bytes += al(p->work_bytes);
+  if (cudaMalloc(&p->mem, bytes) != cudaSuccess) {
+    cudaGetLastError();
+    delete p;
+    return kErrAllocGpu;
+  }
+  p->bytes = bytes;
+  Carver cv(p->mem, bytes);
+  p->geom_p = cv.take<CamGeom>(ncam);
+  p->geom_b = cv.take<CamGeom>(ncam);
+  if (!p->proj.psf_sep.empty()) p->psf = cv.take<float>(p->proj.psf_sep.size());
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  cudaMemcpyAsync(p->geom_p, p->proj.geom.data(), sizeof(CamGeom) * ncam, cudaMemcpyHostToDevice, st);
+  cudaMemcpyAsync(p->geom_b, p->back.geom.data(), sizeof(CamGeom) * ncam, cudaMemcpyHostToDevice, st);
+  if (p->psf)
+    cudaMemcpyAsync(p->psf, p->proj.psf_sep.data(), sizeof(float) * p->proj.psf_sep.size(), cudaMemcpyHostToDevice,
+                    st);
+  if (p->fused) {
+    if (p->has_att) p->mu = cv.take<float>(ncv);
+    p->act_c = cv.take<float>(ncv);
+    p->out_c = cv.take<float>(ncv);
+    p->sino_c = cv.take<float>(nsc);
+    if (p->has_att) {
+      p->carry = cv.take<float>(static_cast<size_t>(ncam) * yg_carry_slabs() * nx * p->cy);
+      s = to_column(d_attenuation, p->mu, nx, ny, p->cy, nz, st);
+      YgArgs a;
+      a.nx = nx;
+      a.ny = ny;
+      a.nz = nz;
+      a.cy = p->cy;
+      a.ncam = ncam;
+      a.geom = p->geom_b;
+      a.mu = p->mu;
+      if (s == kOk) s = yg_mu_carry(a, p->carry, st);
+    }
+  } else if (p->has_att) {
+    p->mu = cv.take<float>(nv);
+    cudaMemcpyAsync(p->mu, d_attenuation, sizeof(float) * nv, cudaMemcpyDeviceToDevice, st);
+  }
+  p->work = cv.take<float>((p->work_bytes + sizeof(float) - 1) / sizeof(float));
+  if (s == kOk) s = check();
+  if (s != kOk || !p->work) {
+    cudaFree(p->mem);
+    delete p;
+    return s != kOk ? s : kErrAllocGpu;
+  }
+  *out_plan = p;
+  return kOk;
+}
+
+int nrgb_plan_destroy(void* plan) {
+  Plan* p = static_cast<Plan*>(plan);
+  if (!p) return kErrParameters;
+  cudaDeviceSynchronize();
+  cudaFree(p->mem);
+  if (p->osem_p) cudaFree(p->osem_p);
+  delete p;
+  return kOk;
+}
+
+// out[0..6] = {nx, ny, nz, cy, n_cameras, n_subsets, fused}
+int nrgb_plan_shape(void* plan, int* out) {
+  Plan* p = static_cast<Plan*>(plan);
+  if (!p || !out) return kErrParameters;
+  out[0] = p->proj.nx;
+  out[1] = p->proj.ny;
+  out[2] = p->proj.nz;
+  out[3] = p->cy;
+  out[4] = p->proj.cams.n;
+  out[5] = p->n_subsets;
+  out[6] = p->fused ? 1 : 0;
+  return kOk;
+}
+
+// Original camera indexes of a subset, in the order its sinogram planes use;
+// returns the subset size (subset -1: all cameras).
+int nrgb_plan_subset_cameras(void* plan, int subset, int* idx_out) {
+  Plan* p = static_cast<Plan*>(plan);
+  if (!p || subset < -1 || subset >= p->n_subsets) return -1;
+  int b, e;
+  range(*p, subset, &b, &e);
+  if (idx_out)
+    for (int i = b; i < e; ++i) idx_out[i - b] = p->order[i];
+  return e - b;
+}
+
+// Project the cameras of `subset` (-1: all) of d_activity into d_sinogram
+// ([n_subset][ny][nx] nifti or [n_subset][nx][cy] column layout).
+int nrgb_plan_project(void* plan, int subset, const float* d_activity, float* d_sinogram, int layout, int truncate,
+                      void* stream) {
+  Plan* p = static_cast<Plan*>(plan);
+  if (!p || subset < -1 || subset >= p->n_subsets || !d_activity || !d_sinogram) return kErrParameters;
+  return plan_project(*p, subset, d_activity, d_sinogram, layout, truncate, static_cast<cudaStream_t>(stream));
+}
+
+// Backproject d_sinogram (cameras of `subset`) into d_out (reference semantics).
+int nrgb_plan_backproject(void* plan, int subset, const float* d_sinogram, float* d_out, int layout, int truncate,
+                          void* stream) {
+  Plan* p = static_cast<Plan*>(plan);
+  if (!p || subset < -1 || subset >= p->n_subsets || !d_sinogram || !d_out) return kErrParameters;
+  return plan_backproject(*p, subset, d_sinogram, d_out, layout, truncate, static_cast<cudaStream_t>(stream));
+}
+
+// Allocate the OSEM buffers for `layout` and compute every subset's
+// sensitivity image (backprojection of ones, truncated; floored at epsilon in
+// the update) once.  Call before capturing OSEM steps in a graph.
+int nrgb_plan_osem_prepare(void* plan, int layout, void* stream) {
+  Plan* p = static_cast<Plan*>(plan);
+  if (!p || (layout != kLayoutNifti && layout != kLayoutColumn)) return kErrParameters;
+  if (layout == kLayoutColumn && !p->fused) return kErrParameters;
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  const Problem& pb = p->proj;
+  const int ny_l = layout == kLayoutColumn ? p->cy : pb.ny;
+  p->vol_elems = static_cast<size_t>(pb.nx) * ny_l * pb.nz;
+  p->plane_elems = static_cast<size_t>(pb.nx) * ny_l;
+  int max_sub = 0;
+  for (int i = 0; i < p->n_subsets; ++i) max_sub = std::max(max_sub, p->sub_begin[i + 1] - p->sub_begin[i]);
+  if (p->osem_p) cudaFree(p->osem_p);
+  p->osem_p = nullptr;
+  const size_t n_p = al(sizeof(float) * p->plane_elems * max_sub);
+  const size_t n_v = al(sizeof(float) * p->vol_elems);
+  if (cudaMalloc(&p->osem_p, n_p + n_v * (1 + p->n_subsets)) != cudaSuccess) {
+    cudaGetLastError();
+    p->osem_p = nullptr;
+    return kErrAllocGpu;
+  }
+  char* base = reinterpret_cast<char*>(p->osem_p);
+  p->osem_num = reinterpret_cast<float*>(base + n_p);
+  p->sens = reinterpret_cast<float*>(base + n_p + n_v);
+  p->osem_layout = layout;
+  cudaMemsetAsync(p->osem_p, 0, n_p + n_v * (1 + p->n_subsets), st);
+  for (int sidx = 0; sidx < p->n_subsets; ++sidx) {
+    const int n = p->sub_begin[sidx + 1] - p->sub_begin[sidx];
+    if (n <= 0) continue;
+    int s = fill(p->osem_p, p->plane_elems * n, 1.0f, st);
+    if (s == kOk && layout == kLayoutColumn) {
+      // column pads stay zero
+      s = to_column(p->osem_p, p->sino_c, pb.nx, pb.ny, p->cy, n, st);
+      if (s == kOk) s = cudaMemcpyAsync(p->osem_p, p->sino_c, sizeof(float) * p->plane_elems * n,
+                                        cudaMemcpyDeviceToDevice, st) == cudaSuccess ? kOk : kErrTransferGpu;
+    }
+    if (s == kOk)
+      s = plan_backproject(*p, sidx, p->osem_p, p->sens + p->vol_elems * sidx, layout, 1, st);
+    if (s != kOk) return s;
+  }
+  return check();
+}
+
+// One OSEM step over `subset` with the reference's update
+// (emission-lib/_et_array_interface.cpp:1017-1044): p = A x (truncated),
+// r = y / max-rule(p), x *= (A^T r, truncated) / max(sensitivity, eps).
+// d_activity and d_counts use the layout given to nrgb_plan_osem_prepare;
+// d_counts holds the subset's planes in nrgb_plan_subset_cameras order.
+int nrgb_plan_osem_step(void* plan, int subset, float* d_activity, const float* d_counts, float epsilon,
+                        void* stream) {
+  Plan* p = static_cast<Plan*>(plan);
+  if (!p || subset < 0 || subset >= p->n_subsets || !d_activity || !d_counts || p->osem_layout < 0)
+    return kErrParameters;
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  const int n = p->sub_begin[subset + 1] - p->sub_begin[subset];
+  if (n <= 0) return kOk;
+  int s = plan_project(*p, subset, d_activity, p->osem_p, p->osem_layout, 1, st);
+  if (s == kOk) s = osem_ratio(d_counts, p->osem_p, p->plane_elems * n, epsilon, st);
+  if (s == kOk) s = plan_backproject(*p, subset, p->osem_p, p->osem_num, p->osem_layout, 1, st);
+  if (s == kOk) s = osem_update(d_activity, p->osem_num, p->sens + p->vol_elems * subset, p->vol_elems, epsilon, st);
+  return s;
+}
+
+// Layout conversion for callers of the column-layout entry points:
+// direction 0: nifti [planes][ny][nx] -> column [planes][nx][cy];
+// direction 1: column -> nifti (truncate: clamp negatives to 0).
+int nrgb_layout_convert(const float* src, float* dst, int nx, int ny, int planes, int direction, int truncate,
+                        void* stream) {
+  if (!src || !dst || nx <= 0 || ny <= 0 || planes <= 0) return kErrParameters;
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  const int cy = round_up(ny, 4);
+  return direction == 0 ? to_column(src, dst, nx, ny, cy, planes, st)
+                        : from_column(src, dst, nx, ny, cy, planes, truncate, st);
+}
+
+}  // extern "C"

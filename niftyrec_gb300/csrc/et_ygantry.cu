@@ -659,6 +659,17 @@ size_t yg_backproject_workspace(int nx, int ny, int nz, int ncam, int group, int
   return sizeof(float) * (slabs + static_cast<size_t>(slots) * vol * std::max(1, std::min(group, ncam)));
 }
 
+int yg_carry_slabs() { return kSlabsB; }
+
+int yg_mu_carry(const YgArgs& a_in, float* out, cudaStream_t st) {
+  YgArgs a = a_in;
+  a.slab_T = out;
+  const int nchunk = (a.nx + 7) / 8;
+  NRGB_LAUNCH_SCOPE("k_mu_carry_yg", st);
+  k_mu_carry_yg<<<a.ncam * nchunk, 32 * kSlabsB, 0, st>>>(a);
+  return cudaGetLastError() == cudaSuccess ? kOk : kErrKernel;
+}
+
 int yg_project(const YgArgs& a, cudaStream_t st) {
   const int R = a.psf ? (a.psf_k - 1) / 2 : 0;
   return project_by_radius(R, a, st);
@@ -699,16 +710,21 @@ int yg_backproject(const YgArgs& a_in, cudaStream_t st) {
   YgArgs a = a_in;
   const int R = a.psf ? (a.psf_k - 1) / 2 : 0;
   const int group = std::max(1, std::min(a.group, a.ncam));
-  // work space: slab carries first, then the camera-group scratch slot(s)
+  // work space: slab carries first (unless given), then the scratch slot(s)
   const size_t vol = static_cast<size_t>(a.nz) * a.nx * a.cy;
-  a.slab_T = a.work;
-  float* slot0 = a.work + static_cast<size_t>(a.ncam) * kSlabsB * a.nx * a.cy;
-  a.group = group;
-  if (a.mu) {
-    const int nchunk = (a.nx + 7) / 8;
-    NRGB_LAUNCH_SCOPE("k_mu_carry_yg", st);
-    k_mu_carry_yg<<<a.ncam * nchunk, 32 * kSlabsB, 0, st>>>(a);
+  float* slot0;
+  if (a.carry || !a.mu) {  // carries given, or not needed without attenuation
+    a.slab_T = const_cast<float*>(a.carry);
+    slot0 = a.work;
+  } else {
+    a.slab_T = a.work;
+    slot0 = a.work + static_cast<size_t>(a.ncam) * kSlabsB * a.nx * a.cy;
+    if (a.mu) {
+      int s = yg_mu_carry(a, a.slab_T, st);
+      if (s != kOk) return s;
+    }
   }
+  a.group = group;
   const int nchunk = (a.nx + kGatherCols - 1) / kGatherCols;
   const int gblocks = (nchunk * a.nz + kGatherWarps - 1) / kGatherWarps;
   const size_t gsmem = sizeof(Tap) * kGatherWarps * kGatherCols * group;
