@@ -314,6 +314,8 @@ def run_ours(args):
         "gpu_launches": int(launches),
         "clocks": clocks,
     }
+    if not args.no_osem:
+        out["osem"] = osem_compare(act, mu, psf, cams, dev)
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         out["cpu_baseline"] = cpu_baseline(act, mu, psf, cams, args.cpu_angles)
     if rank == 0:
@@ -322,6 +324,55 @@ def run_ours(args):
         import torch.distributed as dist
 
         dist.destroy_process_group()
+
+
+# ------------------------------------------------------------------- OSEM
+def osem_compare(act, mu, psf, cams, dev, n_subsets=8, iterations=3):
+    """One OSEM iteration (all subsets) at 128^3 x 120 angles: the plain
+    per-call drop-in (et_array_osem_step_subset with host buffers, one call per
+    subset) against a plan with cached carries/sensitivities whose iteration is
+    captured once as a CUDA graph and replayed."""
+    import torch
+
+    from niftyrec_gb300 import array_api as A
+    from niftyrec_gb300 import synthetic as S
+    from niftyrec_gb300.plan import Plan
+
+    counts = S.poisson_counts(A.project(act, cams, psf, mu), 50, seed=1)
+    x = np.ones_like(act)
+    cams3 = np.zeros((3, NCAM), np.float32)
+    cams3[1] = cams
+    subsets = [list(range(s, NCAM, n_subsets)) for s in range(n_subsets)]
+    x = A.osem_step_subset(x, counts, cams3, subsets[0], mu, psf)  # warm-up
+    t0 = time.perf_counter()
+    for _ in range(iterations):
+        for idx in subsets:
+            x = A.osem_step_subset(x, counts, cams3, idx, mu, psf)
+    per_call = (time.perf_counter() - t0) / iterations * 1e3
+
+    plan = Plan((N, N, N), cams, psf, torch.from_numpy(mu).to(dev), subsets=n_subsets)
+    y = torch.from_numpy(counts).to(dev)
+    plan.osem(y, iterations=1, layout="column", graph=True)  # prepare + capture
+    g, xc, ys = plan._graph
+    stream = torch.cuda.current_stream(dev)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize(dev)
+    e0.record(stream)
+    for _ in range(iterations):
+        g.replay()
+    e1.record(stream)
+    torch.cuda.synchronize(dev)
+    graph_ms = e0.elapsed_time(e1) / iterations
+    e0.record(stream)
+    for _ in range(iterations):
+        for s in range(n_subsets):
+            plan.osem_step(xc, ys[s], s)
+    e1.record(stream)
+    torch.cuda.synchronize(dev)
+    eager_ms = e0.elapsed_time(e1) / iterations
+    return {"workload": f"OSEM iteration, 128^3, {NCAM} angles, {n_subsets} interleaved subsets, PSF 11x11, mu",
+            "per_call_iteration_ms": round(per_call, 3), "plan_eager_iteration_ms": round(eager_ms, 3),
+            "plan_graph_iteration_ms": round(graph_ms, 3), "speedup_graph_vs_per_call": round(per_call / graph_ms, 2)}
 
 
 # ----------------------------------------------------------- CPU baselines
@@ -412,6 +463,7 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--cpu-angles", type=int, default=24)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-osem", action="store_true")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
