@@ -127,13 +127,28 @@ int et_array_osem_step_subset(float *activity_data, int size_x, int size_y, floa
  * cameras and PSF are host arrays; work is enqueued on `stream` (a
  * cudaStream_t) and the call returns without waiting.  size = {nx, ny, nz}.
  * For the backprojection the centre of rotation is (size0, size1, size0),
- * as in SPECT_backproject_parallelholes; mode 0 is the reference backprojector. */
+ * as in SPECT_backproject_parallelholes; mode 0 is the reference backprojector
+ * (inverse-rotation gather), mode 1 the exact transpose of the projector for
+ * the given mu (transposed PSF and bilinear weights; backgrounds do not enter:
+ * they are constants of the projector), used for gradients. */
 int nrgb_project_device(const float *d_activity, const float *d_attenuation, const int *size, float *d_sinogram,
                         const float *cameras, const int *cameras_size, const float *psf, const int *psf_size,
                         float background, float background_attenuation, int truncate, void *stream);
 int nrgb_backproject_device(const float *d_sinogram, const float *d_attenuation, const int *size, float *d_out,
                             const float *cameras, const int *cameras_size, const float *psf, const int *psf_size,
                             float background, float background_attenuation, int truncate, int mode, void *stream);
+
+/* Exact gradient with respect to mu of sum(g * P(activity, mu)), P the
+ * projector without truncation, g = d_grad_sinogram (device, nifti order):
+ * dP/dmu_z' = -(sum_{z >= z'} PSF(rotated activity)_z exp(-T_z) + bg exp(-T_N))
+ * in the rotated frame, mapped back by the transposed trilinear weights.  No
+ * counterpart in the reference: its et_array_gradient_attenuation
+ * (emission-lib/_et.cpp:1679-1924) ignores the PSF coupling, the sign and the
+ * background; that function is kept above with the reference's semantics. */
+int nrgb_attenuation_grad_device(const float *d_grad_sinogram, const float *d_activity, const float *d_attenuation,
+                                 const int *size, float *d_out, const float *cameras, const int *cameras_size,
+                                 const float *psf, const int *psf_size, float background,
+                                 float background_attenuation, void *stream);
 
 /* Backprojection that allocates nothing.  No counterpart in the reference.
  * For callers that cannot call cudaMalloc: code inside a CUDA-graph capture,

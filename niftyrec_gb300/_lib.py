@@ -54,6 +54,7 @@ PROTOTYPES = {
     "nrgb_project_device": (_I, [_P, _P, _PI, _P, _P, _PI, _P, _PI, _F, _F, _I, _P]),
     "nrgb_backproject_device": (_I, [_P, _P, _PI, _P, _P, _PI, _P, _PI, _F, _F, _I, _I, _P]),
     "nrgb_backproject_device_noalloc": (_I, [_P, _P, _PI, _P, _P, _PI, _P, _PI, _F, _F, _I, _P]),
+    "nrgb_attenuation_grad_device": (_I, [_P, _P, _P, _PI, _P, _P, _PI, _P, _PI, _F, _F, _P]),
     "nrgb_plan_create": (_I, [ctypes.POINTER(_P), _PI, _P, _PI, _P, _PI, _P, _F, _F, _PI, _I, _P]),
     "nrgb_plan_destroy": (_I, [_P]),
     "nrgb_plan_shape": (_I, [_P, _PI]),

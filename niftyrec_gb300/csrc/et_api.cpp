@@ -602,11 +602,13 @@ int nrgb_project_device(const float* d_activity, const float* d_attenuation, con
   return s;
 }
 
-// mode: 0 = the reference's inverse-rotation backprojector.
+// mode: 0 = the reference's inverse-rotation backprojector; 1 = the exact
+// transpose of the projector (for gradients).
 int nrgb_backproject_device(const float* d_sinogram, const float* d_attenuation, const int* size, float* d_out,
                             const float* cameras, const int* cameras_size, const float* psf, const int* psf_size,
                             float background, float background_attenuation, int truncate, int mode, void* stream) {
-  if (!size || !cameras || !cameras_size || !d_sinogram || !d_out || mode != kBackReference) return kErrParameters;
+  if (!size || !cameras || !cameras_size || !d_sinogram || !d_out || (mode != kBackReference && mode != kBackAdjoint))
+    return kErrParameters;
   Cameras cc;
   const int csz[3] = {size[0], size[1], size[0]};
   int s = expand_cameras(cameras, cameras_size[0], cameras_size[1], csz, &cc);
@@ -624,6 +626,33 @@ int nrgb_backproject_device(const float* d_sinogram, const float* d_attenuation,
   cudaStreamWaitEvent(st, ds.last_use, 0);
   g_last_path = use_fused(pb) ? 1 : 2;
   s = backproject_device(pb, d_sinogram, d_attenuation, d_out, ds.arena, ds.arena_bytes, &ds.staging, st);
+  cudaEventRecord(ds.last_use, st);
+  return s;
+}
+
+// Exact gradient with respect to mu of sum(g * P(activity, mu)) where P is the
+// projector (no truncation) and g = d_grad_sinogram, all device buffers.
+int nrgb_attenuation_grad_device(const float* d_grad_sinogram, const float* d_activity, const float* d_attenuation,
+                                 const int* size, float* d_out, const float* cameras, const int* cameras_size,
+                                 const float* psf, const int* psf_size, float background,
+                                 float background_attenuation, void* stream) {
+  if (!size || !cameras || !cameras_size || !d_grad_sinogram || !d_activity || !d_attenuation || !d_out)
+    return kErrParameters;
+  Cameras cc;
+  int s = expand_cameras(cameras, cameras_size[0], cameras_size[1], size, &cc);
+  if (s != kOk) return s;
+  Problem pb;
+  s = make_problem(size[0], size[1], size[2], cc, psf, psf_size, background, background_attenuation, 0, &pb);
+  if (s != kOk) return s;
+  DeviceState& ds = current_device_state(&s);
+  if (s != kOk) return s;
+  std::lock_guard<std::mutex> lk(ds.mu);
+  const size_t ws = gradient_workspace(pb);
+  if ((s = ensure_arena(ds, ws)) != kOk) return s;
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  cudaStreamWaitEvent(st, ds.last_use, 0);
+  g_last_path = 2;
+  s = dmu_device(pb, d_grad_sinogram, d_activity, d_attenuation, d_out, ds.arena, ds.arena_bytes, &ds.staging, st);
   cudaEventRecord(ds.last_use, st);
   return s;
 }

@@ -249,7 +249,35 @@ int backproject_device(const Problem& pb, const float* d_sino, const float* d_at
   g.ws_att = cv.take<float>(vol_n(pb));
   g.ws_tmp = cv.take<float>(vol_n(pb));
   if (!g.ws_act || !g.ws_att || !g.ws_tmp) return kErrAllocGpu;
-  return check(general_backproject(g, st));
+  return check(pb.back_mode == kBackAdjoint ? general_adjoint(g, st) : general_backproject(g, st));
+}
+
+int dmu_device(const Problem& pb, const float* d_g, const float* d_act, const float* d_att, float* d_out, char* ws,
+               size_t ws_bytes, Staging* stg, cudaStream_t st) {
+  Carver cv(ws, ws_bytes);
+  CamGeom* d_geom;
+  float* d_psf;
+  int s = upload_common(pb, cv, &d_geom, &d_psf, stg, st);
+  if (s != kOk) return s;
+  GeneralArgs g;
+  g.nx = pb.nx;
+  g.ny = pb.ny;
+  g.nz = pb.nz;
+  g.ncam = pb.cams.n;
+  g.geom_host = pb.geom.data();
+  g.act = d_act;
+  g.att = d_att;
+  g.sino = d_g;
+  g.out = d_out;
+  g.psf_sep = d_psf;
+  g.psf_k = pb.psf_k;
+  g.bg = pb.bg;
+  g.bg_att = pb.bg_att;
+  g.ws_act = cv.take<float>(vol_n(pb));
+  g.ws_att = cv.take<float>(vol_n(pb));
+  g.ws_tmp = cv.take<float>(vol_n(pb));
+  if (!g.ws_act || !g.ws_att || !g.ws_tmp) return kErrAllocGpu;
+  return check(general_dmu(g, st));
 }
 
 int gradient_device(const Problem& pb, const float* d_sino, const float* d_act, const float* d_att, float* d_out,

@@ -98,5 +98,9 @@ int backproject_device(const Problem& pb, const float* d_sino, const float* d_at
                        size_t ws_bytes, Staging* stg, cudaStream_t st);
 int gradient_device(const Problem& pb, const float* d_sino, const float* d_act, const float* d_att, float* d_out,
                     char* ws, size_t ws_bytes, Staging* stg, cudaStream_t st);
+// Exact d/dmu of sum(g * project(act, mu)) (g = d_sino); work space as
+// gradient_workspace.
+int dmu_device(const Problem& pb, const float* d_g, const float* d_act, const float* d_att, float* d_out, char* ws,
+               size_t ws_bytes, Staging* stg, cudaStream_t st);
 
 }  // namespace nrgb

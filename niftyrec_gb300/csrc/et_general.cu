@@ -95,10 +95,60 @@ __global__ void k_resample(const float* __restrict__ src, float* __restrict__ ds
   }
 }
 
+// Transpose of trilinear_ref with bg = 0: add v * weight to each in-grid
+// corner of the footprint of (x, y, z) (atomics: footprints overlap).
+__device__ __forceinline__ void trilinear_scatter(float* __restrict__ dst, int nx, int ny, int nz, const Affine34& A,
+                                                  int x, int y, int z, float v) {
+  const float fx = static_cast<float>(x), fy = static_cast<float>(y), fz = static_cast<float>(z);
+  int prev[3];
+  float b0[3], b1[3];
+#pragma unroll
+  for (int i = 0; i < 3; ++i) {
+    const float pos =
+        fa(fa(fa(fm(A.m[4 * i + 0], fx), fm(A.m[4 * i + 1], fy)), fm(A.m[4 * i + 2], fz)), A.m[4 * i + 3]);
+    prev[i] = static_cast<int>(floorf(pos));
+    float rel = __fsub_rn(pos, static_cast<float>(prev[i]));
+    if (rel < 0.0f) rel = 0.0f;
+    b0[i] = __fsub_rn(1.0f, rel);
+    b1[i] = rel;
+  }
+#pragma unroll
+  for (int c = 0; c < 2; ++c) {
+    const int Z = prev[2] + c;
+    if (Z < 0 || Z >= nz) continue;
+#pragma unroll
+    for (int b = 0; b < 2; ++b) {
+      const int Y = prev[1] + b;
+      if (Y < 0 || Y >= ny) continue;
+#pragma unroll
+      for (int a = 0; a < 2; ++a) {
+        const int X = prev[0] + a;
+        if (X < 0 || X >= nx) continue;
+        const float w = (a ? b1[0] : b0[0]) * (b ? b1[1] : b0[1]) * (c ? b1[2] : b0[2]);
+        if (w != 0.0f) atomicAdd(dst + (static_cast<size_t>(Z) * ny + Y) * nx + X, v * w);
+      }
+    }
+  }
+}
+
+__global__ void k_scatter(const float* __restrict__ src, float* __restrict__ dst, int nx, int ny, int nz, Affine34 A) {
+  const size_t nvox = static_cast<size_t>(nx) * ny * nz;
+  for (size_t i = blockIdx.x * static_cast<size_t>(blockDim.x) + threadIdx.x; i < nvox;
+       i += static_cast<size_t>(gridDim.x) * blockDim.x) {
+    const float v = src[i];
+    if (v == 0.0f) continue;
+    const int x = static_cast<int>(i % nx);
+    const int y = static_cast<int>((i / nx) % ny);
+    const int z = static_cast<int>(i / (static_cast<size_t>(nx) * ny));
+    trilinear_scatter(dst, nx, ny, nz, A, x, y, z, v);
+  }
+}
+
 // Row (x) then column (y) pass of emission-lib/_et_convolveSeparable2D.cpp:13-40:
 // true convolution (kernel index R-k), zero outside the plane, plane z uses
-// kernel plane z.  sep layout [plane][row k | column k].
-template <bool ROWS>
+// kernel plane z.  sep layout [plane][row k | column k].  FLIP: correlation
+// (kernel index R+k), the transpose of the convolution.
+template <bool ROWS, bool FLIP = false>
 __global__ void k_conv(const float* __restrict__ in, float* __restrict__ out, int nx, int ny, int nz,
                        const float* __restrict__ sep, int k) {
   const size_t nvox = static_cast<size_t>(nx) * ny * nz;
@@ -113,10 +163,11 @@ __global__ void k_conv(const float* __restrict__ in, float* __restrict__ out, in
     for (int kk = -R; kk <= R; ++kk) {
       if (ROWS) {
         const int d = x + kk;
-        if (d >= 0 && d < nx) s = fa(s, fm(__ldg(in + i + kk), __ldg(K + R - kk)));
+        if (d >= 0 && d < nx) s = fa(s, fm(__ldg(in + i + kk), __ldg(K + (FLIP ? R + kk : R - kk))));
       } else {
         const int d = y + kk;
-        if (d >= 0 && d < ny) s = fa(s, fm(__ldg(in + i + static_cast<ptrdiff_t>(kk) * nx), __ldg(K + R - kk)));
+        if (d >= 0 && d < ny)
+          s = fa(s, fm(__ldg(in + i + static_cast<ptrdiff_t>(kk) * nx), __ldg(K + (FLIP ? R + kk : R - kk))));
       }
     }
     out[i] = s;
@@ -189,6 +240,37 @@ __global__ void k_grad_scan(const float* __restrict__ act, const float* __restri
   }
 }
 
+// Gradient of a projection plane with respect to the rotated mu.  With
+// p = sum_z v_z exp(-T_z) + bg exp(-T_N) (v: PSF-convolved rotated activity,
+// T inclusive prefix of the rotated mu m), dp/dm_z' = -(S_z' + bg exp(-T_N)),
+// S_z' = sum_{z >= z'} v_z exp(-T_z) = P_v - (prefix of v exp(-T) before z').
+// out[z'] = g * dp/dm_z'.  Not in the reference (whose gradient,
+// emission-lib_gpu/_et_attenuation_gradient_gpu_kernels.cu:15-42, ignores the
+// PSF coupling, the sign and the background).
+__global__ void k_dmu_scan(const float* __restrict__ v, const float* __restrict__ m, const float* __restrict__ g_plane,
+                           float* __restrict__ out, int nx, int ny, int nz, float bg) {
+  const int nxy = nx * ny;
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= nxy) return;
+  float T = 0.0f, Pv = 0.0f;
+  for (int z = 0; z < nz; ++z) {
+    const size_t j = static_cast<size_t>(z) * nxy + i;
+    T += __ldg(m + j);
+    Pv = fmaf(__ldg(v + j), __expf(-T), Pv);
+  }
+  const float tail = bg * __expf(-T);
+  const float g = __ldg(g_plane + i);
+  float prefix = 0.0f;
+  T = 0.0f;
+  for (int z = 0; z < nz; ++z) {
+    const size_t j = static_cast<size_t>(z) * nxy + i;
+    T += __ldg(m + j);
+    const float e = __expf(-T);
+    out[j] = -g * ((Pv - prefix) + tail);
+    prefix = fmaf(__ldg(v + j), e, prefix);
+  }
+}
+
 int grid_for(size_t n, int block) {
   const size_t g = (n + block - 1) / block;
   return static_cast<int>(g < 152 * 64 ? g : 152 * 64);
@@ -240,6 +322,50 @@ int general_backproject(const GeneralArgs& a, cudaStream_t st) {
     { NRGB_LAUNCH_SCOPE("k_resample", st); k_resample<true><<<grid_for(nvox, B), B, 0, st>>>(a.ws_act, a.out, nx, ny, nz, Bk, a.bg); }
   }
   if (a.truncate) launch_truncate(a.out, nvox, st);
+  return cudaGetLastError() == cudaSuccess ? kOk : kErrKernel;
+}
+
+// Exact transpose of general_project for fixed mu (bg terms dropped: the
+// transpose of the projector's linear part): spread, transposed PSF
+// (correlation, column pass first), transposed trilinear scatter.
+int general_adjoint(const GeneralArgs& a, cudaStream_t st) {
+  const int nx = a.nx, ny = a.ny, nz = a.nz;
+  const size_t nvox = static_cast<size_t>(nx) * ny * nz, nxy = static_cast<size_t>(nx) * ny;
+  const int B = 256;
+  cudaMemsetAsync(a.out, 0, nvox * sizeof(float), st);
+  for (int cam = 0; cam < a.ncam; ++cam) {
+    const Affine34 F = affine_of(a.geom_host[cam].fwd);
+    if (a.att) { NRGB_LAUNCH_SCOPE("k_resample", st); k_resample<false><<<grid_for(nvox, B), B, 0, st>>>(a.att, a.ws_att, nx, ny, nz, F, a.bg_att); }
+    { NRGB_LAUNCH_SCOPE("k_spread", st); k_spread<<<static_cast<int>((nxy + B - 1) / B), B, 0, st>>>(a.sino + nxy * cam, a.att ? a.ws_att : nullptr,
+                                                               a.ws_act, nx, ny, nz); }
+    if (a.psf_sep) {
+      { NRGB_LAUNCH_SCOPE("k_conv", st); k_conv<false, true><<<grid_for(nvox, B), B, 0, st>>>(a.ws_act, a.ws_tmp, nx, ny, nz, a.psf_sep, a.psf_k); }
+      { NRGB_LAUNCH_SCOPE("k_conv", st); k_conv<true, true><<<grid_for(nvox, B), B, 0, st>>>(a.ws_tmp, a.ws_act, nx, ny, nz, a.psf_sep, a.psf_k); }
+    }
+    { NRGB_LAUNCH_SCOPE("k_scatter", st); k_scatter<<<grid_for(nvox, B), B, 0, st>>>(a.ws_act, a.out, nx, ny, nz, F); }
+  }
+  return cudaGetLastError() == cudaSuccess ? kOk : kErrKernel;
+}
+
+// Gradient of sum(g * project(act, mu)) with respect to mu (a.sino = g),
+// into a.out.  Per camera: rotate activity and mu, PSF on the activity,
+// k_dmu_scan, transposed trilinear scatter of the rotated-frame gradient.
+int general_dmu(const GeneralArgs& a, cudaStream_t st) {
+  const int nx = a.nx, ny = a.ny, nz = a.nz;
+  const size_t nvox = static_cast<size_t>(nx) * ny * nz, nxy = static_cast<size_t>(nx) * ny;
+  const int B = 256;
+  cudaMemsetAsync(a.out, 0, nvox * sizeof(float), st);
+  for (int cam = 0; cam < a.ncam; ++cam) {
+    const Affine34 F = affine_of(a.geom_host[cam].fwd);
+    { NRGB_LAUNCH_SCOPE("k_resample", st); k_resample<false><<<grid_for(nvox, B), B, 0, st>>>(a.act, a.ws_act, nx, ny, nz, F, a.bg); }
+    { NRGB_LAUNCH_SCOPE("k_resample", st); k_resample<false><<<grid_for(nvox, B), B, 0, st>>>(a.att, a.ws_att, nx, ny, nz, F, a.bg_att); }
+    if (a.psf_sep) {
+      { NRGB_LAUNCH_SCOPE("k_conv", st); k_conv<true><<<grid_for(nvox, B), B, 0, st>>>(a.ws_act, a.ws_tmp, nx, ny, nz, a.psf_sep, a.psf_k); }
+      { NRGB_LAUNCH_SCOPE("k_conv", st); k_conv<false><<<grid_for(nvox, B), B, 0, st>>>(a.ws_tmp, a.ws_act, nx, ny, nz, a.psf_sep, a.psf_k); }
+    }
+    { NRGB_LAUNCH_SCOPE("k_dmu_scan", st); k_dmu_scan<<<static_cast<int>((nxy + B - 1) / B), B, 0, st>>>(a.ws_act, a.ws_att, a.sino + nxy * cam, a.ws_tmp, nx, ny, nz, a.bg); }
+    { NRGB_LAUNCH_SCOPE("k_scatter", st); k_scatter<<<grid_for(nvox, B), B, 0, st>>>(a.ws_tmp, a.out, nx, ny, nz, F); }
+  }
   return cudaGetLastError() == cudaSuccess ? kOk : kErrKernel;
 }
 

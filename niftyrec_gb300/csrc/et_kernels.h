@@ -27,6 +27,10 @@ struct GeneralArgs {
 int general_project(const GeneralArgs& a, cudaStream_t st);
 int general_backproject(const GeneralArgs& a, cudaStream_t st);
 int general_gradient(const GeneralArgs& a, cudaStream_t st);
+// Exact transpose of general_project's linear part (backprojector mode 1).
+int general_adjoint(const GeneralArgs& a, cudaStream_t st);
+// d/dmu of sum(g * project(act, mu)); a.sino = g (sinogram), a.out = gradient.
+int general_dmu(const GeneralArgs& a, cudaStream_t st);
 int general_rotate(const float* src, float* dst, int nx, int ny, int nz, const float* m12, float bg, cudaStream_t st);
 
 // ---- y-gantry fused path (column layout) ----

@@ -398,12 +398,37 @@ __global__ void __launch_bounds__(32 * kSlabsB) k_mu_carry_yg(const YgArgs a) {
   }
 }
 
+// Vector reduction of 4 floats into global memory (sm_90+).
+__device__ __forceinline__ void red4(float* p, const float4& v) {
+  asm volatile("red.global.add.v4.f32 [%0], {%1, %2, %3, %4};" ::"l"(p), "f"(v.x), "f"(v.y), "f"(v.z), "f"(v.w)
+               : "memory");
+}
+
+__device__ __forceinline__ float4 scale4(const float4& v, float w) {
+  return make_float4(v.x * w, v.y * w, v.z * w, v.w * w);
+}
+
+// Transposed bilinear interpolation: add w * v to each corner of footprint t
+// (corners outside the grid have weight 0 and are skipped).
+__device__ __forceinline__ void scatter4(float* __restrict__ base, const Tap& t, int yb, const float4& v) {
+  if (!t.any) return;
+  float* p = base + t.off + yb;
+  if (t.w00 != 0.0f) red4(p, scale4(v, t.w00));
+  if (t.w10 != 0.0f) red4(p + t.dx, scale4(v, t.w10));
+  if (t.w01 != 0.0f) red4(p + t.dz, scale4(v, t.w01));
+  if (t.w11 != 0.0f) red4(p + t.dx + t.dz, scale4(v, t.w11));
+}
+
 // ---------------------------------------- backprojector: spread + PSF
 // temp[g][z][x][y] = PSF_z( s(x', y) * exp(-T_z(x', y)) ) for camera c0+g,
 // T inclusive (emission-lib/_et_line_backproject_attenuated.cpp:24-34), PSF
 // as in the projector.  CTA = (camera, x-tile, depth slab); every sampled
 // column starts its transmission from the slab carry.
-template <int R, bool PSF, bool ATT>
+// ADJ: the exact transpose of the projector instead (not in the reference):
+// the PSF taps are flipped (correlation) and each output column is scattered
+// with the projector's own bilinear weights into the accumulator a.out
+// (vector reductions; all cameras in one launch, no scratch).
+template <int R, bool PSF, bool ATT, bool ADJ>
 __global__ void __launch_bounds__(32 * kW, 2) k_spread_yg(const YgArgs a, int c0) {
   using TS = TileShape<R>;
   constexpr int NS = TS::NS;
@@ -426,11 +451,16 @@ __global__ void __launch_bounds__(32 * kW, 2) k_spread_yg(const YgArgs a, int c0
   const int zbeg = slab * zper, zend = min(a.nz, zbeg + zper);
   if (zbeg >= zend) return;  // uniform over the CTA
   if (PSF) {
-    for (int i = threadIdx.x; i < a.nz * 2 * K; i += blockDim.x) s_psf[i] = __ldg(a.psf + i);
+    for (int i = threadIdx.x; i < a.nz * 2 * K; i += blockDim.x) {
+      const int j = i % (2 * K), base = i - j;
+      // transpose of a convolution = correlation: reverse each kernel
+      const int src = !ADJ ? i : (j < K ? base + (K - 1 - j) : base + K + (2 * K - 1 - j));
+      s_psf[i] = __ldg(a.psf + src);
+    }
   }
   const CamRows cr = cam_rows(a.geom[cam].fwd);
   const size_t vol = static_cast<size_t>(a.nz) * a.nx * a.cy;
-  float* __restrict__ tmp = a.temp + vol * g;
+  float* __restrict__ tmp = ADJ ? a.out : a.temp + vol * g;
   const float* __restrict__ srow = a.sino + static_cast<size_t>(cam) * a.nx * a.cy;
 
   float4 Tc[TS::kOwn];
@@ -447,7 +477,7 @@ __global__ void __launch_bounds__(32 * kW, 2) k_spread_yg(const YgArgs a, int c0
     const int b = z & 1;
     float4* sbuf = sb + b * NS * 32;
     Tap* tb = taps + b * NS;
-    if (ATT && lane < TS::kOwn) {
+    if ((ATT || ADJ) && lane < TS::kOwn) {
       const int c = warp + kW * lane;
       if (c < NS) {
         const int xp = x0 - R + c;
@@ -473,7 +503,11 @@ __global__ void __launch_bounds__(32 * kW, 2) k_spread_yg(const YgArgs a, int c0
     __syncthreads();
     auto emit = [&](int i, const float4& v) {
       const int x = x0 + warp * kTXW + i;
-      if (x < a.nx && yok) *reinterpret_cast<float4*>(tmp + (static_cast<size_t>(z) * a.nx + x) * a.cy + yb) = v;
+      if (x >= a.nx || !yok) return;
+      if (ADJ)
+        scatter4(tmp, tb[warp * kTXW + i + R], yb, v);
+      else
+        *reinterpret_cast<float4*>(tmp + (static_cast<size_t>(z) * a.nx + x) * a.cy + yb) = v;
     };
     if (PSF) {
       const float* kr = s_psf + z * 2 * K;
@@ -588,7 +622,7 @@ int launch_project_R(const YgArgs& a, cudaStream_t st) {
   return cudaGetLastError() == cudaSuccess ? kOk : kErrKernel;
 }
 
-template <int R>
+template <int R, bool ADJ>
 int launch_spread_R(const YgArgs& a, int c0, int gcount, cudaStream_t st) {
   const int ntile = (a.nx + kTXC - 1) / kTXC;
   const dim3 grid(gcount * ntile * kSlabsB), block(32 * kW);
@@ -596,15 +630,15 @@ int launch_spread_R(const YgArgs& a, int c0, int gcount, cudaStream_t st) {
   const size_t smem = tile_smem_bytes<R>(psf ? a.nz : 0);
   auto go = [&](auto k) {
     cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
-    NRGB_LAUNCH_SCOPE("k_spread_yg", st);
+    NRGB_LAUNCH_SCOPE(ADJ ? "k_adjoint_yg" : "k_spread_yg", st);
     k<<<grid, block, smem, st>>>(a, c0);
   };
   if (psf) {
-    if (a.mu) go(k_spread_yg<R, true, true>);
-    else go(k_spread_yg<R, true, false>);
+    if (a.mu) go(k_spread_yg<R, true, true, ADJ>);
+    else go(k_spread_yg<R, true, false, ADJ>);
   } else {
-    if (a.mu) go(k_spread_yg<0, false, true>);
-    else go(k_spread_yg<0, false, false>);
+    if (a.mu) go(k_spread_yg<0, false, true, ADJ>);
+    else go(k_spread_yg<0, false, false, ADJ>);
   }
   return cudaGetLastError() == cudaSuccess ? kOk : kErrKernel;
 }
@@ -623,18 +657,23 @@ int project_by_radius(int R, const YgArgs& a, cudaStream_t st) {
   }
 }
 
-int spread_by_radius(int R, const YgArgs& a, int c0, int gcount, cudaStream_t st) {
+template <bool ADJ>
+int spread_by_radius_t(int R, const YgArgs& a, int c0, int gcount, cudaStream_t st) {
   switch (R) {
-    case 0: return launch_spread_R<0>(a, c0, gcount, st);
-    case 1: return launch_spread_R<1>(a, c0, gcount, st);
-    case 2: return launch_spread_R<2>(a, c0, gcount, st);
-    case 3: return launch_spread_R<3>(a, c0, gcount, st);
-    case 4: return launch_spread_R<4>(a, c0, gcount, st);
-    case 5: return launch_spread_R<5>(a, c0, gcount, st);
-    case 6: return launch_spread_R<6>(a, c0, gcount, st);
-    case 7: return launch_spread_R<7>(a, c0, gcount, st);
+    case 0: return launch_spread_R<0, ADJ>(a, c0, gcount, st);
+    case 1: return launch_spread_R<1, ADJ>(a, c0, gcount, st);
+    case 2: return launch_spread_R<2, ADJ>(a, c0, gcount, st);
+    case 3: return launch_spread_R<3, ADJ>(a, c0, gcount, st);
+    case 4: return launch_spread_R<4, ADJ>(a, c0, gcount, st);
+    case 5: return launch_spread_R<5, ADJ>(a, c0, gcount, st);
+    case 6: return launch_spread_R<6, ADJ>(a, c0, gcount, st);
+    case 7: return launch_spread_R<7, ADJ>(a, c0, gcount, st);
     default: return kErrParameters;
   }
+}
+
+int spread_by_radius(int R, const YgArgs& a, int c0, int gcount, cudaStream_t st) {
+  return spread_by_radius_t<false>(R, a, c0, gcount, st);
 }
 
 }  // namespace
@@ -725,6 +764,12 @@ int yg_backproject(const YgArgs& a_in, cudaStream_t st) {
     }
   }
   a.group = group;
+  if (a.back_mode == kBackAdjoint) {
+    // transpose of the projector: one launch over all cameras, scattered
+    // straight into the zeroed accumulator
+    if (cudaMemsetAsync(a.out, 0, sizeof(float) * vol, st) != cudaSuccess) return kErrKernel;
+    return spread_by_radius_t<true>(R, a, 0, a.ncam, st);
+  }
   const int nchunk = (a.nx + kGatherCols - 1) / kGatherCols;
   const int gblocks = (nchunk * a.nz + kGatherWarps - 1) / kGatherWarps;
   const size_t gsmem = sizeof(Tap) * kGatherWarps * kGatherCols * group;
