@@ -201,7 +201,7 @@ def run_ours(args):
     psf_c = np.ascontiguousarray(psf, np.float32)
     vp = ctypes.c_void_p
 
-    def pair(use_psf=True, use_att=True):
+    def pair(use_psf=True, use_att=True, mode=0):
         sp = vp(stream.cuda_stream)
         st = L.nrgb_project_device(vp(t_act.data_ptr()), vp(t_mu.data_ptr()) if use_att else None, size,
                                    vp(t_sino.data_ptr()), cams_c.ctypes.data_as(vp), csize,
@@ -212,11 +212,11 @@ def run_ours(args):
         st = L.nrgb_backproject_device(vp(t_sino.data_ptr()), vp(t_mu.data_ptr()) if use_att else None, size,
                                        vp(t_bk.data_ptr()), cams_c.ctypes.data_as(vp), csize,
                                        psf_c.ctypes.data_as(vp) if use_psf else None,
-                                       psize if use_psf else (ctypes.c_int * 3)(0, 0, 0), 0.0, 0.0, 1, 0, sp)
+                                       psize if use_psf else (ctypes.c_int * 3)(0, 0, 0), 0.0, 0.0, 1, mode, sp)
         if st:
             raise RuntimeError(f"nrgb_backproject_device status {st}")
 
-    def timed(steps, use_psf=True, use_att=True, profile=False):
+    def timed(steps, use_psf=True, use_att=True, profile=False, mode=0):
         evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(steps)]
         barrier(world)
         torch.cuda.synchronize(dev)
@@ -226,7 +226,7 @@ def run_ours(args):
         for a, b in evs:
             flush.zero_()
             a.record(stream)
-            pair(use_psf, use_att)
+            pair(use_psf, use_att, mode)
             b.record(stream)
         torch.cuda.synchronize(dev)
         barrier(world)
@@ -259,6 +259,10 @@ def run_ours(args):
     # "vs plain": the same pair without PSF and attenuation
     ms_plain, _, _ = timed(max(3, args.steps // 2), use_psf=False, use_att=False)
     plain = world * 1000.0 / reduce_max(sum(ms_plain) / len(ms_plain), world)
+    # the same pair with the exact-transpose backprojector (gradient form)
+    pair(mode=1)
+    ms_adj, _, _ = timed(max(3, args.steps // 2), mode=1)
+    adjoint = world * 1000.0 / reduce_max(sum(ms_adj) / len(ms_adj), world)
 
     # end to end through the reference-facing C-ABI with host buffers
     y = t_sino.cpu().numpy()
@@ -304,6 +308,7 @@ def run_ours(args):
                                "project + reference backproject", "volume": [N, N, N], "angles": NCAM,
                    "psf": [K, K, N], "l2": "flushed (256 MB write) before every step", "parallelism": f"replicas{world}"},
         "plain_pairs_per_s": round(plain, 3),
+        "adjoint_backprojector_pairs_per_s": round(adjoint, 3),
         "vs_plain": round(value / plain, 4),
         "pair_hbm": {"bytes_per_pair": PAIR_BYTES, "achieved_gbs": round(PAIR_BYTES * value / world / 1e9, 1),
                      "frac_of_peak": round(PAIR_BYTES * value / world / 1e9 / peak, 4), "peak_source": peak_kind},

@@ -29,6 +29,7 @@ def main(argv=None):
     ap.add_argument("--psf", type=int, default=11, help="PSF width (0: none)")
     ap.add_argument("--no-att", action="store_true")
     ap.add_argument("--reps", type=int, default=2)
+    ap.add_argument("--mode", type=int, default=0, help="backprojector: 0 reference, 1 exact transpose")
     a = ap.parse_args(argv)
 
     L = _lib.load()
@@ -58,7 +59,7 @@ def main(argv=None):
             assert st == 0, st
         if a.op in ("backproject", "pair"):
             st = L.nrgb_backproject_device(vp(t_sino.data_ptr()), mu_p, size, vp(t_bk.data_ptr()),
-                                           cams.ctypes.data_as(vp), csize, psf_p, psize, 0.0, 0.0, 1, 0, sp)
+                                           cams.ctypes.data_as(vp), csize, psf_p, psize, 0.0, 0.0, 1, a.mode, sp)
             assert st == 0, st
 
     run()
