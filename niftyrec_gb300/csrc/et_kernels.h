@@ -77,6 +77,13 @@ int yg_backproject(const YgArgs& a, cudaStream_t st);
 // planes x [ny][nx] (nifti) <-> planes x [nx][cy] (column), zero pads.
 int to_column(const float* src, float* dst, int nx, int ny, int cy, int planes, cudaStream_t st);
 int from_column(const float* src, float* dst, int nx, int ny, int cy, int planes, int truncate, cudaStream_t st);
+// Row windows: dst column [planes][nx][cy] <- src nifti rows [row0, row0+rows)
+// (planes of ny_src rows); and nifti rows [row0+r_begin, row0+r_end) of dst
+// (planes of ny_dst rows) <- column rows [r_begin, r_end) of src.
+int to_column_rows(const float* src, float* dst, int nx, int ny_src, int row0, int rows, int cy, int planes,
+                   cudaStream_t st);
+int from_column_rows(const float* src, float* dst, int nx, int cy, int r_begin, int r_end, int row0, int ny_dst,
+                     int planes, int truncate, cudaStream_t st);
 void launch_truncate(float* buf, size_t n, cudaStream_t st);
 
 // ---- OSEM / MLEM update kernels ----

@@ -563,39 +563,44 @@ __global__ void __launch_bounds__(32 * kGatherWarps) k_gather_yg(const YgArgs a,
 }
 
 // --------------------------------------------------------------- layouts
-__global__ void k_to_col(const float* __restrict__ src, float* __restrict__ dst, int nx, int ny, int cy) {
+// dst[p][x][r] = src[p][row0 + r][x] for r < rows, zero pads up to cy.
+// src planes have ny_src rows.
+__global__ void k_to_col(const float* __restrict__ src, float* __restrict__ dst, int nx, int ny_src, int row0,
+                         int rows, int cy) {
   __shared__ float tile[32][33];
   const int p = blockIdx.z;
   const int xb = blockIdx.x * 32, yb = blockIdx.y * 32;
   const int tx = threadIdx.x;
   for (int dy = threadIdx.y; dy < 32; dy += blockDim.y) {
-    const int y = yb + dy, x = xb + tx;
-    tile[dy][tx] = (y < ny && x < nx) ? src[(static_cast<size_t>(p) * ny + y) * nx + x] : 0.0f;
+    const int r = yb + dy, x = xb + tx;
+    tile[dy][tx] = (r < rows && x < nx) ? src[(static_cast<size_t>(p) * ny_src + row0 + r) * nx + x] : 0.0f;
   }
   __syncthreads();
   for (int dx = threadIdx.y; dx < 32; dx += blockDim.y) {
-    const int x = xb + dx, y = yb + tx;
-    if (x < nx && y < cy) dst[(static_cast<size_t>(p) * nx + x) * cy + y] = tile[tx][dx];
+    const int x = xb + dx, r = yb + tx;
+    if (x < nx && r < cy) dst[(static_cast<size_t>(p) * nx + x) * cy + r] = tile[tx][dx];
   }
 }
 
-__global__ void k_from_col(const float* __restrict__ src, float* __restrict__ dst, int nx, int ny, int cy,
-                           int truncate) {
+// dst[p][row0 + r][x] = src[p][x][r] for r in [r_begin, r_end); dst planes
+// have ny_dst rows; truncate clamps negatives to zero.
+__global__ void k_from_col(const float* __restrict__ src, float* __restrict__ dst, int nx, int cy, int r_begin,
+                           int r_end, int row0, int ny_dst, int truncate) {
   __shared__ float tile[32][33];
   const int p = blockIdx.z;
-  const int xb = blockIdx.x * 32, yb = blockIdx.y * 32;
+  const int xb = blockIdx.x * 32, yb = r_begin + blockIdx.y * 32;
   const int tx = threadIdx.x;
   for (int dx = threadIdx.y; dx < 32; dx += blockDim.y) {
-    const int x = xb + dx, y = yb + tx;
-    tile[dx][tx] = (x < nx && y < ny) ? src[(static_cast<size_t>(p) * nx + x) * cy + y] : 0.0f;
+    const int x = xb + dx, r = yb + tx;
+    tile[dx][tx] = (x < nx && r < r_end) ? src[(static_cast<size_t>(p) * nx + x) * cy + r] : 0.0f;
   }
   __syncthreads();
   for (int dy = threadIdx.y; dy < 32; dy += blockDim.y) {
-    const int y = yb + dy, x = xb + tx;
-    if (x < nx && y < ny) {
+    const int r = yb + dy, x = xb + tx;
+    if (x < nx && r < r_end) {
       float v = tile[tx][dy];
       if (truncate && v < 0.0f) v = 0.0f;
-      dst[(static_cast<size_t>(p) * ny + y) * nx + x] = v;
+      dst[(static_cast<size_t>(p) * ny_dst + row0 + r) * nx + x] = v;
     }
   }
 }
@@ -810,16 +815,30 @@ int yg_backproject(const YgArgs& a_in, cudaStream_t st) {
   return cudaGetLastError() == cudaSuccess ? kOk : kErrKernel;
 }
 
-int to_column(const float* src, float* dst, int nx, int ny, int cy, int planes, cudaStream_t st) {
+int to_column_rows(const float* src, float* dst, int nx, int ny_src, int row0, int rows, int cy, int planes,
+                   cudaStream_t st) {
   const dim3 grid((nx + 31) / 32, (cy + 31) / 32, planes), block(32, 8);
-  { NRGB_LAUNCH_SCOPE("k_to_col", st); k_to_col<<<grid, block, 0, st>>>(src, dst, nx, ny, cy); }
+  { NRGB_LAUNCH_SCOPE("k_to_col", st); k_to_col<<<grid, block, 0, st>>>(src, dst, nx, ny_src, row0, rows, cy); }
   return cudaGetLastError() == cudaSuccess ? kOk : kErrKernel;
 }
 
-int from_column(const float* src, float* dst, int nx, int ny, int cy, int planes, int truncate, cudaStream_t st) {
-  const dim3 grid((nx + 31) / 32, (ny + 31) / 32, planes), block(32, 8);
-  { NRGB_LAUNCH_SCOPE("k_from_col", st); k_from_col<<<grid, block, 0, st>>>(src, dst, nx, ny, cy, truncate); }
+int from_column_rows(const float* src, float* dst, int nx, int cy, int r_begin, int r_end, int row0, int ny_dst,
+                     int planes, int truncate, cudaStream_t st) {
+  if (r_end <= r_begin) return kOk;
+  const dim3 grid((nx + 31) / 32, (r_end - r_begin + 31) / 32, planes), block(32, 8);
+  {
+    NRGB_LAUNCH_SCOPE("k_from_col", st);
+    k_from_col<<<grid, block, 0, st>>>(src, dst, nx, cy, r_begin, r_end, row0, ny_dst, truncate);
+  }
   return cudaGetLastError() == cudaSuccess ? kOk : kErrKernel;
+}
+
+int to_column(const float* src, float* dst, int nx, int ny, int cy, int planes, cudaStream_t st) {
+  return to_column_rows(src, dst, nx, ny, 0, ny, cy, planes, st);
+}
+
+int from_column(const float* src, float* dst, int nx, int ny, int cy, int planes, int truncate, cudaStream_t st) {
+  return from_column_rows(src, dst, nx, cy, 0, ny, 0, ny, planes, truncate, st);
 }
 
 }  // namespace nrgb

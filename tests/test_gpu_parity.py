@@ -109,16 +109,43 @@ def test_oracle_fresh_inputs(o32, shape, k, ncam):
     assert rel_l2(b, bo) < RTOL
 
 
-def test_general_path_large_ny(o32):
-    """ny > 128 runs on the general-orientation kernels."""
-    shape = (20, 132, 20)  # ny = 132 > 128
+@pytest.mark.parametrize("shape,k", [((20, 132, 20), 5), ((16, 300, 16), 15), ((12, 257, 14), 0),
+                                     ((10, 250, 12), 1)])
+def test_row_windows_large_ny(o32, shape, k):
+    """ny > 128 runs on the fused kernels in row windows with a PSF halo;
+    window seams must not show (checked per row against the oracle)."""
+    act = S.ellipsoid_phantom(shape, seed=4)
+    mu = S.mu_map(shape, seed=4)
+    psf = S.gaussian_psf(k, shape[2]) if k else None
+    cams = S.cameras_about_y(3, 10.0)
+    s = A.project(act, cams, psf, mu)
+    assert A.last_path() == FUSED
+    so = o32.project(act, cams, psf, mu)
+    assert per_plane_rel(s, so) < RTOL
+    # every gantry-axis row, so a seam between windows cannot hide in the norm
+    rows = np.linalg.norm(s - so, axis=(0, 2)) / np.maximum(np.linalg.norm(so, axis=(0, 2)), 1e-12)
+    assert rows.max() < 1e-4, int(rows.argmax())
+    b = A.backproject(so, cams, psf, mu, nz=shape[0])
+    assert A.last_path() == FUSED
+    assert rel_l2(b, o32.backproject(so, cams, psf, mu, nz=shape[0])) < RTOL
+    torch = pytest.importorskip("torch")
+    from niftyrec_gb300.autograd import backproject_raw
+
+    bt = backproject_raw(torch.from_numpy(so).cuda(), torch.from_numpy(mu).cuda(), cams, psf, nz=shape[0], mode=1)
+    bto = o32.backproject(so, cams, psf, mu, truncate=0, adjoint=True, nz=shape[0])
+    assert rel_l2(bt.cpu().numpy(), bto) < RTOL
+
+
+def test_general_path_with_background(o32):
+    """A non-zero background leaves the fused kernels for the general path."""
+    shape = (20, 132, 20)
     act = S.ellipsoid_phantom(shape, seed=4)
     mu = S.mu_map(shape, seed=4)
     psf = S.gaussian_psf(5, 20)
     cams = S.cameras_about_y(3, 10.0)
-    s = A.project(act, cams, psf, mu)
+    s = A.project(act, cams, psf, mu, 0.5, 0.0)
     assert A.last_path() == GENERAL
-    assert per_plane_rel(s, o32.project(act, cams, psf, mu)) < RTOL
+    assert per_plane_rel(s, o32.project(act, cams, psf, mu, 0.5, 0.0)) < RTOL
 
 
 def test_gradient_attenuation_matches_restated_reference(o32):
