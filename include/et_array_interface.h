@@ -138,6 +138,40 @@ int nrgb_backproject_device(const float *d_sinogram, const float *d_attenuation,
                             const float *cameras, const int *cameras_size, const float *psf, const int *psf_size,
                             float background, float background_attenuation, int truncate, int mode, void *stream);
 
+/* bfloat16 storage (additions; the reference is float32 throughout):
+ * d_activity and d_attenuation are device bfloat16 volumes in nifti order;
+ * every product and sum is float32, the depth sums of the fused kernels
+ * (transmission prefix, projection) are Kahan-compensated, and sinograms and
+ * backprojections are float32.  Same arguments and status codes as the
+ * float32 entry points above. */
+int nrgb_project_device_bf16(const void *d_activity, const void *d_attenuation, const int *size, float *d_sinogram,
+                             const float *cameras, const int *cameras_size, const float *psf, const int *psf_size,
+                             float background, float background_attenuation, int truncate, void *stream);
+int nrgb_backproject_device_bf16(const float *d_sinogram, const void *d_attenuation, const int *size, float *d_out,
+                                 const float *cameras, const int *cameras_size, const float *psf, const int *psf_size,
+                                 float background, float background_attenuation, int truncate, int mode,
+                                 void *stream);
+
+/* float64 reference run (additions): the reference projector and
+ * backprojector (general-orientation kernels in the reference's operation
+ * order) with positions, weights, PSF, exp and every sum in double, on device
+ * double buffers in nifti order.  Cameras and PSF are the float32 host arrays
+ * of the float32 entry points, widened exactly.  The float32 and bfloat16
+ * results are measured against this run.  Slow (float64 throughput), for
+ * error reports only. */
+int nrgb_project_device_f64(const double *d_activity, const double *d_attenuation, const int *size,
+                            double *d_sinogram, const float *cameras, const int *cameras_size, const float *psf,
+                            const int *psf_size, double background, double background_attenuation, int truncate,
+                            void *stream);
+int nrgb_backproject_device_f64(const double *d_sinogram, const double *d_attenuation, const int *size,
+                                double *d_out, const float *cameras, const int *cameras_size, const float *psf,
+                                const int *psf_size, double background, double background_attenuation, int truncate,
+                                void *stream);
+int nrgb_osem_ratio_device_f64(const double *d_counts, double *d_projection, long long n, double epsilon,
+                               void *stream);
+int nrgb_osem_update_device_f64(double *d_activity, const double *d_numerator, const double *d_denominator,
+                                long long n, double epsilon, void *stream);
+
 /* Exact gradient with respect to mu of sum(g * P(activity, mu)), P the
  * projector without truncation, g = d_grad_sinogram (device, nifti order):
  * dP/dmu_z' = -(sum_{z >= z'} PSF(rotated activity)_z exp(-T_z) + bg exp(-T_N))
@@ -169,6 +203,17 @@ int nrgb_backproject_device_noalloc(const float *d_sinogram, const float *d_atte
                                     float *d_out, const float *cameras, const int *cameras_size, const float *psf,
                                     const int *psf_size, float background, float background_attenuation,
                                     int truncate, void *stream);
+
+/* The elementwise stages of et_array_osem_step on device buffers (additions;
+ * emission-lib/_et_array_interface.cpp:1022-1028 and :1036-1044 run them on
+ * host arrays inside the step).  ratio overwrites d_projection with
+ * y / p (y / epsilon where p < epsilon); update does
+ * activity *= numerator / max(denominator, epsilon).  For callers that build
+ * the step from partial backprojections, e.g. summed across processes that
+ * each own a share of a subset's cameras. */
+int nrgb_osem_ratio_device(const float *d_counts, float *d_projection, long long n, float epsilon, void *stream);
+int nrgb_osem_update_device(float *d_activity, const float *d_numerator, const float *d_denominator, long long n,
+                            float epsilon, void *stream);
 
 /* Diagnostics: 1 if the calling thread's last call ran the fused y-gantry
  * kernels, 2 if it ran the general-orientation kernels, 0 before any call. */

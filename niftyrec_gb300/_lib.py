@@ -53,8 +53,17 @@ PROTOTYPES = {
     "et_array_mlem": (_I, [_P, _U, _U, _P, _I, _F, _F, _U, _I, _I, _P, _I, _P, _U, _U, _F, _F, _F, _I]),
     "nrgb_project_device": (_I, [_P, _P, _PI, _P, _P, _PI, _P, _PI, _F, _F, _I, _P]),
     "nrgb_backproject_device": (_I, [_P, _P, _PI, _P, _P, _PI, _P, _PI, _F, _F, _I, _I, _P]),
-    "nrgb_backproject_device_noalloc": (_I, [_P, _P, _PI, _P, _P, _PI, _P, _PI, _F, _F, _I, _P]),
+    "nrgb_project_device_bf16": (_I, [_P, _P, _PI, _P, _P, _PI, _P, _PI, _F, _F, _I, _P]),
+    "nrgb_backproject_device_bf16": (_I, [_P, _P, _PI, _P, _P, _PI, _P, _PI, _F, _F, _I, _I, _P]),
+    "nrgb_backproject_device_noalloc":(_I, [_P, _P, _PI, _P, _P, _PI, _P, _PI, _F, _F, _I, _P]),
     "nrgb_attenuation_grad_device": (_I, [_P, _P, _P, _PI, _P, _P, _PI, _P, _PI, _F, _F, _P]),
+    "nrgb_project_device_f64": (_I, [_P, _P, _PI, _P, _P, _PI, _P, _PI, ctypes.c_double, ctypes.c_double, _I, _P]),
+    "nrgb_backproject_device_f64": (_I, [_P, _P, _PI, _P, _P, _PI, _P, _PI, ctypes.c_double, ctypes.c_double, _I,
+                                         _P]),
+    "nrgb_osem_ratio_device_f64": (_I, [_P, _P, ctypes.c_longlong, ctypes.c_double, _P]),
+    "nrgb_osem_update_device_f64": (_I, [_P, _P, _P, ctypes.c_longlong, ctypes.c_double, _P]),
+    "nrgb_osem_ratio_device": (_I, [_P, _P, ctypes.c_longlong, _F, _P]),
+    "nrgb_osem_update_device": (_I, [_P, _P, _P, ctypes.c_longlong, _F, _P]),
     "nrgb_plan_create": (_I, [ctypes.POINTER(_P), _PI, _P, _PI, _P, _PI, _P, _F, _F, _PI, _I, _P]),
     "nrgb_plan_destroy": (_I, [_P]),
     "nrgb_plan_shape": (_I, [_P, _PI]),

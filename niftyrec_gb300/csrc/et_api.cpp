@@ -574,14 +574,18 @@ int et_array_mlem(float* activity_data, unsigned int size_x, unsigned int size_y
   return status;
 }
 
+}  // extern "C"
+
 // ------------------------------------------------ device-pointer additions
 // Same operations on device buffers (nifti layout) on the caller's stream;
 // cameras and PSF stay host arrays.  The call returns once the work is
 // enqueued.  No counterpart in the reference (its GPU path copies host
 // buffers in and out on every call).
-int nrgb_project_device(const float* d_activity, const float* d_attenuation, const int* size, float* d_sinogram,
+namespace {
+
+int project_device_call(const float* d_activity, const float* d_attenuation, const int* size, float* d_sinogram,
                         const float* cameras, const int* cameras_size, const float* psf, const int* psf_size,
-                        float background, float background_attenuation, int truncate, void* stream) {
+                        float background, float background_attenuation, int truncate, bool bf16, void* stream) {
   if (!size || !cameras || !cameras_size || (!d_activity && !d_attenuation) || !d_sinogram) return kErrParameters;
   Cameras cc;
   int s = expand_cameras(cameras, cameras_size[0], cameras_size[1], size, &cc);
@@ -589,6 +593,10 @@ int nrgb_project_device(const float* d_activity, const float* d_attenuation, con
   Problem pb;
   s = make_problem(size[0], size[1], size[2], cc, psf, psf_size, background, background_attenuation, truncate, &pb);
   if (s != kOk) return s;
+  if (bf16) {
+    pb.storage = kStorageBF16;
+    pb.input_bf16 = true;
+  }
   DeviceState& ds = current_device_state(&s);
   if (s != kOk) return s;
   std::lock_guard<std::mutex> lk(ds.mu);
@@ -602,11 +610,10 @@ int nrgb_project_device(const float* d_activity, const float* d_attenuation, con
   return s;
 }
 
-// mode: 0 = the reference's inverse-rotation backprojector; 1 = the exact
-// transpose of the projector (for gradients).
-int nrgb_backproject_device(const float* d_sinogram, const float* d_attenuation, const int* size, float* d_out,
+int backproject_device_call(const float* d_sinogram, const float* d_attenuation, const int* size, float* d_out,
                             const float* cameras, const int* cameras_size, const float* psf, const int* psf_size,
-                            float background, float background_attenuation, int truncate, int mode, void* stream) {
+                            float background, float background_attenuation, int truncate, int mode, bool bf16,
+                            void* stream) {
   if (!size || !cameras || !cameras_size || !d_sinogram || !d_out || (mode != kBackReference && mode != kBackAdjoint))
     return kErrParameters;
   Cameras cc;
@@ -617,6 +624,10 @@ int nrgb_backproject_device(const float* d_sinogram, const float* d_attenuation,
   s = make_problem(size[0], size[1], size[2], cc, psf, psf_size, background, background_attenuation, truncate, &pb);
   if (s != kOk) return s;
   pb.back_mode = mode;
+  if (bf16) {
+    pb.storage = kStorageBF16;
+    pb.input_bf16 = true;
+  }
   DeviceState& ds = current_device_state(&s);
   if (s != kOk) return s;
   std::lock_guard<std::mutex> lk(ds.mu);
@@ -628,6 +639,111 @@ int nrgb_backproject_device(const float* d_sinogram, const float* d_attenuation,
   s = backproject_device(pb, d_sinogram, d_attenuation, d_out, ds.arena, ds.arena_bytes, &ds.staging, st);
   cudaEventRecord(ds.last_use, st);
   return s;
+}
+
+}  // namespace
+
+extern "C" {
+
+int nrgb_project_device(const float* d_activity, const float* d_attenuation, const int* size, float* d_sinogram,
+                        const float* cameras, const int* cameras_size, const float* psf, const int* psf_size,
+                        float background, float background_attenuation, int truncate, void* stream) {
+  return project_device_call(d_activity, d_attenuation, size, d_sinogram, cameras, cameras_size, psf, psf_size,
+                             background, background_attenuation, truncate, false, stream);
+}
+
+// mode: 0 = the reference's inverse-rotation backprojector; 1 = the exact
+// transpose of the projector (for gradients).
+int nrgb_backproject_device(const float* d_sinogram, const float* d_attenuation, const int* size, float* d_out,
+                            const float* cameras, const int* cameras_size, const float* psf, const int* psf_size,
+                            float background, float background_attenuation, int truncate, int mode, void* stream) {
+  return backproject_device_call(d_sinogram, d_attenuation, size, d_out, cameras, cameras_size, psf, psf_size,
+                                 background, background_attenuation, truncate, mode, false, stream);
+}
+
+// bfloat16 activity / mu (nifti order) with float32 arithmetic and
+// Kahan-compensated depth sums; sinograms and backprojections stay float32.
+int nrgb_project_device_bf16(const void* d_activity, const void* d_attenuation, const int* size, float* d_sinogram,
+                             const float* cameras, const int* cameras_size, const float* psf, const int* psf_size,
+                             float background, float background_attenuation, int truncate, void* stream) {
+  return project_device_call(static_cast<const float*>(d_activity), static_cast<const float*>(d_attenuation), size,
+                             d_sinogram, cameras, cameras_size, psf, psf_size, background, background_attenuation,
+                             truncate, true, stream);
+}
+
+int nrgb_backproject_device_bf16(const float* d_sinogram, const void* d_attenuation, const int* size, float* d_out,
+                                 const float* cameras, const int* cameras_size, const float* psf, const int* psf_size,
+                                 float background, float background_attenuation, int truncate, int mode,
+                                 void* stream) {
+  return backproject_device_call(d_sinogram, static_cast<const float*>(d_attenuation), size, d_out, cameras,
+                                 cameras_size, psf, psf_size, background, background_attenuation, truncate, mode, true,
+                                 stream);
+}
+
+// float64 reference run: the general-orientation projector and the reference
+// backprojector with geometry, PSF and all arithmetic in double.
+int nrgb_project_device_f64(const double* d_activity, const double* d_attenuation, const int* size,
+                            double* d_sinogram, const float* cameras, const int* cameras_size, const float* psf,
+                            const int* psf_size, double background, double background_attenuation, int truncate,
+                            void* stream) {
+  if (!size || !cameras || !cameras_size || (!d_activity && !d_attenuation) || !d_sinogram) return kErrParameters;
+  Cameras cc;
+  int s = expand_cameras(cameras, cameras_size[0], cameras_size[1], size, &cc);
+  if (s != kOk) return s;
+  Problem pb;
+  s = make_problem(size[0], size[1], size[2], cc, psf, psf_size, static_cast<float>(background),
+                   static_cast<float>(background_attenuation), truncate, &pb);
+  if (s != kOk) return s;
+  DeviceState& ds = current_device_state(&s);
+  if (s != kOk) return s;
+  std::lock_guard<std::mutex> lk(ds.mu);
+  if ((s = ensure_arena(ds, workspace64(pb))) != kOk) return s;
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  cudaStreamWaitEvent(st, ds.last_use, 0);
+  g_last_path = 2;
+  s = project_device64(pb, d_activity, d_attenuation, d_sinogram, ds.arena, ds.arena_bytes, st);
+  cudaEventRecord(ds.last_use, st);
+  return s;
+}
+
+int nrgb_backproject_device_f64(const double* d_sinogram, const double* d_attenuation, const int* size,
+                                double* d_out, const float* cameras, const int* cameras_size, const float* psf,
+                                const int* psf_size, double background, double background_attenuation, int truncate,
+                                void* stream) {
+  if (!size || !cameras || !cameras_size || !d_sinogram || !d_out) return kErrParameters;
+  Cameras cc;
+  const int csz[3] = {size[0], size[1], size[0]};
+  int s = expand_cameras(cameras, cameras_size[0], cameras_size[1], csz, &cc);
+  if (s != kOk) return s;
+  Problem pb;
+  s = make_problem(size[0], size[1], size[2], cc, psf, psf_size, static_cast<float>(background),
+                   static_cast<float>(background_attenuation), truncate, &pb);
+  if (s != kOk) return s;
+  DeviceState& ds = current_device_state(&s);
+  if (s != kOk) return s;
+  std::lock_guard<std::mutex> lk(ds.mu);
+  if ((s = ensure_arena(ds, workspace64(pb))) != kOk) return s;
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  cudaStreamWaitEvent(st, ds.last_use, 0);
+  g_last_path = 2;
+  s = backproject_device64(pb, d_sinogram, d_attenuation, d_out, ds.arena, ds.arena_bytes, st);
+  cudaEventRecord(ds.last_use, st);
+  return s;
+}
+
+int nrgb_osem_ratio_device_f64(const double* d_counts, double* d_projection, long long n, double epsilon,
+                               void* stream) {
+  if (!d_counts || !d_projection || n < 0) return kErrParameters;
+  if (n == 0) return kOk;
+  return osem_ratio64(d_counts, d_projection, static_cast<size_t>(n), epsilon, static_cast<cudaStream_t>(stream));
+}
+
+int nrgb_osem_update_device_f64(double* d_activity, const double* d_numerator, const double* d_denominator,
+                                long long n, double epsilon, void* stream) {
+  if (!d_activity || !d_numerator || !d_denominator || n < 0) return kErrParameters;
+  if (n == 0) return kOk;
+  return osem_update64(d_activity, d_numerator, d_denominator, static_cast<size_t>(n), epsilon,
+                       static_cast<cudaStream_t>(stream));
 }
 
 // Exact gradient with respect to mu of sum(g * P(activity, mu)) where P is the
@@ -655,6 +771,26 @@ int nrgb_attenuation_grad_device(const float* d_grad_sinogram, const float* d_ac
   s = dmu_device(pb, d_grad_sinogram, d_activity, d_attenuation, d_out, ds.arena, ds.arena_bytes, &ds.staging, st);
   cudaEventRecord(ds.last_use, st);
   return s;
+}
+
+// The two elementwise stages of et_array_osem_step on device buffers, for
+// callers that assemble the step themselves (e.g. with partial
+// backprojections summed across processes in between):
+// ratio (emission-lib/_et_array_interface.cpp:1022-1028) overwrites the
+// projection with y / p (y / eps where p < eps); update (:1036-1044) does
+// x *= num / max(den, eps).
+int nrgb_osem_ratio_device(const float* d_counts, float* d_projection, long long n, float epsilon, void* stream) {
+  if (!d_counts || !d_projection || n < 0) return kErrParameters;
+  if (n == 0) return kOk;
+  return osem_ratio(d_counts, d_projection, static_cast<size_t>(n), epsilon, static_cast<cudaStream_t>(stream));
+}
+
+int nrgb_osem_update_device(float* d_activity, const float* d_numerator, const float* d_denominator, long long n,
+                            float epsilon, void* stream) {
+  if (!d_activity || !d_numerator || !d_denominator || n < 0) return kErrParameters;
+  if (n == 0) return kOk;
+  return osem_update(d_activity, d_numerator, d_denominator, static_cast<size_t>(n), epsilon,
+                     static_cast<cudaStream_t>(stream));
 }
 
 // Tuning table of the fused backprojector: cameras per scratch group for the

@@ -39,10 +39,13 @@ enum Layout : int { kLayoutNifti = 0, kLayoutColumn = 1 };
 // order, +theta, about the centre); bwd: the backprojector's inverse
 // resampling matrix (ZYX order, -theta).  Row-major 3x4: p_i = m[4i+0]*x +
 // m[4i+1]*y + m[4i+2]*z + m[4i+3].
-struct CamGeom {
-  float fwd[12];
-  float bwd[12];
+template <class T>
+struct CamGeomT {
+  T fwd[12];
+  T bwd[12];
 };
+using CamGeom = CamGeomT<float>;
+using CamGeom64 = CamGeomT<double>;  // geometry of the float64 reference path
 
 // Backprojector variants.
 //  kBackReference: the reference's inverse-rotation gather
@@ -50,6 +53,14 @@ struct CamGeom {
 //  kBackAdjoint  : exact transpose of the projector (transposed PSF and
 //                  transposed trilinear interpolation); not in the reference.
 enum BackMode : int { kBackReference = 0, kBackAdjoint = 1 };
+
+// Storage type of the volumes the fused kernels sample (activity, mu).
+//  kStorageF32 : float32, the reference's type.
+//  kStorageBF16: bfloat16 (half the bytes), widened exactly to float32 on
+//                load; all arithmetic stays float32 and the depth sums (the
+//                transmission prefix and the projection) are
+//                Kahan-compensated.
+enum Storage : int { kStorageF32 = 0, kStorageBF16 = 1 };
 
 inline int round_up(int v, int m) { return (v + m - 1) / m * m; }
 

@@ -55,6 +55,7 @@ int make_problem(int nx, int ny, int nz, const Cameras& cams, const float* psf, 
     if (kx % 2 != 1 || ky % 2 != 1 || kx != ky || planes < nz) return kErrParameters;
     pb.psf_k = kx;
     pb.psf_sep = separate_psf(psf, kx, nz);
+    pb.psf_host = psf;
   }
   *out = std::move(pb);
   return kOk;
@@ -143,6 +144,24 @@ int check(int status) {
   return cudaGetLastError() == cudaSuccess ? kOk : kErrKernel;
 }
 
+// float32 copies of bfloat16 inputs for the general-orientation path
+size_t widen_bytes(const Problem& pb) { return pb.input_bf16 ? 2 * (sizeof(float) * vol_n(pb) + 256) : 0; }
+
+// Widen the caller's bfloat16 activity / mu (nifti order) into float32 work
+// volumes; the pointers are replaced by the copies.
+int widen_inputs(const Problem& pb, Carver& cv, const float** act, const float** att, cudaStream_t st) {
+  const float** ps[2] = {act, att};
+  for (const float** p : ps) {
+    if (!p || !*p) continue;
+    float* w = cv.take<float>(vol_n(pb));
+    if (!w) return kErrAllocGpu;
+    int s = from_bf16(*p, w, vol_n(pb), st);
+    if (s != kOk) return s;
+    *p = w;
+  }
+  return kOk;
+}
+
 }  // namespace
 
 size_t project_workspace(const Problem& pb, bool has_act, bool has_att) {
@@ -150,7 +169,7 @@ size_t project_workspace(const Problem& pb, bool has_act, bool has_att) {
   if (use_fused(pb) && has_act)
     b += sizeof(float) * (col_n(pb) * (has_att ? 2 : 1) + sino_col_n(pb));
   else
-    b += sizeof(float) * vol_n(pb) * 3;
+    b += sizeof(float) * vol_n(pb) * 3 + widen_bytes(pb);
   return b;
 }
 
@@ -160,11 +179,25 @@ size_t backproject_workspace(const Problem& pb, bool has_att) {
     b += sizeof(float) * (col_n(pb) * (has_att ? 2 : 1) + sino_col_n(pb)) +
          yg_backproject_workspace(pb.nx, std::min(pb.ny, kWindowRows), pb.nz, pb.cams.n, pb.group) + kSlack;
   else
-    b += sizeof(float) * vol_n(pb) * 3;
+    b += sizeof(float) * vol_n(pb) * 3 + widen_bytes(pb);
   return b;
 }
 
 size_t gradient_workspace(const Problem& pb) { return common_bytes(pb) + sizeof(float) * vol_n(pb) * 3; }
+
+namespace {
+
+// One row window of a caller volume (nifti, float32 or bfloat16) into the
+// fused kernels' column buffer in the problem's storage type.
+int stage_column(const Problem& pb, const float* src, float* dst, const YWindow& w, int cy, int planes,
+                 cudaStream_t st) {
+  if (pb.storage == kStorageBF16)
+    return to_column_rows_bf16(pb.input_bf16 ? nullptr : src, pb.input_bf16 ? src : nullptr, dst, pb.nx, pb.ny,
+                               w.in0, w.rows, cy, planes, st);
+  return to_column_rows(src, dst, pb.nx, pb.ny, w.in0, w.rows, cy, planes, st);
+}
+
+}  // namespace
 
 int project_device(const Problem& pb, const float* d_act, const float* d_att, float* d_sino, char* ws,
                    size_t ws_bytes, Staging* stg, cudaStream_t st) {
@@ -180,9 +213,10 @@ int project_device(const Problem& pb, const float* d_act, const float* d_att, fl
     if (!act_c || !sino_c || (d_att && !mu_c)) return kErrAllocGpu;
     for (const YWindow& w : y_windows(pb.ny, pb.psf_k / 2)) {
       const int cy = round_up(w.rows, 4);
-      if ((s = to_column_rows(d_act, act_c, pb.nx, pb.ny, w.in0, w.rows, cy, pb.nz, st)) != kOk) return s;
-      if (d_att && (s = to_column_rows(d_att, mu_c, pb.nx, pb.ny, w.in0, w.rows, cy, pb.nz, st)) != kOk) return s;
+      if ((s = stage_column(pb, d_act, act_c, w, cy, pb.nz, st)) != kOk) return s;
+      if (d_att && (s = stage_column(pb, d_att, mu_c, w, cy, pb.nz, st)) != kOk) return s;
       YgArgs a;
+      a.storage = pb.storage;
       a.nx = pb.nx;
       a.ny = w.rows;
       a.nz = pb.nz;
@@ -202,6 +236,7 @@ int project_device(const Problem& pb, const float* d_act, const float* d_att, fl
     }
     return check(kOk);
   }
+  if (pb.input_bf16 && (s = widen_inputs(pb, cv, &d_act, &d_att, st)) != kOk) return s;
   GeneralArgs g;
   g.nx = pb.nx;
   g.ny = pb.ny;
@@ -241,8 +276,9 @@ int backproject_device(const Problem& pb, const float* d_sino, const float* d_at
     for (const YWindow& w : y_windows(pb.ny, pb.psf_k / 2)) {
       const int cy = round_up(w.rows, 4);
       if ((s = to_column_rows(d_sino, sino_c, pb.nx, pb.ny, w.in0, w.rows, cy, pb.cams.n, st)) != kOk) return s;
-      if (d_att && (s = to_column_rows(d_att, mu_c, pb.nx, pb.ny, w.in0, w.rows, cy, pb.nz, st)) != kOk) return s;
+      if (d_att && (s = stage_column(pb, d_att, mu_c, w, cy, pb.nz, st)) != kOk) return s;
       YgArgs a;
+      a.storage = pb.storage;
       a.nx = pb.nx;
       a.ny = w.rows;
       a.nz = pb.nz;
@@ -265,6 +301,7 @@ int backproject_device(const Problem& pb, const float* d_sino, const float* d_at
     }
     return check(kOk);
   }
+  if (pb.input_bf16 && (s = widen_inputs(pb, cv, nullptr, &d_att, st)) != kOk) return s;
   GeneralArgs g;
   g.nx = pb.nx;
   g.ny = pb.ny;
@@ -341,6 +378,70 @@ int gradient_device(const Problem& pb, const float* d_sino, const float* d_act, 
   g.ws_tmp = cv.take<float>(vol_n(pb));
   if (!g.ws_act || !g.ws_att || !g.ws_tmp) return kErrAllocGpu;
   return check(general_gradient(g, st));
+}
+
+// ------------------------------------------------------------ float64 run
+size_t workspace64(const Problem& pb) {
+  return sizeof(double) * (3 * vol_n(pb) + static_cast<size_t>(2 * pb.psf_k) * pb.nz) + kSlack;
+}
+
+namespace {
+
+// Fills the float64 arguments: double geometry and separated PSF (uploaded
+// from a host vector that the synchronous pageable copy has consumed when
+// cudaMemcpyAsync returns), three work volumes.
+int setup64(const Problem& pb, const float* psf_host, Carver& cv, std::vector<CamGeom64>* geom, GeneralArgs64* g,
+            cudaStream_t st) {
+  *geom = camera_geometry64(pb.cams);
+  g->nx = pb.nx;
+  g->ny = pb.ny;
+  g->nz = pb.nz;
+  g->ncam = pb.cams.n;
+  g->geom_host = geom->data();
+  g->psf_k = pb.psf_k;
+  g->bg = pb.bg;
+  g->bg_att = pb.bg_att;
+  g->truncate = pb.truncate;
+  if (pb.psf_k) {
+    const std::vector<double> sep = separate_psf64(psf_host, pb.psf_k, pb.nz);
+    double* d = cv.take<double>(sep.size());
+    if (!d) return kErrAllocGpu;
+    if (cudaMemcpyAsync(d, sep.data(), sizeof(double) * sep.size(), cudaMemcpyHostToDevice, st) != cudaSuccess)
+      return kErrTransferGpu;
+    g->psf_sep = d;
+  }
+  g->ws_act = cv.take<double>(vol_n(pb));
+  g->ws_att = cv.take<double>(vol_n(pb));
+  g->ws_tmp = cv.take<double>(vol_n(pb));
+  return (g->ws_act && g->ws_att && g->ws_tmp) ? kOk : kErrAllocGpu;
+}
+
+}  // namespace
+
+int project_device64(const Problem& pb, const double* d_act, const double* d_att, double* d_sino, char* ws,
+                     size_t ws_bytes, cudaStream_t st) {
+  Carver cv(ws, ws_bytes);
+  std::vector<CamGeom64> geom;
+  GeneralArgs64 g;
+  int s = setup64(pb, pb.psf_host, cv, &geom, &g, st);
+  if (s != kOk) return s;
+  g.act = d_act;
+  g.att = d_att;
+  g.out = d_sino;
+  return check(general_project64(g, st));
+}
+
+int backproject_device64(const Problem& pb, const double* d_sino, const double* d_att, double* d_out, char* ws,
+                         size_t ws_bytes, cudaStream_t st) {
+  Carver cv(ws, ws_bytes);
+  std::vector<CamGeom64> geom;
+  GeneralArgs64 g;
+  int s = setup64(pb, pb.psf_host, cv, &geom, &g, st);
+  if (s != kOk) return s;
+  g.att = d_att;
+  g.sino = d_sino;
+  g.out = d_out;
+  return check(general_backproject64(g, st));
 }
 
 // ------------------------------------------------------------ device state

@@ -20,10 +20,17 @@ struct Problem {
   bool ygantry = false;
   int psf_k = 0;               // 0: no PSF
   std::vector<float> psf_sep;  // [nz][2k]
+  const float* psf_host = nullptr;  // the caller's PSF, valid during the call only
   float bg = 0.0f, bg_att = 0.0f;
   int truncate = 0;
   int back_mode = kBackReference;
   int group = 8;  // cameras per backprojection scratch group
+  // Storage of the sampled volumes inside the fused kernels, and whether the
+  // caller's activity / mu buffers are bfloat16 (nifti order) rather than
+  // float32.  bfloat16 inputs imply bfloat16 storage; the general-orientation
+  // path widens them to float32 first.
+  int storage = kStorageF32;
+  bool input_bf16 = false;
 };
 
 // Build a Problem; psf may be null.  psf_size = {kx, ky, planes}.  Returns
@@ -112,6 +119,14 @@ int backproject_device(const Problem& pb, const float* d_sino, const float* d_at
                        size_t ws_bytes, Staging* stg, cudaStream_t st);
 int gradient_device(const Problem& pb, const float* d_sino, const float* d_act, const float* d_att, float* d_out,
                     char* ws, size_t ws_bytes, Staging* stg, cudaStream_t st);
+// float64 reference run of the general-orientation projector and the
+// reference backprojector (geometry, PSF and every operation in double);
+// device buffers are double, nifti order.
+size_t workspace64(const Problem& pb);
+int project_device64(const Problem& pb, const double* d_act, const double* d_att, double* d_sino, char* ws,
+                     size_t ws_bytes, cudaStream_t st);
+int backproject_device64(const Problem& pb, const double* d_sino, const double* d_att, double* d_out, char* ws,
+                         size_t ws_bytes, cudaStream_t st);
 // Exact d/dmu of sum(g * project(act, mu)) (g = d_sino); work space as
 // gradient_workspace.
 int dmu_device(const Problem& pb, const float* d_g, const float* d_act, const float* d_att, float* d_out, char* ws,

@@ -11,51 +11,64 @@ namespace nrgb {
 
 namespace {
 
-struct Affine34 {
-  float m[12];
+template <class T>
+struct Affine34T {
+  T m[12];
 };
+using Affine34 = Affine34T<float>;
 
+// Separately rounded arithmetic in the working type (float: the reference's
+// type; double: the float64 reference path).
 __device__ __forceinline__ float fm(float a, float b) { return __fmul_rn(a, b); }
 __device__ __forceinline__ float fa(float a, float b) { return __fadd_rn(a, b); }
+__device__ __forceinline__ float fs(float a, float b) { return __fsub_rn(a, b); }
+__device__ __forceinline__ double fm(double a, double b) { return __dmul_rn(a, b); }
+__device__ __forceinline__ double fa(double a, double b) { return __dadd_rn(a, b); }
+__device__ __forceinline__ double fs(double a, double b) { return __dsub_rn(a, b); }
+__device__ __forceinline__ float flo(float v) { return floorf(v); }
+__device__ __forceinline__ double flo(double v) { return floor(v); }
+__device__ __forceinline__ float ex(float v) { return expf(v); }
+__device__ __forceinline__ double ex(double v) { return exp(v); }
 
 // Trilinear resampling of one voxel, reg-lib/_reg_resampling.cpp:334-450
 // (positions from reg-lib/_reg_affineTransformation.cpp:116-132 with an
 // identity voxel-to-world matrix).  With bg != 0 every neighbour outside the
 // grid adds bg * xBasis[.] to a separate background weight, as the reference
 // does (:366-396).
-__device__ __forceinline__ float trilinear_ref(const float* __restrict__ src, int nx, int ny, int nz,
-                                               const Affine34& A, int x, int y, int z, float bg) {
-  const float fx = static_cast<float>(x), fy = static_cast<float>(y), fz = static_cast<float>(z);
-  float pos[3];
+template <class T>
+__device__ __forceinline__ T trilinear_ref(const T* __restrict__ src, int nx, int ny, int nz, const Affine34T<T>& A,
+                                           int x, int y, int z, T bg) {
+  const T fx = static_cast<T>(x), fy = static_cast<T>(y), fz = static_cast<T>(z);
+  T pos[3];
 #pragma unroll
   for (int i = 0; i < 3; ++i)
     pos[i] = fa(fa(fa(fm(A.m[4 * i + 0], fx), fm(A.m[4 * i + 1], fy)), fm(A.m[4 * i + 2], fz)), A.m[4 * i + 3]);
   int prev[3];
-  float b0[3], b1[3];
+  T b0[3], b1[3];
 #pragma unroll
   for (int i = 0; i < 3; ++i) {
-    prev[i] = static_cast<int>(floorf(pos[i]));
-    float rel = __fsub_rn(pos[i], static_cast<float>(prev[i]));
-    if (rel < 0.0f) rel = 0.0f;
-    b0[i] = __fsub_rn(1.0f, rel);
+    prev[i] = static_cast<int>(flo(pos[i]));
+    T rel = fs(pos[i], static_cast<T>(prev[i]));
+    if (rel < T(0)) rel = T(0);
+    b0[i] = fs(T(1), rel);
     b1[i] = rel;
   }
-  const float bx[2] = {b0[0], b1[0]};
-  const float by[2] = {b0[1], b1[1]};
-  const float bz[2] = {b0[2], b1[2]};
-  float val = 0.0f, bgw = 0.0f;
-  const bool use_bg = (bg != 0.0f);
+  const T bx[2] = {b0[0], b1[0]};
+  const T by[2] = {b0[1], b1[1]};
+  const T bz[2] = {b0[2], b1[2]};
+  T val = T(0), bgw = T(0);
+  const bool use_bg = (bg != T(0));
 #pragma unroll
   for (int c = 0; c < 2; ++c) {
     const int Z = prev[2] + c;
     if (Z >= 0 && Z < nz) {
-      float ysum = 0.0f;
+      T ysum = T(0);
 #pragma unroll
       for (int b = 0; b < 2; ++b) {
         const int Y = prev[1] + b;
         if (Y >= 0 && Y < ny) {
-          const float* row = src + (static_cast<size_t>(Z) * ny + Y) * nx;
-          float xsum = 0.0f;
+          const T* row = src + (static_cast<size_t>(Z) * ny + Y) * nx;
+          T xsum = T(0);
 #pragma unroll
           for (int a = 0; a < 2; ++a) {
             const int X = prev[0] + a;
@@ -78,16 +91,16 @@ __device__ __forceinline__ float trilinear_ref(const float* __restrict__ src, in
   return val;
 }
 
-template <bool ACCUM>
-__global__ void k_resample(const float* __restrict__ src, float* __restrict__ dst, int nx, int ny, int nz,
-                           Affine34 A, float bg) {
+template <bool ACCUM, class T = float>
+__global__ void k_resample(const T* __restrict__ src, T* __restrict__ dst, int nx, int ny, int nz, Affine34T<T> A,
+                           T bg) {
   const size_t nvox = static_cast<size_t>(nx) * ny * nz;
   for (size_t i = blockIdx.x * static_cast<size_t>(blockDim.x) + threadIdx.x; i < nvox;
        i += static_cast<size_t>(gridDim.x) * blockDim.x) {
     const int x = static_cast<int>(i % nx);
     const int y = static_cast<int>((i / nx) % ny);
     const int z = static_cast<int>(i / (static_cast<size_t>(nx) * ny));
-    const float v = trilinear_ref(src, nx, ny, nz, A, x, y, z, bg);
+    const T v = trilinear_ref<T>(src, nx, ny, nz, A, x, y, z, bg);
     if (ACCUM)
       dst[i] = fa(dst[i], v);
     else
@@ -148,9 +161,9 @@ __global__ void k_scatter(const float* __restrict__ src, float* __restrict__ dst
 // true convolution (kernel index R-k), zero outside the plane, plane z uses
 // kernel plane z.  sep layout [plane][row k | column k].  FLIP: correlation
 // (kernel index R+k), the transpose of the convolution.
-template <bool ROWS, bool FLIP = false>
-__global__ void k_conv(const float* __restrict__ in, float* __restrict__ out, int nx, int ny, int nz,
-                       const float* __restrict__ sep, int k) {
+template <bool ROWS, bool FLIP = false, class T = float>
+__global__ void k_conv(const T* __restrict__ in, T* __restrict__ out, int nx, int ny, int nz, const T* __restrict__ sep,
+                       int k) {
   const size_t nvox = static_cast<size_t>(nx) * ny * nz;
   const int R = (k - 1) / 2;
   for (size_t i = blockIdx.x * static_cast<size_t>(blockDim.x) + threadIdx.x; i < nvox;
@@ -158,8 +171,8 @@ __global__ void k_conv(const float* __restrict__ in, float* __restrict__ out, in
     const int x = static_cast<int>(i % nx);
     const int y = static_cast<int>((i / nx) % ny);
     const int z = static_cast<int>(i / (static_cast<size_t>(nx) * ny));
-    const float* K = sep + static_cast<size_t>(2 * k) * z + (ROWS ? 0 : k);
-    float s = 0.0f;
+    const T* K = sep + static_cast<size_t>(2 * k) * z + (ROWS ? 0 : k);
+    T s = T(0);
     for (int kk = -R; kk <= R; ++kk) {
       if (ROWS) {
         const int d = x + kk;
@@ -175,46 +188,55 @@ __global__ void k_conv(const float* __restrict__ in, float* __restrict__ out, in
 }
 
 // Attenuated line integral along z, emission-lib/_et_line_integral_attenuated.cpp:14-68.
-__global__ void k_line_integral(const float* __restrict__ act, const float* __restrict__ att,
-                                float* __restrict__ out, int nx, int ny, int nz, float bg) {
+template <class R = float>
+__global__ void k_line_integral(const R* __restrict__ act, const R* __restrict__ att, R* __restrict__ out, int nx,
+                                int ny, int nz, R bg) {
   const int nxy = nx * ny;
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= nxy) return;
-  float p = 0.0f, T = 0.0f;
+  R p = R(0), T = R(0);
   if (act && att) {
     for (int z = 0; z < nz; ++z) {
       T = fa(T, __ldg(att + static_cast<size_t>(z) * nxy + i));
-      p = fa(p, fm(__ldg(act + static_cast<size_t>(z) * nxy + i), expf(-T)));
+      p = fa(p, fm(__ldg(act + static_cast<size_t>(z) * nxy + i), ex(-T)));
     }
-    p = fa(p, fm(bg, expf(-T)));
+    p = fa(p, fm(bg, ex(-T)));
   } else if (act) {
     for (int z = 0; z < nz; ++z) p = fa(p, __ldg(act + static_cast<size_t>(z) * nxy + i));
     p = fa(p, bg);
   } else {
     for (int z = 0; z < nz; ++z) T = fa(T, __ldg(att + static_cast<size_t>(z) * nxy + i));
-    p = fm(bg, expf(-T));
+    p = fm(bg, ex(-T));
   }
   out[i] = p;
 }
 
 // Spread along z, emission-lib/_et_line_backproject_attenuated.cpp:17-36 and
 // emission-lib/_et_line_backproject.cpp:17-30.
-__global__ void k_spread(const float* __restrict__ plane, const float* __restrict__ att, float* __restrict__ vol,
-                         int nx, int ny, int nz) {
+template <class R = float>
+__global__ void k_spread(const R* __restrict__ plane, const R* __restrict__ att, R* __restrict__ vol, int nx, int ny,
+                         int nz) {
   const int nxy = nx * ny;
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= nxy) return;
-  const float s = __ldg(plane + i);
-  float T = 0.0f;
+  const R s = __ldg(plane + i);
+  R T = R(0);
   for (int z = 0; z < nz; ++z) {
     const size_t j = static_cast<size_t>(z) * nxy + i;
     if (att) {
       T = fa(T, __ldg(att + j));
-      vol[j] = fm(s, expf(-T));
+      vol[j] = fm(s, ex(-T));
     } else {
       vol[j] = s;
     }
   }
+}
+
+template <class R>
+__global__ void k_truncate_t(R* __restrict__ buf, size_t n) {
+  for (size_t i = blockIdx.x * static_cast<size_t>(blockDim.x) + threadIdx.x; i < n;
+       i += static_cast<size_t>(gridDim.x) * blockDim.x)
+    if (buf[i] < R(0)) buf[i] = R(0);
 }
 
 // Attenuation-gradient scan, emission-lib_gpu/_et_attenuation_gradient_gpu_kernels.cu:24-39:
@@ -276,54 +298,72 @@ int grid_for(size_t n, int block) {
   return static_cast<int>(g < 152 * 64 ? g : 152 * 64);
 }
 
-Affine34 affine_of(const float* m12) {
-  Affine34 a;
+template <class T>
+Affine34T<T> affine_of(const T* m12) {
+  Affine34T<T> a;
   for (int i = 0; i < 12; ++i) a.m[i] = m12[i];
   return a;
 }
 
-}  // namespace
+template <class T>
+void launch_truncate_t(T* buf, size_t n, cudaStream_t st) {
+  NRGB_LAUNCH_SCOPE("k_truncate", st);
+  k_truncate_t<T><<<grid_for(n, 256), 256, 0, st>>>(buf, n);
+}
 
-int general_project(const GeneralArgs& a, cudaStream_t st) {
+// et_project (emission-lib/_et.cpp:218-281): per camera rotate activity and
+// mu, PSF, attenuated line integral; truncation at the end (:283-292).
+template <class T>
+int general_project_t(const GeneralArgsT<T>& a, cudaStream_t st) {
   const int nx = a.nx, ny = a.ny, nz = a.nz;
   const size_t nvox = static_cast<size_t>(nx) * ny * nz, nxy = static_cast<size_t>(nx) * ny;
   const int B = 256;
   for (int cam = 0; cam < a.ncam; ++cam) {
-    const Affine34 F = affine_of(a.geom_host[cam].fwd);
-    if (a.act) { NRGB_LAUNCH_SCOPE("k_resample", st); k_resample<false><<<grid_for(nvox, B), B, 0, st>>>(a.act, a.ws_act, nx, ny, nz, F, a.bg); }
-    if (a.att) { NRGB_LAUNCH_SCOPE("k_resample", st); k_resample<false><<<grid_for(nvox, B), B, 0, st>>>(a.att, a.ws_att, nx, ny, nz, F, a.bg_att); }
+    const Affine34T<T> F = affine_of<T>(a.geom_host[cam].fwd);
+    if (a.act) { NRGB_LAUNCH_SCOPE("k_resample", st); k_resample<false, T><<<grid_for(nvox, B), B, 0, st>>>(a.act, a.ws_act, nx, ny, nz, F, a.bg); }
+    if (a.att) { NRGB_LAUNCH_SCOPE("k_resample", st); k_resample<false, T><<<grid_for(nvox, B), B, 0, st>>>(a.att, a.ws_att, nx, ny, nz, F, a.bg_att); }
     if (a.psf_sep && a.act) {
-      { NRGB_LAUNCH_SCOPE("k_conv", st); k_conv<true><<<grid_for(nvox, B), B, 0, st>>>(a.ws_act, a.ws_tmp, nx, ny, nz, a.psf_sep, a.psf_k); }
-      { NRGB_LAUNCH_SCOPE("k_conv", st); k_conv<false><<<grid_for(nvox, B), B, 0, st>>>(a.ws_tmp, a.ws_act, nx, ny, nz, a.psf_sep, a.psf_k); }
+      { NRGB_LAUNCH_SCOPE("k_conv", st); k_conv<true, false, T><<<grid_for(nvox, B), B, 0, st>>>(a.ws_act, a.ws_tmp, nx, ny, nz, a.psf_sep, a.psf_k); }
+      { NRGB_LAUNCH_SCOPE("k_conv", st); k_conv<false, false, T><<<grid_for(nvox, B), B, 0, st>>>(a.ws_tmp, a.ws_act, nx, ny, nz, a.psf_sep, a.psf_k); }
     }
-    { NRGB_LAUNCH_SCOPE("k_line_integral", st); k_line_integral<<<static_cast<int>((nxy + B - 1) / B), B, 0, st>>>(a.act ? a.ws_act : nullptr,
+    { NRGB_LAUNCH_SCOPE("k_line_integral", st); k_line_integral<T><<<static_cast<int>((nxy + B - 1) / B), B, 0, st>>>(a.act ? a.ws_act : nullptr,
                                                                       a.att ? a.ws_att : nullptr,
                                                                       a.out + nxy * cam, nx, ny, nz, a.bg); }
   }
-  if (a.truncate) launch_truncate(a.out, nxy * a.ncam, st);
+  if (a.truncate) launch_truncate_t<T>(a.out, nxy * a.ncam, st);
   return cudaGetLastError() == cudaSuccess ? kOk : kErrKernel;
 }
 
-int general_backproject(const GeneralArgs& a, cudaStream_t st) {
+// et_backproject (emission-lib/_et.cpp:415-499): per camera rotate mu, spread
+// the attenuated plane, PSF, rotate back with the inverse matrix, accumulate.
+template <class T>
+int general_backproject_t(const GeneralArgsT<T>& a, cudaStream_t st) {
   const int nx = a.nx, ny = a.ny, nz = a.nz;
   const size_t nvox = static_cast<size_t>(nx) * ny * nz, nxy = static_cast<size_t>(nx) * ny;
   const int B = 256;
-  cudaMemsetAsync(a.out, 0, nvox * sizeof(float), st);
+  cudaMemsetAsync(a.out, 0, nvox * sizeof(T), st);
   for (int cam = 0; cam < a.ncam; ++cam) {
-    const Affine34 F = affine_of(a.geom_host[cam].fwd);
-    const Affine34 Bk = affine_of(a.geom_host[cam].bwd);
-    if (a.att) { NRGB_LAUNCH_SCOPE("k_resample", st); k_resample<false><<<grid_for(nvox, B), B, 0, st>>>(a.att, a.ws_att, nx, ny, nz, F, a.bg_att); }
-    { NRGB_LAUNCH_SCOPE("k_spread", st); k_spread<<<static_cast<int>((nxy + B - 1) / B), B, 0, st>>>(a.sino + nxy * cam, a.att ? a.ws_att : nullptr,
+    const Affine34T<T> F = affine_of<T>(a.geom_host[cam].fwd);
+    const Affine34T<T> Bk = affine_of<T>(a.geom_host[cam].bwd);
+    if (a.att) { NRGB_LAUNCH_SCOPE("k_resample", st); k_resample<false, T><<<grid_for(nvox, B), B, 0, st>>>(a.att, a.ws_att, nx, ny, nz, F, a.bg_att); }
+    { NRGB_LAUNCH_SCOPE("k_spread", st); k_spread<T><<<static_cast<int>((nxy + B - 1) / B), B, 0, st>>>(a.sino + nxy * cam, a.att ? a.ws_att : nullptr,
                                                                a.ws_act, nx, ny, nz); }
     if (a.psf_sep) {
-      { NRGB_LAUNCH_SCOPE("k_conv", st); k_conv<true><<<grid_for(nvox, B), B, 0, st>>>(a.ws_act, a.ws_tmp, nx, ny, nz, a.psf_sep, a.psf_k); }
-      { NRGB_LAUNCH_SCOPE("k_conv", st); k_conv<false><<<grid_for(nvox, B), B, 0, st>>>(a.ws_tmp, a.ws_act, nx, ny, nz, a.psf_sep, a.psf_k); }
+      { NRGB_LAUNCH_SCOPE("k_conv", st); k_conv<true, false, T><<<grid_for(nvox, B), B, 0, st>>>(a.ws_act, a.ws_tmp, nx, ny, nz, a.psf_sep, a.psf_k); }
+      { NRGB_LAUNCH_SCOPE("k_conv", st); k_conv<false, false, T><<<grid_for(nvox, B), B, 0, st>>>(a.ws_tmp, a.ws_act, nx, ny, nz, a.psf_sep, a.psf_k); }
     }
-    { NRGB_LAUNCH_SCOPE("k_resample", st); k_resample<true><<<grid_for(nvox, B), B, 0, st>>>(a.ws_act, a.out, nx, ny, nz, Bk, a.bg); }
+    { NRGB_LAUNCH_SCOPE("k_resample", st); k_resample<true, T><<<grid_for(nvox, B), B, 0, st>>>(a.ws_act, a.out, nx, ny, nz, Bk, a.bg); }
   }
-  if (a.truncate) launch_truncate(a.out, nvox, st);
+  if (a.truncate) launch_truncate_t<T>(a.out, nvox, st);
   return cudaGetLastError() == cudaSuccess ? kOk : kErrKernel;
 }
+
+}  // namespace
+
+int general_project(const GeneralArgs& a, cudaStream_t st) { return general_project_t<float>(a, st); }
+int general_backproject(const GeneralArgs& a, cudaStream_t st) { return general_backproject_t<float>(a, st); }
+int general_project64(const GeneralArgs64& a, cudaStream_t st) { return general_project_t<double>(a, st); }
+int general_backproject64(const GeneralArgs64& a, cudaStream_t st) { return general_backproject_t<double>(a, st); }
 
 // Exact transpose of general_project for fixed mu (bg terms dropped: the
 // transpose of the projector's linear part): spread, transposed PSF

@@ -10,11 +10,12 @@ namespace nrgb {
 namespace {
 
 // C = A * B, 4x4 row-major, each entry ((a0*b0 + a1*b1) + a2*b2) + a3*b3.
-void mul44(const float* A, const float* B, float* C) {
-  float t[16];
+template <class T>
+void mul44(const T* A, const T* B, T* C) {
+  T t[16];
   for (int i = 0; i < 4; ++i)
     for (int j = 0; j < 4; ++j) {
-      float s = A[4 * i + 0] * B[j];
+      T s = A[4 * i + 0] * B[j];
       s = s + A[4 * i + 1] * B[4 + j];
       s = s + A[4 * i + 2] * B[8 + j];
       s = s + A[4 * i + 3] * B[12 + j];
@@ -25,25 +26,30 @@ void mul44(const float* A, const float* B, float* C) {
 
 }  // namespace
 
-void rotation_matrix(float M[16], float tx, float ty, float tz, float cx, float cy, float cz, int axis_order) {
-  const float sx = std::sin(tx), cxs = std::cos(tx);
-  const float sy = std::sin(ty), cys = std::cos(ty);
-  const float sz = std::sin(tz), czs = std::cos(tz);
-  const float Rx[16] = {1, 0, 0, 0, 0, cxs, -sx, 0, 0, sx, cxs, 0, 0, 0, 0, 1};
-  const float Ry[16] = {cys, 0, sy, 0, 0, 1, 0, 0, -sy, 0, cys, 0, 0, 0, 0, 1};
-  const float Rz[16] = {czs, -sz, 0, 0, sz, czs, 0, 0, 0, 0, 1, 0, 0, 0, 0, 1};
-  const float T[16] = {0, 0, 0, cx, 0, 0, 0, cy, 0, 0, 0, cz, 0, 0, 0, 1};
+template <class T>
+void rotation_matrix_t(T M[16], T tx, T ty, T tz, T cx, T cy, T cz, int axis_order) {
+  const T sx = std::sin(tx), cxs = std::cos(tx);
+  const T sy = std::sin(ty), cys = std::cos(ty);
+  const T sz = std::sin(tz), czs = std::cos(tz);
+  const T Rx[16] = {1, 0, 0, 0, 0, cxs, -sx, 0, 0, sx, cxs, 0, 0, 0, 0, 1};
+  const T Ry[16] = {cys, 0, sy, 0, 0, 1, 0, 0, -sy, 0, cys, 0, 0, 0, 0, 1};
+  const T Rz[16] = {czs, -sz, 0, 0, sz, czs, 0, 0, 0, 0, 1, 0, 0, 0, 0, 1};
+  const T Tr[16] = {0, 0, 0, cx, 0, 0, 0, cy, 0, 0, 0, cz, 0, 0, 0, 1};
   // The first-applied rotation is the innermost factor: order "ABC" = C*(B*A).
-  const float* order[6][3] = {{Rx, Ry, Rz}, {Rx, Rz, Ry}, {Ry, Rx, Rz},
-                              {Ry, Rz, Rx}, {Rz, Rx, Ry}, {Rz, Ry, Rx}};
+  const T* order[6][3] = {{Rx, Ry, Rz}, {Rx, Rz, Ry}, {Ry, Rx, Rz},
+                          {Ry, Rz, Rx}, {Rz, Rx, Ry}, {Rz, Ry, Rx}};
   const int o = (axis_order >= 0 && axis_order < 6) ? axis_order : 0;
-  float P[16], RT[16];
+  T P[16], RT[16];
   mul44(order[o][1], order[o][0], P);
   mul44(order[o][2], P, M);
-  mul44(M, T, RT);
+  mul44(M, Tr, RT);
   M[3] = cx - RT[3];
   M[7] = cy - RT[7];
   M[11] = cz - RT[11];
+}
+
+void rotation_matrix(float M[16], float tx, float ty, float tz, float cx, float cy, float cz, int axis_order) {
+  rotation_matrix_t<float>(M, tx, ty, tz, cx, cy, cz, axis_order);
 }
 
 int expand_cameras(const float* cameras, int n, int ncols, const int center_size[3], Cameras* out) {
@@ -67,20 +73,24 @@ int expand_cameras(const float* cameras, int n, int ncols, const int center_size
   return kOk;
 }
 
-std::vector<CamGeom> camera_geometry(const Cameras& cams) {
-  std::vector<CamGeom> g(cams.n);
+template <class T>
+std::vector<CamGeomT<T>> camera_geometry_t(const Cameras& cams) {
+  std::vector<CamGeomT<T>> g(cams.n);
   const int n = cams.n;
   for (int c = 0; c < n; ++c) {
-    const float tx = cams.angles[c], ty = cams.angles[n + c], tz = cams.angles[2 * n + c];
-    const float cx = cams.centers[c], cy = cams.centers[n + c], cz = cams.centers[2 * n + c];
-    float M[16];
-    rotation_matrix(M, tx, ty, tz, cx, cy, cz, 0);
-    std::memcpy(g[c].fwd, M, sizeof(float) * 12);
-    rotation_matrix(M, -tx, -ty, -tz, cx, cy, cz, 5);
-    std::memcpy(g[c].bwd, M, sizeof(float) * 12);
+    const T tx = cams.angles[c], ty = cams.angles[n + c], tz = cams.angles[2 * n + c];
+    const T cx = cams.centers[c], cy = cams.centers[n + c], cz = cams.centers[2 * n + c];
+    T M[16];
+    rotation_matrix_t<T>(M, tx, ty, tz, cx, cy, cz, 0);
+    std::memcpy(g[c].fwd, M, sizeof(T) * 12);
+    rotation_matrix_t<T>(M, -tx, -ty, -tz, cx, cy, cz, 5);
+    std::memcpy(g[c].bwd, M, sizeof(T) * 12);
   }
   return g;
 }
+
+std::vector<CamGeom> camera_geometry(const Cameras& cams) { return camera_geometry_t<float>(cams); }
+std::vector<CamGeom64> camera_geometry64(const Cameras& cams) { return camera_geometry_t<double>(cams); }
 
 bool is_y_gantry(const Cameras& cams) {
   for (int c = 0; c < cams.n; ++c)
@@ -88,18 +98,24 @@ bool is_y_gantry(const Cameras& cams) {
   return true;
 }
 
-std::vector<float> separate_psf(const float* psf, int k, int nplanes) {
-  std::vector<float> sep(static_cast<size_t>(2 * k) * nplanes);
+template <class T>
+std::vector<T> separate_psf_t(const float* psf, int k, int nplanes) {
+  std::vector<T> sep(static_cast<size_t>(2 * k) * nplanes);
   const int c = (k - 1) / 2;
   for (int n = 0; n < nplanes; ++n) {
     const float* plane = psf + static_cast<size_t>(k) * k * n;
-    const float norm = plane[c * k + c];
+    const T norm = plane[c * k + c];
     for (int i = 0; i < k; ++i) {
       sep[static_cast<size_t>(2 * k) * n + i] = plane[c * k + i];
-      sep[static_cast<size_t>(2 * k) * n + k + i] = plane[c + i * k] / norm;
+      sep[static_cast<size_t>(2 * k) * n + k + i] = static_cast<T>(plane[c + i * k]) / norm;
     }
   }
   return sep;
+}
+
+std::vector<float> separate_psf(const float* psf, int k, int nplanes) { return separate_psf_t<float>(psf, k, nplanes); }
+std::vector<double> separate_psf64(const float* psf, int k, int nplanes) {
+  return separate_psf_t<double>(psf, k, nplanes);
 }
 
 }  // namespace nrgb

@@ -27,8 +27,10 @@ struct Cameras {
 // other column counts.
 int expand_cameras(const float* cameras, int n, int ncols, const int center_size[3], Cameras* out);
 
-// Forward/backward matrices per camera (see CamGeom).
+// Forward/backward matrices per camera (see CamGeom); the float64 variant
+// evaluates the same formulas in double from the float angles and centres.
 std::vector<CamGeom> camera_geometry(const Cameras& cams);
+std::vector<CamGeom64> camera_geometry64(const Cameras& cams);
 
 // True when every camera rotates about the gantry axis only (theta_x ==
 // theta_z == 0), so that the resampling matrices are exact rotations about y.
@@ -40,5 +42,6 @@ bool is_y_gantry(const Cameras& cams);
 // kernels stored as given (the convolution reverses them).  Square kernels
 // only (k = kx = ky).
 std::vector<float> separate_psf(const float* psf, int k, int nplanes);
+std::vector<double> separate_psf64(const float* psf, int k, int nplanes);
 
 }  // namespace nrgb

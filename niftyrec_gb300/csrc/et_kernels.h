@@ -9,21 +9,29 @@
 namespace nrgb {
 
 // ---- general-orientation path (nifti layout) ----
-struct GeneralArgs {
+template <class T>
+struct GeneralArgsT {
   int nx = 0, ny = 0, nz = 0, ncam = 0;
-  const CamGeom* geom_host = nullptr;  // host array; matrices go to kernels by value
-  const float* act = nullptr;          // device volume or null
-  const float* att = nullptr;          // device volume or null
-  const float* sino = nullptr;         // device sinogram input (backprojection, gradient)
-  float* out = nullptr;                // device output
-  const float* psf_sep = nullptr;      // device [nz][2k] or null
+  const CamGeomT<T>* geom_host = nullptr;  // host array; matrices go to kernels by value
+  const T* act = nullptr;                  // device volume or null
+  const T* att = nullptr;                  // device volume or null
+  const T* sino = nullptr;                 // device sinogram input (backprojection, gradient)
+  T* out = nullptr;                        // device output
+  const T* psf_sep = nullptr;              // device [nz][2k] or null
   int psf_k = 0;
-  float bg = 0.0f, bg_att = 0.0f;
+  T bg = 0, bg_att = 0;
   int truncate = 0;
-  float* ws_act = nullptr;  // three nvox work volumes
-  float* ws_att = nullptr;
-  float* ws_tmp = nullptr;
+  T* ws_act = nullptr;  // three nvox work volumes
+  T* ws_att = nullptr;
+  T* ws_tmp = nullptr;
 };
+using GeneralArgs = GeneralArgsT<float>;
+// The same projector / backprojector evaluated in float64 (every product,
+// sum, position and exp in double): the float64 reference run that the
+// float32 and bfloat16-storage results are measured against.
+using GeneralArgs64 = GeneralArgsT<double>;
+int general_project64(const GeneralArgs64& a, cudaStream_t st);
+int general_backproject64(const GeneralArgs64& a, cudaStream_t st);
 int general_project(const GeneralArgs& a, cudaStream_t st);
 int general_backproject(const GeneralArgs& a, cudaStream_t st);
 int general_gradient(const GeneralArgs& a, cudaStream_t st);
@@ -37,14 +45,15 @@ int general_rotate(const float* src, float* dst, int nx, int ny, int nz, const f
 struct YgArgs {
   int nx = 0, ny = 0, nz = 0, cy = 0, ncam = 0;
   const CamGeom* geom = nullptr;  // device [ncam]
-  const float* act = nullptr;     // [nz][nx][cy]
-  const float* mu = nullptr;      // [nz][nx][cy] or null
+  const float* act = nullptr;     // [nz][nx][cy] (bfloat16 data when storage == kStorageBF16)
+  const float* mu = nullptr;      // [nz][nx][cy] or null (same storage as act)
   const float* sino = nullptr;    // [ncam][nx][cy] (backprojection input)
   float* out = nullptr;           // projector: [ncam][nx][cy]; backprojector: [nz][nx][cy]
   const float* psf = nullptr;     // device [nz][2k] or null
   int psf_k = 0;
   int truncate = 0;
   int back_mode = kBackReference;
+  int storage = kStorageF32;  // type of act and mu
   // backprojector work space (yg_backproject_workspace bytes); the kernels
   // see it as slab sums [ncam][slabs][nx][cy] then scratch [group][nz][nx][cy]
   float* work = nullptr;
@@ -84,6 +93,12 @@ int to_column_rows(const float* src, float* dst, int nx, int ny_src, int row0, i
                    cudaStream_t st);
 int from_column_rows(const float* src, float* dst, int nx, int cy, int r_begin, int r_end, int row0, int ny_dst,
                      int planes, int truncate, cudaStream_t st);
+// bfloat16 column layout (round to nearest even) from float32 or bfloat16
+// nifti rows [row0, row0 + rows); and elementwise float32 -> bfloat16.
+int to_column_rows_bf16(const float* src_f32, const void* src_bf16, void* dst, int nx, int ny_src, int row0, int rows,
+                        int cy, int planes, cudaStream_t st);
+int to_bf16(const float* src, void* dst, size_t n, cudaStream_t st);
+int from_bf16(const void* src, float* dst, size_t n, cudaStream_t st);
 void launch_truncate(float* buf, size_t n, cudaStream_t st);
 
 // ---- OSEM / MLEM update kernels ----
@@ -91,6 +106,9 @@ void launch_truncate(float* buf, size_t n, cudaStream_t st);
 int osem_ratio(const float* y, float* p_to_ratio, size_t n, float eps, cudaStream_t st);
 // x[i] *= num[i] / max(den[i], eps)            (:1036-1044)
 int osem_update(float* x, const float* num, const float* den, size_t n, float eps, cudaStream_t st);
+// float64 variants of the two, for the float64 reference run.
+int osem_ratio64(const double* y, double* p_to_ratio, size_t n, double eps, cudaStream_t st);
+int osem_update64(double* x, const double* num, const double* den, size_t n, double eps, cudaStream_t st);
 // FP64 totals: out[0] = sum(a), out[1] = sum(b) (b may be null), device doubles.
 int sum_fp64(const float* a, const float* b, size_t n, double* out, cudaStream_t st);
 // out[i] = value

@@ -16,23 +16,29 @@ int grid_for(size_t n) {
   return static_cast<int>(g < cap ? (g == 0 ? 1 : g) : cap);
 }
 
+__device__ __forceinline__ float dv(float a, float b) { return __fdiv_rn(a, b); }
+__device__ __forceinline__ double dv(double a, double b) { return __ddiv_rn(a, b); }
+__device__ __forceinline__ float ml(float a, float b) { return __fmul_rn(a, b); }
+__device__ __forceinline__ double ml(double a, double b) { return __dmul_rn(a, b); }
+
 // emission-lib/_et_array_interface.cpp:1022-1028: y/eps where p < eps, else y/p.
-__global__ void k_ratio(const float* __restrict__ y, float* __restrict__ p, size_t n, float eps) {
+template <class T>
+__global__ void k_ratio(const T* __restrict__ y, T* __restrict__ p, size_t n, T eps) {
   for (size_t i = blockIdx.x * static_cast<size_t>(blockDim.x) + threadIdx.x; i < n;
        i += static_cast<size_t>(gridDim.x) * blockDim.x) {
-    const float pv = p[i];
-    p[i] = (pv < eps) ? __fdiv_rn(y[i], eps) : __fdiv_rn(y[i], pv);
+    const T pv = p[i];
+    p[i] = (pv < eps) ? dv(y[i], eps) : dv(y[i], pv);
   }
 }
 
 // emission-lib/_et_array_interface.cpp:1036-1044: den < eps -> eps; x *= num / den.
-__global__ void k_update(float* __restrict__ x, const float* __restrict__ num, const float* __restrict__ den,
-                         size_t n, float eps) {
+template <class T>
+__global__ void k_update(T* __restrict__ x, const T* __restrict__ num, const T* __restrict__ den, size_t n, T eps) {
   for (size_t i = blockIdx.x * static_cast<size_t>(blockDim.x) + threadIdx.x; i < n;
        i += static_cast<size_t>(gridDim.x) * blockDim.x) {
-    float d = den[i];
+    T d = den[i];
     if (d < eps) d = eps;
-    x[i] = __fmul_rn(x[i], __fdiv_rn(num[i], d));
+    x[i] = ml(x[i], dv(num[i], d));
   }
 }
 
@@ -101,12 +107,22 @@ __global__ void k_sum_final(const double* __restrict__ part, int nparts, double*
 }  // namespace
 
 int osem_ratio(const float* y, float* p, size_t n, float eps, cudaStream_t st) {
-  { NRGB_LAUNCH_SCOPE("k_ratio", st); k_ratio<<<grid_for(n), kBlock, 0, st>>>(y, p, n, eps); }
+  { NRGB_LAUNCH_SCOPE("k_ratio", st); k_ratio<float><<<grid_for(n), kBlock, 0, st>>>(y, p, n, eps); }
   return cudaGetLastError() == cudaSuccess ? kOk : kErrKernel;
 }
 
 int osem_update(float* x, const float* num, const float* den, size_t n, float eps, cudaStream_t st) {
-  { NRGB_LAUNCH_SCOPE("k_update", st); k_update<<<grid_for(n), kBlock, 0, st>>>(x, num, den, n, eps); }
+  { NRGB_LAUNCH_SCOPE("k_update", st); k_update<float><<<grid_for(n), kBlock, 0, st>>>(x, num, den, n, eps); }
+  return cudaGetLastError() == cudaSuccess ? kOk : kErrKernel;
+}
+
+int osem_ratio64(const double* y, double* p, size_t n, double eps, cudaStream_t st) {
+  { NRGB_LAUNCH_SCOPE("k_ratio", st); k_ratio<double><<<grid_for(n), kBlock, 0, st>>>(y, p, n, eps); }
+  return cudaGetLastError() == cudaSuccess ? kOk : kErrKernel;
+}
+
+int osem_update64(double* x, const double* num, const double* den, size_t n, double eps, cudaStream_t st) {
+  { NRGB_LAUNCH_SCOPE("k_update", st); k_update<double><<<grid_for(n), kBlock, 0, st>>>(x, num, den, n, eps); }
   return cudaGetLastError() == cudaSuccess ? kOk : kErrKernel;
 }
 

@@ -21,6 +21,7 @@
 #include "et_profile.h"
 
 #include <cooperative_groups.h>
+#include <cuda_bf16.h>
 
 #include <algorithm>
 #include <map>
@@ -88,10 +89,20 @@ __device__ __forceinline__ Tap make_tap(int xp, int zp, float m00, float m02, fl
 
 __device__ __forceinline__ float4 ldg4(const float* p) { return __ldg(reinterpret_cast<const float4*>(p)); }
 
-__device__ __forceinline__ float4 sample4(const float* __restrict__ base, const Tap& t, int yb, bool yok) {
+// Four consecutive rows of a bfloat16 column (8 bytes, 8-byte aligned since
+// cy and the lane's first row are multiples of 4), widened to float32: a
+// bfloat16 is the high half of the float32 with the same value.
+__device__ __forceinline__ float4 ldg4(const __nv_bfloat16* p) {
+  const uint2 u = __ldg(reinterpret_cast<const uint2*>(p));
+  return make_float4(__uint_as_float(u.x << 16), __uint_as_float(u.x & 0xffff0000u), __uint_as_float(u.y << 16),
+                     __uint_as_float(u.y & 0xffff0000u));
+}
+
+template <class V>
+__device__ __forceinline__ float4 sample4(const V* __restrict__ base, const Tap& t, int yb, bool yok) {
   float4 r = make_float4(0.f, 0.f, 0.f, 0.f);
   if (!t.any || !yok) return r;
-  const float* p = base + t.off + yb;
+  const V* p = base + t.off + yb;
   const float4 a = ldg4(p), b = ldg4(p + t.dx), c = ldg4(p + t.dz), d = ldg4(p + t.dx + t.dz);
   r.x = fmaf(d.x, t.w11, fmaf(c.x, t.w01, fmaf(b.x, t.w10, a.x * t.w00)));
   r.y = fmaf(d.y, t.w11, fmaf(c.y, t.w01, fmaf(b.y, t.w10, a.y * t.w00)));
@@ -176,6 +187,54 @@ __device__ __forceinline__ float4 mul4(const float4& a, const float4& b) {
   return make_float4(a.x * b.x, a.y * b.y, a.z * b.z, a.w * b.w);
 }
 
+// Compensated summation (Kahan, CACM 8(1):40, 1965): s + (-c) tracks the
+// exact sum of the added terms far better than s alone; c holds the rounding
+// excess of the previous additions.  Each operation rounds separately.
+__device__ __forceinline__ void kahan_add(float& s, float& c, float v) {
+  const float y = __fsub_rn(v, c);
+  const float t = __fadd_rn(s, y);
+  c = __fsub_rn(__fsub_rn(t, s), y);
+  s = t;
+}
+
+__device__ __forceinline__ void kahan_add4(float4& s, float4& c, const float4& v) {
+  kahan_add(s.x, c.x, v.x);
+  kahan_add(s.y, c.y, v.y);
+  kahan_add(s.z, c.z, v.z);
+  kahan_add(s.w, c.w, v.w);
+}
+
+// Compensated value of a Kahan pair.
+__device__ __forceinline__ float4 kahan_value4(const float4& s, const float4& c) {
+  return make_float4(__fsub_rn(s.x, c.x), __fsub_rn(s.y, c.y), __fsub_rn(s.z, c.z), __fsub_rn(s.w, c.w));
+}
+
+// Depth sum s += v: plain float32 (the reference's order) or compensated.
+template <bool KAHAN>
+__device__ __forceinline__ void depth_add4(float4& s, float4& c, const float4& v) {
+  if (KAHAN)
+    kahan_add4(s, c, v);
+  else
+    add4(s, v);
+}
+
+template <bool KAHAN>
+__device__ __forceinline__ float4 depth_value4(const float4& s, const float4& c) {
+  return KAHAN ? kahan_value4(s, c) : s;
+}
+
+// Storage type of the sampled volumes; bfloat16 storage sums with Kahan.
+template <class V>
+struct StorageTraits {
+  static constexpr bool kKahan = false;
+  static constexpr int kMinBlocks = 2;
+};
+template <>
+struct StorageTraits<__nv_bfloat16> {
+  static constexpr bool kKahan = true;
+  static constexpr int kMinBlocks = 1;  // room for the compensation registers
+};
+
 struct CamRows {
   float m00, m02, m03, m20, m22, m23;
 };
@@ -243,9 +302,14 @@ __device__ __forceinline__ void rowpass_from_tile(const float4* __restrict__ sbu
 // Cluster of kSlabsP CTAs = the depth slabs of one (camera, x-tile).  Each
 // CTA accumulates (T, p) over its slab; the cluster merges through
 // distributed shared memory: p = p0 + exp(-T0) p1 + exp(-T0-T1) p2 + ...
-template <int R, bool PSF, bool ATT>
-__global__ void __cluster_dims__(kSlabsP, 1, 1) __launch_bounds__(32 * kW, 2) k_project_yg(const YgArgs a) {
+// V: storage type of activity and mu (float or bfloat16; bfloat16 sums with Kahan).
+template <int R, bool PSF, bool ATT, class V>
+__global__ void __cluster_dims__(kSlabsP, 1, 1) __launch_bounds__(32 * kW, StorageTraits<V>::kMinBlocks)
+    k_project_yg(const YgArgs a) {
   using TS = TileShape<R>;
+  constexpr bool KAHAN = StorageTraits<V>::kKahan;
+  const V* __restrict__ act = reinterpret_cast<const V*>(a.act);
+  const V* __restrict__ mu = reinterpret_cast<const V*>(a.mu);
   constexpr int NS = TS::NS;
   constexpr int K = 2 * R + 1;
   extern __shared__ __align__(16) unsigned char smem[];
@@ -270,11 +334,13 @@ __global__ void __cluster_dims__(kSlabsP, 1, 1) __launch_bounds__(32 * kW, 2) k_
   const int zper = (a.nz + kSlabsP - 1) / kSlabsP;
   const int zbeg = slab * zper, zend = min(a.nz, zbeg + zper);
 
-  float4 T[kTXW], P[kTXW];
+  float4 T[kTXW], P[kTXW], cT[kTXW], cP[kTXW];  // c*: Kahan compensations (KAHAN only)
 #pragma unroll
   for (int i = 0; i < kTXW; ++i) {
     T[i] = make_float4(0.f, 0.f, 0.f, 0.f);
     P[i] = make_float4(0.f, 0.f, 0.f, 0.f);
+    cT[i] = make_float4(0.f, 0.f, 0.f, 0.f);
+    cP[i] = make_float4(0.f, 0.f, 0.f, 0.f);
   }
   __syncthreads();
 
@@ -295,16 +361,21 @@ __global__ void __cluster_dims__(kSlabsP, 1, 1) __launch_bounds__(32 * kW, 2) k_
 #pragma unroll
     for (int k = 0; k < TS::kOwn; ++k) {
       const int c = warp + kW * k;
-      if (c < NS) sbuf[c * 32 + lane] = sample4(a.act, tb[c], yb, yok);
+      if (c < NS) sbuf[c * 32 + lane] = sample4(act, tb[c], yb, yok);
     }
     __syncthreads();
     auto emit = [&](int i, const float4& v) {
       if (ATT) {
-        const float4 m = sample4(a.mu, tb[warp * kTXW + i + R], yb, yok);
-        add4(T[i], m);
-        fma4(P[i], v, exp_neg4(T[i]));
+        const float4 m = sample4(mu, tb[warp * kTXW + i + R], yb, yok);
+        if (KAHAN) {
+          kahan_add4(T[i], cT[i], m);
+          kahan_add4(P[i], cP[i], mul4(v, exp_neg4(kahan_value4(T[i], cT[i]))));
+        } else {
+          add4(T[i], m);
+          fma4(P[i], v, exp_neg4(T[i]));
+        }
       } else {
-        add4(P[i], v);
+        depth_add4<KAHAN>(P[i], cP[i], v);
       }
     };
     if (PSF) {
@@ -322,8 +393,8 @@ __global__ void __cluster_dims__(kSlabsP, 1, 1) __launch_bounds__(32 * kW, 2) k_
   float4* sP = sb + kTXC * 32;    // [kTXC][32]
 #pragma unroll
   for (int i = 0; i < kTXW; ++i) {
-    sT[(warp * kTXW + i) * 32 + lane] = T[i];
-    sP[(warp * kTXW + i) * 32 + lane] = P[i];
+    sT[(warp * kTXW + i) * 32 + lane] = depth_value4<KAHAN>(T[i], cT[i]);
+    sP[(warp * kTXW + i) * 32 + lane] = depth_value4<KAHAN>(P[i], cP[i]);
   }
   cluster.sync();
   constexpr int kPerRank = kTXC / kSlabsP;  // outputs merged by each CTA of the cluster
@@ -358,8 +429,11 @@ __global__ void __cluster_dims__(kSlabsP, 1, 1) __launch_bounds__(32 * kW, 2) k_
 // ------------------------------------------------ backprojector: slab carry
 // carry[cam][s][x][y] = sum of the rotated mu over the depth slabs before s
 // (exclusive prefix): the transmission a depth slab starts from.
+template <class V>
 __global__ void __launch_bounds__(32 * kSlabsB) k_mu_carry_yg(const YgArgs a) {
   constexpr int C = 8;
+  constexpr bool KAHAN = StorageTraits<V>::kKahan;
+  const V* __restrict__ mu = reinterpret_cast<const V*>(a.mu);
   __shared__ Tap s_tap[kSlabsB][C];
   __shared__ float4 s_sum[kSlabsB][C][32];
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -371,9 +445,12 @@ __global__ void __launch_bounds__(32 * kSlabsB) k_mu_carry_yg(const YgArgs a) {
   const CamRows cr = cam_rows(a.geom[cam].fwd);
   const int zper = (a.nz + kSlabsB - 1) / kSlabsB;
   const int zbeg = warp * zper, zend = min(a.nz, zbeg + zper);
-  float4 S[C];
+  float4 S[C], cS[C];
 #pragma unroll
-  for (int i = 0; i < C; ++i) S[i] = make_float4(0.f, 0.f, 0.f, 0.f);
+  for (int i = 0; i < C; ++i) {
+    S[i] = make_float4(0.f, 0.f, 0.f, 0.f);
+    cS[i] = make_float4(0.f, 0.f, 0.f, 0.f);
+  }
   for (int z = zbeg; z < zend; ++z) {
     if (lane < C) {
       const int xp = x0 + lane;
@@ -381,11 +458,11 @@ __global__ void __launch_bounds__(32 * kSlabsB) k_mu_carry_yg(const YgArgs a) {
     }
     __syncwarp();
 #pragma unroll
-    for (int i = 0; i < C; ++i) add4(S[i], sample4(a.mu, s_tap[warp][i], yb, yok));
+    for (int i = 0; i < C; ++i) depth_add4<KAHAN>(S[i], cS[i], sample4(mu, s_tap[warp][i], yb, yok));
     __syncwarp();
   }
 #pragma unroll
-  for (int i = 0; i < C; ++i) s_sum[warp][i][lane] = S[i];
+  for (int i = 0; i < C; ++i) s_sum[warp][i][lane] = depth_value4<KAHAN>(S[i], cS[i]);
   __syncthreads();
   if (!yok) return;
 #pragma unroll
@@ -428,9 +505,11 @@ __device__ __forceinline__ void scatter4(float* __restrict__ base, const Tap& t,
 // the PSF taps are flipped (correlation) and each output column is scattered
 // with the projector's own bilinear weights into the accumulator a.out
 // (vector reductions; all cameras in one launch, no scratch).
-template <int R, bool PSF, bool ATT, bool ADJ>
-__global__ void __launch_bounds__(32 * kW, 2) k_spread_yg(const YgArgs a, int c0) {
+template <int R, bool PSF, bool ATT, bool ADJ, class V>
+__global__ void __launch_bounds__(32 * kW, StorageTraits<V>::kMinBlocks) k_spread_yg(const YgArgs a, int c0) {
   using TS = TileShape<R>;
+  constexpr bool KAHAN = StorageTraits<V>::kKahan;
+  const V* __restrict__ mu = reinterpret_cast<const V*>(a.mu);
   constexpr int NS = TS::NS;
   constexpr int K = 2 * R + 1;
   extern __shared__ __align__(16) unsigned char smem[];
@@ -463,10 +542,11 @@ __global__ void __launch_bounds__(32 * kW, 2) k_spread_yg(const YgArgs a, int c0
   float* __restrict__ tmp = ADJ ? a.out : a.temp + vol * g;
   const float* __restrict__ srow = a.sino + static_cast<size_t>(cam) * a.nx * a.cy;
 
-  float4 Tc[TS::kOwn];
+  float4 Tc[TS::kOwn], cTc[TS::kOwn];  // transmission per sampled column (+ Kahan compensation)
 #pragma unroll
   for (int k = 0; k < TS::kOwn; ++k) {
     Tc[k] = make_float4(0.f, 0.f, 0.f, 0.f);
+    cTc[k] = make_float4(0.f, 0.f, 0.f, 0.f);
     const int xp = x0 - R + warp + kW * k;
     if (ATT && warp + kW * k < NS && xp >= 0 && xp < a.nx && yok)
       Tc[k] = ldg4(a.slab_T + ((static_cast<size_t>(cam) * kSlabsB + slab) * a.nx + xp) * a.cy + yb);
@@ -494,8 +574,8 @@ __global__ void __launch_bounds__(32 * kW, 2) k_spread_yg(const YgArgs a, int c0
         float4 s = make_float4(0.f, 0.f, 0.f, 0.f);
         if (xp >= 0 && xp < a.nx && yok) s = ldg4(srow + static_cast<size_t>(xp) * a.cy + yb);
         if (ATT) {
-          add4(Tc[k], sample4(a.mu, tb[c], yb, yok));
-          s = mul4(s, exp_neg4(Tc[k]));
+          depth_add4<KAHAN>(Tc[k], cTc[k], sample4(mu, tb[c], yb, yok));
+          s = mul4(s, exp_neg4(depth_value4<KAHAN>(Tc[k], cTc[k])));
         }
         sbuf[c * 32 + lane] = s;
       }
@@ -582,6 +662,40 @@ __global__ void k_to_col(const float* __restrict__ src, float* __restrict__ dst,
   }
 }
 
+// bfloat16 variant of k_to_col: the source is float32 (rounded to nearest
+// even) or already bfloat16 (copied).
+template <class S>
+__global__ void k_to_col_bf16(const S* __restrict__ src, __nv_bfloat16* __restrict__ dst, int nx, int ny_src,
+                              int row0, int rows, int cy) {
+  __shared__ float tile[32][33];
+  const int p = blockIdx.z;
+  const int xb = blockIdx.x * 32, yb = blockIdx.y * 32;
+  const int tx = threadIdx.x;
+  for (int dy = threadIdx.y; dy < 32; dy += blockDim.y) {
+    const int r = yb + dy, x = xb + tx;
+    float v = 0.0f;
+    if (r < rows && x < nx) v = static_cast<float>(src[(static_cast<size_t>(p) * ny_src + row0 + r) * nx + x]);
+    tile[dy][tx] = v;
+  }
+  __syncthreads();
+  for (int dx = threadIdx.y; dx < 32; dx += blockDim.y) {
+    const int x = xb + dx, r = yb + tx;
+    if (x < nx && r < cy) dst[(static_cast<size_t>(p) * nx + x) * cy + r] = __float2bfloat16_rn(tile[tx][dx]);
+  }
+}
+
+__global__ void k_to_bf16(const float* __restrict__ src, __nv_bfloat16* __restrict__ dst, size_t n) {
+  for (size_t i = blockIdx.x * static_cast<size_t>(blockDim.x) + threadIdx.x; i < n;
+       i += static_cast<size_t>(gridDim.x) * blockDim.x)
+    dst[i] = __float2bfloat16_rn(src[i]);
+}
+
+__global__ void k_from_bf16(const __nv_bfloat16* __restrict__ src, float* __restrict__ dst, size_t n) {
+  for (size_t i = blockIdx.x * static_cast<size_t>(blockDim.x) + threadIdx.x; i < n;
+       i += static_cast<size_t>(gridDim.x) * blockDim.x)
+    dst[i] = __bfloat162float(src[i]);
+}
+
 // dst[p][row0 + r][x] = src[p][x][r] for r in [r_begin, r_end); dst planes
 // have ny_dst rows; truncate clamps negatives to zero.
 __global__ void k_from_col(const float* __restrict__ src, float* __restrict__ dst, int nx, int cy, int r_begin,
@@ -617,13 +731,20 @@ int launch_project_R(const YgArgs& a, cudaStream_t st) {
     NRGB_LAUNCH_SCOPE("k_project_yg", st);
     k<<<grid, block, smem, st>>>(a);
   };
-  if (psf) {
-    if (a.mu) go(k_project_yg<R, true, true>);
-    else go(k_project_yg<R, true, false>);
-  } else {
-    if (a.mu) go(k_project_yg<0, false, true>);
-    else go(k_project_yg<0, false, false>);
-  }
+  auto pick = [&](auto v) {
+    using V = decltype(v);
+    if (psf) {
+      if (a.mu) go(k_project_yg<R, true, true, V>);
+      else go(k_project_yg<R, true, false, V>);
+    } else {
+      if (a.mu) go(k_project_yg<0, false, true, V>);
+      else go(k_project_yg<0, false, false, V>);
+    }
+  };
+  if (a.storage == kStorageBF16)
+    pick(__nv_bfloat16());
+  else
+    pick(0.0f);
   return cudaGetLastError() == cudaSuccess ? kOk : kErrKernel;
 }
 
@@ -638,12 +759,16 @@ int launch_spread_R(const YgArgs& a, int c0, int gcount, cudaStream_t st) {
     NRGB_LAUNCH_SCOPE(ADJ ? "k_adjoint_yg" : "k_spread_yg", st);
     k<<<grid, block, smem, st>>>(a, c0);
   };
+  // only mu is sampled from storage here (the sinogram is float32)
+  const bool bf16 = a.storage == kStorageBF16;
   if (psf) {
-    if (a.mu) go(k_spread_yg<R, true, true, ADJ>);
-    else go(k_spread_yg<R, true, false, ADJ>);
+    if (a.mu && bf16) go(k_spread_yg<R, true, true, ADJ, __nv_bfloat16>);
+    else if (a.mu) go(k_spread_yg<R, true, true, ADJ, float>);
+    else go(k_spread_yg<R, true, false, ADJ, float>);
   } else {
-    if (a.mu) go(k_spread_yg<0, false, true, ADJ>);
-    else go(k_spread_yg<0, false, false, ADJ>);
+    if (a.mu && bf16) go(k_spread_yg<0, false, true, ADJ, __nv_bfloat16>);
+    else if (a.mu) go(k_spread_yg<0, false, true, ADJ, float>);
+    else go(k_spread_yg<0, false, false, ADJ, float>);
   }
   return cudaGetLastError() == cudaSuccess ? kOk : kErrKernel;
 }
@@ -710,7 +835,10 @@ int yg_mu_carry(const YgArgs& a_in, float* out, cudaStream_t st) {
   a.slab_T = out;
   const int nchunk = (a.nx + 7) / 8;
   NRGB_LAUNCH_SCOPE("k_mu_carry_yg", st);
-  k_mu_carry_yg<<<a.ncam * nchunk, 32 * kSlabsB, 0, st>>>(a);
+  if (a.storage == kStorageBF16)
+    k_mu_carry_yg<__nv_bfloat16><<<a.ncam * nchunk, 32 * kSlabsB, 0, st>>>(a);
+  else
+    k_mu_carry_yg<float><<<a.ncam * nchunk, 32 * kSlabsB, 0, st>>>(a);
   return cudaGetLastError() == cudaSuccess ? kOk : kErrKernel;
 }
 
@@ -830,6 +958,35 @@ int from_column_rows(const float* src, float* dst, int nx, int cy, int r_begin, 
     NRGB_LAUNCH_SCOPE("k_from_col", st);
     k_from_col<<<grid, block, 0, st>>>(src, dst, nx, cy, r_begin, r_end, row0, ny_dst, truncate);
   }
+  return cudaGetLastError() == cudaSuccess ? kOk : kErrKernel;
+}
+
+int to_column_rows_bf16(const float* src_f32, const void* src_bf16, void* dst, int nx, int ny_src, int row0, int rows,
+                        int cy, int planes, cudaStream_t st) {
+  const dim3 grid((nx + 31) / 32, (cy + 31) / 32, planes), block(32, 8);
+  __nv_bfloat16* d = static_cast<__nv_bfloat16*>(dst);
+  NRGB_LAUNCH_SCOPE("k_to_col_bf16", st);
+  if (src_f32)
+    k_to_col_bf16<float><<<grid, block, 0, st>>>(src_f32, d, nx, ny_src, row0, rows, cy);
+  else
+    k_to_col_bf16<__nv_bfloat16>
+        <<<grid, block, 0, st>>>(static_cast<const __nv_bfloat16*>(src_bf16), d, nx, ny_src, row0, rows, cy);
+  return cudaGetLastError() == cudaSuccess ? kOk : kErrKernel;
+}
+
+int to_bf16(const float* src, void* dst, size_t n, cudaStream_t st) {
+  if (n == 0) return kOk;
+  const int grid = static_cast<int>(std::min<size_t>((n + 255) / 256, 152 * 16));
+  NRGB_LAUNCH_SCOPE("k_to_bf16", st);
+  k_to_bf16<<<grid, 256, 0, st>>>(src, static_cast<__nv_bfloat16*>(dst), n);
+  return cudaGetLastError() == cudaSuccess ? kOk : kErrKernel;
+}
+
+int from_bf16(const void* src, float* dst, size_t n, cudaStream_t st) {
+  if (n == 0) return kOk;
+  const int grid = static_cast<int>(std::min<size_t>((n + 255) / 256, 152 * 16));
+  NRGB_LAUNCH_SCOPE("k_from_bf16", st);
+  k_from_bf16<<<grid, 256, 0, st>>>(static_cast<const __nv_bfloat16*>(src), dst, n);
   return cudaGetLastError() == cudaSuccess ? kOk : kErrKernel;
 }
 

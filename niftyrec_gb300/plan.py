@@ -33,7 +33,10 @@ def interleaved_subsets(n_cameras, n_subsets):
 
 class Plan:
     def __init__(self, shape, cameras, psf=None, attenuation=None, subsets=None, background=0.0,
-                 background_attenuation=0.0):
+                 background_attenuation=0.0, n_subsets=None):
+        """subsets: None (one subset), a count (interleaved subsets) or the
+        subset id of every camera; n_subsets overrides the count implied by
+        the ids (subsets may then be empty)."""
         import torch
 
         self.torch = torch
@@ -52,7 +55,7 @@ class Plan:
             self.n_subsets = int(subsets)
         else:
             sub = np.ascontiguousarray(np.asarray(subsets, dtype=np.int32))
-            self.n_subsets = int(sub.max()) + 1
+            self.n_subsets = int(sub.max()) + 1 if n_subsets is None else int(n_subsets)
         self._psf = None if psf is None else np.ascontiguousarray(np.asarray(psf, dtype=np.float32))
         self.device = attenuation.device if attenuation is not None else torch.device("cuda", torch.cuda.current_device())
         stream = torch.cuda.current_stream(self.device)

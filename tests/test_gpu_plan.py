@@ -91,3 +91,37 @@ def test_plan_general_orientation(data):
     assert rel_l2(s, yy[order]) < RTOL
     b = p.backproject(cuda(yy[order])).cpu().numpy()
     assert rel_l2(b, A.backproject(yy, cams, psf, mu)) < RTOL
+
+
+@pytest.mark.parametrize("world", [1, 2])
+def test_sharded_osem_plan_operator(data, world):
+    """Angle-sharded OSEM on the GPU operator.  world=1 is the plain step;
+    world=2 runs both ranks' operators in this one process and sums their
+    partial volumes by hand (the all_reduce of a real run), which must give
+    the single-process step up to float32 summation order."""
+    from niftyrec_gb300 import sharded as SH
+
+    act, mu, psf, cams, y = data
+    n_sub = 4
+    sub = np.arange(NCAM) % n_sub
+    ops, counts = [], []
+    for r in range(world):
+        ids, sids = SH.camera_shares(sub, r, world)
+        ops.append(SH.PlanOperator(SHAPE, cams, ids, sids, n_sub, psf, cuda(mu)))
+        counts.append(SH.split_counts(cuda(y), ids, sids, n_sub))
+    sens = [sum(op.sensitivity(s) for op in ops) for s in range(n_sub)]
+    x = torch.ones(SHAPE, dtype=torch.float32, device="cuda")
+    for _ in range(2):
+        for s in range(n_sub):
+            num = sum(op.numerator(x, c[s], s, 1e-6) for op, c in zip(ops, counts))
+            ops[0].update(x, num, sens[s], 1e-6)
+    xr = np.ones(SHAPE, np.float32)
+    for _ in range(2):
+        for s in range(n_sub):
+            xr = A.osem_step_subset(xr, y, cams, np.flatnonzero(sub == s), mu, psf)
+    assert rel_l2(x.cpu().numpy(), xr) < 2 * RTOL
+    if world == 1:
+        rec = SH.ShardedOSEM(ops[0], counts[0], n_sub)
+        x1 = rec.run(torch.ones(SHAPE, dtype=torch.float32, device="cuda"), 2)
+        assert rec.collectives == 0
+        assert rel_l2(x1.cpu().numpy(), xr) < 2 * RTOL
