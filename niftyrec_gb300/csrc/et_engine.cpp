@@ -62,37 +62,14 @@ int make_problem(int nx, int ny, int nz, const Cameras& cams, const float* psf, 
 }
 
 bool use_fused(const Problem& pb) {
-  return pb.ygantry && pb.bg == 0.0f && pb.bg_att == 0.0f &&
-         yg_supported(pb.nx, std::min(pb.ny, kWindowRows), pb.nz, pb.psf_k);
-}
-
-std::vector<YWindow> y_windows(int ny, int halo) {
-  std::vector<YWindow> w;
-  if (ny <= kWindowRows) {
-    w.push_back({0, ny, 0, ny});
-    return w;
-  }
-  int out0 = 0;
-  while (out0 < ny) {
-    const int in0 = std::max(0, out0 - halo);
-    if (in0 + kWindowRows >= ny) {
-      w.push_back({in0, ny - in0, out0, ny});
-      break;
-    }
-    const int out1 = in0 + kWindowRows - halo;
-    w.push_back({in0, kWindowRows, out0, out1});
-    out0 = out1;
-  }
-  return w;
+  return pb.ygantry && pb.bg == 0.0f && pb.bg_att == 0.0f && yg_supported(pb.nx, pb.ny, pb.nz, pb.psf_k);
 }
 
 namespace {
 
 size_t vol_n(const Problem& pb) { return static_cast<size_t>(pb.nx) * pb.ny * pb.nz; }
-// column buffers of the fused path hold one row window
-int window_cy(const Problem& pb) { return round_up(std::min(pb.ny, kWindowRows), 4); }
-size_t col_n(const Problem& pb) { return static_cast<size_t>(pb.nx) * window_cy(pb) * pb.nz; }
-size_t sino_col_n(const Problem& pb) { return static_cast<size_t>(pb.nx) * window_cy(pb) * pb.cams.n; }
+size_t col_n(const Problem& pb) { return static_cast<size_t>(pb.nx) * round_up(pb.ny, 4) * pb.nz; }
+size_t sino_col_n(const Problem& pb) { return static_cast<size_t>(pb.nx) * round_up(pb.ny, 4) * pb.cams.n; }
 constexpr size_t kSlack = 8 * 256;
 
 size_t common_bytes(const Problem& pb) {
@@ -177,7 +154,7 @@ size_t backproject_workspace(const Problem& pb, bool has_att) {
   size_t b = common_bytes(pb);
   if (use_fused(pb))
     b += sizeof(float) * (col_n(pb) * (has_att ? 2 : 1) + sino_col_n(pb)) +
-         yg_backproject_workspace(pb.nx, std::min(pb.ny, kWindowRows), pb.nz, pb.cams.n, pb.group) + kSlack;
+         yg_backproject_workspace(pb.nx, pb.ny, pb.nz, pb.cams.n, pb.group) + kSlack;
   else
     b += sizeof(float) * vol_n(pb) * 3 + widen_bytes(pb);
   return b;
@@ -187,14 +164,13 @@ size_t gradient_workspace(const Problem& pb) { return common_bytes(pb) + sizeof(
 
 namespace {
 
-// One row window of a caller volume (nifti, float32 or bfloat16) into the
-// fused kernels' column buffer in the problem's storage type.
-int stage_column(const Problem& pb, const float* src, float* dst, const YWindow& w, int cy, int planes,
-                 cudaStream_t st) {
+// A caller volume (nifti, float32 or bfloat16) into the fused kernels'
+// column buffer in the problem's storage type.
+int stage_column(const Problem& pb, const float* src, float* dst, int cy, int planes, cudaStream_t st) {
   if (pb.storage == kStorageBF16)
-    return to_column_rows_bf16(pb.input_bf16 ? nullptr : src, pb.input_bf16 ? src : nullptr, dst, pb.nx, pb.ny,
-                               w.in0, w.rows, cy, planes, st);
-  return to_column_rows(src, dst, pb.nx, pb.ny, w.in0, w.rows, cy, planes, st);
+    return to_column_rows_bf16(pb.input_bf16 ? nullptr : src, pb.input_bf16 ? src : nullptr, dst, pb.nx, pb.ny, 0,
+                               pb.ny, cy, planes, st);
+  return to_column(src, dst, pb.nx, pb.ny, cy, planes, st);
 }
 
 }  // namespace
@@ -211,30 +187,25 @@ int project_device(const Problem& pb, const float* d_act, const float* d_att, fl
     float* mu_c = d_att ? cv.take<float>(col_n(pb)) : nullptr;
     float* sino_c = cv.take<float>(sino_col_n(pb));
     if (!act_c || !sino_c || (d_att && !mu_c)) return kErrAllocGpu;
-    for (const YWindow& w : y_windows(pb.ny, pb.psf_k / 2)) {
-      const int cy = round_up(w.rows, 4);
-      if ((s = stage_column(pb, d_act, act_c, w, cy, pb.nz, st)) != kOk) return s;
-      if (d_att && (s = stage_column(pb, d_att, mu_c, w, cy, pb.nz, st)) != kOk) return s;
-      YgArgs a;
-      a.storage = pb.storage;
-      a.nx = pb.nx;
-      a.ny = w.rows;
-      a.nz = pb.nz;
-      a.cy = cy;
-      a.ncam = pb.cams.n;
-      a.geom = d_geom;
-      a.act = act_c;
-      a.mu = mu_c;
-      a.out = sino_c;
-      a.psf = d_psf;
-      a.psf_k = pb.psf_k;
-      a.truncate = pb.truncate;
-      if ((s = yg_project(a, st)) != kOk) return s;
-      if ((s = from_column_rows(sino_c, d_sino, pb.nx, cy, w.out0 - w.in0, w.out1 - w.in0, w.in0, pb.ny, pb.cams.n,
-                                0, st)) != kOk)
-        return s;
-    }
-    return check(kOk);
+    const int cy = round_up(pb.ny, 4);
+    if ((s = stage_column(pb, d_act, act_c, cy, pb.nz, st)) != kOk) return s;
+    if (d_att && (s = stage_column(pb, d_att, mu_c, cy, pb.nz, st)) != kOk) return s;
+    YgArgs a;
+    a.storage = pb.storage;
+    a.nx = pb.nx;
+    a.ny = pb.ny;
+    a.nz = pb.nz;
+    a.cy = cy;
+    a.ncam = pb.cams.n;
+    a.geom = d_geom;
+    a.act = act_c;
+    a.mu = mu_c;
+    a.out = sino_c;
+    a.psf = d_psf;
+    a.psf_k = pb.psf_k;
+    a.truncate = pb.truncate;
+    if ((s = yg_project(a, st)) != kOk) return s;
+    return check(from_column(sino_c, d_sino, pb.nx, pb.ny, cy, pb.cams.n, 0, st));
   }
   if (pb.input_bf16 && (s = widen_inputs(pb, cv, &d_act, &d_att, st)) != kOk) return s;
   GeneralArgs g;
@@ -270,36 +241,30 @@ int backproject_device(const Problem& pb, const float* d_sino, const float* d_at
     float* mu_c = d_att ? cv.take<float>(col_n(pb)) : nullptr;
     float* out_c = cv.take<float>(col_n(pb));
     const int group = std::max(1, std::min(pb.group, pb.cams.n));
-    float* slab = cv.take<float>(
-        yg_backproject_workspace(pb.nx, std::min(pb.ny, kWindowRows), pb.nz, pb.cams.n, group) / sizeof(float));
+    float* slab = cv.take<float>(yg_backproject_workspace(pb.nx, pb.ny, pb.nz, pb.cams.n, group) / sizeof(float));
     if (!sino_c || !out_c || !slab || (d_att && !mu_c)) return kErrAllocGpu;
-    for (const YWindow& w : y_windows(pb.ny, pb.psf_k / 2)) {
-      const int cy = round_up(w.rows, 4);
-      if ((s = to_column_rows(d_sino, sino_c, pb.nx, pb.ny, w.in0, w.rows, cy, pb.cams.n, st)) != kOk) return s;
-      if (d_att && (s = stage_column(pb, d_att, mu_c, w, cy, pb.nz, st)) != kOk) return s;
-      YgArgs a;
-      a.storage = pb.storage;
-      a.nx = pb.nx;
-      a.ny = w.rows;
-      a.nz = pb.nz;
-      a.cy = cy;
-      a.ncam = pb.cams.n;
-      a.geom = d_geom;
-      a.mu = mu_c;
-      a.sino = sino_c;
-      a.out = out_c;
-      a.psf = d_psf;
-      a.psf_k = pb.psf_k;
-      a.truncate = pb.truncate;
-      a.back_mode = pb.back_mode;
-      a.group = group;
-      a.work = slab;
-      if ((s = yg_backproject(a, st)) != kOk) return s;
-      if ((s = from_column_rows(out_c, d_out, pb.nx, cy, w.out0 - w.in0, w.out1 - w.in0, w.in0, pb.ny, pb.nz,
-                                pb.truncate, st)) != kOk)
-        return s;
-    }
-    return check(kOk);
+    const int cy = round_up(pb.ny, 4);
+    if ((s = to_column(d_sino, sino_c, pb.nx, pb.ny, cy, pb.cams.n, st)) != kOk) return s;
+    if (d_att && (s = stage_column(pb, d_att, mu_c, cy, pb.nz, st)) != kOk) return s;
+    YgArgs a;
+    a.storage = pb.storage;
+    a.nx = pb.nx;
+    a.ny = pb.ny;
+    a.nz = pb.nz;
+    a.cy = cy;
+    a.ncam = pb.cams.n;
+    a.geom = d_geom;
+    a.mu = mu_c;
+    a.sino = sino_c;
+    a.out = out_c;
+    a.psf = d_psf;
+    a.psf_k = pb.psf_k;
+    a.truncate = pb.truncate;
+    a.back_mode = pb.back_mode;
+    a.group = group;
+    a.work = slab;
+    if ((s = yg_backproject(a, st)) != kOk) return s;
+    return check(from_column(out_c, d_out, pb.nx, pb.ny, cy, pb.nz, pb.truncate, st));
   }
   if (pb.input_bf16 && (s = widen_inputs(pb, cv, nullptr, &d_att, st)) != kOk) return s;
   GeneralArgs g;

@@ -39,22 +39,9 @@ struct Problem {
 int make_problem(int nx, int ny, int nz, const Cameras& cams, const float* psf, const int* psf_size, float bg,
                  float bg_att, int truncate, Problem* out);
 
-// Whether the fused y-gantry kernels handle this problem (in row windows when
-// ny exceeds kWindowRows).
+// Whether the fused y-gantry kernels handle this problem (any ny: volumes
+// taller than 128 rows run in row windows inside the kernels' launchers).
 bool use_fused(const Problem& pb);
-
-// Row windows of the fused path.  The fused kernels hold at most kWindowRows
-// gantry-axis rows per column; a taller volume runs as independent windows of
-// input rows [in0, in0 + rows) whose output rows [out0, out1) have their whole
-// PSF halo inside the window (or lie at the volume's own edge, where the
-// convolution pads with zeros anyway).  Y-gantry rotations keep y, so each
-// output row depends on input rows y - halo .. y + halo only, and a window
-// computes its valid rows with exactly the arithmetic of a single pass.
-constexpr int kWindowRows = 128;
-struct YWindow {
-  int in0, rows, out0, out1;
-};
-std::vector<YWindow> y_windows(int ny, int halo);
 
 // Cameras per backprojection scratch group for a problem shape (tuning table;
 // all-zero shape = default for shapes without an entry).

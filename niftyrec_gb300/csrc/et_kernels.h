@@ -42,8 +42,15 @@ int general_dmu(const GeneralArgs& a, cudaStream_t st);
 int general_rotate(const float* src, float* dst, int nx, int ny, int nz, const float* m12, float bg, cudaStream_t st);
 
 // ---- y-gantry fused path (column layout) ----
+// Callers describe whole volumes (ny rows, column stride cy = round_up(ny, 4));
+// yg_project / yg_backproject split them into row windows of at most 128
+// rows and fill row0 / out_lo / out_hi / cs per launch (ny then counts the
+// window's rows).
 struct YgArgs {
   int nx = 0, ny = 0, nz = 0, cy = 0, ncam = 0;
+  int row0 = 0;                   // first row of the window (multiple of 4)
+  int out_lo = 0, out_hi = 1 << 30;  // valid output rows of the window, relative to row0
+  int cs = 0;                     // column stride of the backprojector's scratch
   const CamGeom* geom = nullptr;  // device [ncam]
   const float* act = nullptr;     // [nz][nx][cy] (bfloat16 data when storage == kStorageBF16)
   const float* mu = nullptr;      // [nz][nx][cy] or null (same storage as act)

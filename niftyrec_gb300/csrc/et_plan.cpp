@@ -236,8 +236,7 @@ int nrgb_plan_create(void** out_plan, const int* size, const float* cameras, con
     delete p;
     return s;
   }
-  // plans keep whole volumes in column layout: one row window only
-  p->fused = use_fused(p->proj) && ny <= kWindowRows;
+  p->fused = use_fused(p->proj);
   p->has_att = d_attenuation != nullptr;
   p->cy = round_up(ny, 4);
   p->n_subsets = n_subsets;

@@ -26,6 +26,7 @@
 #include <algorithm>
 #include <map>
 #include <mutex>
+#include <vector>
 
 namespace nrgb {
 
@@ -224,15 +225,15 @@ __device__ __forceinline__ float4 depth_value4(const float4& s, const float4& c)
 }
 
 // Storage type of the sampled volumes; bfloat16 storage sums with Kahan.
+// Both keep two CTAs per SM (the compensations fit in 128 registers with at
+// most a few bytes of spill).
 template <class V>
 struct StorageTraits {
   static constexpr bool kKahan = false;
-  static constexpr int kMinBlocks = 2;
 };
 template <>
 struct StorageTraits<__nv_bfloat16> {
   static constexpr bool kKahan = true;
-  static constexpr int kMinBlocks = 1;  // room for the compensation registers
 };
 
 struct CamRows {
@@ -299,20 +300,30 @@ __device__ __forceinline__ void rowpass_from_tile(const float4* __restrict__ sbu
 }
 
 // ---------------------------------------------------------------- projector
-// Cluster of kSlabsP CTAs = the depth slabs of one (camera, x-tile).  Each
-// CTA accumulates (T, p) over its slab; the cluster merges through
+// Row windows: a column holds cy >= ny rows, the kernels see one window of at
+// most 128 rows at a time: rows [row0, row0 + ny) of the columns (row0 a
+// multiple of 4, so lane loads stay aligned), valid output rows [out_lo,
+// out_hi) relative to row0.  Rows past a window's end read as zero (lanes past
+// round_up(ny, 4) sample nothing; the rows inside the last lane are the zero
+// pads of the column layout at the volume's end, the only place a window
+// ends off a multiple of 4).
+__device__ __forceinline__ bool lane_rows_ok(const YgArgs& a, int yb) { return yb < ((a.ny + 3) & ~3); }
+__device__ __forceinline__ bool lane_writes(const YgArgs& a, int yb) { return yb >= a.out_lo && yb < a.out_hi; }
+
+// One projector work item: camera `cam`, output columns x0 .. x0 + kTXC - 1;
+// the CTAs of the cluster walk the depth slabs and merge (T, p) through
 // distributed shared memory: p = p0 + exp(-T0) p1 + exp(-T0-T1) p2 + ...
-// V: storage type of activity and mu (float or bfloat16; bfloat16 sums with Kahan).
+// V: storage type of activity and mu (float or bfloat16; bfloat16 sums with
+// Kahan).  Ends with a cluster barrier, after which the shared memory may be
+// reused.
 template <int R, bool PSF, bool ATT, class V>
-__global__ void __cluster_dims__(kSlabsP, 1, 1) __launch_bounds__(32 * kW, StorageTraits<V>::kMinBlocks)
-    k_project_yg(const YgArgs a) {
+__device__ __forceinline__ void project_item(const YgArgs& a, int cam, int x0, unsigned char* smem) {
   using TS = TileShape<R>;
   constexpr bool KAHAN = StorageTraits<V>::kKahan;
-  const V* __restrict__ act = reinterpret_cast<const V*>(a.act);
-  const V* __restrict__ mu = reinterpret_cast<const V*>(a.mu);
+  const V* __restrict__ act = reinterpret_cast<const V*>(a.act) + a.row0;
+  const V* __restrict__ mu = reinterpret_cast<const V*>(a.mu) + a.row0;
   constexpr int NS = TS::NS;
   constexpr int K = 2 * R + 1;
-  extern __shared__ __align__(16) unsigned char smem[];
   float4* sb = reinterpret_cast<float4*>(smem);                       // [2][NS][32]
   Tap* taps = reinterpret_cast<Tap*>(smem + TS::kSbBytes);             // [2][NS]
   float* s_psf = reinterpret_cast<float*>(smem + TS::kSbBytes + TS::kTapBytes);  // [nz][2K]
@@ -320,19 +331,15 @@ __global__ void __cluster_dims__(kSlabsP, 1, 1) __launch_bounds__(32 * kW, Stora
   cg::cluster_group cluster = cg::this_cluster();
   const int slab = static_cast<int>(cluster.block_rank());
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int ntile = (a.nx + kTXC - 1) / kTXC;
-  const int item = blockIdx.x / kSlabsP;
-  const int cam = item / ntile;
-  const int x0 = (item % ntile) * kTXC;
   const int yb = lane * 4;
-  const bool yok = yb < a.cy;
+  const bool yok = lane_rows_ok(a, yb);
 
-  if (PSF) {
-    for (int i = threadIdx.x; i < a.nz * 2 * K; i += blockDim.x) s_psf[i] = __ldg(a.psf + i);
-  }
-  const CamRows cr = cam_rows(a.geom[cam].fwd);
   const int zper = (a.nz + kSlabsP - 1) / kSlabsP;
   const int zbeg = slab * zper, zend = min(a.nz, zbeg + zper);
+  if (PSF) {  // this slab's planes only
+    for (int i = zbeg * 2 * K + threadIdx.x; i < zend * 2 * K; i += blockDim.x) s_psf[i] = __ldg(a.psf + i);
+  }
+  const CamRows cr = cam_rows(a.geom[cam].fwd);
 
   float4 T[kTXW], P[kTXW], cT[kTXW], cP[kTXW];  // c*: Kahan compensations (KAHAN only)
 #pragma unroll
@@ -402,7 +409,7 @@ __global__ void __cluster_dims__(kSlabsP, 1, 1) __launch_bounds__(32 * kW, Stora
   for (int i = 0; i < kTXW; ++i) {
     const int o = warp * kTXW + i;
     const int x = x0 + o;
-    if (o / kPerRank != slab || x >= a.nx || !yok) continue;
+    if (o / kPerRank != slab || x >= a.nx || !yok || !lane_writes(a, yb)) continue;
     float4 Pt = make_float4(0.f, 0.f, 0.f, 0.f), Tt = make_float4(0.f, 0.f, 0.f, 0.f);
     for (int s = 0; s < kSlabsP; ++s) {
       const float4* rT = cluster.map_shared_rank(sT, s);
@@ -421,9 +428,19 @@ __global__ void __cluster_dims__(kSlabsP, 1, 1) __launch_bounds__(32 * kW, Stora
       Pt.z = fmaxf(Pt.z, 0.f);
       Pt.w = fmaxf(Pt.w, 0.f);
     }
-    *reinterpret_cast<float4*>(a.out + (static_cast<size_t>(cam) * a.nx + x) * a.cy + yb) = Pt;
+    *reinterpret_cast<float4*>(a.out + (static_cast<size_t>(cam) * a.nx + x) * a.cy + a.row0 + yb) = Pt;
   }
   cluster.sync();  // keep this CTA's shared memory alive until the others have read it
+}
+
+// One work item per cluster: blockIdx.x / kSlabsP = (camera, x-tile).
+template <int R, bool PSF, bool ATT, class V>
+__global__ void __cluster_dims__(kSlabsP, 1, 1) __launch_bounds__(32 * kW, 2)
+    k_project_yg(const YgArgs a) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  const int ntile = (a.nx + kTXC - 1) / kTXC;
+  const int item = blockIdx.x / kSlabsP;
+  project_item<R, PSF, ATT, V>(a, item / ntile, (item % ntile) * kTXC, smem);
 }
 
 // ------------------------------------------------ backprojector: slab carry
@@ -433,7 +450,7 @@ template <class V>
 __global__ void __launch_bounds__(32 * kSlabsB) k_mu_carry_yg(const YgArgs a) {
   constexpr int C = 8;
   constexpr bool KAHAN = StorageTraits<V>::kKahan;
-  const V* __restrict__ mu = reinterpret_cast<const V*>(a.mu);
+  const V* __restrict__ mu = reinterpret_cast<const V*>(a.mu) + a.row0;
   __shared__ Tap s_tap[kSlabsB][C];
   __shared__ float4 s_sum[kSlabsB][C][32];
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -441,7 +458,7 @@ __global__ void __launch_bounds__(32 * kSlabsB) k_mu_carry_yg(const YgArgs a) {
   const int cam = blockIdx.x / nchunk;
   const int x0 = (blockIdx.x % nchunk) * C;
   const int yb = lane * 4;
-  const bool yok = yb < a.cy;
+  const bool yok = lane_rows_ok(a, yb);
   const CamRows cr = cam_rows(a.geom[cam].fwd);
   const int zper = (a.nz + kSlabsB - 1) / kSlabsB;
   const int zbeg = warp * zper, zend = min(a.nz, zbeg + zper);
@@ -464,14 +481,15 @@ __global__ void __launch_bounds__(32 * kSlabsB) k_mu_carry_yg(const YgArgs a) {
 #pragma unroll
   for (int i = 0; i < C; ++i) s_sum[warp][i][lane] = depth_value4<KAHAN>(S[i], cS[i]);
   __syncthreads();
-  if (!yok) return;
+  if (!yok || !lane_writes(a, yb)) return;
 #pragma unroll
   for (int i = 0; i < C; ++i) {
     const int x = x0 + i;
     if (x >= a.nx) continue;
     float4 pre = make_float4(0.f, 0.f, 0.f, 0.f);
     for (int s = 0; s < warp; ++s) add4(pre, s_sum[s][i][lane]);
-    *reinterpret_cast<float4*>(a.slab_T + ((static_cast<size_t>(cam) * kSlabsB + warp) * a.nx + x) * a.cy + yb) = pre;
+    *reinterpret_cast<float4*>(a.slab_T + ((static_cast<size_t>(cam) * kSlabsB + warp) * a.nx + x) * a.cy + a.row0 +
+                               yb) = pre;
   }
 }
 
@@ -506,10 +524,10 @@ __device__ __forceinline__ void scatter4(float* __restrict__ base, const Tap& t,
 // with the projector's own bilinear weights into the accumulator a.out
 // (vector reductions; all cameras in one launch, no scratch).
 template <int R, bool PSF, bool ATT, bool ADJ, class V>
-__global__ void __launch_bounds__(32 * kW, StorageTraits<V>::kMinBlocks) k_spread_yg(const YgArgs a, int c0) {
+__global__ void __launch_bounds__(32 * kW, 2) k_spread_yg(const YgArgs a, int c0) {
   using TS = TileShape<R>;
   constexpr bool KAHAN = StorageTraits<V>::kKahan;
-  const V* __restrict__ mu = reinterpret_cast<const V*>(a.mu);
+  const V* __restrict__ mu = reinterpret_cast<const V*>(a.mu) + a.row0;
   constexpr int NS = TS::NS;
   constexpr int K = 2 * R + 1;
   extern __shared__ __align__(16) unsigned char smem[];
@@ -525,12 +543,12 @@ __global__ void __launch_bounds__(32 * kW, StorageTraits<V>::kMinBlocks) k_sprea
   const int cam = c0 + g;
   const int x0 = (item % ntile) * kTXC;
   const int yb = lane * 4;
-  const bool yok = yb < a.cy;
+  const bool yok = lane_rows_ok(a, yb);
   const int zper = (a.nz + kSlabsB - 1) / kSlabsB;
   const int zbeg = slab * zper, zend = min(a.nz, zbeg + zper);
   if (zbeg >= zend) return;  // uniform over the CTA
-  if (PSF) {
-    for (int i = threadIdx.x; i < a.nz * 2 * K; i += blockDim.x) {
+  if (PSF) {  // this slab's planes only
+    for (int i = zbeg * 2 * K + threadIdx.x; i < zend * 2 * K; i += blockDim.x) {
       const int j = i % (2 * K), base = i - j;
       // transpose of a convolution = correlation: reverse each kernel
       const int src = !ADJ ? i : (j < K ? base + (K - 1 - j) : base + K + (2 * K - 1 - j));
@@ -538,9 +556,9 @@ __global__ void __launch_bounds__(32 * kW, StorageTraits<V>::kMinBlocks) k_sprea
     }
   }
   const CamRows cr = cam_rows(a.geom[cam].fwd);
-  const size_t vol = static_cast<size_t>(a.nz) * a.nx * a.cy;
-  float* __restrict__ tmp = ADJ ? a.out : a.temp + vol * g;
-  const float* __restrict__ srow = a.sino + static_cast<size_t>(cam) * a.nx * a.cy;
+  const size_t vol = static_cast<size_t>(a.nz) * a.nx * a.cs;  // one scratch volume
+  float* __restrict__ tmp = ADJ ? a.out + a.row0 : a.temp + vol * g;
+  const float* __restrict__ srow = a.sino + static_cast<size_t>(cam) * a.nx * a.cy + a.row0;
 
   float4 Tc[TS::kOwn], cTc[TS::kOwn];  // transmission per sampled column (+ Kahan compensation)
 #pragma unroll
@@ -549,7 +567,7 @@ __global__ void __launch_bounds__(32 * kW, StorageTraits<V>::kMinBlocks) k_sprea
     cTc[k] = make_float4(0.f, 0.f, 0.f, 0.f);
     const int xp = x0 - R + warp + kW * k;
     if (ATT && warp + kW * k < NS && xp >= 0 && xp < a.nx && yok)
-      Tc[k] = ldg4(a.slab_T + ((static_cast<size_t>(cam) * kSlabsB + slab) * a.nx + xp) * a.cy + yb);
+      Tc[k] = ldg4(a.slab_T + ((static_cast<size_t>(cam) * kSlabsB + slab) * a.nx + xp) * a.cy + a.row0 + yb);
   }
   __syncthreads();
 
@@ -584,10 +602,12 @@ __global__ void __launch_bounds__(32 * kW, StorageTraits<V>::kMinBlocks) k_sprea
     auto emit = [&](int i, const float4& v) {
       const int x = x0 + warp * kTXW + i;
       if (x >= a.nx || !yok) return;
-      if (ADJ)
-        scatter4(tmp, tb[warp * kTXW + i + R], yb, v);
-      else
-        *reinterpret_cast<float4*>(tmp + (static_cast<size_t>(z) * a.nx + x) * a.cy + yb) = v;
+      if (ADJ) {
+        // halo rows lack part of their PSF support: their owner window adds them
+        if (lane_writes(a, yb)) scatter4(tmp, tb[warp * kTXW + i + R], yb, v);
+      } else {
+        *reinterpret_cast<float4*>(tmp + (static_cast<size_t>(z) * a.nx + x) * a.cs + yb) = v;
+      }
     };
     if (PSF) {
       const float* kr = s_psf + z * 2 * K;
@@ -612,16 +632,16 @@ __global__ void __launch_bounds__(32 * kGatherWarps) k_gather_yg(const YgArgs a,
   const int Z = item / nchunk;
   const int X0 = (item % nchunk) * C;
   const int yb = lane * 4;
-  const bool yok = yb < a.cy;
   Tap* tap = s_gtap + warp * C * a.group;
   for (int e = lane; e < C * gcount; e += 32) {
     const int g = e / C, X = X0 + e % C;
     const CamRows cr = cam_rows(a.geom[c0 + g].bwd);
-    tap[e] = make_tap(X, Z, cr.m00, cr.m02, cr.m03, cr.m20, cr.m22, cr.m23, a.nx, a.nz, a.cy, X < a.nx);
+    // footprints in the scratch (column stride cs)
+    tap[e] = make_tap(X, Z, cr.m00, cr.m02, cr.m03, cr.m20, cr.m22, cr.m23, a.nx, a.nz, a.cs, X < a.nx);
   }
   __syncwarp();
-  if (!yok) return;
-  const size_t vol = static_cast<size_t>(a.nz) * a.nx * a.cy;
+  if (!lane_rows_ok(a, yb) || !lane_writes(a, yb)) return;
+  const size_t vol = static_cast<size_t>(a.nz) * a.nx * a.cs;
   // camera outer, columns inner: neighbouring accumulator columns of one
   // camera share footprint columns, which then hit in L1
   float4 acc[C];
@@ -636,7 +656,7 @@ __global__ void __launch_bounds__(32 * kGatherWarps) k_gather_yg(const YgArgs a,
   for (int i = 0; i < C; ++i) {
     const int X = X0 + i;
     if (X >= a.nx) continue;
-    float4* dst = reinterpret_cast<float4*>(a.out + (static_cast<size_t>(Z) * a.nx + X) * a.cy + yb);
+    float4* dst = reinterpret_cast<float4*>(a.out + (static_cast<size_t>(Z) * a.nx + X) * a.cy + a.row0 + yb);
     if (!first) add4(acc[i], *dst);
     *dst = acc[i];
   }
@@ -808,21 +828,68 @@ int spread_by_radius(int R, const YgArgs& a, int c0, int gcount, cudaStream_t st
 
 }  // namespace
 
+namespace {
+
+constexpr int kWindowRows = 128;  // rows one warp covers (32 lanes x 4)
+
+// Row windows of a volume for a PSF halo: window starts and valid ranges are
+// multiples of 4 (the halo is rounded up), every row is valid in exactly one
+// window, and a valid row's whole PSF support lies inside its window or past
+// the volume's edge.  Y-gantry rotations keep y, so a window computes its
+// valid rows with exactly the arithmetic of a single pass.
+struct Window {
+  int row0, rows, lo, hi;  // rows [row0, row0 + rows); valid [row0 + lo, row0 + hi)
+};
+
+std::vector<Window> row_windows(int ny, int halo) {
+  const int h = (halo + 3) & ~3;
+  std::vector<Window> w;
+  if (ny <= kWindowRows) {
+    w.push_back({0, ny, 0, ny});
+    return w;
+  }
+  int out0 = 0;
+  while (out0 < ny) {
+    const int in0 = std::max(0, out0 - h);
+    if (in0 + kWindowRows >= ny) {
+      w.push_back({in0, ny - in0, out0 - in0, ny - in0});
+      break;
+    }
+    const int out1 = in0 + kWindowRows - h;
+    w.push_back({in0, kWindowRows, out0 - in0, out1 - in0});
+    out0 = out1;
+  }
+  return w;
+}
+
+YgArgs windowed(const YgArgs& a, const Window& w) {
+  YgArgs b = a;
+  b.row0 = w.row0;
+  b.ny = w.rows;
+  b.out_lo = w.lo;
+  b.out_hi = w.hi;
+  b.cs = round_up(w.rows, 4);
+  return b;
+}
+
+int scratch_rows(int ny) { return round_up(std::min(ny, kWindowRows), 4); }
+
+}  // namespace
+
 bool yg_supported(int nx, int ny, int nz, int psf_k) {
   const int cy = round_up(ny, 4);
   if (nx < 1 || ny < 1 || nz < 1) return false;
-  if (cy > 128) return false;
   if (psf_k != 0 && (psf_k % 2 != 1 || psf_k > 15)) return false;
   // the PSF table of one CTA lives in shared memory next to the tile
   if (psf_k != 0 && tile_smem_bytes<7>(nz) > 110 * 1024) return false;
-  // 32-bit element offsets inside one volume / scratch slot
+  // 32-bit element offsets inside one volume
   if (static_cast<size_t>(nz) * nx * cy >= (1u << 31)) return false;
   return true;
 }
 
 size_t yg_backproject_workspace(int nx, int ny, int nz, int ncam, int group, int slots) {
   const size_t cy = round_up(ny, 4);
-  const size_t vol = static_cast<size_t>(nz) * nx * cy;
+  const size_t vol = static_cast<size_t>(nz) * nx * scratch_rows(ny);  // one window's scratch volume
   const size_t slabs = static_cast<size_t>(ncam) * kSlabsB * nx * cy;
   // with two slots the spread of group g+1 overlaps the gather of group g
   return sizeof(float) * (slabs + static_cast<size_t>(slots) * vol * std::max(1, std::min(group, ncam)));
@@ -831,20 +898,26 @@ size_t yg_backproject_workspace(int nx, int ny, int nz, int ncam, int group, int
 int yg_carry_slabs() { return kSlabsB; }
 
 int yg_mu_carry(const YgArgs& a_in, float* out, cudaStream_t st) {
-  YgArgs a = a_in;
-  a.slab_T = out;
-  const int nchunk = (a.nx + 7) / 8;
-  NRGB_LAUNCH_SCOPE("k_mu_carry_yg", st);
-  if (a.storage == kStorageBF16)
-    k_mu_carry_yg<__nv_bfloat16><<<a.ncam * nchunk, 32 * kSlabsB, 0, st>>>(a);
-  else
-    k_mu_carry_yg<float><<<a.ncam * nchunk, 32 * kSlabsB, 0, st>>>(a);
+  const int nchunk = (a_in.nx + 7) / 8;
+  for (const Window& w : row_windows(a_in.ny, 0)) {  // carries need no halo
+    YgArgs a = windowed(a_in, w);
+    a.slab_T = out;
+    NRGB_LAUNCH_SCOPE("k_mu_carry_yg", st);
+    if (a.storage == kStorageBF16)
+      k_mu_carry_yg<__nv_bfloat16><<<a.ncam * nchunk, 32 * kSlabsB, 0, st>>>(a);
+    else
+      k_mu_carry_yg<float><<<a.ncam * nchunk, 32 * kSlabsB, 0, st>>>(a);
+  }
   return cudaGetLastError() == cudaSuccess ? kOk : kErrKernel;
 }
 
 int yg_project(const YgArgs& a, cudaStream_t st) {
   const int R = a.psf ? (a.psf_k - 1) / 2 : 0;
-  return project_by_radius(R, a, st);
+  for (const Window& w : row_windows(a.ny, R)) {
+    const int s = project_by_radius(R, windowed(a, w), st);
+    if (s != kOk) return s;
+  }
+  return kOk;
 }
 
 namespace {
@@ -875,15 +948,16 @@ Pipe* pipe_for_current_device() {
 
 }  // namespace
 
-// Spreads run on the caller's stream, gathers on a second stream; group g
-// uses scratch slot g % 2, so the spread of group g+1 runs while the gather of
-// group g reads the other slot.
+// Per row window and camera group: spread on the caller's stream, gather on
+// a second stream; step g (over all windows' groups) uses scratch slot g % 2,
+// so the spread of step g+1 runs while the gather of step g reads the other
+// slot.
 int yg_backproject(const YgArgs& a_in, cudaStream_t st) {
   YgArgs a = a_in;
   const int R = a.psf ? (a.psf_k - 1) / 2 : 0;
   const int group = std::max(1, std::min(a.group, a.ncam));
   // work space: slab carries first (unless given), then the scratch slot(s)
-  const size_t vol = static_cast<size_t>(a.nz) * a.nx * a.cy;
+  const size_t vol = static_cast<size_t>(a.nz) * a.nx * scratch_rows(a.ny);
   float* slot0;
   if (a.carry || !a.mu) {  // carries given, or not needed without attenuation
     a.slab_T = const_cast<float*>(a.carry);
@@ -891,30 +965,37 @@ int yg_backproject(const YgArgs& a_in, cudaStream_t st) {
   } else {
     a.slab_T = a.work;
     slot0 = a.work + static_cast<size_t>(a.ncam) * kSlabsB * a.nx * a.cy;
-    if (a.mu) {
-      int s = yg_mu_carry(a, a.slab_T, st);
-      if (s != kOk) return s;
-    }
+    int s = yg_mu_carry(a, a.slab_T, st);
+    if (s != kOk) return s;
   }
   a.group = group;
+  const std::vector<Window> wins = row_windows(a.ny, R);
   if (a.back_mode == kBackAdjoint) {
-    // transpose of the projector: one launch over all cameras, scattered
-    // straight into the zeroed accumulator
-    if (cudaMemsetAsync(a.out, 0, sizeof(float) * vol, st) != cudaSuccess) return kErrKernel;
-    return spread_by_radius_t<true>(R, a, 0, a.ncam, st);
+    // transpose of the projector: one launch per window over all cameras,
+    // scattered straight into the zeroed accumulator
+    const size_t full = static_cast<size_t>(a.nz) * a.nx * a.cy;
+    if (cudaMemsetAsync(a.out, 0, sizeof(float) * full, st) != cudaSuccess) return kErrKernel;
+    for (const Window& w : wins) {
+      const int s = spread_by_radius_t<true>(R, windowed(a, w), 0, a.ncam, st);
+      if (s != kOk) return s;
+    }
+    return kOk;
   }
   const int nchunk = (a.nx + kGatherCols - 1) / kGatherCols;
   const int gblocks = (nchunk * a.nz + kGatherWarps - 1) / kGatherWarps;
   const size_t gsmem = sizeof(Tap) * kGatherWarps * kGatherCols * group;
   cudaFuncSetAttribute(k_gather_yg, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(gsmem));
   if (!a.pipelined) {
-    a.temp = slot0;
-    for (int c0 = 0; c0 < a.ncam; c0 += group) {
-      const int gcount = std::min(group, a.ncam - c0);
-      int st_ = spread_by_radius(R, a, c0, gcount, st);
-      if (st_ != kOk) return st_;
-      NRGB_LAUNCH_SCOPE("k_gather_yg", st);
-      k_gather_yg<<<gblocks, 32 * kGatherWarps, gsmem, st>>>(a, c0, gcount, c0 == 0 ? 1 : 0);
+    for (const Window& w : wins) {
+      YgArgs b = windowed(a, w);
+      b.temp = slot0;
+      for (int c0 = 0; c0 < b.ncam; c0 += group) {
+        const int gcount = std::min(group, b.ncam - c0);
+        int st_ = spread_by_radius(R, b, c0, gcount, st);
+        if (st_ != kOk) return st_;
+        NRGB_LAUNCH_SCOPE("k_gather_yg", st);
+        k_gather_yg<<<gblocks, 32 * kGatherWarps, gsmem, st>>>(b, c0, gcount, c0 == 0 ? 1 : 0);
+      }
     }
     return cudaGetLastError() == cudaSuccess ? kOk : kErrKernel;
   }
@@ -923,20 +1004,23 @@ int yg_backproject(const YgArgs& a_in, cudaStream_t st) {
   cudaEventRecord(pp->fork, st);
   cudaStreamWaitEvent(pp->aux, pp->fork, 0);
   int gi = 0;
-  for (int c0 = 0; c0 < a.ncam; c0 += group, ++gi) {
-    const int gcount = std::min(group, a.ncam - c0);
-    const int slot = gi & 1;
-    a.temp = slot0 + vol * group * slot;
-    if (gi >= 2) cudaStreamWaitEvent(st, pp->gather_done[slot], 0);
-    int st_ = spread_by_radius(R, a, c0, gcount, st);
-    if (st_ != kOk) return st_;
-    cudaEventRecord(pp->spread_done[slot], st);
-    cudaStreamWaitEvent(pp->aux, pp->spread_done[slot], 0);
-    {
-      NRGB_LAUNCH_SCOPE("k_gather_yg", pp->aux);
-      k_gather_yg<<<gblocks, 32 * kGatherWarps, gsmem, pp->aux>>>(a, c0, gcount, c0 == 0 ? 1 : 0);
+  for (const Window& w : wins) {
+    YgArgs b = windowed(a, w);
+    for (int c0 = 0; c0 < b.ncam; c0 += group, ++gi) {
+      const int gcount = std::min(group, b.ncam - c0);
+      const int slot = gi & 1;
+      b.temp = slot0 + vol * group * slot;
+      if (gi >= 2) cudaStreamWaitEvent(st, pp->gather_done[slot], 0);
+      int st_ = spread_by_radius(R, b, c0, gcount, st);
+      if (st_ != kOk) return st_;
+      cudaEventRecord(pp->spread_done[slot], st);
+      cudaStreamWaitEvent(pp->aux, pp->spread_done[slot], 0);
+      {
+        NRGB_LAUNCH_SCOPE("k_gather_yg", pp->aux);
+        k_gather_yg<<<gblocks, 32 * kGatherWarps, gsmem, pp->aux>>>(b, c0, gcount, c0 == 0 ? 1 : 0);
+      }
+      cudaEventRecord(pp->gather_done[slot], pp->aux);
     }
-    cudaEventRecord(pp->gather_done[slot], pp->aux);
   }
   cudaEventRecord(pp->join, pp->aux);
   cudaStreamWaitEvent(st, pp->join, 0);

@@ -30,17 +30,20 @@ def main(argv=None):
     ap.add_argument("--no-att", action="store_true")
     ap.add_argument("--reps", type=int, default=2)
     ap.add_argument("--mode", type=int, default=0, help="backprojector: 0 reference, 1 exact transpose")
+    ap.add_argument("--bf16", action="store_true", help="activity and mu stored in bfloat16")
+    ap.add_argument("--slope", type=float, default=0.02, help="PSF sigma = 0.5 + slope * depth")
     a = ap.parse_args(argv)
 
     L = _lib.load()
     n = a.n
     act = S.ellipsoid_phantom((n, n, n), seed=0)
     mu = S.mu_map((n, n, n), seed=0)
-    psf = S.gaussian_psf(a.psf, n, 0.5, 0.02) if a.psf else None
+    psf = S.gaussian_psf(a.psf, n, 0.5, a.slope) if a.psf else None
     cams = S.cameras_about_y(a.ncam)[1].copy()
     dev = torch.device("cuda", 0)
-    t_act = torch.from_numpy(act).to(dev)
-    t_mu = None if a.no_att else torch.from_numpy(mu).to(dev)
+    store = torch.bfloat16 if a.bf16 else torch.float32
+    t_act = torch.from_numpy(act).to(dev).to(store)
+    t_mu = None if a.no_att else torch.from_numpy(mu).to(dev).to(store)
     t_sino = torch.zeros((a.ncam, n, n), dtype=torch.float32, device=dev)
     t_bk = torch.zeros((n, n, n), dtype=torch.float32, device=dev)
     vp = ctypes.c_void_p
@@ -54,12 +57,14 @@ def main(argv=None):
     def run():
         sp = vp(stream.cuda_stream)
         if a.op in ("project", "pair"):
-            st = L.nrgb_project_device(vp(t_act.data_ptr()), mu_p, size, vp(t_sino.data_ptr()),
-                                       cams.ctypes.data_as(vp), csize, psf_p, psize, 0.0, 0.0, 1, sp)
+            fn = L.nrgb_project_device_bf16 if a.bf16 else L.nrgb_project_device
+            st = fn(vp(t_act.data_ptr()), mu_p, size, vp(t_sino.data_ptr()), cams.ctypes.data_as(vp), csize, psf_p,
+                    psize, 0.0, 0.0, 1, sp)
             assert st == 0, st
         if a.op in ("backproject", "pair"):
-            st = L.nrgb_backproject_device(vp(t_sino.data_ptr()), mu_p, size, vp(t_bk.data_ptr()),
-                                           cams.ctypes.data_as(vp), csize, psf_p, psize, 0.0, 0.0, 1, a.mode, sp)
+            fn = L.nrgb_backproject_device_bf16 if a.bf16 else L.nrgb_backproject_device
+            st = fn(vp(t_sino.data_ptr()), mu_p, size, vp(t_bk.data_ptr()), cams.ctypes.data_as(vp), csize, psf_p,
+                    psize, 0.0, 0.0, 1, a.mode, sp)
             assert st == 0, st
 
     run()
@@ -70,7 +75,7 @@ def main(argv=None):
         run()
     ev[1].record(stream)
     torch.cuda.synchronize()
-    print(f"{a.op} n={n} ncam={a.ncam} psf={a.psf} att={not a.no_att}: "
+    print(f"{a.op} n={n} ncam={a.ncam} psf={a.psf} att={not a.no_att} bf16={a.bf16}: "
           f"{ev[0].elapsed_time(ev[1]) / a.reps:.3f} ms per repetition")
     return 0
 

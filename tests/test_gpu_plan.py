@@ -125,3 +125,27 @@ def test_sharded_osem_plan_operator(data, world):
         x1 = rec.run(torch.ones(SHAPE, dtype=torch.float32, device="cuda"), 2)
         assert rec.collectives == 0
         assert rel_l2(x1.cpu().numpy(), xr) < 2 * RTOL
+
+
+def test_plan_tall_volume_row_windows():
+    """ny > 128: plans run the fused kernels in row windows (PSF halo 8 rows)."""
+    from niftyrec_gb300.plan import Plan
+
+    shape = (24, 260, 24)  # nz == nx: et_array_osem_step_subset's cubic-in-x volumes
+    act = S.ellipsoid_phantom(shape, seed=61)
+    mu = S.mu_map(shape, seed=61)
+    psf = S.gaussian_psf(15, shape[2], 0.5, 0.05)
+    cams = S.cameras_about_y(8, 2.0)
+    y = S.poisson_counts(A.project(act, cams, psf, mu), 80, seed=10)
+    p = Plan(shape, cams, psf, cuda(mu), subsets=2)
+    assert p.fused
+    order = p.subset_cameras(-1)
+    s = p.project(cuda(act)).cpu().numpy()
+    assert rel_l2(s, A.project(act, cams, psf, mu)[order]) < RTOL
+    b = p.backproject(cuda(y[order])).cpu().numpy()
+    assert rel_l2(b, A.backproject(y, cams, psf, mu, nz=shape[0])) < RTOL
+    x = p.osem(cuda(y), iterations=1, layout="column", graph=True).cpu().numpy()
+    xr = np.ones(shape, np.float32)
+    for sub in range(2):
+        xr = A.osem_step_subset(xr, y, cams, p.subset_cameras(sub), mu, psf)
+    assert rel_l2(x, xr) < 2 * RTOL
