@@ -248,6 +248,25 @@ int nrgb_plan_osem_step(void *plan, int subset, float *d_activity, const float *
 int nrgb_layout_convert(const float *src, float *dst, int nx, int ny, int planes, int direction, int truncate,
                         void *stream);
 
+/* Batches (no counterpart in the reference): one OSEM subset step of up to 64
+ * plans at once -- a persistent projector launch whose clusters take
+ * (volume, row window, camera, x-tile) work items from a queue, one ratio
+ * launch, each plan's backprojection, one update launch.  Plans must be fused
+ * and prepared for OSEM in column layout (nrgb_plan_osem_prepare(plan, 1)).
+ * The batch owns each volume's activity and counts (column layout); set them
+ * with nrgb_batch_set_activity / nrgb_batch_set_counts (device nifti arrays,
+ * counts in original camera order) and read the activity back with
+ * nrgb_batch_get_activity.  nrgb_batch_osem_step allocates nothing and copies
+ * nothing from the host, so steps can be captured in a CUDA graph; volume v
+ * runs subset (step mod n_subsets_v), and with iterations > 0 sits out steps
+ * >= iterations * n_subsets_v. */
+int nrgb_batch_create(void **out_batch, void *const *plans, int n_plans, void *stream);
+int nrgb_batch_destroy(void *batch);
+int nrgb_batch_set_counts(void *batch, int volume, const float *d_counts, void *stream);
+int nrgb_batch_set_activity(void *batch, int volume, const float *d_activity, void *stream);
+int nrgb_batch_get_activity(void *batch, int volume, float *d_activity, void *stream);
+int nrgb_batch_osem_step(void *batch, int step, int iterations, float epsilon, void *stream);
+
 /* Tuning table of the fused backprojector (no counterpart in the reference):
  * cameras per L2-resident scratch group for a problem shape (nx, ny, nz,
  * n_cameras); an all-zero shape sets the default for shapes without an entry

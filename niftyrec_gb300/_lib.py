@@ -72,6 +72,12 @@ PROTOTYPES = {
     "nrgb_plan_backproject": (_I, [_P, _I, _P, _P, _I, _I, _P]),
     "nrgb_plan_osem_prepare": (_I, [_P, _I, _P]),
     "nrgb_plan_osem_step": (_I, [_P, _I, _P, _P, _F, _P]),
+    "nrgb_batch_create": (_I, [ctypes.POINTER(_P), ctypes.POINTER(_P), _I, _P]),
+    "nrgb_batch_destroy": (_I, [_P]),
+    "nrgb_batch_set_counts": (_I, [_P, _I, _P, _P]),
+    "nrgb_batch_set_activity": (_I, [_P, _I, _P, _P]),
+    "nrgb_batch_get_activity": (_I, [_P, _I, _P, _P]),
+    "nrgb_batch_osem_step": (_I, [_P, _I, _I, _F, _P]),
     "nrgb_layout_convert": (_I, [_P, _P, _I, _I, _I, _I, _I, _P]),
     "nrgb_set_backproject_group": (_I, [_I, _I, _I, _I, _I]),
     "nrgb_get_backproject_group": (_I, [_I, _I, _I, _I]),

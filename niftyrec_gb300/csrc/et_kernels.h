@@ -89,6 +89,50 @@ size_t yg_backproject_workspace(int nx, int ny, int nz, int ncam, int group, int
 int yg_project(const YgArgs& a, cudaStream_t st);
 int yg_backproject(const YgArgs& a, cudaStream_t st);
 
+// ---- batches of volumes (one OSEM subset step of many plans at once) ----
+constexpr int kMaxBatch = 64;    // volumes per batched launch
+constexpr int kMaxWindows = 8;   // row windows per volume (ny up to ~900)
+// Device descriptor of one (volume, subset): the projector arguments for the
+// whole volume and the subset's cameras, its row windows, and the OSEM
+// buffers of that subset step.
+struct BatchStepDesc {
+  YgArgs proj;
+  int nwin = 0;
+  int win[kMaxWindows][4] = {};  // row0, rows, lo, hi (as the launchers' windows)
+  const float* counts = nullptr;   // subset counts, column layout
+  float* act = nullptr;            // activity (column layout; proj.act), written by the update
+  float* num = nullptr;            // backprojected ratio
+  const float* sens = nullptr;     // sensitivity of the subset
+  long long sino_elems = 0, vol_elems = 0;
+};
+// Selection of one batched projector launch, passed by value: descriptor per
+// volume and the prefix of its work items (window x camera x x-tile).
+struct BatchSel {
+  int n = 0, total = 0;
+  int desc[kMaxBatch] = {};
+  int begin[kMaxBatch + 1] = {};
+};
+// Selection of a batched elementwise launch: descriptor per volume and the
+// prefix of its elements.
+struct BatchElems {
+  int n = 0;
+  int desc[kMaxBatch] = {};
+  long long begin[kMaxBatch + 1] = {};
+};
+// Row windows the fused launchers use for ny rows and PSF width psf_k (0: no
+// PSF); writes 4 ints per window (row0, rows, lo, hi), returns the count or
+// -1 if more than max_windows.
+int yg_row_windows(int ny, int psf_k, int* out, int max_windows);
+// Persistent projector over all selected volumes: clusters take work items
+// from the counter (zeroed by the caller) until none are left.  Volumes of
+// one launch share psf_k and whether they have mu; max_nz sizes the PSF table.
+int yg_project_batch(const BatchStepDesc* d_desc, const BatchSel& sel, int psf_k, bool att, int max_nz,
+                     int* d_counter, cudaStream_t st);
+// ratio (desc.proj.out <- counts / max-rule(proj.out)) and update
+// (proj.act *= num / max(sens, eps)) over all selected volumes in one launch.
+int osem_ratio_batch(const BatchStepDesc* d_desc, const BatchElems& e, float eps, cudaStream_t st);
+int osem_update_batch(const BatchStepDesc* d_desc, const BatchElems& e, float eps, cudaStream_t st);
+
 // ---- layout conversion and elementwise helpers ----
 // planes x [ny][nx] (nifti) <-> planes x [nx][cy] (column), zero pads.
 int to_column(const float* src, float* dst, int nx, int ny, int cy, int planes, cudaStream_t st);

@@ -439,3 +439,219 @@ int nrgb_layout_convert(const float* src, float* dst, int nx, int ny, int planes
 }
 
 }  // extern "C"
+
+// ------------------------------------------------------------------ batches
+// A batch runs one OSEM subset step of many plans at once: one persistent
+// projector launch over every volume's subset cameras (per PSF width and
+// attenuation kind), one ratio launch, each plan's reference backprojection,
+// one update launch.  The batch owns each volume's activity and counts in
+// column layout; its descriptors are built once, so a step allocates nothing,
+// copies nothing from the host and can be captured in a CUDA graph.
+namespace nrgb {
+namespace {
+
+struct Batch {
+  int device = 0;
+  std::vector<Plan*> plans;
+  std::vector<int> order;      // volumes by decreasing work per item (large first)
+  char* mem = nullptr;
+  std::vector<float*> act;     // per volume: [nz][nx][cy]
+  std::vector<float*> counts;  // per volume: [ncam][nx][cy], plan camera order
+  std::vector<int> desc_base;  // per volume: descriptor index of subset 0
+  std::vector<BatchStepDesc> h_desc;
+  BatchStepDesc* d_desc = nullptr;
+  int* d_counter = nullptr;    // one per projector launch of a step
+};
+
+}  // namespace
+}  // namespace nrgb
+
+extern "C" {
+
+// Build a batch over fused plans prepared for OSEM in column layout
+// (nrgb_plan_osem_prepare(plan, 1, ...)).  At most 64 plans, one device.
+int nrgb_batch_create(void** out_batch, void* const* plans, int n_plans, void* stream) {
+  if (!out_batch || !plans || n_plans < 1 || n_plans > kMaxBatch) return kErrParameters;
+  *out_batch = nullptr;
+  Batch* b = new (std::nothrow) Batch();
+  if (!b) return kErrAllocCpu;
+  cudaGetDevice(&b->device);
+  size_t bytes = al(sizeof(int) * kMaxBatch);
+  int ndesc = 0;
+  for (int v = 0; v < n_plans; ++v) {
+    Plan* p = static_cast<Plan*>(plans[v]);
+    if (!p || !p->fused || p->osem_layout != kLayoutColumn || p->device != b->device) {
+      delete b;
+      return kErrParameters;
+    }
+    b->plans.push_back(p);
+    const Problem& pb = p->proj;
+    bytes += al(sizeof(float) * static_cast<size_t>(pb.nz) * pb.nx * p->cy);
+    bytes += al(sizeof(float) * static_cast<size_t>(pb.cams.n) * pb.nx * p->cy);
+    b->desc_base.push_back(ndesc);
+    ndesc += p->n_subsets;
+  }
+  bytes += al(sizeof(BatchStepDesc) * ndesc);
+  if (cudaMalloc(&b->mem, bytes) != cudaSuccess) {
+    cudaGetLastError();
+    delete b;
+    return kErrAllocGpu;
+  }
+  Carver cv(b->mem, bytes);
+  b->d_counter = cv.take<int>(kMaxBatch);
+  b->h_desc.resize(ndesc);
+  for (int v = 0; v < n_plans; ++v) {
+    Plan* p = b->plans[v];
+    const Problem& pb = p->proj;
+    b->act.push_back(cv.take<float>(static_cast<size_t>(pb.nz) * pb.nx * p->cy));
+    b->counts.push_back(cv.take<float>(static_cast<size_t>(pb.cams.n) * pb.nx * p->cy));
+    for (int s = 0; s < p->n_subsets; ++s) {
+      BatchStepDesc& d = b->h_desc[b->desc_base[v] + s];
+      const int c0 = p->sub_begin[s], n = p->sub_begin[s + 1] - c0;
+      const size_t plane = static_cast<size_t>(pb.nx) * p->cy;
+      YgArgs& a = d.proj;
+      a.nx = pb.nx;
+      a.ny = pb.ny;
+      a.nz = pb.nz;
+      a.cy = p->cy;
+      a.ncam = n;
+      a.geom = p->geom_p + c0;
+      a.act = b->act[v];
+      a.mu = p->has_att ? p->mu : nullptr;
+      a.out = p->osem_p;
+      a.psf = p->psf;
+      a.psf_k = pb.psf_k;
+      a.truncate = 1;
+      d.nwin = yg_row_windows(pb.ny, pb.psf_k, &d.win[0][0], kMaxWindows);
+      if (d.nwin < 0) {
+        cudaFree(b->mem);
+        delete b;
+        return kErrParameters;
+      }
+      d.counts = b->counts[v] + plane * c0;
+      d.act = b->act[v];
+      d.num = p->osem_num;
+      d.sens = p->sens + p->vol_elems * s;
+      d.sino_elems = static_cast<long long>(plane) * n;
+      d.vol_elems = static_cast<long long>(p->vol_elems);
+    }
+  }
+  b->d_desc = cv.take<BatchStepDesc>(ndesc);
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  if (cudaMemcpyAsync(b->d_desc, b->h_desc.data(), sizeof(BatchStepDesc) * ndesc, cudaMemcpyHostToDevice, st) !=
+      cudaSuccess) {
+    cudaFree(b->mem);
+    delete b;
+    return kErrTransferGpu;
+  }
+  cudaStreamSynchronize(st);  // the host descriptors are pageable
+  // large items first: the persistent projector then ends on small items
+  b->order.resize(n_plans);
+  for (int v = 0; v < n_plans; ++v) b->order[v] = v;
+  std::stable_sort(b->order.begin(), b->order.end(), [&](int x, int y) {
+    const Problem& px = b->plans[x]->proj;
+    const Problem& py = b->plans[y]->proj;
+    return static_cast<long long>(px.nz) * b->plans[x]->cy > static_cast<long long>(py.nz) * b->plans[y]->cy;
+  });
+  *out_batch = b;
+  return kOk;
+}
+
+int nrgb_batch_destroy(void* batch) {
+  Batch* b = static_cast<Batch*>(batch);
+  if (!b) return kErrParameters;
+  cudaDeviceSynchronize();
+  cudaFree(b->mem);
+  delete b;
+  return kOk;
+}
+
+// Counts of volume v: device (n_cameras, ny, nx) nifti, original camera order.
+int nrgb_batch_set_counts(void* batch, int v, const float* d_counts, void* stream) {
+  Batch* b = static_cast<Batch*>(batch);
+  if (!b || v < 0 || v >= static_cast<int>(b->plans.size()) || !d_counts) return kErrParameters;
+  const Plan& p = *b->plans[v];
+  const Problem& pb = p.proj;
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  const size_t in_plane = static_cast<size_t>(pb.nx) * pb.ny, out_plane = static_cast<size_t>(pb.nx) * p.cy;
+  for (int i = 0; i < pb.cams.n; ++i) {
+    const int s = to_column(d_counts + in_plane * p.order[i], b->counts[v] + out_plane * i, pb.nx, pb.ny, p.cy, 1, st);
+    if (s != kOk) return s;
+  }
+  return kOk;
+}
+
+// Activity of volume v in and out, device (nz, ny, nx) nifti.
+int nrgb_batch_set_activity(void* batch, int v, const float* d_activity, void* stream) {
+  Batch* b = static_cast<Batch*>(batch);
+  if (!b || v < 0 || v >= static_cast<int>(b->plans.size()) || !d_activity) return kErrParameters;
+  const Plan& p = *b->plans[v];
+  return to_column(d_activity, b->act[v], p.proj.nx, p.proj.ny, p.cy, p.proj.nz, static_cast<cudaStream_t>(stream));
+}
+
+int nrgb_batch_get_activity(void* batch, int v, float* d_activity, void* stream) {
+  Batch* b = static_cast<Batch*>(batch);
+  if (!b || v < 0 || v >= static_cast<int>(b->plans.size()) || !d_activity) return kErrParameters;
+  const Plan& p = *b->plans[v];
+  return from_column(b->act[v], d_activity, p.proj.nx, p.proj.ny, p.cy, p.proj.nz, 0,
+                     static_cast<cudaStream_t>(stream));
+}
+
+// One OSEM subset step of every volume: volume v runs its subset
+// (step mod n_subsets_v) with the update of nrgb_plan_osem_step.  With
+// iterations > 0, volumes that have completed that many passes over their
+// subsets (step >= iterations * n_subsets_v) sit the step out, so volumes with
+// different subset counts all end after `iterations` iterations.
+int nrgb_batch_osem_step(void* batch, int step, int iterations, float epsilon, void* stream) {
+  Batch* b = static_cast<Batch*>(batch);
+  if (!b || step < 0) return kErrParameters;
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  BatchElems ratio_e, vol_e;
+  // projector launches: one per (PSF width, attenuation) among the volumes
+  std::vector<std::pair<int, int>> kinds;
+  std::vector<int> sub(b->plans.size(), -1);
+  for (int v : b->order) {
+    Plan& p = *b->plans[v];
+    if (iterations > 0 && step >= iterations * p.n_subsets) continue;
+    const int s = step % p.n_subsets;
+    if (p.sub_begin[s + 1] - p.sub_begin[s] <= 0) continue;
+    sub[v] = s;
+    const std::pair<int, int> kind(p.proj.psf_k, p.has_att ? 1 : 0);
+    if (std::find(kinds.begin(), kinds.end(), kind) == kinds.end()) kinds.push_back(kind);
+    const BatchStepDesc& d = b->h_desc[b->desc_base[v] + s];
+    ratio_e.desc[ratio_e.n] = vol_e.desc[vol_e.n] = b->desc_base[v] + s;
+    ratio_e.begin[ratio_e.n + 1] = ratio_e.begin[ratio_e.n] + d.sino_elems;
+    vol_e.begin[vol_e.n + 1] = vol_e.begin[vol_e.n] + d.vol_elems;
+    ++ratio_e.n;
+    ++vol_e.n;
+  }
+  if (static_cast<int>(kinds.size()) > kMaxBatch) return kErrParameters;
+  if (cudaMemsetAsync(b->d_counter, 0, sizeof(int) * kinds.size(), st) != cudaSuccess) return kErrKernel;
+  for (size_t k = 0; k < kinds.size(); ++k) {
+    BatchSel sel;
+    int max_nz = 0;
+    for (int v : b->order) {
+      const Plan& p = *b->plans[v];
+      if (sub[v] < 0 || p.proj.psf_k != kinds[k].first || (p.has_att ? 1 : 0) != kinds[k].second) continue;
+      const BatchStepDesc& d = b->h_desc[b->desc_base[v] + sub[v]];
+      const int ntile = (d.proj.nx + 31) / 32;
+      sel.desc[sel.n] = b->desc_base[v] + sub[v];
+      sel.begin[sel.n + 1] = sel.begin[sel.n] + d.nwin * d.proj.ncam * ntile;
+      ++sel.n;
+      max_nz = std::max(max_nz, d.proj.nz);
+    }
+    sel.total = sel.begin[sel.n];
+    const int s = yg_project_batch(b->d_desc, sel, kinds[k].first, kinds[k].second != 0, max_nz, b->d_counter + k, st);
+    if (s != kOk) return s;
+  }
+  int s = osem_ratio_batch(b->d_desc, ratio_e, epsilon, st);
+  for (size_t v = 0; v < b->plans.size() && s == kOk; ++v) {
+    if (sub[v] < 0) continue;
+    Plan& p = *b->plans[v];
+    s = plan_backproject(p, sub[v], p.osem_p, p.osem_num, kLayoutColumn, 1, st);
+  }
+  if (s == kOk) s = osem_update_batch(b->d_desc, vol_e, epsilon, st);
+  return s;
+}
+
+}  // extern "C"

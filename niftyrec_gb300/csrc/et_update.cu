@@ -104,7 +104,52 @@ __global__ void k_sum_final(const double* __restrict__ part, int nparts, double*
   }
 }
 
+// The same two stages over a batch of volumes: a grid-stride loop over the
+// concatenation of the selected volumes' elements (prefix in e.begin).
+__device__ __forceinline__ int batch_volume(const BatchElems& e, long long i) {
+  int v = 0;
+  while (v + 1 < e.n && i >= e.begin[v + 1]) ++v;
+  return v;
+}
+
+__global__ void k_ratio_batch(const BatchStepDesc* __restrict__ d, const BatchElems e, float eps) {
+  const long long n = e.begin[e.n];
+  for (long long i = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; i < n;
+       i += static_cast<long long>(gridDim.x) * blockDim.x) {
+    const int v = batch_volume(e, i);
+    const BatchStepDesc& s = d[e.desc[v]];
+    const long long j = i - e.begin[v];
+    const float pv = s.proj.out[j];
+    s.proj.out[j] = (pv < eps) ? __fdiv_rn(s.counts[j], eps) : __fdiv_rn(s.counts[j], pv);
+  }
+}
+
+__global__ void k_update_batch(const BatchStepDesc* __restrict__ d, const BatchElems e, float eps) {
+  const long long n = e.begin[e.n];
+  for (long long i = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; i < n;
+       i += static_cast<long long>(gridDim.x) * blockDim.x) {
+    const int v = batch_volume(e, i);
+    const BatchStepDesc& s = d[e.desc[v]];
+    const long long j = i - e.begin[v];
+    float den = s.sens[j];
+    if (den < eps) den = eps;
+    s.act[j] = __fmul_rn(s.act[j], __fdiv_rn(s.num[j], den));
+  }
+}
+
 }  // namespace
+
+int osem_ratio_batch(const BatchStepDesc* d_desc, const BatchElems& e, float eps, cudaStream_t st) {
+  if (e.n <= 0) return kOk;
+  { NRGB_LAUNCH_SCOPE("k_ratio_batch", st); k_ratio_batch<<<grid_for(static_cast<size_t>(e.begin[e.n])), kBlock, 0, st>>>(d_desc, e, eps); }
+  return cudaGetLastError() == cudaSuccess ? kOk : kErrKernel;
+}
+
+int osem_update_batch(const BatchStepDesc* d_desc, const BatchElems& e, float eps, cudaStream_t st) {
+  if (e.n <= 0) return kOk;
+  { NRGB_LAUNCH_SCOPE("k_update_batch", st); k_update_batch<<<grid_for(static_cast<size_t>(e.begin[e.n])), kBlock, 0, st>>>(d_desc, e, eps); }
+  return cudaGetLastError() == cudaSuccess ? kOk : kErrKernel;
+}
 
 int osem_ratio(const float* y, float* p, size_t n, float eps, cudaStream_t st) {
   { NRGB_LAUNCH_SCOPE("k_ratio", st); k_ratio<float><<<grid_for(n), kBlock, 0, st>>>(y, p, n, eps); }

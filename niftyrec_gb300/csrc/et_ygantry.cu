@@ -443,6 +443,44 @@ __global__ void __cluster_dims__(kSlabsP, 1, 1) __launch_bounds__(32 * kW, 2)
   project_item<R, PSF, ATT, V>(a, item / ntile, (item % ntile) * kTXC, smem);
 }
 
+// Persistent projector over a batch of volumes: each cluster takes work items
+// (volume, row window, camera, x-tile) from a global counter until none are
+// left, so volumes of any size share the GPU in one launch.  The item number
+// is drawn by the cluster's first thread and read by the other CTAs from its
+// shared memory (double-buffered: the slot of item i is rewritten at item i+2,
+// after the barriers of item i+1).
+template <int R, bool PSF, bool ATT>
+__global__ void __cluster_dims__(kSlabsP, 1, 1) __launch_bounds__(32 * kW, 2)
+    k_project_batch_yg(const BatchStepDesc* __restrict__ descs, const BatchSel sel, int* __restrict__ counter) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  __shared__ int s_item[2];
+  cg::cluster_group cluster = cg::this_cluster();
+  const bool leader = cluster.block_rank() == 0 && threadIdx.x == 0;
+  for (int it = 0;; ++it) {
+    int* slot = &s_item[it & 1];
+    if (leader) *slot = atomicAdd(counter, 1);
+    cluster.sync();
+    const int item = *cluster.map_shared_rank(slot, 0);
+    if (item >= sel.total) {
+      cluster.sync();  // rank 0's shared memory stays alive until every CTA has read it
+      return;
+    }
+    int v = 0;
+    while (v + 1 < sel.n && item >= sel.begin[v + 1]) ++v;
+    const BatchStepDesc& d = descs[sel.desc[v]];
+    const int ntile = (d.proj.nx + kTXC - 1) / kTXC;
+    const int per_win = d.proj.ncam * ntile;
+    const int local = item - sel.begin[v];
+    const int w = local / per_win, r = local % per_win;
+    YgArgs a = d.proj;
+    a.row0 = d.win[w][0];
+    a.ny = d.win[w][1];
+    a.out_lo = d.win[w][2];
+    a.out_hi = d.win[w][3];
+    project_item<R, PSF, ATT, float>(a, r / ntile, (r % ntile) * kTXC, smem);
+  }
+}
+
 // ------------------------------------------------ backprojector: slab carry
 // carry[cam][s][x][y] = sum of the rotated mu over the depth slabs before s
 // (exclusive prefix): the transmission a depth slab starts from.
@@ -807,6 +845,41 @@ int project_by_radius(int R, const YgArgs& a, cudaStream_t st) {
   }
 }
 
+// Persistent grid: two CTAs per SM, whole clusters.
+constexpr int kBatchClusters = 152 * 2 / kSlabsP;
+
+template <int R, bool PSF>
+int launch_project_batch_R(const BatchStepDesc* d, const BatchSel& sel, bool att, int max_nz, int* counter,
+                           cudaStream_t st) {
+  const size_t smem = tile_smem_bytes<R>(PSF ? max_nz : 0);
+  auto go = [&](auto k) {
+    cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
+    NRGB_LAUNCH_SCOPE("k_project_batch_yg", st);
+    k<<<kBatchClusters * kSlabsP, 32 * kW, smem, st>>>(d, sel, counter);
+  };
+  if (att)
+    go(k_project_batch_yg<R, PSF, true>);
+  else
+    go(k_project_batch_yg<R, PSF, false>);
+  return cudaGetLastError() == cudaSuccess ? kOk : kErrKernel;
+}
+
+int project_batch_by_radius(int psf_k, const BatchStepDesc* d, const BatchSel& sel, bool att, int max_nz,
+                            int* counter, cudaStream_t st) {
+  if (psf_k == 0) return launch_project_batch_R<0, false>(d, sel, att, max_nz, counter, st);
+  switch ((psf_k - 1) / 2) {
+    case 0: return launch_project_batch_R<0, true>(d, sel, att, max_nz, counter, st);
+    case 1: return launch_project_batch_R<1, true>(d, sel, att, max_nz, counter, st);
+    case 2: return launch_project_batch_R<2, true>(d, sel, att, max_nz, counter, st);
+    case 3: return launch_project_batch_R<3, true>(d, sel, att, max_nz, counter, st);
+    case 4: return launch_project_batch_R<4, true>(d, sel, att, max_nz, counter, st);
+    case 5: return launch_project_batch_R<5, true>(d, sel, att, max_nz, counter, st);
+    case 6: return launch_project_batch_R<6, true>(d, sel, att, max_nz, counter, st);
+    case 7: return launch_project_batch_R<7, true>(d, sel, att, max_nz, counter, st);
+    default: return kErrParameters;
+  }
+}
+
 template <bool ADJ>
 int spread_by_radius_t(int R, const YgArgs& a, int c0, int gcount, cudaStream_t st) {
   switch (R) {
@@ -875,6 +948,24 @@ YgArgs windowed(const YgArgs& a, const Window& w) {
 int scratch_rows(int ny) { return round_up(std::min(ny, kWindowRows), 4); }
 
 }  // namespace
+
+int yg_row_windows(int ny, int psf_k, int* out, int max_windows) {
+  const std::vector<Window> w = row_windows(ny, psf_k > 0 ? (psf_k - 1) / 2 : 0);
+  if (static_cast<int>(w.size()) > max_windows) return -1;
+  for (size_t i = 0; i < w.size(); ++i) {
+    out[4 * i + 0] = w[i].row0;
+    out[4 * i + 1] = w[i].rows;
+    out[4 * i + 2] = w[i].lo;
+    out[4 * i + 3] = w[i].hi;
+  }
+  return static_cast<int>(w.size());
+}
+
+int yg_project_batch(const BatchStepDesc* d_desc, const BatchSel& sel, int psf_k, bool att, int max_nz,
+                     int* d_counter, cudaStream_t st) {
+  if (sel.n <= 0 || sel.total <= 0) return kOk;
+  return project_batch_by_radius(psf_k, d_desc, sel, att, max_nz, d_counter, st);
+}
 
 bool yg_supported(int nx, int ny, int nz, int psf_k) {
   const int cy = round_up(ny, 4);
