@@ -321,6 +321,8 @@ def run_ours(args):
     }
     if not args.no_osem:
         out["osem"] = osem_compare(act, mu, psf, cams, dev)
+    if not args.no_batch:
+        out["batch_osem"] = batch_compare(dev)
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         out["cpu_baseline"] = cpu_baseline(act, mu, psf, cams, args.cpu_angles)
     if rank == 0:
@@ -378,6 +380,100 @@ def osem_compare(act, mu, psf, cams, dev, n_subsets=8, iterations=3):
     return {"workload": f"OSEM iteration, 128^3, {NCAM} angles, {n_subsets} interleaved subsets, PSF 11x11, mu",
             "per_call_iteration_ms": round(per_call, 3), "plan_eager_iteration_ms": round(eager_ms, 3),
             "plan_graph_iteration_ms": round(graph_ms, 3), "speedup_graph_vs_per_call": round(per_call / graph_ms, 2)}
+
+
+# ------------------------------------------------------------ batched OSEM
+def batch_compare(dev, n_volumes=24, reps=5):
+    """One OSEM subset step of 24 volumes of uneven size (64^3, 96x96x80,
+    128^3, 160x160x128; 60/90/120/180 angles; 4-16 interleaved subsets; PSF
+    11x11 with per-volume sigma slope; mu): the plain per-call drop-in
+    (et_array_osem_step_subset with host buffers, one call per volume) against
+    per-volume plan steps (eager and in one CUDA graph) and the batch (one
+    persistent projector launch for all volumes; eager and graph-replayed)."""
+    import torch
+
+    from niftyrec_gb300 import array_api as A
+    from niftyrec_gb300 import synthetic as S
+    from niftyrec_gb300.batch import Batch, config_volumes
+    from niftyrec_gb300.plan import Plan
+
+    vols = []
+    for c in config_volumes(n_volumes):
+        shape = c["shape"]
+        act = S.ellipsoid_phantom(shape, seed=c["seed"])
+        mu = S.mu_map(shape, seed=c["seed"])
+        psf = S.gaussian_psf(K, shape[2], 0.5, c["slope"])
+        cams = S.cameras_about_y(c["ncam"], 0.0, 360.0 / c["ncam"])
+        y = S.poisson_counts(A.project(act, cams, psf, mu), 50, seed=c["seed"])
+        vols.append((c, act, mu, psf, cams, y))
+    stream = torch.cuda.current_stream(dev)
+
+    def dev_ms(fn, n=reps):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        fn()
+        torch.cuda.synchronize(dev)
+        e0.record(stream)
+        for _ in range(n):
+            fn()
+        e1.record(stream)
+        torch.cuda.synchronize(dev)
+        return e0.elapsed_time(e1) / n
+
+    # plain per-call drop-in: one subset step per volume composed from the host
+    # C-ABI projection / backprojection calls with the update on the host, as
+    # et_array_osem_step does (emission-lib/_et_array_interface.cpp:1017-1044;
+    # the entry itself takes cubic-in-x volumes only)
+    def per_call():
+        for c, act, mu, psf, cams, y in vols:
+            idx = list(range(0, c["ncam"], c["subsets"]))
+            sub = np.ascontiguousarray(cams[:, idx])
+            x = np.ones_like(act)
+            p = A.project(x, sub, psf, mu)
+            r = np.where(p < 1e-6, y[idx] / np.float32(1e-6), y[idx] / np.maximum(p, 1e-6)).astype(np.float32)
+            num = A.backproject(r, sub, psf, mu, nz=act.shape[0])
+            den = A.backproject(np.ones_like(r), sub, psf, mu, nz=act.shape[0])
+            x *= num / np.maximum(den, np.float32(1e-6))
+
+    per_call()
+    t0 = time.perf_counter()
+    for _ in range(2):
+        per_call()
+    per_call_ms = (time.perf_counter() - t0) / 2 * 1e3
+
+    plans = [Plan(c["shape"], cams, psf, torch.from_numpy(mu).to(dev), subsets=c["subsets"])
+             for c, act, mu, psf, cams, y in vols]
+    for p in plans:
+        p.osem_prepare("column")
+    ys = [p.split_counts(torch.from_numpy(v[5]).to(dev), "column") for p, v in zip(plans, vols)]
+    xs = [p.to_column(torch.ones(p.shape, dtype=torch.float32, device=dev)) for p in plans]
+
+    def plan_steps():
+        for p, x, y in zip(plans, xs, ys):
+            p.osem_step(x, y[0], 0)
+
+    plan_eager = dev_ms(plan_steps)
+    g_plans = torch.cuda.CUDAGraph()
+    with torch.cuda.graph(g_plans):
+        plan_steps()
+    plan_graph = dev_ms(g_plans.replay)
+
+    b = Batch(plans)
+    for v, vv in enumerate(vols):
+        b.set_counts(v, torch.from_numpy(vv[5]).to(dev))
+        b.set_activity(v, torch.ones(plans[v].shape, dtype=torch.float32, device=dev))
+    batch_eager = dev_ms(lambda: b.step(0))
+    g_batch = torch.cuda.CUDAGraph()
+    with torch.cuda.graph(g_batch):
+        b.step(0)
+    batch_graph = dev_ms(g_batch.replay)
+    n_angles = sum(len(range(0, c["ncam"], c["subsets"])) for c, *_ in vols)
+    return {"workload": f"one OSEM subset step of {n_volumes} volumes (64^3, 96x96x80, 128^3, 160x160x128; "
+                        f"60/90/120/180 angles; 4-16 subsets; PSF 11x11; mu), {n_angles} angles in the step",
+            "per_call_ms": round(per_call_ms, 3), "plan_eager_ms": round(plan_eager, 3),
+            "plan_graph_ms": round(plan_graph, 3), "batch_eager_ms": round(batch_eager, 3),
+            "batch_graph_ms": round(batch_graph, 3),
+            "speedup_batch_graph_vs_per_call": round(per_call_ms / batch_graph, 2),
+            "speedup_batch_graph_vs_plan_graph": round(plan_graph / batch_graph, 3)}
 
 
 # ----------------------------------------------------------- CPU baselines
@@ -469,6 +565,7 @@ def main():
     ap.add_argument("--cpu-angles", type=int, default=24)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-osem", action="store_true")
+    ap.add_argument("--no-batch", action="store_true")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
