@@ -77,7 +77,20 @@ int et_array_attenuation_gradient(float *sino, int *sino_size, float *activity, 
                                   int *psf_size, float *attenuation, int *attenuation_size, float background,
                                   float background_attenuation, int GPU, int truncate_negative_values);
 
-/* PSF / camera helpers -- emission-lib/_et_array_interface.h:53-55. */
+/* Projection with partial sums -- emission-lib/_et_array_interface.h:47
+ * (GPU semantics of et_project_partial_gpu, emission-lib/_et.cpp:2106-2436;
+ * the reference's CPU path is a stub).  Per camera: the projection, and in
+ * partialsum ([nx, ny, nz, n_cameras]) the emission reaching each depth from
+ * the far side, in the rotated frame or, with do_rotate_partial, rotated back
+ * to the image frame.  background_image ([nx, ny]) scales the background or
+ * is NULL. */
+int et_array_project_partial(float *activity, int *activity_size, float *sinogram, int *sinogram_size,
+                             float *partialsum, int *partialsum_size, float *cameras, int *cameras_size, float *psf,
+                             int *psf_size, float *attenuation, int *attenuation_size, float background,
+                             float *background_image, float background_attenuation, int GPU,
+                             int truncate_negative_values, int do_rotate_partial);
+
+/* PSF / camera helpers -- emission-lib/_et_array_interface.h:53-55. *//* PSF / camera helpers -- emission-lib/_et_array_interface.h:53-55. */
 int et_array_calculate_size_psf(unsigned int *psf_size_x, unsigned int *psf_size_y, float fwhm_pixels_dist0,
                                 float sensitivity0, float dist0, float fwhm_pixels_dist1, float sensitivity1,
                                 float dist1);
@@ -247,6 +260,16 @@ int nrgb_plan_osem_step(void *plan, int subset, float *d_activity, const float *
                         void *stream);
 int nrgb_layout_convert(const float *src, float *dst, int nx, int ny, int planes, int direction, int truncate,
                         void *stream);
+/* One-step-late MAP-EM step with the quadratic MRF prior on a plan (the
+ * reference runs it in Python on host arrays: et_osmapem_step,
+ * Python/NiftyRec/NiftyRec/NiftyRec.py:224-245, prior gradient :400-404).  The
+ * prior gradient (26 x minus the 26 neighbours, zero outside the grid) is
+ * computed from the current activity; x *= max(A^T(y / (max(Ax, 0) + eps)), 0)
+ * / (max(sens - beta g, 0) + eps).  Layouts as nrgb_plan_osem_step. */
+int nrgb_plan_osmapem_step(void *plan, int subset, float *d_activity, const float *d_counts, float beta,
+                           float epsilon, void *stream);
+/* The prior gradient alone, device volume in nifti order; size = {nx, ny, nz}. */
+int nrgb_mrf_gradient_device(const float *d_activity, float *d_gradient, const int *size, void *stream);
 
 /* Batches (no counterpart in the reference): one OSEM subset step of up to 64
  * plans at once -- a persistent projector launch whose clusters take

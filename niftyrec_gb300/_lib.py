@@ -42,6 +42,8 @@ PROTOTYPES = {
     "et_array_backproject": (_I, [_P, _PI, _P, _PI, _P, _PI, _P, _PI, _P, _PI, _F, _F, _I, _I]),
     "et_array_gradient_attenuation": (_I, [_P, _PI, _P, _PI, _P, _PI, _P, _PI, _P, _PI, _P, _PI, _F, _F, _I, _I]),
     "et_array_attenuation_gradient": (_I, [_P, _PI, _P, _PI, _P, _PI, _P, _PI, _P, _PI, _P, _PI, _F, _F, _I, _I]),
+    "et_array_project_partial": (_I, [_P, _PI, _P, _PI, _P, _PI, _P, _PI, _P, _PI, _P, _PI, _F, _P, _F, _I, _I,
+                                      _I]),
     "et_array_calculate_size_psf": (_I, [ctypes.POINTER(_U), ctypes.POINTER(_U), _F, _F, _F, _F, _F, _F]),
     "et_array_make_psf": (_I, [_P, _U, _U, _F, _F, _F, _F, _F, _F, _U]),
     "et_array_make_cameras": (_I, [_P, _F, _F, _U, _U]),
@@ -78,6 +80,8 @@ PROTOTYPES = {
     "nrgb_batch_set_activity": (_I, [_P, _I, _P, _P]),
     "nrgb_batch_get_activity": (_I, [_P, _I, _P, _P]),
     "nrgb_batch_osem_step": (_I, [_P, _I, _I, _F, _P]),
+    "nrgb_plan_osmapem_step": (_I, [_P, _I, _P, _P, _F, _F, _P]),
+    "nrgb_mrf_gradient_device": (_I, [_P, _P, _PI, _P]),
     "nrgb_layout_convert": (_I, [_P, _P, _I, _I, _I, _I, _I, _P]),
     "nrgb_set_backproject_group": (_I, [_I, _I, _I, _I, _I]),
     "nrgb_get_backproject_group": (_I, [_I, _I, _I, _I]),

@@ -65,6 +65,31 @@ def project(activity, cameras, psf=None, attenuation=None, background=0.0, backg
     return sino
 
 
+def project_partial(activity, cameras, psf=None, attenuation=None, background=0.0, background_image=None,
+                    background_attenuation=0.0, truncate_negative_values=1, rotate_partial=0):
+    """et_array_project_partial; returns (sinogram (n_cameras, ny, nx),
+    partial sums (n_cameras, nz, ny, nx)): per camera the emission reaching
+    each depth from the far side, in the rotated frame or (rotate_partial=1)
+    rotated back to the image frame."""
+    L = load()
+    act, att, psf, cams = _f32(activity), _f32(attenuation), _f32(psf), _f32(cameras)
+    bgi = _f32(background_image)
+    ref = act if act is not None else att
+    nz, ny, nx = ref.shape
+    cs = _cam_size(cams)
+    sino = np.zeros((cs[0], ny, nx), np.float32)
+    part = np.zeros((cs[0], nz, ny, nx), np.float32)
+    asz = _ints([nx, ny, nz] if act is not None else [0, 0, 0])
+    tsz = _ints([nx, ny, nz] if att is not None else [0, 0, 0])
+    psz = _ints(psf.shape[::-1] if psf is not None else [0, 0, 0])
+    st = L.et_array_project_partial(_p(act), _pi(asz), _p(sino), _pi(_ints([nx, ny, cs[0]])), _p(part),
+                                    _pi(_ints([nx, ny, nz, cs[0]])), _p(cams), _pi(_ints(cs)), _p(psf), _pi(psz),
+                                    _p(att), _pi(tsz), background, _p(bgi), background_attenuation, 1,
+                                    truncate_negative_values, rotate_partial)
+    _check("et_array_project_partial", st)
+    return sino, part
+
+
 def backproject(sinogram, cameras, psf=None, attenuation=None, background=0.0, background_attenuation=0.0,
                 truncate_negative_values=1, nz=None):
     """SPECT_backproject_parallelholes; returns the volume (nz, ny, nx), nz defaults to nx."""

@@ -155,6 +155,36 @@ int osem_step_host(const Problem& pb, float* act, const float* ysub, const float
   return finish(ds, s);
 }
 
+int project_partial_host(const Problem& pb, const float* act, const float* att, const float* bg_image, float* sino,
+                         float* partial, int do_rotate) {
+  int s;
+  DeviceState& ds = current_device_state(&s);
+  if (s != kOk) return s;
+  std::lock_guard<std::mutex> lk(ds.mu);
+  const size_t nvox = static_cast<size_t>(pb.nx) * pb.ny * pb.nz;
+  const size_t nxy = static_cast<size_t>(pb.nx) * pb.ny;
+  const size_t nsino = nxy * pb.cams.n;
+  const size_t npart = nvox * pb.cams.n;
+  const size_t ws = partial_workspace(pb);
+  if ((s = ensure_arena(ds, fbytes(2 * nvox + nxy + nsino + npart) + 6 * 256 + ws)) != kOk) return s;
+  Carver cv(ds.arena, ds.arena_bytes);
+  float* d_act = act ? cv.take<float>(nvox) : nullptr;
+  float* d_att = att ? cv.take<float>(nvox) : nullptr;
+  float* d_bgi = bg_image ? cv.take<float>(nxy) : nullptr;
+  float* d_sino = cv.take<float>(nsino);
+  float* d_part = cv.take<float>(npart);
+  char* w = cv.take<char>(ws);
+  cudaStream_t st = ds.stream;
+  if (act && (s = h2d(d_act, act, nvox, st)) != kOk) return finish(ds, s);
+  if (att && (s = h2d(d_att, att, nvox, st)) != kOk) return finish(ds, s);
+  if (bg_image && (s = h2d(d_bgi, bg_image, nxy, st)) != kOk) return finish(ds, s);
+  g_last_path = 2;
+  s = project_partial_device(pb, d_act, d_att, d_bgi, d_sino, d_part, do_rotate, w, ws, &ds.staging, st);
+  if (s == kOk) s = d2h(sino, d_sino, nsino, st);
+  if (s == kOk) s = d2h(partial, d_part, npart, st);
+  return finish(ds, s);
+}
+
 // random_0_1 of emission-lib/_et_array_interface.cpp:961-967 (two rand() draws).
 float random_0_1() {
   const float scale = RAND_MAX + 1.;
@@ -524,6 +554,47 @@ int et_array_osem_step_subset(float* activity_data, int size_x, int size_y, floa
   return subset_step(activity_data, size_x, size_y, sinogram_data, n_cameras, cameras_data, idx, use_attenuation,
                      attenuation_data, use_psf, psf_data, psf_size_x, psf_size_y, background, background_attenuation,
                      epsilon);
+}
+
+// emission-lib/_et_array_interface.cpp:1561-1760 (GPU semantics of
+// et_project_partial_gpu, emission-lib/_et.cpp:2106-2436; the reference's CPU
+// path is a stub).  partialsum is [nx, ny, nz, n_cameras]; background_image
+// [nx, ny] or NULL.
+int et_array_project_partial(float* activity, int* activity_size, float* sinogram, int* sinogram_size,
+                             float* partialsum, int* partialsum_size, float* cameras, int* cameras_size, float* psf,
+                             int* psf_size, float* attenuation, int* attenuation_size, float background,
+                             float* background_image, float background_attenuation, int GPU,
+                             int truncate_negative_values, int do_rotate_partial) {
+  (void)GPU;
+  if (!activity_size || !cameras_size || !psf_size || !attenuation_size || !sinogram || !partialsum ||
+      !partialsum_size)
+    return kErrParameters;
+  int asz[3] = {activity_size[0], activity_size[1], activity_size[2]};
+  const bool no_act = all_zero3(asz);
+  const bool no_psf = all_zero3(psf_size);
+  const bool no_att = all_zero3(attenuation_size);
+  if (no_act && no_att) return kErrParameters;
+  if (no_act) std::memcpy(asz, attenuation_size, sizeof(asz));
+  const int ncam = cameras_size[0], ncols = cameras_size[1];
+  if (!(ncols == 1 || ncols == 3 || ncols == 6)) return kErrParameters;
+  if (!no_psf && (psf_size[0] % 2 != 1 || psf_size[1] % 2 != 1 || psf_size[2] != asz[0])) return kErrParameters;
+  const long long nvox = static_cast<long long>(asz[0]) * asz[1] * asz[2];
+  if (static_cast<long long>(partialsum_size[0]) * partialsum_size[1] * partialsum_size[2] * partialsum_size[3] <
+      nvox * ncam)
+    return kErrParameters;
+  if (sinogram_size &&
+      static_cast<long long>(sinogram_size[0]) * sinogram_size[1] * sinogram_size[2] <
+          static_cast<long long>(asz[0]) * asz[1] * ncam)
+    return kErrParameters;
+  Cameras cc;
+  int s = expand_cameras(cameras, ncam, ncols, asz, &cc);
+  if (s != kOk) return s;
+  Problem pb;
+  s = make_problem(asz[0], asz[1], asz[2], cc, no_psf ? nullptr : psf, psf_size, background, background_attenuation,
+                   truncate_negative_values, &pb);
+  if (s != kOk) return s;
+  return project_partial_host(pb, no_act ? nullptr : activity, no_att ? nullptr : attenuation, background_image,
+                              sinogram, partialsum, do_rotate_partial);
 }
 
 // emission-lib/_et_array_interface.cpp:1080-1131.

@@ -288,6 +288,37 @@ int backproject_device(const Problem& pb, const float* d_sino, const float* d_at
   return check(pb.back_mode == kBackAdjoint ? general_adjoint(g, st) : general_backproject(g, st));
 }
 
+size_t partial_workspace(const Problem& pb) { return common_bytes(pb) + sizeof(float) * vol_n(pb) * 3 + 3 * 256; }
+
+int project_partial_device(const Problem& pb, const float* d_act, const float* d_att, const float* d_bg_image,
+                           float* d_sino, float* d_partial, int do_rotate, char* ws, size_t ws_bytes, Staging* stg,
+                           cudaStream_t st) {
+  Carver cv(ws, ws_bytes);
+  CamGeom* d_geom;
+  float* d_psf;
+  int s = upload_common(pb, cv, &d_geom, &d_psf, stg, st);
+  if (s != kOk) return s;
+  GeneralArgs g;
+  g.nx = pb.nx;
+  g.ny = pb.ny;
+  g.nz = pb.nz;
+  g.ncam = pb.cams.n;
+  g.geom_host = pb.geom.data();
+  g.act = d_act;
+  g.att = d_att;
+  g.out = d_sino;
+  g.psf_sep = d_psf;
+  g.psf_k = pb.psf_k;
+  g.bg = pb.bg;
+  g.bg_att = pb.bg_att;
+  g.truncate = pb.truncate;
+  g.ws_act = cv.take<float>(vol_n(pb));
+  g.ws_att = cv.take<float>(vol_n(pb));
+  g.ws_tmp = cv.take<float>(vol_n(pb));
+  if (!g.ws_act || !g.ws_att || !g.ws_tmp) return kErrAllocGpu;
+  return check(general_project_partial(g, d_bg_image, d_partial, do_rotate, st));
+}
+
 int dmu_device(const Problem& pb, const float* d_g, const float* d_act, const float* d_att, float* d_out, char* ws,
                size_t ws_bytes, Staging* stg, cudaStream_t st) {
   Carver cv(ws, ws_bytes);

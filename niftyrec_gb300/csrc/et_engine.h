@@ -106,6 +106,12 @@ int backproject_device(const Problem& pb, const float* d_sino, const float* d_at
                        size_t ws_bytes, Staging* stg, cudaStream_t st);
 int gradient_device(const Problem& pb, const float* d_sino, const float* d_act, const float* d_att, float* d_out,
                     char* ws, size_t ws_bytes, Staging* stg, cudaStream_t st);
+// Projection with partial sums (et_project_partial): d_partial receives
+// [ncam][nz][ny][nx]; d_bg_image [ny][nx] or null.
+size_t partial_workspace(const Problem& pb);
+int project_partial_device(const Problem& pb, const float* d_act, const float* d_att, const float* d_bg_image,
+                           float* d_sino, float* d_partial, int do_rotate, char* ws, size_t ws_bytes, Staging* stg,
+                           cudaStream_t st);
 // float64 reference run of the general-orientation projector and the
 // reference backprojector (geometry, PSF and every operation in double);
 // device buffers are double, nifti order.

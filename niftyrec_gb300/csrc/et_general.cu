@@ -232,6 +232,32 @@ __global__ void k_spread(const R* __restrict__ plane, const R* __restrict__ att,
   }
 }
 
+// Partial-sum line integral, the partial-sum branch of
+// emission-lib_gpu/_et_line_integral_attenuated_gpu_kernels.cu:57-103: walk
+// depth from the far end, partial[z] = s before voxel z is added and
+// attenuated; s starts at bg (times bg_image[x, y]); the projection is the
+// final s.
+__global__ void k_line_partial(const float* __restrict__ act, const float* __restrict__ att,
+                               const float* __restrict__ bg_image, float* __restrict__ out,
+                               float* __restrict__ partial, int nx, int ny, int nz, float bg) {
+  const int nxy = nx * ny;
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= nxy) return;
+  float s = bg;
+  if (bg_image) s = fm(s, __ldg(bg_image + i));
+  for (int z = nz - 1; z >= 0; --z) {
+    const size_t j = static_cast<size_t>(z) * nxy + i;
+    partial[j] = s;
+    if (act && att)
+      s = fm(fa(s, __ldg(act + j)), expf(-__ldg(att + j)));
+    else if (att)
+      s = fm(s, expf(-__ldg(att + j)));
+    else
+      s = fa(s, __ldg(act + j));
+  }
+  out[i] = s;
+}
+
 template <class R>
 __global__ void k_truncate_t(R* __restrict__ buf, size_t n) {
   for (size_t i = blockIdx.x * static_cast<size_t>(blockDim.x) + threadIdx.x; i < n;
@@ -359,6 +385,40 @@ int general_backproject_t(const GeneralArgsT<T>& a, cudaStream_t st) {
 }
 
 }  // namespace
+
+// et_project_partial_gpu (emission-lib/_et.cpp:2106-2436): per camera rotate
+// activity (bg) and mu (bg_att), PSF, partial-sum line integral; with
+// do_rotate the camera's partial-sum volume is rotated back to the image frame
+// (-theta, ZYX, background bg, :2373-2404).  partial: [ncam][nz][ny][nx].
+int general_project_partial(const GeneralArgs& a, const float* bg_image, float* partial, int do_rotate,
+                            cudaStream_t st) {
+  const int nx = a.nx, ny = a.ny, nz = a.nz;
+  const size_t nvox = static_cast<size_t>(nx) * ny * nz, nxy = static_cast<size_t>(nx) * ny;
+  const int B = 256;
+  for (int cam = 0; cam < a.ncam; ++cam) {
+    const Affine34 F = affine_of(a.geom_host[cam].fwd);
+    if (a.act) { NRGB_LAUNCH_SCOPE("k_resample", st); k_resample<false><<<grid_for(nvox, B), B, 0, st>>>(a.act, a.ws_act, nx, ny, nz, F, a.bg); }
+    if (a.att) { NRGB_LAUNCH_SCOPE("k_resample", st); k_resample<false><<<grid_for(nvox, B), B, 0, st>>>(a.att, a.ws_att, nx, ny, nz, F, a.bg_att); }
+    if (a.psf_sep && a.act) {
+      { NRGB_LAUNCH_SCOPE("k_conv", st); k_conv<true><<<grid_for(nvox, B), B, 0, st>>>(a.ws_act, a.ws_tmp, nx, ny, nz, a.psf_sep, a.psf_k); }
+      { NRGB_LAUNCH_SCOPE("k_conv", st); k_conv<false><<<grid_for(nvox, B), B, 0, st>>>(a.ws_tmp, a.ws_act, nx, ny, nz, a.psf_sep, a.psf_k); }
+    }
+    float* dst = partial + nvox * cam;
+    {
+      NRGB_LAUNCH_SCOPE("k_line_partial", st);
+      k_line_partial<<<static_cast<int>((nxy + B - 1) / B), B, 0, st>>>(
+          a.act ? a.ws_act : nullptr, a.att ? a.ws_att : nullptr, bg_image, a.out + nxy * cam,
+          do_rotate ? a.ws_tmp : dst, nx, ny, nz, a.bg);
+    }
+    if (do_rotate) {
+      NRGB_LAUNCH_SCOPE("k_resample", st);
+      k_resample<false><<<grid_for(nvox, B), B, 0, st>>>(a.ws_tmp, dst, nx, ny, nz, affine_of(a.geom_host[cam].bwd),
+                                                          a.bg);
+    }
+  }
+  if (a.truncate) launch_truncate_t<float>(a.out, nxy * a.ncam, st);
+  return cudaGetLastError() == cudaSuccess ? kOk : kErrKernel;
+}
 
 int general_project(const GeneralArgs& a, cudaStream_t st) { return general_project_t<float>(a, st); }
 int general_backproject(const GeneralArgs& a, cudaStream_t st) { return general_backproject_t<float>(a, st); }

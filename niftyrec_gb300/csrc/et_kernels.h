@@ -33,6 +33,11 @@ using GeneralArgs64 = GeneralArgsT<double>;
 int general_project64(const GeneralArgs64& a, cudaStream_t st);
 int general_backproject64(const GeneralArgs64& a, cudaStream_t st);
 int general_project(const GeneralArgs& a, cudaStream_t st);
+// Projection with partial sums (et_project_partial): a.out the sinogram,
+// partial [ncam][nz][ny][nx] the emission reaching each depth from behind,
+// in the rotated frame or (do_rotate) rotated back; bg_image [ny][nx] or null.
+int general_project_partial(const GeneralArgs& a, const float* bg_image, float* partial, int do_rotate,
+                            cudaStream_t st);
 int general_backproject(const GeneralArgs& a, cudaStream_t st);
 int general_gradient(const GeneralArgs& a, cudaStream_t st);
 // Exact transpose of general_project's linear part (backprojector mode 1).
@@ -157,6 +162,15 @@ void launch_truncate(float* buf, size_t n, cudaStream_t st);
 int osem_ratio(const float* y, float* p_to_ratio, size_t n, float eps, cudaStream_t st);
 // x[i] *= num[i] / max(den[i], eps)            (:1036-1044)
 int osem_update(float* x, const float* num, const float* den, size_t n, float eps, cudaStream_t st);
+// One-step-late MAP-EM (et_osmapem_step, Python/NiftyRec/NiftyRec/NiftyRec.py:224-245):
+// ratio y / (max(p, 0) + eps); update x *= max(upd, 0) / (max(sens - beta g, 0) + eps)
+// (g may be null: no prior).
+int osem_ratio_osl(const float* y, float* p_to_ratio, size_t n, float eps, cudaStream_t st);
+int osem_update_osl(float* x, const float* upd, const float* sens, const float* grad, size_t n, float beta, float eps,
+                    cudaStream_t st);
+// Quadratic MRF prior gradient: 26 x - sum of the in-grid 3x3x3 neighbours
+// (n0 fastest).
+int mrf_gradient(const float* x, float* g, int n0, int n1, int n2, cudaStream_t st);
 // float64 variants of the two, for the float64 reference run.
 int osem_ratio64(const double* y, double* p_to_ratio, size_t n, double eps, cudaStream_t st);
 int osem_update64(double* x, const double* num, const double* den, size_t n, double eps, cudaStream_t st);

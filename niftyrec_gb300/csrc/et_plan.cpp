@@ -47,6 +47,7 @@ struct Plan {
   float* osem_p = nullptr;
   float* osem_num = nullptr;
   float* sens = nullptr;  // [n_subsets][volume]
+  float* prior_grad = nullptr;  // MRF prior gradient (one volume)
   size_t vol_elems = 0, plane_elems = 0;  // per layout of the OSEM buffers
 };
 
@@ -379,7 +380,7 @@ int nrgb_plan_osem_prepare(void* plan, int layout, void* stream) {
   p->osem_p = nullptr;
   const size_t n_p = al(sizeof(float) * p->plane_elems * max_sub);
   const size_t n_v = al(sizeof(float) * p->vol_elems);
-  if (cudaMalloc(&p->osem_p, n_p + n_v * (1 + p->n_subsets)) != cudaSuccess) {
+  if (cudaMalloc(&p->osem_p, n_p + n_v * (2 + p->n_subsets)) != cudaSuccess) {
     cudaGetLastError();
     p->osem_p = nullptr;
     return kErrAllocGpu;
@@ -387,8 +388,9 @@ int nrgb_plan_osem_prepare(void* plan, int layout, void* stream) {
   char* base = reinterpret_cast<char*>(p->osem_p);
   p->osem_num = reinterpret_cast<float*>(base + n_p);
   p->sens = reinterpret_cast<float*>(base + n_p + n_v);
+  p->prior_grad = reinterpret_cast<float*>(base + n_p + n_v * (1 + p->n_subsets));
   p->osem_layout = layout;
-  cudaMemsetAsync(p->osem_p, 0, n_p + n_v * (1 + p->n_subsets), st);
+  cudaMemsetAsync(p->osem_p, 0, n_p + n_v * (2 + p->n_subsets), st);
   for (int sidx = 0; sidx < p->n_subsets; ++sidx) {
     const int n = p->sub_begin[sidx + 1] - p->sub_begin[sidx];
     if (n <= 0) continue;
@@ -424,6 +426,40 @@ int nrgb_plan_osem_step(void* plan, int subset, float* d_activity, const float* 
   if (s == kOk) s = plan_backproject(*p, subset, p->osem_p, p->osem_num, p->osem_layout, 1, st);
   if (s == kOk) s = osem_update(d_activity, p->osem_num, p->sens + p->vol_elems * subset, p->vol_elems, epsilon, st);
   return s;
+}
+
+// One-step-late MAP-EM step with the quadratic MRF prior
+// (et_osmapem_step, Python/NiftyRec/NiftyRec/NiftyRec.py:224-245, prior
+// gradient of :400-404 computed from the current activity): p = A x
+// (truncated), r = y / (max(p, 0) + eps), u = A^T r (truncated),
+// x *= max(u, 0) / (max(sens - beta * g, 0) + eps).  beta = 0 is OSEM with the
+// OSL ratio rule.  Same layouts as nrgb_plan_osem_step.
+int nrgb_plan_osmapem_step(void* plan, int subset, float* d_activity, const float* d_counts, float beta,
+                           float epsilon, void* stream) {
+  Plan* p = static_cast<Plan*>(plan);
+  if (!p || subset < 0 || subset >= p->n_subsets || !d_activity || !d_counts || p->osem_layout < 0)
+    return kErrParameters;
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  const int n = p->sub_begin[subset + 1] - p->sub_begin[subset];
+  if (n <= 0) return kOk;
+  const Problem& pb = p->proj;
+  const bool col = p->osem_layout == kLayoutColumn;
+  int s = kOk;
+  if (beta != 0.0f)
+    s = mrf_gradient(d_activity, p->prior_grad, col ? p->cy : pb.nx, col ? pb.nx : pb.ny, pb.nz, st);
+  if (s == kOk) s = plan_project(*p, subset, d_activity, p->osem_p, p->osem_layout, 1, st);
+  if (s == kOk) s = osem_ratio_osl(d_counts, p->osem_p, p->plane_elems * n, epsilon, st);
+  if (s == kOk) s = plan_backproject(*p, subset, p->osem_p, p->osem_num, p->osem_layout, 1, st);
+  if (s == kOk)
+    s = osem_update_osl(d_activity, p->osem_num, p->sens + p->vol_elems * subset, beta != 0.0f ? p->prior_grad : nullptr,
+                        p->vol_elems, beta, epsilon, st);
+  return s;
+}
+
+// Quadratic MRF prior gradient of a device volume in nifti order (nx fastest).
+int nrgb_mrf_gradient_device(const float* d_activity, float* d_gradient, const int* size, void* stream) {
+  if (!d_activity || !d_gradient || !size || size[0] <= 0 || size[1] <= 0 || size[2] <= 0) return kErrParameters;
+  return mrf_gradient(d_activity, d_gradient, size[0], size[1], size[2], static_cast<cudaStream_t>(stream));
 }
 
 // Layout conversion for callers of the column-layout entry points:

@@ -137,7 +137,76 @@ __global__ void k_update_batch(const BatchStepDesc* __restrict__ d, const BatchE
   }
 }
 
+// One-step-late MAP-EM (et_osmapem_step, Python/NiftyRec/NiftyRec/NiftyRec.py:224-245).
+// Ratio: y / (max(p, 0) + eps).
+__global__ void k_ratio_osl(const float* __restrict__ y, float* __restrict__ p, size_t n, float eps) {
+  for (size_t i = blockIdx.x * static_cast<size_t>(blockDim.x) + threadIdx.x; i < n;
+       i += static_cast<size_t>(gridDim.x) * blockDim.x) {
+    const float pv = p[i];
+    p[i] = __fdiv_rn(y[i], __fadd_rn(pv > 0.0f ? pv : 0.0f, eps));
+  }
+}
+
+// x *= max(update, 0) / (max(sens - beta * grad, 0) + eps).
+__global__ void k_update_osl(float* __restrict__ x, const float* __restrict__ upd, const float* __restrict__ sens,
+                             const float* __restrict__ grad, size_t n, float beta, float eps) {
+  for (size_t i = blockIdx.x * static_cast<size_t>(blockDim.x) + threadIdx.x; i < n;
+       i += static_cast<size_t>(gridDim.x) * blockDim.x) {
+    float norm = __fsub_rn(sens[i], __fmul_rn(beta, grad ? grad[i] : 0.0f));
+    norm = __fadd_rn(norm > 0.0f ? norm : 0.0f, eps);
+    const float u = upd[i] > 0.0f ? upd[i] : 0.0f;
+    x[i] = __fdiv_rn(__fmul_rn(x[i], u), norm);
+  }
+}
+
+// Gradient of the quadratic MRF prior (Python/NiftyRec/NiftyRec/NiftyRec.py:400-404):
+// the 3x3x3 convolution with 26 at the centre and -1 elsewhere, zero outside
+// the grid: g = 26 x - (sum of the in-grid neighbours).  Dimensions n0
+// (fastest), n1, n2 of the buffer's own layout.
+__global__ void k_mrf_gradient(const float* __restrict__ x, float* __restrict__ g, int n0, int n1, int n2) {
+  const size_t n = static_cast<size_t>(n0) * n1 * n2;
+  for (size_t i = blockIdx.x * static_cast<size_t>(blockDim.x) + threadIdx.x; i < n;
+       i += static_cast<size_t>(gridDim.x) * blockDim.x) {
+    const int a = static_cast<int>(i % n0);
+    const int b = static_cast<int>((i / n0) % n1);
+    const int c = static_cast<int>(i / (static_cast<size_t>(n0) * n1));
+    float nb = 0.0f;
+    for (int dc = -1; dc <= 1; ++dc) {
+      const int cc = c + dc;
+      if (cc < 0 || cc >= n2) continue;
+      for (int db = -1; db <= 1; ++db) {
+        const int bb = b + db;
+        if (bb < 0 || bb >= n1) continue;
+        const float* row = x + (static_cast<size_t>(cc) * n1 + bb) * n0;
+        for (int da = -1; da <= 1; ++da) {
+          const int aa = a + da;
+          if (aa < 0 || aa >= n0 || (da == 0 && db == 0 && dc == 0)) continue;
+          nb = __fadd_rn(nb, __ldg(row + aa));
+        }
+      }
+    }
+    g[i] = __fsub_rn(__fmul_rn(26.0f, x[i]), nb);
+  }
+}
+
 }  // namespace
+
+int osem_ratio_osl(const float* y, float* p, size_t n, float eps, cudaStream_t st) {
+  { NRGB_LAUNCH_SCOPE("k_ratio_osl", st); k_ratio_osl<<<grid_for(n), kBlock, 0, st>>>(y, p, n, eps); }
+  return cudaGetLastError() == cudaSuccess ? kOk : kErrKernel;
+}
+
+int osem_update_osl(float* x, const float* upd, const float* sens, const float* grad, size_t n, float beta, float eps,
+                    cudaStream_t st) {
+  { NRGB_LAUNCH_SCOPE("k_update_osl", st); k_update_osl<<<grid_for(n), kBlock, 0, st>>>(x, upd, sens, grad, n, beta, eps); }
+  return cudaGetLastError() == cudaSuccess ? kOk : kErrKernel;
+}
+
+int mrf_gradient(const float* x, float* g, int n0, int n1, int n2, cudaStream_t st) {
+  const size_t n = static_cast<size_t>(n0) * n1 * n2;
+  { NRGB_LAUNCH_SCOPE("k_mrf_gradient", st); k_mrf_gradient<<<grid_for(n), kBlock, 0, st>>>(x, g, n0, n1, n2); }
+  return cudaGetLastError() == cudaSuccess ? kOk : kErrKernel;
+}
 
 int osem_ratio_batch(const BatchStepDesc* d_desc, const BatchElems& e, float eps, cudaStream_t st) {
   if (e.n <= 0) return kOk;

@@ -170,8 +170,19 @@ class Plan:
         if st:
             raise NiftyRecError("nrgb_plan_osem_step", st)
 
-    def osem(self, counts, iterations, activity=None, layout="column", epsilon=1e-6, graph=False):
-        """OSEM from full-size counts (n, ny, nx); returns the activity in nifti order."""
+    def osmapem_step(self, activity, counts_subset, subset, beta, epsilon=1e-6):
+        """One-step-late MAP-EM step with the quadratic MRF prior (et_osmapem_step
+        of the reference's Python package; beta is its beta_osl)."""
+        st = self.L.nrgb_plan_osmapem_step(self.handle, subset, _vp(activity.data_ptr()),
+                                           _vp(counts_subset.data_ptr()), float(beta), float(epsilon),
+                                           self._stream())
+        if st:
+            raise NiftyRecError("nrgb_plan_osmapem_step", st)
+
+    def osem(self, counts, iterations, activity=None, layout="column", epsilon=1e-6, graph=False, beta=None):
+        """OSEM from full-size counts (n, ny, nx); returns the activity in nifti order.
+        beta: run one-step-late MAP-EM with the quadratic MRF prior instead
+        (beta_osl of the reference's et_osmapem_step)."""
         torch = self.torch
         lay = _layout(layout)
         if self._osem_layout != lay:
@@ -183,7 +194,10 @@ class Plan:
 
         def one_iteration():
             for s in range(self.n_subsets):
-                self.osem_step(x, ys[s], s, epsilon)
+                if beta is None:
+                    self.osem_step(x, ys[s], s, epsilon)
+                else:
+                    self.osmapem_step(x, ys[s], s, beta, epsilon)
 
         if graph:
             x0 = x.clone()

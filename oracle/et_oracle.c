@@ -503,6 +503,104 @@ int ORC(spect_project)(const REAL *act, const int act_size[3], REAL *sino, const
     return st;
 }
 
+/* Partial-sum projector: et_project_partial_gpu, emission-lib/_et.cpp:2106-2436
+ * (the CPU entry point et_project_partial is a stub returning 1,
+ * emission-lib/_et.cpp:783-786), with the partial-sum branch of the line
+ * integral kernel emission-lib_gpu/_et_line_integral_attenuated_gpu_kernels.cu:57-103
+ * restated on the CPU pieces (resampler, separable PSF).  Per camera: rotate
+ * activity (bg) and mu (bg_att), PSF, then walk depth from the far end:
+ * partial[z] = s; s = (s + a[z]) * exp(-mu[z]) (mu only: s *= exp(-mu[z]);
+ * activity only: s += a[z]), s starting at bg (times bg_image[x, y] if
+ * given); the projection is the final s.  do_rotate: the partial-sum volume is
+ * rotated back to the image frame (-theta, ZYX, background bg,
+ * emission-lib/_et.cpp:2373-2404).  partial is [nx, ny, nz, ncam]. */
+static void line_partial(const REAL *act, const REAL *att, const REAL *bg_image, REAL *plane_out, REAL *partial,
+                         int nx, int ny, int nz, REAL bg)
+{
+    size_t nxy = (size_t)nx * ny;
+    for (size_t i0 = 0; i0 < nxy; i0++) {
+        REAL s = bg;
+        if (bg_image) s = s * bg_image[i0];
+        for (int z = nz - 1; z >= 0; z--) {
+            size_t j = i0 + nxy * z;
+            partial[j] = s;
+            if (act && att)
+                s = (s + act[j]) * R_EXP(-att[j]);
+            else if (att)
+                s = s * R_EXP(-att[j]);
+            else
+                s = s + act[j];
+        }
+        plane_out[i0] = s;
+    }
+}
+
+int ORC(project_partial)(const REAL *act, const REAL *att, const int size[3], REAL *sino, REAL *partial,
+                         const REAL *angles, const REAL *centers, int ncam, const REAL *psf, const int psf_size[3],
+                         REAL bg, const REAL *bg_image, REAL bg_att, int truncate, int do_rotate)
+{
+    int nx = size[0], ny = size[1], nz = size[2];
+    size_t nvox = (size_t)nx * ny * nz, nxy = (size_t)nx * ny;
+    if (!act && !att) return ORC_ERR_PARAMETERS;
+    REAL *ract = act ? (REAL *)malloc(sizeof(REAL) * nvox) : NULL;
+    REAL *ratt = att ? (REAL *)malloc(sizeof(REAL) * nvox) : NULL;
+    REAL *rpart = (REAL *)malloc(sizeof(REAL) * nvox);
+    REAL *sep = NULL;
+    if (psf) {
+        sep = (REAL *)malloc(sizeof(REAL) * (size_t)(psf_size[0] + psf_size[1]) * psf_size[2]);
+        ORC(psf_separate)(psf, psf_size[0], psf_size[1], psf_size[2], sep);
+    }
+    REAL A[16];
+    for (int cam = 0; cam < ncam; cam++) {
+        ORC(rotation_matrix)(A, angles[cam], angles[ncam + cam], angles[2 * ncam + cam],
+                             centers[cam], centers[ncam + cam], centers[2 * ncam + cam], 0);
+        if (act) ORC(affine_resample)(act, ract, nx, ny, nz, A, bg);
+        if (att) ORC(affine_resample)(att, ratt, nx, ny, nz, A, bg_att);
+        if (psf && act) ORC(convolve_separable)(ract, nx, ny, nz, sep, psf_size[0], psf_size[1]);
+        REAL *dst = partial + nvox * cam;
+        line_partial(ract, ratt, bg_image, sino + nxy * cam, do_rotate ? rpart : dst, nx, ny, nz, bg);
+        if (do_rotate) {
+            ORC(rotation_matrix)(A, -angles[cam], -angles[ncam + cam], -angles[2 * ncam + cam],
+                                 centers[cam], centers[ncam + cam], centers[2 * ncam + cam], 5);
+            ORC(affine_resample)(rpart, dst, nx, ny, nz, A, bg);
+        }
+    }
+    if (truncate)
+        for (size_t i = 0; i < nxy * ncam; i++)
+            if (sino[i] < 0) sino[i] = 0;
+    free(ract);
+    free(ratt);
+    free(rpart);
+    free(sep);
+    return ORC_OK;
+}
+
+/* et_array_project_partial, emission-lib/_et_array_interface.cpp:1561-1760:
+ * argument rules of SPECT_project_parallelholes; bg_image [nx, ny] or NULL. */
+int ORC(spect_project_partial)(const REAL *act, const int act_size[3], REAL *sino, REAL *partial,
+                               const REAL *cameras, const int cam_size[2], const REAL *psf, const int psf_size[3],
+                               const REAL *att, const int att_size[3], REAL bg, const REAL *bg_image, REAL bg_att,
+                               int truncate, int do_rotate)
+{
+    int asz[3] = {act_size[0], act_size[1], act_size[2]};
+    int no_act = (asz[0] == 0 && asz[1] == 0 && asz[2] == 0);
+    int no_psf = (psf_size[0] == 0 && psf_size[1] == 0 && psf_size[2] == 0);
+    int no_att = (att_size[0] == 0 && att_size[1] == 0 && att_size[2] == 0);
+    if (no_act) { asz[0] = att_size[0]; asz[1] = att_size[1]; asz[2] = att_size[2]; }
+    if (no_act && no_att) return ORC_ERR_PARAMETERS;
+    int ncam = cam_size[0], ncols = cam_size[1];
+    if (!no_psf && (psf_size[0] % 2 != 1 || psf_size[1] % 2 != 1 || psf_size[2] != asz[0])) return ORC_ERR_PARAMETERS;
+    REAL *angles = (REAL *)malloc(sizeof(REAL) * 3 * ncam);
+    REAL *centers = (REAL *)malloc(sizeof(REAL) * 3 * ncam);
+    int st = expand_cameras(cameras, ncam, ncols, asz, angles, centers);
+    if (st == ORC_OK)
+        st = ORC(project_partial)(no_act ? NULL : act, no_att ? NULL : att, asz, sino, partial, angles, centers, ncam,
+                                  no_psf ? NULL : psf, psf_size, bg, bg_image, bg_att, truncate, do_rotate);
+    free(angles);
+    free(centers);
+    return st;
+}
+
 /* SPECT_backproject_parallelholes, emission-lib/_et_array_interface.cpp:547-710:
  * the centre comes from (sino0, sino1, sino0), the volume grid from bkpr_size. */
 int ORC(spect_backproject)(const REAL *sino, const int sino_size[3], REAL *bkpr, const int bkpr_size[3],

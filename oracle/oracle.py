@@ -128,6 +128,29 @@ class Restated:
             raise RuntimeError(f"oracle backproject status {st}")
         return out
 
+    def project_partial(self, act, cameras, psf=None, att=None, bg=0.0, bg_image=None, bg_att=0.0, truncate=1,
+                        rotate=0):
+        """et_array_project_partial: (sinogram [ncam, ny, nx], partial sums [ncam, nz, ny, nx])."""
+        act = self._arr(act)
+        att = self._arr(att)
+        psf = self._arr(psf)
+        bgi = self._arr(bg_image)
+        cams = self._arr(cameras)
+        ref = act if act is not None else att
+        nz, ny, nx = ref.shape
+        cs = _cam_size(cams)
+        sino = np.zeros((cs[0], ny, nx), dtype=self.dtype)
+        part = np.zeros((cs[0], nz, ny, nx), dtype=self.dtype)
+        asz = _ints([nx, ny, nz] if act is not None else [0, 0, 0])
+        tsz = _ints([nx, ny, nz] if att is not None else [0, 0, 0])
+        psz = _ints(list(psf.shape[::-1]) if psf is not None else [0, 0, 0])
+        st = self._f("spect_project_partial")(_ptr(act), _ptr(asz), _ptr(sino), _ptr(part), _ptr(cams),
+                                              _ptr(_ints(cs)), _ptr(psf), _ptr(psz), _ptr(att), _ptr(tsz),
+                                              self.real(bg), _ptr(bgi), self.real(bg_att), _I(truncate), _I(rotate))
+        if st:
+            raise RuntimeError(f"oracle project_partial status {st}")
+        return sino, part
+
     def gradient_attenuation(self, sino, act, att, cameras, psf=None, bg=0.0, bg_att=0.0, truncate=0):
         sino = self._arr(sino)
         act = self._arr(act)

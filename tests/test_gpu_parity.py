@@ -178,3 +178,19 @@ def test_parameter_errors():
     with pytest.raises(Exception) as e:
         A.backproject(np.ones((3, 8, 8), np.float32), cams)  # n_cameras mismatch
     assert getattr(e.value, "status", None) == 2
+
+
+@pytest.mark.parametrize("rotate,att,bgi", [(0, True, False), (1, True, True), (0, False, True), (1, False, False)])
+def test_partial_sum_projector(o32, rotate, att, bgi):
+    """et_array_project_partial against the oracle's restatement of
+    et_project_partial_gpu: projections and partial-sum volumes."""
+    shape = (20, 18, 24)
+    act = S.ellipsoid_phantom(shape, seed=91)
+    mu = S.mu_map(shape, seed=91) if att else None
+    psf = S.gaussian_psf(5, shape[2], 0.5, 0.05)
+    cams = S.cameras_about_y(5, 17.0)
+    img = np.random.default_rng(2).uniform(0.5, 1.5, shape[1:]).astype(np.float32) if bgi else None
+    s, part = A.project_partial(act, cams, psf, mu, 0.2, img, 0.0, 1, rotate)
+    so, po = o32.project_partial(act, cams, psf, mu, bg=0.2, bg_image=img, truncate=1, rotate=rotate)
+    assert per_plane_rel(s, so) < RTOL
+    assert rel_l2(part, po) < RTOL

@@ -149,3 +149,55 @@ def test_plan_tall_volume_row_windows():
     for sub in range(2):
         xr = A.osem_step_subset(xr, y, cams, p.subset_cameras(sub), mu, psf)
     assert rel_l2(x, xr) < 2 * RTOL
+
+
+@pytest.mark.parametrize("layout", ["nifti", "column"])
+def test_plan_osmapem_matches_numpy_restatement(data, layout):
+    """One-step-late MAP-EM with the quadratic MRF prior against a numpy
+    restatement of et_osmapem_step (Python/NiftyRec/NiftyRec/NiftyRec.py:224-245,
+    prior :400-404) on the oracle's projector and backprojector."""
+    from scipy.signal import convolve
+
+    from oracle.oracle import Restated
+
+    act, mu, psf, cams, y = data
+    p = make_plan(data, subsets=4)
+    # small against sensitivity / gradient of counts-scaled activity, so that
+    # max(sens - beta g, 0) + eps stays away from eps (where OSL diverges)
+    beta = 1e-4
+    x = p.osem(cuda(y), iterations=1, layout=layout, beta=beta).cpu().numpy()
+    o = Restated("f32")
+    kernel = -np.ones((3, 3, 3), np.float32)
+    kernel[1, 1, 1] = 26
+    xr = np.ones(SHAPE, np.float32)
+    eps = np.float32(1e-6)
+    for sub in range(4):
+        idx = p.subset_cameras(sub)
+        c = cams[:, idx]
+        grad = convolve(xr, kernel, "same").astype(np.float32)
+        norm = o.backproject(np.ones((len(idx),) + SHAPE[1:], np.float32), c, psf, mu, nz=SHAPE[0])
+        norm = np.maximum(norm - np.float32(beta) * grad, 0) + eps
+        pr = np.maximum(o.project(xr, c, psf, mu), 0) + eps
+        upd = np.maximum(o.backproject(y[idx] / pr, c, psf, mu, nz=SHAPE[0]), 0)
+        xr = (xr * upd / norm).astype(np.float32)
+    assert np.isfinite(x).all() and x.max() < 1e4
+    assert rel_l2(x, xr) < 2 * RTOL
+
+
+def test_mrf_gradient_kernel():
+    from scipy.signal import convolve
+
+    from niftyrec_gb300 import _lib
+    import ctypes
+
+    L = _lib.load()
+    x = np.random.default_rng(4).random((10, 12, 14)).astype(np.float32)
+    g = torch.empty(x.shape, dtype=torch.float32, device="cuda")
+    xt = cuda(x)
+    st = L.nrgb_mrf_gradient_device(ctypes.c_void_p(xt.data_ptr()), ctypes.c_void_p(g.data_ptr()),
+                                    (ctypes.c_int * 3)(14, 12, 10), None)
+    assert st == 0
+    kernel = -np.ones((3, 3, 3))
+    kernel[1, 1, 1] = 26
+    ref = convolve(x.astype(np.float64), kernel, "same")
+    np.testing.assert_allclose(g.cpu().numpy(), ref, rtol=1e-5, atol=1e-5)

@@ -113,3 +113,30 @@ def test_against_compiled_reference_fresh_inputs(o32):
         s = R.project(act, cams, psf, mu)
         assert np.array_equal(R.backproject(s, cams, psf, mu, nz=shape[0]),
                               o32.backproject(s, cams, psf, mu, nz=shape[0]))
+
+
+def test_partial_sum_projector_restatement():
+    """The partial-sum projector (emission-lib/_et.cpp:2106-2436, GPU-only in
+    the reference) sums the same terms as the projector in the opposite depth
+    order: equal projections to float32 rounding; the farthest partial sum is
+    the background (times the background image) and, without attenuation,
+    partial sums fall monotonically toward the detector."""
+    from oracle.oracle import Restated
+
+    o = Restated("f32")
+    shape = (14, 12, 16)
+    act = S.ellipsoid_phantom(shape, seed=90)
+    mu = S.mu_map(shape, seed=90)
+    psf = S.gaussian_psf(5, shape[2], 0.5, 0.05)
+    cams = S.cameras_about_y(4, 20.0)
+    bgi = np.random.default_rng(1).uniform(0.5, 1.5, shape[1:]).astype(np.float32)
+    s, part = o.project_partial(act, cams, psf, mu, bg=0.3, truncate=0)
+    ref = o.project(act, cams, psf, mu, 0.3, truncate=0)
+    assert np.linalg.norm(s - ref) / np.linalg.norm(ref) < 1e-5
+    s2, part2 = o.project_partial(act, cams, psf, mu, bg=0.3, bg_image=bgi, truncate=0)
+    np.testing.assert_array_equal(part2[:, -1], np.broadcast_to(np.float32(0.3) * bgi, part2[:, -1].shape))
+    _, part3 = o.project_partial(act, cams, psf, None, truncate=0)
+    assert np.all(np.diff(part3, axis=1) <= 0)
+    sr, partr = o.project_partial(act, cams, psf, mu, bg=0.0, truncate=0, rotate=1)
+    np.testing.assert_allclose(sr, o.project(act, cams, psf, mu, truncate=0), rtol=1e-4, atol=1e-5)
+    assert partr.shape == (4,) + shape
