@@ -293,8 +293,8 @@ int nrgb_batch_osem_step(void *batch, int step, int iterations, float epsilon, v
 /* Tuning table of the fused backprojector (no counterpart in the reference):
  * cameras per L2-resident scratch group for a problem shape (nx, ny, nz,
  * n_cameras); an all-zero shape sets the default for shapes without an entry
- * (8 initially).  niftyrec_gb300.autotune measures candidates and records the
- * fastest. */
+ * (none initially: then min(16, n_cameras / 2), at least 4).
+ * niftyrec_gb300.autotune measures candidates and records the fastest. */
 int nrgb_set_backproject_group(int nx, int ny, int nz, int ncam, int group);
 int nrgb_get_backproject_group(int nx, int ny, int nz, int ncam);
 

@@ -21,7 +21,7 @@ import os
 
 import numpy as np
 
-CANDIDATES = (2, 4, 6, 8, 12, 16)
+CANDIDATES = (4, 8, 12, 16, 24, 32)
 CACHE = os.path.join(os.path.expanduser("~"), ".cache", "niftyrec_gb300", "tune.json")
 
 

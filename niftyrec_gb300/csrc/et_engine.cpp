@@ -17,6 +17,11 @@ namespace nrgb {
 // key of zeros is the default.  Filled by nrgb_tune_set (the autotuner in
 // niftyrec_gb300/autotune.py measures candidates and records the fastest).
 namespace {
+// Cameras per group without a table entry: up to 16 (the fastest on GB300 at
+// 128^3 x 120 and 256^3 x 180: 1.60 ms and 25.7 ms per backprojection against
+// 1.77 / 28.2 ms with 8), but at least two groups so that the spread of one
+// overlaps the gather of the other (OSEM subsets of 15 cameras: 8).
+int default_group(int ncam) { return std::max(4, std::min(16, (ncam + 1) / 2)); }
 std::mutex g_tune_mu;
 std::map<std::tuple<int, int, int, int>, int> g_tune_group;
 }  // namespace
@@ -26,7 +31,7 @@ int tuned_group(int nx, int ny, int nz, int ncam) {
   auto it = g_tune_group.find(std::make_tuple(nx, ny, nz, ncam));
   if (it != g_tune_group.end()) return it->second;
   it = g_tune_group.find(std::make_tuple(0, 0, 0, 0));
-  return it != g_tune_group.end() ? it->second : 8;
+  return it != g_tune_group.end() ? it->second : default_group(ncam);
 }
 
 void set_tuned_group(int nx, int ny, int nz, int ncam, int group) {

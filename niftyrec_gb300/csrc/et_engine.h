@@ -24,7 +24,7 @@ struct Problem {
   float bg = 0.0f, bg_att = 0.0f;
   int truncate = 0;
   int back_mode = kBackReference;
-  int group = 8;  // cameras per backprojection scratch group
+  int group = 16;  // cameras per backprojection scratch group (set from the tuning table)
   // Storage of the sampled volumes inside the fused kernels, and whether the
   // caller's activity / mu buffers are bfloat16 (nifti order) rather than
   // float32.  bfloat16 inputs imply bfloat16 storage; the general-orientation

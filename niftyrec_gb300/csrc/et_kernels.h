@@ -71,7 +71,7 @@ struct YgArgs {
   float* work = nullptr;
   float* slab_T = nullptr;
   float* temp = nullptr;
-  int group = 8;
+  int group = 16;
   // 1: spread on the caller's stream, gather on a second stream, two scratch
   // slots; 0: both on the caller's stream with one slot (creates no stream
   // or event).

@@ -147,7 +147,7 @@ int plan_backproject(Plan& p, int subset, const float* d_sino, float* d_out, int
     a.psf = p.psf;
     a.psf_k = pb.psf_k;
     a.truncate = truncate;
-    a.group = pb.group;
+    a.group = std::min(pb.group, tuned_group(pb.nx, pb.ny, pb.nz, n));  // by the subset's camera count
     a.work = p.work;
     a.carry = p.carry ? p.carry + static_cast<size_t>(b) * yg_carry_slabs() * pb.nx * p.cy : nullptr;
     int s = yg_backproject(a, st);

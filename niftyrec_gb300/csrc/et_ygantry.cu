@@ -26,6 +26,7 @@
 #include <algorithm>
 #include <map>
 #include <mutex>
+#include <type_traits>
 #include <vector>
 
 namespace nrgb {
@@ -38,7 +39,8 @@ constexpr int kW = 8;             // warps per CTA of the tile engine
 constexpr int kTXW = 4;           // output columns per warp
 constexpr int kTXC = kW * kTXW;   // output columns per CTA
 constexpr int kSlabsP = 4;        // projector depth slabs = cluster size
-constexpr int kSlabsB = 8;        // backprojector depth slabs
+constexpr int kSlabsB = 16;       // backprojector depth slabs
+constexpr int kCarryCols = 64 / kSlabsB;  // columns per CTA of the carry pass (32 KB of slab sums)
 constexpr int kGatherWarps = 4;   // warps per CTA of the inverse-rotation gather
 constexpr int kGatherCols = 8;    // accumulator columns per warp in the gather
 constexpr unsigned kFull = 0xffffffffu;
@@ -225,8 +227,6 @@ __device__ __forceinline__ float4 depth_value4(const float4& s, const float4& c)
 }
 
 // Storage type of the sampled volumes; bfloat16 storage sums with Kahan.
-// Both keep two CTAs per SM (the compensations fit in 128 registers with at
-// most a few bytes of spill).
 template <class V>
 struct StorageTraits {
   static constexpr bool kKahan = false;
@@ -264,9 +264,18 @@ template <int R>
 struct TileShape {
   static constexpr int NS = kTXC + 2 * R;            // sampled columns per CTA
   static constexpr int kOwn = (NS + kW - 1) / kW;    // sampled columns per warp (max)
+  static constexpr int kTapSlots = kW * kOwn;         // footprint slots per stage (see tap_slot)
   static constexpr size_t kSbBytes = sizeof(float4) * 2 * NS * 32;
-  static constexpr size_t kTapBytes = sizeof(Tap) * 2 * NS;
+  static constexpr size_t kTapBytes = sizeof(Tap) * 2 * kTapSlots;
 };
+
+// Footprint slot of sampled column c in the tap buffer: the columns one warp
+// computes (c = warp + kW * k) sit next to each other, so the footprint
+// stores of a warp do not collide in shared-memory banks.
+template <int R>
+__device__ __forceinline__ int tap_slot(int c) {
+  return (c % kW) * TileShape<R>::kOwn + c / kW;
+}
 
 template <int R>
 __host__ __device__ constexpr size_t tile_smem_bytes(int nz) {
@@ -325,7 +334,7 @@ __device__ __forceinline__ void project_item(const YgArgs& a, int cam, int x0, u
   constexpr int NS = TS::NS;
   constexpr int K = 2 * R + 1;
   float4* sb = reinterpret_cast<float4*>(smem);                       // [2][NS][32]
-  Tap* taps = reinterpret_cast<Tap*>(smem + TS::kSbBytes);             // [2][NS]
+  Tap* taps = reinterpret_cast<Tap*>(smem + TS::kSbBytes);             // [2][kTapSlots]
   float* s_psf = reinterpret_cast<float*>(smem + TS::kSbBytes + TS::kTapBytes);  // [nz][2K]
 
   cg::cluster_group cluster = cg::this_cluster();
@@ -354,13 +363,13 @@ __device__ __forceinline__ void project_item(const YgArgs& a, int cam, int x0, u
   for (int z = zbeg; z < zend; ++z) {
     const int b = z & 1;
     float4* sbuf = sb + b * NS * 32;
-    Tap* tb = taps + b * NS;
+    Tap* tb = taps + b * TS::kTapSlots;
     // footprints of the columns this warp samples (c = warp + kW * k)
     if (lane < TS::kOwn) {
       const int c = warp + kW * lane;
       if (c < NS) {
         const int xp = x0 - R + c;
-        tb[c] = make_tap(xp, z, cr.m00, cr.m02, cr.m03, cr.m20, cr.m22, cr.m23, a.nx, a.nz, a.cy,
+        tb[tap_slot<R>(c)] = make_tap(xp, z, cr.m00, cr.m02, cr.m03, cr.m20, cr.m22, cr.m23, a.nx, a.nz, a.cy,
                          xp >= 0 && xp < a.nx);
       }
     }
@@ -368,12 +377,12 @@ __device__ __forceinline__ void project_item(const YgArgs& a, int cam, int x0, u
 #pragma unroll
     for (int k = 0; k < TS::kOwn; ++k) {
       const int c = warp + kW * k;
-      if (c < NS) sbuf[c * 32 + lane] = sample4(act, tb[c], yb, yok);
+      if (c < NS) sbuf[c * 32 + lane] = sample4(act, tb[tap_slot<R>(c)], yb, yok);
     }
     __syncthreads();
     auto emit = [&](int i, const float4& v) {
       if (ATT) {
-        const float4 m = sample4(mu, tb[warp * kTXW + i + R], yb, yok);
+        const float4 m = sample4(mu, tb[tap_slot<R>(warp * kTXW + i + R)], yb, yok);
         if (KAHAN) {
           kahan_add4(T[i], cT[i], m);
           kahan_add4(P[i], cP[i], mul4(v, exp_neg4(kahan_value4(T[i], cT[i]))));
@@ -433,9 +442,13 @@ __device__ __forceinline__ void project_item(const YgArgs& a, int cam, int x0, u
   cluster.sync();  // keep this CTA's shared memory alive until the others have read it
 }
 
-// One work item per cluster: blockIdx.x / kSlabsP = (camera, x-tile).
-template <int R, bool PSF, bool ATT, class V>
-__global__ void __cluster_dims__(kSlabsP, 1, 1) __launch_bounds__(32 * kW, 2)
+// One work item per cluster: blockIdx.x / kSlabsP = (camera, x-tile).  CTAS:
+// CTAs per SM the kernel is compiled for -- 3 (80 registers, more warps to
+// hide the gathers' latency) where three tiles fit in shared memory and the
+// storage is float32, else 2 (128 registers; bfloat16 needs them for its
+// Kahan compensations).
+template <int R, bool PSF, bool ATT, class V, int CTAS>
+__global__ void __cluster_dims__(kSlabsP, 1, 1) __launch_bounds__(32 * kW, CTAS)
     k_project_yg(const YgArgs a) {
   extern __shared__ __align__(16) unsigned char smem[];
   const int ntile = (a.nx + kTXC - 1) / kTXC;
@@ -486,7 +499,7 @@ __global__ void __cluster_dims__(kSlabsP, 1, 1) __launch_bounds__(32 * kW, 2)
 // (exclusive prefix): the transmission a depth slab starts from.
 template <class V>
 __global__ void __launch_bounds__(32 * kSlabsB) k_mu_carry_yg(const YgArgs a) {
-  constexpr int C = 8;
+  constexpr int C = kCarryCols;
   constexpr bool KAHAN = StorageTraits<V>::kKahan;
   const V* __restrict__ mu = reinterpret_cast<const V*>(a.mu) + a.row0;
   __shared__ Tap s_tap[kSlabsB][C];
@@ -612,12 +625,12 @@ __global__ void __launch_bounds__(32 * kW, 2) k_spread_yg(const YgArgs a, int c0
   for (int z = zbeg; z < zend; ++z) {
     const int b = z & 1;
     float4* sbuf = sb + b * NS * 32;
-    Tap* tb = taps + b * NS;
+    Tap* tb = taps + b * TS::kTapSlots;
     if ((ATT || ADJ) && lane < TS::kOwn) {
       const int c = warp + kW * lane;
       if (c < NS) {
         const int xp = x0 - R + c;
-        tb[c] = make_tap(xp, z, cr.m00, cr.m02, cr.m03, cr.m20, cr.m22, cr.m23, a.nx, a.nz, a.cy,
+        tb[tap_slot<R>(c)] = make_tap(xp, z, cr.m00, cr.m02, cr.m03, cr.m20, cr.m22, cr.m23, a.nx, a.nz, a.cy,
                          xp >= 0 && xp < a.nx);
       }
     }
@@ -630,7 +643,7 @@ __global__ void __launch_bounds__(32 * kW, 2) k_spread_yg(const YgArgs a, int c0
         float4 s = make_float4(0.f, 0.f, 0.f, 0.f);
         if (xp >= 0 && xp < a.nx && yok) s = ldg4(srow + static_cast<size_t>(xp) * a.cy + yb);
         if (ATT) {
-          depth_add4<KAHAN>(Tc[k], cTc[k], sample4(mu, tb[c], yb, yok));
+          depth_add4<KAHAN>(Tc[k], cTc[k], sample4(mu, tb[tap_slot<R>(c)], yb, yok));
           s = mul4(s, exp_neg4(depth_value4<KAHAN>(Tc[k], cTc[k])));
         }
         sbuf[c * 32 + lane] = s;
@@ -642,7 +655,7 @@ __global__ void __launch_bounds__(32 * kW, 2) k_spread_yg(const YgArgs a, int c0
       if (x >= a.nx || !yok) return;
       if (ADJ) {
         // halo rows lack part of their PSF support: their owner window adds them
-        if (lane_writes(a, yb)) scatter4(tmp, tb[warp * kTXW + i + R], yb, v);
+        if (lane_writes(a, yb)) scatter4(tmp, tb[tap_slot<R>(warp * kTXW + i + R)], yb, v);
       } else {
         *reinterpret_cast<float4*>(tmp + (static_cast<size_t>(z) * a.nx + x) * a.cs + yb) = v;
       }
@@ -789,20 +802,25 @@ int launch_project_R(const YgArgs& a, cudaStream_t st) {
     NRGB_LAUNCH_SCOPE("k_project_yg", st);
     k<<<grid, block, smem, st>>>(a);
   };
-  auto pick = [&](auto v) {
+  auto pick = [&](auto v, auto ctas) {
     using V = decltype(v);
+    constexpr int C = decltype(ctas)::value;
     if (psf) {
-      if (a.mu) go(k_project_yg<R, true, true, V>);
-      else go(k_project_yg<R, true, false, V>);
+      if (a.mu) go(k_project_yg<R, true, true, V, C>);
+      else go(k_project_yg<R, true, false, V, C>);
     } else {
-      if (a.mu) go(k_project_yg<0, false, true, V>);
-      else go(k_project_yg<0, false, false, V>);
+      if (a.mu) go(k_project_yg<0, false, true, V, C>);
+      else go(k_project_yg<0, false, false, V, C>);
     }
   };
+  // three CTAs per SM need three tiles (plus 1 KB reserved each) in the 228 KB
+  const bool three = 3 * (smem + 1024) <= 228 * 1024;
   if (a.storage == kStorageBF16)
-    pick(__nv_bfloat16());
+    pick(__nv_bfloat16(), std::integral_constant<int, 2>());
+  else if (three)
+    pick(0.0f, std::integral_constant<int, 3>());
   else
-    pick(0.0f);
+    pick(0.0f, std::integral_constant<int, 2>());
   return cudaGetLastError() == cudaSuccess ? kOk : kErrKernel;
 }
 
@@ -989,7 +1007,7 @@ size_t yg_backproject_workspace(int nx, int ny, int nz, int ncam, int group, int
 int yg_carry_slabs() { return kSlabsB; }
 
 int yg_mu_carry(const YgArgs& a_in, float* out, cudaStream_t st) {
-  const int nchunk = (a_in.nx + 7) / 8;
+  const int nchunk = (a_in.nx + kCarryCols - 1) / kCarryCols;
   for (const Window& w : row_windows(a_in.ny, 0)) {  // carries need no halo
     YgArgs a = windowed(a_in, w);
     a.slab_T = out;

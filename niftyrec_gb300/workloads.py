@@ -32,9 +32,12 @@ def main(argv=None):
     ap.add_argument("--mode", type=int, default=0, help="backprojector: 0 reference, 1 exact transpose")
     ap.add_argument("--bf16", action="store_true", help="activity and mu stored in bfloat16")
     ap.add_argument("--slope", type=float, default=0.02, help="PSF sigma = 0.5 + slope * depth")
+    ap.add_argument("--group", type=int, default=0, help="backprojector cameras per scratch group (0: tuned)")
     a = ap.parse_args(argv)
 
     L = _lib.load()
+    if a.group:
+        L.nrgb_set_backproject_group(a.n, a.n, a.n, a.ncam, a.group)
     n = a.n
     act = S.ellipsoid_phantom((n, n, n), seed=0)
     mu = S.mu_map((n, n, n), seed=0)
