@@ -42,7 +42,7 @@ constexpr int kSlabsP = 4;        // projector depth slabs = cluster size
 constexpr int kSlabsB = 16;       // backprojector depth slabs
 constexpr int kCarryCols = 64 / kSlabsB;  // columns per CTA of the carry pass (32 KB of slab sums)
 constexpr int kGatherWarps = 4;   // warps per CTA of the inverse-rotation gather
-constexpr int kGatherCols = 8;    // accumulator columns per warp in the gather
+constexpr int kGatherCols = 4;    // accumulator columns per warp in the gather
 constexpr unsigned kFull = 0xffffffffu;
 
 __device__ __forceinline__ float fm(float a, float b) { return __fmul_rn(a, b); }
