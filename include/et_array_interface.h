@@ -90,7 +90,7 @@ int et_array_project_partial(float *activity, int *activity_size, float *sinogra
                              float *background_image, float background_attenuation, int GPU,
                              int truncate_negative_values, int do_rotate_partial);
 
-/* PSF / camera helpers -- emission-lib/_et_array_interface.h:53-55. *//* PSF / camera helpers -- emission-lib/_et_array_interface.h:53-55. */
+/* PSF / camera helpers -- emission-lib/_et_array_interface.h:53-55. */
 int et_array_calculate_size_psf(unsigned int *psf_size_x, unsigned int *psf_size_y, float fwhm_pixels_dist0,
                                 float sensitivity0, float dist0, float fwhm_pixels_dist1, float sensitivity1,
                                 float dist1);
@@ -293,8 +293,9 @@ int nrgb_batch_osem_step(void *batch, int step, int iterations, float epsilon, v
 /* Tuning table of the fused backprojector (no counterpart in the reference):
  * cameras per L2-resident scratch group for a problem shape (nx, ny, nz,
  * n_cameras); an all-zero shape sets the default for shapes without an entry
- * (none initially: then min(16, n_cameras / 2), at least 4).
- * niftyrec_gb300.autotune measures candidates and records the fastest. */
+ * (none initially: then even groups of at most 48 cameras, at most 2 GiB of
+ * scratch each).  niftyrec_gb300.autotune measures candidates and records the
+ * fastest. */
 int nrgb_set_backproject_group(int nx, int ny, int nz, int ncam, int group);
 int nrgb_get_backproject_group(int nx, int ny, int nz, int ncam);
 

@@ -21,7 +21,7 @@ import os
 
 import numpy as np
 
-CANDIDATES = (4, 8, 12, 16, 24, 32)
+CANDIDATES = (8, 16, 24, 32, 40, 48, 64)
 CACHE = os.path.join(os.path.expanduser("~"), ".cache", "niftyrec_gb300", "tune.json")
 
 

@@ -17,11 +17,18 @@ namespace nrgb {
 // key of zeros is the default.  Filled by nrgb_tune_set (the autotuner in
 // niftyrec_gb300/autotune.py measures candidates and records the fastest).
 namespace {
-// Cameras per group without a table entry: up to 16 (the fastest on GB300 at
-// 128^3 x 120 and 256^3 x 180: 1.60 ms and 25.7 ms per backprojection against
-// 1.77 / 28.2 ms with 8), but at least two groups so that the spread of one
-// overlaps the gather of the other (OSEM subsets of 15 cameras: 8).
-int default_group(int ncam) { return std::max(4, std::min(16, (ncam + 1) / 2)); }
+// Cameras per group without a table entry: groups of at most 48 cameras, as
+// even as possible (larger launches fill the GPU better; measured on GB300:
+// 128^3 x 120 cameras 1.23 ms per backprojection with 40, 1.42 ms with one
+// group of 120, 1.60 ms with 16; 256^3 x 180: 22.8 ms with 45; 15 or 45
+// cameras: one group is fastest), and at most 2 GiB of scratch per slot.
+int default_group(int nx, int ny, int nz, int ncam) {
+  const int groups = (ncam + 47) / 48;
+  const int g = (ncam + groups - 1) / groups;
+  const size_t per_cam = sizeof(float) * static_cast<size_t>(nz) * nx * round_up(std::min(ny, 128), 4);
+  const size_t cap = std::max<size_t>(1, (static_cast<size_t>(2) << 30) / per_cam);
+  return std::max(1, static_cast<int>(std::min<size_t>(g, cap)));
+}
 std::mutex g_tune_mu;
 std::map<std::tuple<int, int, int, int>, int> g_tune_group;
 }  // namespace
@@ -31,7 +38,7 @@ int tuned_group(int nx, int ny, int nz, int ncam) {
   auto it = g_tune_group.find(std::make_tuple(nx, ny, nz, ncam));
   if (it != g_tune_group.end()) return it->second;
   it = g_tune_group.find(std::make_tuple(0, 0, 0, 0));
-  return it != g_tune_group.end() ? it->second : default_group(ncam);
+  return it != g_tune_group.end() ? it->second : default_group(nx, ny, nz, ncam);
 }
 
 void set_tuned_group(int nx, int ny, int nz, int ncam, int group) {

@@ -42,7 +42,7 @@ constexpr int kSlabsP = 4;        // projector depth slabs = cluster size
 constexpr int kSlabsB = 16;       // backprojector depth slabs
 constexpr int kCarryCols = 64 / kSlabsB;  // columns per CTA of the carry pass (32 KB of slab sums)
 constexpr int kGatherWarps = 4;   // warps per CTA of the inverse-rotation gather
-constexpr int kGatherCols = 4;    // accumulator columns per warp in the gather
+constexpr int kGatherCols = 2;    // accumulator columns per warp in the gather
 constexpr unsigned kFull = 0xffffffffu;
 
 __device__ __forceinline__ float fm(float a, float b) { return __fmul_rn(a, b); }
@@ -574,8 +574,10 @@ __device__ __forceinline__ void scatter4(float* __restrict__ base, const Tap& t,
 // the PSF taps are flipped (correlation) and each output column is scattered
 // with the projector's own bilinear weights into the accumulator a.out
 // (vector reductions; all cameras in one launch, no scratch).
-template <int R, bool PSF, bool ATT, bool ADJ, class V>
-__global__ void __launch_bounds__(32 * kW, 2) k_spread_yg(const YgArgs a, int c0) {
+// CTAS: CTAs per SM the kernel is compiled for (3 where three tiles fit in
+// shared memory, for the float32 reference spread; else 2).
+template <int R, bool PSF, bool ATT, bool ADJ, class V, int CTAS = 2>
+__global__ void __launch_bounds__(32 * kW, CTAS) k_spread_yg(const YgArgs a, int c0) {
   using TS = TileShape<R>;
   constexpr bool KAHAN = StorageTraits<V>::kKahan;
   const V* __restrict__ mu = reinterpret_cast<const V*>(a.mu) + a.row0;
@@ -837,10 +839,22 @@ int launch_spread_R(const YgArgs& a, int c0, int gcount, cudaStream_t st) {
   };
   // only mu is sampled from storage here (the sinogram is float32)
   const bool bf16 = a.storage == kStorageBF16;
+  const bool three = 3 * (smem + 1024) <= 228 * 1024;
   if (psf) {
-    if (a.mu && bf16) go(k_spread_yg<R, true, true, ADJ, __nv_bfloat16>);
-    else if (a.mu) go(k_spread_yg<R, true, true, ADJ, float>);
-    else go(k_spread_yg<R, true, false, ADJ, float>);
+    if (a.mu && bf16) {
+      go(k_spread_yg<R, true, true, ADJ, __nv_bfloat16>);
+    } else if (a.mu) {
+      if constexpr (!ADJ) {
+        if (three)
+          go(k_spread_yg<R, true, true, false, float, 3>);
+        else
+          go(k_spread_yg<R, true, true, false, float>);
+      } else {
+        go(k_spread_yg<R, true, true, true, float>);
+      }
+    } else {
+      go(k_spread_yg<R, true, false, ADJ, float>);
+    }
   } else {
     if (a.mu && bf16) go(k_spread_yg<0, false, true, ADJ, __nv_bfloat16>);
     else if (a.mu) go(k_spread_yg<0, false, true, ADJ, float>);
