@@ -90,6 +90,23 @@ int et_array_project_partial(float *activity, int *activity_size, float *sinogra
                              float *background_image, float background_attenuation, int GPU,
                              int truncate_negative_values, int do_rotate_partial);
 
+/* Fisher information of a grid of points -- emission-lib/_et_array_interface.h:50-51
+ * (et_fisher_grid, emission-lib/_et.cpp:531-746).  grid_ptr: a volume with
+ * values 1..n at the n grid points (n = fisher_size[0]), 0 elsewhere;
+ * fisher_ptr / fisher_prior_ptr: [n, n] outputs (the prior may be NULL).  The
+ * first form projects the activity; the second takes a projection
+ * (sinogram_size) and the grid volume's size (bkpr_size).  epsilon is unused,
+ * as in the reference.  A PSF is required. */
+int et_array_fisher_grid(float *activity_ptr, int *activity_size, float *cameras, int *cameras_size, float *psf,
+                         int *psf_size, float *grid_ptr, float *fisher_ptr, float *fisher_prior_ptr, int *fisher_size,
+                         float *attenuation, int *attenuation_size, float epsilon, float background,
+                         float background_attenuation, int GPU);
+int et_array_fisher_grid_projection(float *sinogram_ptr, int *sinogram_size, int *bkpr_size, float *cameras,
+                                    int *cameras_size, float *psf, int *psf_size, float *grid_ptr, float *fisher_ptr,
+                                    float *fisher_prior_ptr, int *fisher_size, float *attenuation,
+                                    int *attenuation_size, float epsilon, float background,
+                                    float background_attenuation, int GPU);
+
 /* PSF / camera helpers -- emission-lib/_et_array_interface.h:53-55. */
 int et_array_calculate_size_psf(unsigned int *psf_size_x, unsigned int *psf_size_y, float fwhm_pixels_dist0,
                                 float sensitivity0, float dist0, float fwhm_pixels_dist1, float sensitivity1,

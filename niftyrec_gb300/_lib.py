@@ -44,6 +44,9 @@ PROTOTYPES = {
     "et_array_attenuation_gradient": (_I, [_P, _PI, _P, _PI, _P, _PI, _P, _PI, _P, _PI, _P, _PI, _F, _F, _I, _I]),
     "et_array_project_partial": (_I, [_P, _PI, _P, _PI, _P, _PI, _P, _PI, _P, _PI, _P, _PI, _F, _P, _F, _I, _I,
                                       _I]),
+    "et_array_fisher_grid": (_I, [_P, _PI, _P, _PI, _P, _PI, _P, _P, _P, _PI, _P, _PI, _F, _F, _F, _I]),
+    "et_array_fisher_grid_projection": (_I, [_P, _PI, _PI, _P, _PI, _P, _PI, _P, _P, _P, _PI, _P, _PI, _F, _F, _F,
+                                             _I]),
     "et_array_calculate_size_psf": (_I, [ctypes.POINTER(_U), ctypes.POINTER(_U), _F, _F, _F, _F, _F, _F]),
     "et_array_make_psf": (_I, [_P, _U, _U, _F, _F, _F, _F, _F, _F, _U]),
     "et_array_make_cameras": (_I, [_P, _F, _F, _U, _U]),

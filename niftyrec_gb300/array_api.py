@@ -90,6 +90,42 @@ def project_partial(activity, cameras, psf=None, attenuation=None, background=0.
     return sino, part
 
 
+def fisher_grid(activity, cameras, psf, grid, n, attenuation=None, background=0.0, background_attenuation=0.0,
+                prior=True):
+    """et_array_fisher_grid: Fisher information [n, n] of the grid points
+    (grid: volume with values 1..n at the points, 0 elsewhere) for the
+    projection of the activity, and the 26-neighbour prior matrix (or None)."""
+    L = load()
+    act, att, psf, grid, cams = _f32(activity), _f32(attenuation), _f32(psf), _f32(grid), _f32(cameras)
+    nz, ny, nx = act.shape
+    cs = _cam_size(cams)
+    f = np.zeros((n, n), np.float32)
+    pr = np.zeros((n, n), np.float32) if prior else None
+    tsz = _ints([nx, ny, nz] if att is not None else [0, 0, 0])
+    st = L.et_array_fisher_grid(_p(act), _pi(_ints([nx, ny, nz])), _p(cams), _pi(_ints(cs)), _p(psf),
+                                _pi(_ints(psf.shape[::-1])), _p(grid), _p(f), _p(pr), _pi(_ints([n, n])), _p(att),
+                                _pi(tsz), 0.0, background, background_attenuation, 1)
+    _check("et_array_fisher_grid", st)
+    return f, pr
+
+
+def fisher_grid_projection(sinogram, cameras, psf, grid, n, prior=True):
+    """et_array_fisher_grid_projection: as fisher_grid from a given projection
+    (n_cameras, ny, nx); grid is the volume (nz, ny, nx) of grid indexes."""
+    L = load()
+    sino, psf, grid, cams = _f32(sinogram), _f32(psf), _f32(grid), _f32(cameras)
+    ncam, ny, nx = sino.shape
+    gz, gy, gx = grid.shape
+    cs = _cam_size(cams)
+    f = np.zeros((n, n), np.float32)
+    pr = np.zeros((n, n), np.float32) if prior else None
+    st = L.et_array_fisher_grid_projection(_p(sino), _pi(_ints([nx, ny, ncam])), _pi(_ints([gx, gy, gz])), _p(cams),
+                                           _pi(_ints(cs)), _p(psf), _pi(_ints(psf.shape[::-1])), _p(grid), _p(f),
+                                           _p(pr), _pi(_ints([n, n])), None, _pi(_ints([0, 0, 0])), 0.0, 0.0, 0.0, 1)
+    _check("et_array_fisher_grid_projection", st)
+    return f, pr
+
+
 def backproject(sinogram, cameras, psf=None, attenuation=None, background=0.0, background_attenuation=0.0,
                 truncate_negative_values=1, nz=None):
     """SPECT_backproject_parallelholes; returns the volume (nz, ny, nx), nz defaults to nx."""

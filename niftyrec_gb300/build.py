@@ -21,7 +21,7 @@ LIB = os.path.join(HERE, "lib_et_array_interface.so")
 INCLUDE = os.path.join(os.path.dirname(HERE), "include")
 
 SOURCES = ["et_geometry.cpp", "et_engine.cpp", "et_api.cpp", "et_profile.cpp", "et_general.cu", "et_ygantry.cu", "et_update.cu",
-           "et_noalloc.cu", "et_plan.cpp"]
+           "et_noalloc.cu", "et_plan.cpp", "et_fisher.cu"]
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC,-ffp-contract=off,-fvisibility=hidden",

@@ -155,6 +155,72 @@ int osem_step_host(const Problem& pb, float* act, const float* ysub, const float
   return finish(ds, s);
 }
 
+// Grid points of a Fisher-information grid volume (values 1..n at the points,
+// 0 elsewhere), scanned x outer, z inner as emission-lib/_et.cpp:580-598;
+// kErrParameters (the reference's ET_ERROR_BADGRID) for a repeated or
+// out-of-range index.
+int grid_points(const float* grid, int nx, int ny, int nz, int n, std::vector<int>* xyz) {
+  xyz->assign(3 * static_cast<size_t>(n), -1);
+  for (int x = 0; x < nx; ++x)
+    for (int y = 0; y < ny; ++y)
+      for (int z = 0; z < nz; ++z) {
+        const float g = grid[(static_cast<size_t>(z) * ny + y) * nx + x];
+        if (g == 0.0f) continue;
+        const int k = static_cast<int>(g) - 1;
+        if (k < 0 || k >= n || (*xyz)[3 * k] != -1) return kErrParameters;
+        (*xyz)[3 * k] = x;
+        (*xyz)[3 * k + 1] = y;
+        (*xyz)[3 * k + 2] = z;
+      }
+  return kOk;
+}
+
+// Grid points rotated into every camera's frame (XYZ, +theta), with
+// reg_mat44_mul's float order (reg-lib/_reg_affineTransformation.cpp:44-51)
+// and the implicit truncation to integers of emission-lib/_et.cpp:619-623.
+std::vector<int> rotated_grid(const Cameras& cc, const std::vector<int>& xyz, int n) {
+  std::vector<int> out(static_cast<size_t>(cc.n) * n * 3);
+  const int nc = cc.n;
+  for (int cam = 0; cam < nc; ++cam) {
+    float M[16];
+    rotation_matrix(M, cc.angles[cam], cc.angles[nc + cam], cc.angles[2 * nc + cam], cc.centers[cam],
+                    cc.centers[nc + cam], cc.centers[2 * nc + cam], 0);
+    for (int k = 0; k < n; ++k) {
+      const float p0 = static_cast<float>(xyz[3 * k]), p1 = static_cast<float>(xyz[3 * k + 1]),
+                  p2 = static_cast<float>(xyz[3 * k + 2]);
+      for (int r = 0; r < 3; ++r) {
+        const float v = M[4 * r] * p0 + M[4 * r + 1] * p1 + M[4 * r + 2] * p2 + M[4 * r + 3];
+        out[(static_cast<size_t>(cam) * n + k) * 3 + r] = static_cast<int>(v);
+      }
+    }
+  }
+  return out;
+}
+
+// Fisher matrix on the device from a projection (device, [ncam][npy][npx]),
+// grid points and PSF planes (host); fisher / prior are host [n][n].
+int fisher_from_projection(DeviceState& ds, Carver& cv, const float* d_proj, int npx, int npy, int nz,
+                           const Cameras& cc, const std::vector<int>& xyz, int n, const float* psf, int kx, int ky,
+                           int psf_planes, float* fisher, float* prior, cudaStream_t st) {
+  const std::vector<int> coords = rotated_grid(cc, xyz, n);
+  int* d_coords = cv.take<int>(coords.size());
+  int* d_xyz = cv.take<int>(xyz.size());
+  float* d_psf = cv.take<float>(static_cast<size_t>(kx) * ky * psf_planes);
+  float* d_f = cv.take<float>(static_cast<size_t>(n) * n);
+  float* d_p = prior ? cv.take<float>(static_cast<size_t>(n) * n) : nullptr;
+  if (!d_coords || !d_xyz || !d_psf || !d_f || (prior && !d_p)) return kErrAllocGpu;
+  if (cudaMemcpyAsync(d_coords, coords.data(), sizeof(int) * coords.size(), cudaMemcpyHostToDevice, st) !=
+          cudaSuccess ||
+      cudaMemcpyAsync(d_xyz, xyz.data(), sizeof(int) * xyz.size(), cudaMemcpyHostToDevice, st) != cudaSuccess ||
+      cudaMemcpyAsync(d_psf, psf, sizeof(float) * kx * ky * psf_planes, cudaMemcpyHostToDevice, st) != cudaSuccess)
+    return kErrTransferGpu;
+  int s = fisher_pairs(d_proj, npx, npy, d_coords, d_xyz, n, cc.n, d_psf, kx, ky, nz, d_f, d_p, st);
+  if (s == kOk) s = d2h(fisher, d_f, static_cast<size_t>(n) * n, st);
+  if (s == kOk && prior) s = d2h(prior, d_p, static_cast<size_t>(n) * n, st);
+  (void)ds;
+  return s;
+}
+
 int project_partial_host(const Problem& pb, const float* act, const float* att, const float* bg_image, float* sino,
                          float* partial, int do_rotate) {
   int s;
@@ -595,6 +661,103 @@ int et_array_project_partial(float* activity, int* activity_size, float* sinogra
   if (s != kOk) return s;
   return project_partial_host(pb, no_act ? nullptr : activity, no_att ? nullptr : attenuation, background_image,
                               sinogram, partialsum, do_rotate_partial);
+}
+
+// emission-lib/_et_array_interface.cpp:1135-1340 (et_fisher_grid,
+// emission-lib/_et.cpp:531-746): Fisher information of the grid points of
+// grid_ptr (values 1..n, n = fisher_size[0]) for the projection of the
+// activity (truncated).  fisher_prior_ptr may be NULL.  A PSF is required
+// (the reference dereferences it unconditionally).
+int et_array_fisher_grid(float* activity_ptr, int* activity_size, float* cameras, int* cameras_size, float* psf,
+                         int* psf_size, float* grid_ptr, float* fisher_ptr, float* fisher_prior_ptr, int* fisher_size,
+                         float* attenuation, int* attenuation_size, float epsilon, float background,
+                         float background_attenuation, int GPU) {
+  (void)epsilon;
+  (void)GPU;
+  if (!activity_ptr || !activity_size || !cameras || !cameras_size || !psf || !psf_size || !grid_ptr ||
+      !fisher_ptr || !fisher_size || !attenuation_size)
+    return kErrParameters;
+  const int nx = activity_size[0], ny = activity_size[1], nz = activity_size[2];
+  const int ncam = cameras_size[0], ncols = cameras_size[1], n = fisher_size[0];
+  if (!(ncols == 1 || ncols == 3 || ncols == 6) || n <= 0 || nx <= 0 || ny <= 0 || nz <= 0) return kErrParameters;
+  if (psf_size[0] % 2 != 1 || psf_size[1] % 2 != 1 || psf_size[2] != nx) return kErrParameters;
+  const bool no_att = all_zero3(attenuation_size);
+  std::vector<int> xyz;
+  int s = grid_points(grid_ptr, nx, ny, nz, n, &xyz);
+  if (s != kOk) return s;
+  Cameras cc;
+  const int asz[3] = {nx, ny, nz};
+  if ((s = expand_cameras(cameras, ncam, ncols, asz, &cc)) != kOk) return s;
+  Problem pb;
+  if ((s = make_problem(nx, ny, nz, cc, psf, psf_size, background, background_attenuation, 1, &pb)) != kOk) return s;
+  DeviceState& ds = current_device_state(&s);
+  if (s != kOk) return s;
+  std::lock_guard<std::mutex> lk(ds.mu);
+  const size_t nvox = static_cast<size_t>(nx) * ny * nz, nsino = static_cast<size_t>(nx) * ny * ncam;
+  const size_t extra = sizeof(int) * (3 * static_cast<size_t>(n) * (ncam + 1)) +
+                       sizeof(float) * (static_cast<size_t>(psf_size[0]) * psf_size[1] * psf_size[2] +
+                                        2 * static_cast<size_t>(n) * n) + 8 * 256;
+  const size_t ws = project_workspace(pb, true, !no_att);
+  if ((s = ensure_arena(ds, fbytes(2 * nvox + nsino) + 4 * 256 + ws + extra)) != kOk) return s;
+  Carver cv(ds.arena, ds.arena_bytes);
+  float* d_act = cv.take<float>(nvox);
+  float* d_att = no_att ? nullptr : cv.take<float>(nvox);
+  float* d_sino = cv.take<float>(nsino);
+  char* w = cv.take<char>(ws);
+  cudaStream_t st = ds.stream;
+  if ((s = h2d(d_act, activity_ptr, nvox, st)) != kOk) return finish(ds, s);
+  if (d_att && (s = h2d(d_att, attenuation, nvox, st)) != kOk) return finish(ds, s);
+  g_last_path = use_fused(pb) ? 1 : 2;
+  if ((s = project_device(pb, d_act, d_att, d_sino, w, ws, &ds.staging, st)) != kOk) return finish(ds, s);
+  s = fisher_from_projection(ds, cv, d_sino, nx, ny, nz, cc, xyz, n, psf, psf_size[0], psf_size[1], psf_size[2],
+                             fisher_ptr, fisher_prior_ptr, st);
+  return finish(ds, s);
+}
+
+// emission-lib/_et_array_interface.cpp:1344-1540: the same from a given
+// projection (sinogram_size = {nx, ny, n_cameras}); the grid volume has
+// bkpr_size and the camera centres follow (nx, ny, nx).
+int et_array_fisher_grid_projection(float* sinogram_ptr, int* sinogram_size, int* bkpr_size, float* cameras,
+                                    int* cameras_size, float* psf, int* psf_size, float* grid_ptr, float* fisher_ptr,
+                                    float* fisher_prior_ptr, int* fisher_size, float* attenuation,
+                                    int* attenuation_size, float epsilon, float background,
+                                    float background_attenuation, int GPU) {
+  (void)epsilon;
+  (void)GPU;
+  (void)attenuation;
+  (void)attenuation_size;
+  (void)background;
+  (void)background_attenuation;
+  if (!sinogram_ptr || !sinogram_size || !bkpr_size || !cameras || !cameras_size || !psf || !psf_size || !grid_ptr ||
+      !fisher_ptr || !fisher_size)
+    return kErrParameters;
+  const int npx = sinogram_size[0], npy = sinogram_size[1], ncam = cameras_size[0], ncols = cameras_size[1];
+  const int n = fisher_size[0];
+  if (!(ncols == 1 || ncols == 3 || ncols == 6) || n <= 0 || npx <= 0 || npy <= 0 || sinogram_size[2] < ncam)
+    return kErrParameters;
+  if (psf_size[0] % 2 != 1 || psf_size[1] % 2 != 1 || psf_size[2] != bkpr_size[0]) return kErrParameters;
+  std::vector<int> xyz;
+  int s = grid_points(grid_ptr, bkpr_size[0], bkpr_size[1], bkpr_size[2], n, &xyz);
+  if (s != kOk) return s;
+  Cameras cc;
+  const int csz[3] = {npx, npy, npx};
+  if ((s = expand_cameras(cameras, ncam, ncols, csz, &cc)) != kOk) return s;
+  DeviceState& ds = current_device_state(&s);
+  if (s != kOk) return s;
+  std::lock_guard<std::mutex> lk(ds.mu);
+  const size_t nsino = static_cast<size_t>(npx) * npy * ncam;
+  const size_t extra = sizeof(int) * (3 * static_cast<size_t>(n) * (ncam + 1)) +
+                       sizeof(float) * (static_cast<size_t>(psf_size[0]) * psf_size[1] * psf_size[2] +
+                                        2 * static_cast<size_t>(n) * n) + 8 * 256;
+  if ((s = ensure_arena(ds, fbytes(nsino) + 256 + extra)) != kOk) return s;
+  Carver cv(ds.arena, ds.arena_bytes);
+  float* d_sino = cv.take<float>(nsino);
+  cudaStream_t st = ds.stream;
+  g_last_path = 2;
+  if ((s = h2d(d_sino, sinogram_ptr, nsino, st)) != kOk) return finish(ds, s);
+  s = fisher_from_projection(ds, cv, d_sino, npx, npy, bkpr_size[2], cc, xyz, n, psf, psf_size[0], psf_size[1],
+                             psf_size[2], fisher_ptr, fisher_prior_ptr, st);
+  return finish(ds, s);
 }
 
 // emission-lib/_et_array_interface.cpp:1080-1131.

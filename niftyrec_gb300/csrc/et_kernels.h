@@ -138,6 +138,15 @@ int yg_project_batch(const BatchStepDesc* d_desc, const BatchSel& sel, int psf_k
 int osem_ratio_batch(const BatchStepDesc* d_desc, const BatchElems& e, float eps, cudaStream_t st);
 int osem_update_batch(const BatchStepDesc* d_desc, const BatchElems& e, float eps, cudaStream_t st);
 
+// ---- Fisher information of a grid of points ----
+// fisher[i][j] (and [j][i]) = sum over cameras and the overlap of the two
+// points' PSF footprints of PSF_i * PSF_j * proj, in the order of
+// emission-lib/_et.cpp:626-700; proj [ncam][npy][npx]; coords [ncam][n][3]
+// rotated integer coordinates; grid_xyz [n][3]; psf planes [plane][ky][kx];
+// prior (optional) 1 for 26-neighbour pairs.
+int fisher_pairs(const float* proj, int npx, int npy, const int* coords, const int* grid_xyz, int n, int ncam,
+                 const float* psf, int kx, int ky, int nz, float* fisher, float* prior, cudaStream_t st);
+
 // ---- layout conversion and elementwise helpers ----
 // planes x [ny][nx] (nifti) <-> planes x [nx][cy] (column), zero pads.
 int to_column(const float* src, float* dst, int nx, int ny, int cy, int planes, cudaStream_t st);

@@ -601,6 +601,121 @@ int ORC(spect_project_partial)(const REAL *act, const int act_size[3], REAL *sin
     return st;
 }
 
+/* Fisher information of a grid of voxels, et_fisher_grid
+ * (emission-lib/_et.cpp:531-746).  grid: volume [nx, ny, nz] holding 1..n at
+ * the grid points, 0 elsewhere (scanned x outer, z inner, :580-598).  proj:
+ * the projection [npx, npy, ncam] (the "inverse sinogram" of the reference,
+ * whose inversion is commented out at :572-574, so it is the projection
+ * itself).  Per camera the grid points are rotated (XYZ, +theta, about the
+ * camera centre, reg_mat44_mul order, truncated to integers :619-623); for
+ * every pair i <= j whose PSFs (plane = rotated depth) overlap, the products
+ * of the two shifted PSFs times the projection are summed over the overlap
+ * box (:626-700).  prior (optional): 1 where two points are 26-neighbours
+ * (:703-721).  Both matrices symmetric [n, n].  Returns 2 for a malformed grid. */
+int ORC(fisher_grid)(const REAL *proj, int npx, int npy, const REAL *grid, const int size[3], REAL *fisher,
+                     REAL *prior, int n, const REAL *psf, int kx, int ky, const REAL *angles, const REAL *centers,
+                     int ncam)
+{
+    int nx = size[0], ny = size[1], nz = size[2];
+    int semi_x = (kx - 1) / 2, semi_y = (ky - 1) / 2;
+    int *gc = (int *)malloc(sizeof(int) * 3 * (size_t)n);
+    int *gr = (int *)malloc(sizeof(int) * 3 * (size_t)n);
+    for (int i = 0; i < 3 * n; i++) gc[i] = -1;
+    for (int x = 0; x < nx; x++)
+        for (int y = 0; y < ny; y++)
+            for (int z = 0; z < nz; z++) {
+                REAL g = grid[(size_t)z * ny * nx + (size_t)y * nx + x];
+                if (g != 0) {
+                    int k = (int)g - 1;
+                    if (k < 0 || k >= n || gc[3 * k] != -1) {
+                        free(gc);
+                        free(gr);
+                        return ORC_ERR_PARAMETERS;
+                    }
+                    gc[3 * k] = x;
+                    gc[3 * k + 1] = y;
+                    gc[3 * k + 2] = z;
+                }
+            }
+    for (size_t i = 0; i < (size_t)n * n; i++) fisher[i] = 0;
+    if (prior)
+        for (size_t i = 0; i < (size_t)n * n; i++) prior[i] = 0;
+    REAL A[16];
+    for (int cam = 0; cam < ncam; cam++) {
+        const REAL *plane = proj + (size_t)npx * npy * cam;
+        ORC(rotation_matrix)(A, angles[cam], angles[ncam + cam], angles[2 * ncam + cam],
+                             centers[cam], centers[ncam + cam], centers[2 * ncam + cam], 0);
+        for (int k = 0; k < n; k++) {
+            REAL p0 = (REAL)gc[3 * k], p1 = (REAL)gc[3 * k + 1], p2 = (REAL)gc[3 * k + 2];
+            for (int r = 0; r < 3; r++)
+                gr[3 * k + r] = (int)(A[4 * r] * p0 + A[4 * r + 1] * p1 + A[4 * r + 2] * p2 + A[4 * r + 3]);
+        }
+        for (int i = 0; i < n; i++) {
+            int ix = gr[3 * i], iy = gr[3 * i + 1], iz = gr[3 * i + 2];
+            for (int j = i; j < n; j++) {
+                int jx = gr[3 * j], jy = gr[3 * j + 1], jz = gr[3 * j + 2];
+                int bx = kx - abs(jx - ix), by = ky - abs(jy - iy);
+                int px = (ix > jx ? ix : jx) - semi_x, py = (iy > jy ? iy : jy) - semi_y;
+                if (!(bx > 0 && by > 0 && iz >= 0 && jz >= 0 && iz < nz && jz < nz)) continue;
+                int pix, piy, pjx, pjy;
+                if (jx >= ix && jy > iy) { pix = jx - ix; piy = jy - iy; pjx = 0; pjy = 0; }
+                else if (jx < ix && jy >= iy) { pix = 0; piy = jy - iy; pjx = ix - jx; pjy = 0; }
+                else if (jx <= ix && jy < iy) { pix = 0; piy = 0; pjx = ix - jx; pjy = iy - jy; }
+                else { pix = jx - ix; piy = 0; pjx = 0; pjy = iy - jy; }
+                const REAL *Pi = psf + (size_t)iz * kx * ky, *Pj = psf + (size_t)jz * kx * ky;
+                REAL f = fisher[(size_t)i * n + j];
+                for (int x = 0; x < bx; x++)
+                    for (int y = 0; y < by; y++) {
+                        int qx = px + x, qy = py + y;
+                        if (qx >= 0 && qy >= 0 && qx < npx && qy < npy)
+                            f = f + Pj[(pjy + y) * kx + (pjx + x)] * Pi[(piy + y) * kx + (pix + x)] * plane[qy * npx + qx];
+                    }
+                fisher[(size_t)i * n + j] = f;
+            }
+        }
+    }
+    if (prior)
+        for (int i = 0; i < n; i++)
+            for (int j = i; j < n; j++)
+                if (abs(gc[3 * i] - gc[3 * j]) <= 1 && abs(gc[3 * i + 1] - gc[3 * j + 1]) <= 1 &&
+                    abs(gc[3 * i + 2] - gc[3 * j + 2]) <= 1)
+                    prior[(size_t)i * n + j] = 1;
+    for (int i = 0; i < n; i++)
+        for (int j = i + 1; j < n; j++) {
+            fisher[(size_t)j * n + i] = fisher[(size_t)i * n + j];
+            if (prior) prior[(size_t)j * n + i] = prior[(size_t)i * n + j];
+        }
+    free(gc);
+    free(gr);
+    return ORC_OK;
+}
+
+/* et_array_fisher_grid (emission-lib/_et_array_interface.cpp:1135-1340):
+ * project the activity (truncated, :557) and accumulate the Fisher matrix of
+ * the grid; the projection planes are [nx, ny] (the reference sizes them
+ * [nx, nz], equal for its cubic volumes). */
+int ORC(spect_fisher_grid)(const REAL *act, const int act_size[3], const REAL *cameras, const int cam_size[2],
+                           const REAL *psf, const int psf_size[3], const REAL *grid, REAL *fisher, REAL *prior, int n,
+                           const REAL *att, const int att_size[3], REAL bg, REAL bg_att)
+{
+    int ncam = cam_size[0], ncols = cam_size[1];
+    int no_att = (att_size[0] == 0 && att_size[1] == 0 && att_size[2] == 0);
+    if (!psf || psf_size[0] % 2 != 1 || psf_size[1] % 2 != 1 || psf_size[2] != act_size[0]) return ORC_ERR_PARAMETERS;
+    REAL *angles = (REAL *)malloc(sizeof(REAL) * 3 * ncam);
+    REAL *centers = (REAL *)malloc(sizeof(REAL) * 3 * ncam);
+    REAL *proj = (REAL *)malloc(sizeof(REAL) * (size_t)act_size[0] * act_size[1] * ncam);
+    int st = expand_cameras(cameras, ncam, ncols, act_size, angles, centers);
+    if (st == ORC_OK)
+        st = ORC(project)(act, no_att ? NULL : att, act_size, proj, angles, centers, ncam, psf, psf_size, bg, bg_att, 1);
+    if (st == ORC_OK)
+        st = ORC(fisher_grid)(proj, act_size[0], act_size[1], grid, act_size, fisher, prior, n, psf, psf_size[0],
+                              psf_size[1], angles, centers, ncam);
+    free(angles);
+    free(centers);
+    free(proj);
+    return st;
+}
+
 /* SPECT_backproject_parallelholes, emission-lib/_et_array_interface.cpp:547-710:
  * the centre comes from (sino0, sino1, sino0), the volume grid from bkpr_size. */
 int ORC(spect_backproject)(const REAL *sino, const int sino_size[3], REAL *bkpr, const int bkpr_size[3],

@@ -151,6 +151,21 @@ class Restated:
             raise RuntimeError(f"oracle project_partial status {st}")
         return sino, part
 
+    def fisher_grid(self, act, cameras, psf, grid, n, att=None, bg=0.0, bg_att=0.0, prior=True):
+        """et_array_fisher_grid: (Fisher matrix [n, n], prior matrix [n, n] or None)."""
+        act, att, psf, grid, cams = (self._arr(a) for a in (act, att, psf, grid, cameras))
+        nz, ny, nx = act.shape
+        cs = _cam_size(cams)
+        fisher = np.zeros((n, n), dtype=self.dtype)
+        pr = np.zeros((n, n), dtype=self.dtype) if prior else None
+        tsz = _ints([nx, ny, nz] if att is not None else [0, 0, 0])
+        st = self._f("spect_fisher_grid")(_ptr(act), _ptr(_ints([nx, ny, nz])), _ptr(cams), _ptr(_ints(cs)), _ptr(psf),
+                                          _ptr(_ints(list(psf.shape[::-1]))), _ptr(grid), _ptr(fisher), _ptr(pr),
+                                          _I(n), _ptr(att), _ptr(tsz), self.real(bg), self.real(bg_att))
+        if st:
+            raise RuntimeError(f"oracle fisher_grid status {st}")
+        return fisher, pr
+
     def gradient_attenuation(self, sino, act, att, cameras, psf=None, bg=0.0, bg_att=0.0, truncate=0):
         sino = self._arr(sino)
         act = self._arr(act)
@@ -256,6 +271,22 @@ class Reference:
         if st:
             raise RuntimeError(f"reference mlem status {st}")
         return act
+
+    def fisher_grid(self, act, cameras, psf, grid, n, att=None, bg=0.0, bg_att=0.0, prior=True):
+        act, att, psf, grid, cams = (self._f32(a) for a in (act, att, psf, grid, cameras))
+        nz, ny, nx = act.shape
+        cs = _cam_size(cams)
+        fisher = np.zeros((n, n), dtype=np.float32)
+        pr = np.zeros((n, n), dtype=np.float32) if prior else None
+        tsz = _ints([nx, ny, nz] if att is not None else [0, 0, 0])
+        fn = self.lib.et_array_fisher_grid
+        fn.restype = _I
+        st = fn(_ptr(act), _ptr(_ints([nx, ny, nz])), _ptr(cams), _ptr(_ints(cs)), _ptr(psf),
+                _ptr(_ints(list(psf.shape[::-1]))), _ptr(grid), _ptr(fisher), _ptr(pr), _ptr(_ints([n, n])), _ptr(att),
+                _ptr(tsz), ctypes.c_float(0.0), ctypes.c_float(bg), ctypes.c_float(bg_att), _I(0))
+        if st:
+            raise RuntimeError(f"reference fisher_grid status {st}")
+        return fisher, pr
 
     def make_cameras(self, first_deg, last_deg, n, axis=1):
         cams = np.zeros(3 * n, dtype=np.float32)

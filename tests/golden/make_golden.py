@@ -103,6 +103,26 @@ def main():
     save("make_cameras", c60=R.make_cameras(0.0, 354.0, 60, 1), c7x=R.make_cameras(-30.0, 45.0, 7, 0),
          c5z=R.make_cameras(10.0, 100.0, 5, 2))
 
+    fisher(R)
+
+
+def fisher(R):
+    # 8. Fisher information of a 24-point grid (et_array_fisher_grid), PSF + attenuation.
+    shape = (16, 16, 16)
+    act = S.ellipsoid_phantom(shape, seed=17)
+    mu = S.mu_map(shape, seed=17)
+    psf = S.gaussian_psf(5, 16, 0.5, 0.05)
+    cams = S.cameras_about_y(8, 5.0)
+    grid = np.zeros(shape, np.float32)
+    pts = np.random.default_rng(17).choice(grid.size, 24, replace=False)
+    grid.flat[pts] = np.arange(1, 25, dtype=np.float32)
+    f, pr = R.fisher_grid(act, cams, psf, grid, 24, mu)
+    save("fisher_16", act=act, mu=mu, psf=psf, cameras=cams, grid=grid, fisher=f, prior=pr)
+
 
 if __name__ == "__main__":
-    main()
+    # `python tests/golden/make_golden.py fisher` regenerates that fixture only
+    if len(sys.argv) > 1 and sys.argv[1] == "fisher":
+        fisher(Reference())
+    else:
+        main()

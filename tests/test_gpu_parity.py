@@ -194,3 +194,23 @@ def test_partial_sum_projector(o32, rotate, att, bgi):
     so, po = o32.project_partial(act, cams, psf, mu, bg=0.2, bg_image=img, truncate=1, rotate=rotate)
     assert per_plane_rel(s, so) < RTOL
     assert rel_l2(part, po) < RTOL
+
+
+def test_fisher_grid_golden(golden, o32):
+    """et_array_fisher_grid on the GPU against the compiled reference's
+    (golden fixture) and, from the reference's own projection, exactly the
+    reference's accumulation (et_array_fisher_grid_projection)."""
+    g = golden("fisher_16")
+    f, pr = A.fisher_grid(g["act"], g["cameras"], g["psf"], g["grid"], 24, g["mu"])
+    assert rel_l2(f, g["fisher"]) < RTOL
+    np.testing.assert_array_equal(pr, g["prior"])
+    # from the oracle's projection (bit-exact to the reference's) the
+    # accumulation is the reference's own order: bit-exact
+    so = o32.project(g["act"], g["cameras"], g["psf"], g["mu"])
+    f2, _ = A.fisher_grid_projection(so, g["cameras"], g["psf"], g["grid"], 24)
+    np.testing.assert_array_equal(f2, g["fisher"])
+    bad = g["grid"].copy()
+    bad.flat[np.flatnonzero(bad)[:2]] = 1.0  # repeated index
+    with pytest.raises(Exception) as e:
+        A.fisher_grid(g["act"], g["cameras"], g["psf"], bad, 24, g["mu"])
+    assert getattr(e.value, "status", None) == 2

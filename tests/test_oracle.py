@@ -140,3 +140,15 @@ def test_partial_sum_projector_restatement():
     sr, partr = o.project_partial(act, cams, psf, mu, bg=0.0, truncate=0, rotate=1)
     np.testing.assert_allclose(sr, o.project(act, cams, psf, mu, truncate=0), rtol=1e-4, atol=1e-5)
     assert partr.shape == (4,) + shape
+
+
+def test_fisher_grid_restatement_matches_golden(golden):
+    """et_fisher_grid (emission-lib/_et.cpp:531-746) restated: bit-exact to the
+    compiled reference's et_array_fisher_grid on the committed fixture."""
+    from oracle.oracle import Restated
+
+    g = golden("fisher_16")
+    f, pr = Restated("f32").fisher_grid(g["act"], g["cameras"], g["psf"], g["grid"], 24, g["mu"])
+    np.testing.assert_array_equal(f, g["fisher"])
+    np.testing.assert_array_equal(pr, g["prior"])
+    assert np.allclose(f, f.T) and (np.diag(f) > 0).any()
