@@ -66,6 +66,7 @@ struct YgArgs {
   int truncate = 0;
   int back_mode = kBackReference;
   int storage = kStorageF32;  // type of act and mu
+  int pslabs = 0;  // projector depth slabs = cluster size (2, 4, 8; 0: chosen by the launcher)
   // backprojector work space (yg_backproject_workspace bytes); the kernels
   // see it as slab sums [ncam][slabs][nx][cy] then scratch [group][nz][nx][cy]
   float* work = nullptr;

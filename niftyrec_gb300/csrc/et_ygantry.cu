@@ -38,7 +38,7 @@ namespace cg = cooperative_groups;
 constexpr int kW = 8;             // warps per CTA of the tile engine
 constexpr int kTXW = 4;           // output columns per warp
 constexpr int kTXC = kW * kTXW;   // output columns per CTA
-constexpr int kSlabsP = 4;        // projector depth slabs = cluster size
+constexpr int kSlabsP = 4;        // depth slabs (= cluster size) of the batched projector
 constexpr int kSlabsB = 16;       // backprojector depth slabs
 constexpr int kCarryCols = 64 / kSlabsB;  // columns per CTA of the carry pass (32 KB of slab sums)
 constexpr int kGatherWarps = 4;   // warps per CTA of the inverse-rotation gather
@@ -343,7 +343,8 @@ __device__ __forceinline__ void project_item(const YgArgs& a, int cam, int x0, u
   const int yb = lane * 4;
   const bool yok = lane_rows_ok(a, yb);
 
-  const int zper = (a.nz + kSlabsP - 1) / kSlabsP;
+  const int nslabs = static_cast<int>(cluster.num_blocks());  // depth slabs = cluster size (2, 4 or 8)
+  const int zper = (a.nz + nslabs - 1) / nslabs;
   const int zbeg = slab * zper, zend = min(a.nz, zbeg + zper);
   if (PSF) {  // this slab's planes only
     for (int i = zbeg * 2 * K + threadIdx.x; i < zend * 2 * K; i += blockDim.x) s_psf[i] = __ldg(a.psf + i);
@@ -413,14 +414,14 @@ __device__ __forceinline__ void project_item(const YgArgs& a, int cam, int x0, u
     sP[(warp * kTXW + i) * 32 + lane] = depth_value4<KAHAN>(P[i], cP[i]);
   }
   cluster.sync();
-  constexpr int kPerRank = kTXC / kSlabsP;  // outputs merged by each CTA of the cluster
+  const int per_rank = kTXC / nslabs;  // outputs merged by each CTA of the cluster
 #pragma unroll
   for (int i = 0; i < kTXW; ++i) {
     const int o = warp * kTXW + i;
     const int x = x0 + o;
-    if (o / kPerRank != slab || x >= a.nx || !yok || !lane_writes(a, yb)) continue;
+    if (o / per_rank != slab || x >= a.nx || !yok || !lane_writes(a, yb)) continue;
     float4 Pt = make_float4(0.f, 0.f, 0.f, 0.f), Tt = make_float4(0.f, 0.f, 0.f, 0.f);
-    for (int s = 0; s < kSlabsP; ++s) {
+    for (int s = 0; s < nslabs; ++s) {
       const float4* rT = cluster.map_shared_rank(sT, s);
       const float4* rP = cluster.map_shared_rank(sP, s);
       const float4 ps = rP[o * 32 + lane];
@@ -442,17 +443,17 @@ __device__ __forceinline__ void project_item(const YgArgs& a, int cam, int x0, u
   cluster.sync();  // keep this CTA's shared memory alive until the others have read it
 }
 
-// One work item per cluster: blockIdx.x / kSlabsP = (camera, x-tile).  CTAS:
-// CTAs per SM the kernel is compiled for -- 3 (80 registers, more warps to
-// hide the gathers' latency) where three tiles fit in shared memory and the
-// storage is float32, else 2 (128 registers; bfloat16 needs them for its
-// Kahan compensations).
+// One work item per cluster of a.pslabs CTAs (the cluster size is set at
+// launch): blockIdx.x / a.pslabs = (camera, x-tile).  CTAS: CTAs per SM the
+// kernel is compiled for -- 3 (80 registers, more warps to hide the gathers'
+// latency) where three tiles fit in shared memory and the storage is
+// float32, else 2 (128 registers; bfloat16 needs them for its Kahan
+// compensations).
 template <int R, bool PSF, bool ATT, class V, int CTAS>
-__global__ void __cluster_dims__(kSlabsP, 1, 1) __launch_bounds__(32 * kW, CTAS)
-    k_project_yg(const YgArgs a) {
+__global__ void __launch_bounds__(32 * kW, CTAS) k_project_yg(const YgArgs a) {
   extern __shared__ __align__(16) unsigned char smem[];
   const int ntile = (a.nx + kTXC - 1) / kTXC;
-  const int item = blockIdx.x / kSlabsP;
+  const int item = blockIdx.x / a.pslabs;
   project_item<R, PSF, ATT, V>(a, item / ntile, (item % ntile) * kTXC, smem);
 }
 
@@ -793,16 +794,44 @@ __global__ void k_from_col(const float* __restrict__ src, float* __restrict__ ds
 }
 
 // ------------------------------------------------------------- dispatch
+// Depth slabs (cluster size) of the projector: the fewest of 2, 4, 8 that
+// give at least four waves of CTAs (fewer slabs merge less; more slabs fill
+// the GPU for small problems).  Measured on GB300: 128^3 x 120 cameras 4
+// (0.84 ms; 2: 0.87, 8: 0.87), 256^3 x 180: 2 (15.9 ms; 4: 16.7),
+// 64^3 x 60: 8 (0.149 ms; 4: 0.158).
+int project_slabs(int items, int ctas_per_sm) {
+  const int slots = 152 * ctas_per_sm;
+  for (int s = 2; s < 8; s *= 2)
+    if (items * s >= 4 * slots) return s;
+  return 8;
+}
+
 template <int R>
-int launch_project_R(const YgArgs& a, cudaStream_t st) {
+int launch_project_R(const YgArgs& a_in, cudaStream_t st) {
+  YgArgs a = a_in;
   const int ntile = (a.nx + kTXC - 1) / kTXC;
-  const dim3 grid(a.ncam * ntile * kSlabsP), block(32 * kW);
   const bool psf = a.psf != nullptr;
   const size_t smem = tile_smem_bytes<R>(psf ? a.nz : 0);
+  // three CTAs per SM need three tiles (plus 1 KB reserved each) in the 228 KB
+  const bool three = 3 * (smem + 1024) <= 228 * 1024;
+  const bool bf16 = a.storage == kStorageBF16;
+  if (a.pslabs != 2 && a.pslabs != 4 && a.pslabs != 8) a.pslabs = project_slabs(a.ncam * ntile, three && !bf16 ? 3 : 2);
   auto go = [&](auto k) {
     cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(a.ncam * ntile * a.pslabs);
+    cfg.blockDim = dim3(32 * kW);
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = st;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeClusterDimension;
+    attr[0].val.clusterDim.x = a.pslabs;
+    attr[0].val.clusterDim.y = 1;
+    attr[0].val.clusterDim.z = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
     NRGB_LAUNCH_SCOPE("k_project_yg", st);
-    k<<<grid, block, smem, st>>>(a);
+    cudaLaunchKernelEx(&cfg, k, a);
   };
   auto pick = [&](auto v, auto ctas) {
     using V = decltype(v);
@@ -815,9 +844,7 @@ int launch_project_R(const YgArgs& a, cudaStream_t st) {
       else go(k_project_yg<0, false, false, V, C>);
     }
   };
-  // three CTAs per SM need three tiles (plus 1 KB reserved each) in the 228 KB
-  const bool three = 3 * (smem + 1024) <= 228 * 1024;
-  if (a.storage == kStorageBF16)
+  if (bf16)
     pick(__nv_bfloat16(), std::integral_constant<int, 2>());
   else if (three)
     pick(0.0f, std::integral_constant<int, 3>());
