@@ -311,10 +311,17 @@ int nrgb_batch_osem_step(void *batch, int step, int iterations, float epsilon, v
  * cameras per L2-resident scratch group for a problem shape (nx, ny, nz,
  * n_cameras); an all-zero shape sets the default for shapes without an entry
  * (none initially: then even groups of at most 48 cameras, at most 2 GiB of
- * scratch each).  niftyrec_gb300.autotune measures candidates and records the
- * fastest. */
+ * scratch each); group 0 removes the entry.  niftyrec_gb300.autotune measures
+ * candidates and records the fastest. */
 int nrgb_set_backproject_group(int nx, int ny, int nz, int ncam, int group);
 int nrgb_get_backproject_group(int nx, int ny, int nz, int ncam);
+/* Tuning table of the fused projector (no counterpart in the reference):
+ * depth slabs per (camera, x-tile) item -- the thread-block cluster size, 2,
+ * 4 or 8 -- for a problem shape; 0 (the initial state) lets the launcher take
+ * the fewest slabs that give four waves of thread blocks.
+ * niftyrec_gb300.autotune measures the candidates and records the fastest. */
+int nrgb_set_project_slabs(int nx, int ny, int nz, int ncam, int slabs);
+int nrgb_get_project_slabs(int nx, int ny, int nz, int ncam);
 
 /* Instrumentation (no counterpart in the reference).  nrgb_launch_count: CUDA
  * kernels this library launched since it was loaded.  nrgb_profile_enable(1)

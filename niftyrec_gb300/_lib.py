@@ -88,6 +88,8 @@ PROTOTYPES = {
     "nrgb_layout_convert": (_I, [_P, _P, _I, _I, _I, _I, _I, _P]),
     "nrgb_set_backproject_group": (_I, [_I, _I, _I, _I, _I]),
     "nrgb_get_backproject_group": (_I, [_I, _I, _I, _I]),
+    "nrgb_set_project_slabs": (_I, [_I, _I, _I, _I, _I]),
+    "nrgb_get_project_slabs": (_I, [_I, _I, _I, _I]),
     "nrgb_last_path": (_I, []),
     "nrgb_launch_count": (ctypes.c_longlong, []),
     "nrgb_profile_enable": (_I, [_I]),

@@ -1030,12 +1030,22 @@ int nrgb_osem_update_device(float* d_activity, const float* d_numerator, const f
 // Tuning table of the fused backprojector: cameras per scratch group for the
 // shape (nx, ny, nz, n_cameras); an all-zero shape sets the default.
 int nrgb_set_backproject_group(int nx, int ny, int nz, int ncam, int group) {
-  if (group < 1 || group > 64) return kErrParameters;
+  if (group < 0 || group > 64) return kErrParameters;
   set_tuned_group(nx, ny, nz, ncam, group);
   return kOk;
 }
 
 int nrgb_get_backproject_group(int nx, int ny, int nz, int ncam) { return tuned_group(nx, ny, nz, ncam); }
+
+// Tuning table of the fused projector: depth slabs (cluster size 2, 4, 8;
+// 0 removes the entry) for the shape (nx, ny, nz, n_cameras).
+int nrgb_set_project_slabs(int nx, int ny, int nz, int ncam, int slabs) {
+  if (slabs != 0 && slabs != 2 && slabs != 4 && slabs != 8) return kErrParameters;
+  set_tuned_project_slabs(nx, ny, nz, ncam, slabs);
+  return kOk;
+}
+
+int nrgb_get_project_slabs(int nx, int ny, int nz, int ncam) { return tuned_project_slabs(nx, ny, nz, ncam); }
 
 // 1 when the last call of this thread ran the fused y-gantry kernels, 2 when
 // it ran the general-orientation path, 0 before any call.

@@ -43,7 +43,28 @@ int tuned_group(int nx, int ny, int nz, int ncam) {
 
 void set_tuned_group(int nx, int ny, int nz, int ncam, int group) {
   std::lock_guard<std::mutex> lk(g_tune_mu);
-  g_tune_group[std::make_tuple(nx, ny, nz, ncam)] = group;
+  if (group > 0)
+    g_tune_group[std::make_tuple(nx, ny, nz, ncam)] = group;
+  else
+    g_tune_group.erase(std::make_tuple(nx, ny, nz, ncam));
+}
+
+namespace {
+std::map<std::tuple<int, int, int, int>, int> g_tune_slabs;
+}  // namespace
+
+int tuned_project_slabs(int nx, int ny, int nz, int ncam) {
+  std::lock_guard<std::mutex> lk(g_tune_mu);
+  auto it = g_tune_slabs.find(std::make_tuple(nx, ny, nz, ncam));
+  return it != g_tune_slabs.end() ? it->second : 0;
+}
+
+void set_tuned_project_slabs(int nx, int ny, int nz, int ncam, int slabs) {
+  std::lock_guard<std::mutex> lk(g_tune_mu);
+  if (slabs > 0)
+    g_tune_slabs[std::make_tuple(nx, ny, nz, ncam)] = slabs;
+  else
+    g_tune_slabs.erase(std::make_tuple(nx, ny, nz, ncam));
 }
 
 int make_problem(int nx, int ny, int nz, const Cameras& cams, const float* psf, const int* psf_size, float bg,
@@ -60,6 +81,7 @@ int make_problem(int nx, int ny, int nz, const Cameras& cams, const float* psf, 
   pb.bg_att = bg_att;
   pb.truncate = truncate;
   pb.group = tuned_group(nx, ny, nz, cams.n);
+  pb.pslabs = tuned_project_slabs(nx, ny, nz, cams.n);
   if (psf) {
     const int kx = psf_size[0], ky = psf_size[1], planes = psf_size[2];
     // The reference separates the PSF assuming kx == ky (emission-lib/_et.cpp:199-213
@@ -204,6 +226,7 @@ int project_device(const Problem& pb, const float* d_act, const float* d_att, fl
     if (d_att && (s = stage_column(pb, d_att, mu_c, cy, pb.nz, st)) != kOk) return s;
     YgArgs a;
     a.storage = pb.storage;
+    a.pslabs = pb.pslabs;
     a.nx = pb.nx;
     a.ny = pb.ny;
     a.nz = pb.nz;

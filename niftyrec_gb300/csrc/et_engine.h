@@ -25,6 +25,7 @@ struct Problem {
   int truncate = 0;
   int back_mode = kBackReference;
   int group = 16;  // cameras per backprojection scratch group (set from the tuning table)
+  int pslabs = 0;  // projector depth slabs (tuning table; 0: the launcher's choice)
   // Storage of the sampled volumes inside the fused kernels, and whether the
   // caller's activity / mu buffers are bfloat16 (nifti order) rather than
   // float32.  bfloat16 inputs imply bfloat16 storage; the general-orientation
@@ -47,6 +48,10 @@ bool use_fused(const Problem& pb);
 // all-zero shape = default for shapes without an entry).
 int tuned_group(int nx, int ny, int nz, int ncam);
 void set_tuned_group(int nx, int ny, int nz, int ncam, int group);
+// Projector depth slabs (cluster size 2, 4 or 8) for a shape; 0 = none
+// recorded (the launcher then chooses).
+int tuned_project_slabs(int nx, int ny, int nz, int ncam);
+void set_tuned_project_slabs(int nx, int ny, int nz, int ncam, int slabs);
 
 // Pinned, double-buffered staging of the per-call parameters (camera
 // matrices, separated PSF): copies from pinned memory stay asynchronous,

@@ -79,6 +79,7 @@ int plan_project(Plan& p, int subset, const float* d_act, float* d_sino, int lay
       act = p.act_c;
     }
     YgArgs a;
+    a.pslabs = tuned_project_slabs(pb.nx, pb.ny, pb.nz, n);  // by the subset's camera count
     a.nx = pb.nx;
     a.ny = pb.ny;
     a.nz = pb.nz;

@@ -75,3 +75,22 @@ def test_psf_stub_like_reference(lib):
     buf = np.zeros(5 * 5 * 3, np.float32)
     assert lib.et_array_make_psf(buf.ctypes.data_as(ctypes.c_void_p), 5, 5, 1, 1, 1, 1, 1, 1, 3) == 0
     assert np.all(buf == 1)
+
+
+def test_tuning_tables(lib):
+    """The host-side tuning tables: set, read back, reject bad values, clear."""
+    shape = (40, 44, 36, 7)
+    assert lib.nrgb_get_project_slabs(*shape) == 0
+    for s in (2, 4, 8):
+        assert lib.nrgb_set_project_slabs(*shape, s) == 0
+        assert lib.nrgb_get_project_slabs(*shape) == s
+    for bad in (1, 3, 16, -2):
+        assert lib.nrgb_set_project_slabs(*shape, bad) == 2
+    assert lib.nrgb_get_project_slabs(*shape) == 8
+    assert lib.nrgb_set_project_slabs(*shape, 0) == 0
+    assert lib.nrgb_get_project_slabs(*shape) == 0
+    g0 = lib.nrgb_get_backproject_group(*shape)
+    assert lib.nrgb_set_backproject_group(*shape, 5) == 0
+    assert lib.nrgb_get_backproject_group(*shape) == 5
+    assert lib.nrgb_set_backproject_group(*shape, 0) == 0
+    assert lib.nrgb_get_backproject_group(*shape) == g0

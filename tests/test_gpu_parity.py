@@ -214,3 +214,25 @@ def test_fisher_grid_golden(golden, o32):
     with pytest.raises(Exception) as e:
         A.fisher_grid(g["act"], g["cameras"], g["psf"], bad, 24, g["mu"])
     assert getattr(e.value, "status", None) == 2
+
+
+@pytest.mark.parametrize("slabs", [2, 4, 8])
+def test_project_slab_counts(o32, slabs):
+    """Every depth-slab count of the projector (cluster size, from the tuning
+    table) gives the oracle's projection; the entry is removed afterwards."""
+    from niftyrec_gb300 import _lib
+
+    L = _lib.load()
+    shape = (40, 36, 44)
+    act = S.ellipsoid_phantom(shape, seed=33)
+    mu = S.mu_map(shape, seed=33)
+    psf = S.gaussian_psf(9, shape[2], 0.5, 0.05)
+    cams = S.cameras_about_y(7, 3.0)
+    key = (shape[2], shape[1], shape[0], 7)
+    assert L.nrgb_set_project_slabs(*key, slabs) == 0
+    try:
+        s = A.project(act, cams, psf, mu)
+        assert A.last_path() == FUSED
+    finally:
+        L.nrgb_set_project_slabs(*key, 0)
+    assert per_plane_rel(s, o32.project(act, cams, psf, mu)) < RTOL
