@@ -322,6 +322,16 @@ int nrgb_get_backproject_group(int nx, int ny, int nz, int ncam);
  * niftyrec_gb300.autotune measures the candidates and records the fastest. */
 int nrgb_set_project_slabs(int nx, int ny, int nz, int ncam, int slabs);
 int nrgb_get_project_slabs(int nx, int ny, int nz, int ncam);
+/* Mirror cameras (no counterpart in the reference).  Two gantry cameras at
+ * opposite angles (difference pi within 1e-6 rad) about the grid centre
+ * sample the same points: the second one's rotated volume is the first one's
+ * mirrored in x and z.  With on = 1 (the default) the fused projector serves
+ * such a pair from one set of bilinear samples (the second camera's sampling
+ * positions are the first one's, mirrored, instead of those of its own float
+ * matrix: a difference below 1e-6 of the projection); 0 computes every camera
+ * from its own matrix, as the reference.  Applies to calls made afterwards. */
+int nrgb_set_mirror_pairs(int on);
+int nrgb_get_mirror_pairs(void);
 
 /* Instrumentation (no counterpart in the reference).  nrgb_launch_count: CUDA
  * kernels this library launched since it was loaded.  nrgb_profile_enable(1)

@@ -90,6 +90,8 @@ PROTOTYPES = {
     "nrgb_get_backproject_group": (_I, [_I, _I, _I, _I]),
     "nrgb_set_project_slabs": (_I, [_I, _I, _I, _I, _I]),
     "nrgb_get_project_slabs": (_I, [_I, _I, _I, _I]),
+    "nrgb_set_mirror_pairs": (_I, [_I]),
+    "nrgb_get_mirror_pairs": (_I, []),
     "nrgb_last_path": (_I, []),
     "nrgb_launch_count": (ctypes.c_longlong, []),
     "nrgb_profile_enable": (_I, [_I]),

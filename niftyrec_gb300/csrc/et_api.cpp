@@ -1047,6 +1047,16 @@ int nrgb_set_project_slabs(int nx, int ny, int nz, int ncam, int slabs) {
 
 int nrgb_get_project_slabs(int nx, int ny, int nz, int ncam) { return tuned_project_slabs(nx, ny, nz, ncam); }
 
+// Mirror cameras: 1 (default) serves a camera at the opposite angle about the
+// grid centre from the same bilinear samples; 0 computes every camera from
+// its own matrix.  Applies to calls made afterwards.
+int nrgb_set_mirror_pairs(int on) {
+  set_mirror_pairs(on);
+  return kOk;
+}
+
+int nrgb_get_mirror_pairs(void) { return mirror_pairs(); }
+
 // 1 when the last call of this thread ran the fused y-gantry kernels, 2 when
 // it ran the general-orientation path, 0 before any call.
 int nrgb_last_path(void) { return g_last_path; }

@@ -3,6 +3,7 @@
 #include "et_engine.h"
 
 #include <algorithm>
+#include <atomic>
 #include <cstring>
 #include <map>
 #include <memory>
@@ -67,6 +68,13 @@ void set_tuned_project_slabs(int nx, int ny, int nz, int ncam, int slabs) {
     g_tune_slabs.erase(std::make_tuple(nx, ny, nz, ncam));
 }
 
+namespace {
+std::atomic<int> g_mirror_pairs{1};
+}  // namespace
+
+void set_mirror_pairs(int on) { g_mirror_pairs.store(on ? 1 : 0); }
+int mirror_pairs() { return g_mirror_pairs.load(); }
+
 int make_problem(int nx, int ny, int nz, const Cameras& cams, const float* psf, const int* psf_size, float bg,
                  float bg_att, int truncate, Problem* out) {
   if (nx <= 0 || ny <= 0 || nz <= 0 || cams.n <= 0) return kErrParameters;
@@ -77,6 +85,7 @@ int make_problem(int nx, int ny, int nz, const Cameras& cams, const float* psf, 
   pb.cams = cams;
   pb.geom = camera_geometry(cams);
   pb.ygantry = is_y_gantry(cams);
+  if (pb.ygantry && mirror_pairs()) pb.units = mirror_units(cams, nx, nz);
   pb.bg = bg;
   pb.bg_att = bg_att;
   pb.truncate = truncate;
@@ -107,18 +116,25 @@ size_t sino_col_n(const Problem& pb) { return static_cast<size_t>(pb.nx) * round
 constexpr size_t kSlack = 8 * 256;
 
 size_t common_bytes(const Problem& pb) {
-  return sizeof(CamGeom) * pb.cams.n + sizeof(float) * pb.psf_sep.size() + kSlack;
+  return sizeof(CamGeom) * pb.cams.n + sizeof(float) * pb.psf_sep.size() + sizeof(int) * pb.units.size() + kSlack;
 }
 
-// Uploads camera matrices and the separated PSF through the pinned staging
-// slot that is not in flight (waiting for its previous copy if needed).
-int upload_common(const Problem& pb, Carver& cv, CamGeom** d_geom, float** d_psf, Staging* stg, cudaStream_t st) {
+// Uploads camera matrices, the separated PSF and the mirror-camera units
+// through the pinned staging slot that is not in flight (waiting for its
+// previous copy if needed).
+int upload_common(const Problem& pb, Carver& cv, CamGeom** d_geom, float** d_psf, Staging* stg, cudaStream_t st,
+                  int2** d_units = nullptr) {
   *d_geom = cv.take<CamGeom>(pb.cams.n);
   *d_psf = nullptr;
   if (!*d_geom) return kErrAllocGpu;
   if (pb.psf_k) {
     *d_psf = cv.take<float>(pb.psf_sep.size());
     if (!*d_psf) return kErrAllocGpu;
+  }
+  const size_t ubytes = d_units ? sizeof(int) * pb.units.size() : 0;
+  if (d_units) {
+    *d_units = nullptr;
+    if (ubytes && !(*d_units = cv.take<int2>(pb.units.size() / 2))) return kErrAllocGpu;
   }
   const size_t gbytes = sizeof(CamGeom) * pb.cams.n;
   const size_t pbytes = sizeof(float) * pb.psf_sep.size();
@@ -129,11 +145,11 @@ int upload_common(const Problem& pb, Carver& cv, CamGeom** d_geom, float** d_psf
   } else if (cudaEventCreateWithFlags(&stg->done[slot], cudaEventDisableTiming) != cudaSuccess) {
     return kErrUnspecified;
   }
-  if (stg->bytes[slot] < gbytes + pbytes) {
+  if (stg->bytes[slot] < gbytes + pbytes + ubytes) {
     if (stg->pinned[slot]) cudaFreeHost(stg->pinned[slot]);
     stg->pinned[slot] = nullptr;
     stg->bytes[slot] = 0;
-    const size_t want = std::max(gbytes + pbytes, static_cast<size_t>(1) << 20);
+    const size_t want = std::max(gbytes + pbytes + ubytes, static_cast<size_t>(1) << 20);
     if (cudaMallocHost(&stg->pinned[slot], want) != cudaSuccess) {
       cudaGetLastError();
       return kErrAllocCpu;
@@ -146,6 +162,11 @@ int upload_common(const Problem& pb, Carver& cv, CamGeom** d_geom, float** d_psf
   if (cudaMemcpyAsync(*d_geom, h, gbytes, cudaMemcpyHostToDevice, st) != cudaSuccess) return kErrTransferGpu;
   if (pbytes && cudaMemcpyAsync(*d_psf, h + gbytes, pbytes, cudaMemcpyHostToDevice, st) != cudaSuccess)
     return kErrTransferGpu;
+  if (ubytes) {
+    std::memcpy(h + gbytes + pbytes, pb.units.data(), ubytes);
+    if (cudaMemcpyAsync(*d_units, h + gbytes + pbytes, ubytes, cudaMemcpyHostToDevice, st) != cudaSuccess)
+      return kErrTransferGpu;
+  }
   cudaEventRecord(stg->done[slot], st);
   return kOk;
 }
@@ -214,7 +235,8 @@ int project_device(const Problem& pb, const float* d_act, const float* d_att, fl
   Carver cv(ws, ws_bytes);
   CamGeom* d_geom;
   float* d_psf;
-  int s = upload_common(pb, cv, &d_geom, &d_psf, stg, st);
+  int2* d_units;
+  int s = upload_common(pb, cv, &d_geom, &d_psf, stg, st, &d_units);
   if (s != kOk) return s;
   if (use_fused(pb) && d_act) {
     float* act_c = cv.take<float>(col_n(pb));
@@ -233,6 +255,8 @@ int project_device(const Problem& pb, const float* d_act, const float* d_att, fl
     a.cy = cy;
     a.ncam = pb.cams.n;
     a.geom = d_geom;
+    a.units = d_units;
+    a.nunits = static_cast<int>(pb.units.size() / 2);
     a.act = act_c;
     a.mu = mu_c;
     a.out = sino_c;

@@ -17,6 +17,7 @@ struct Problem {
   int nx = 0, ny = 0, nz = 0;
   Cameras cams;
   std::vector<CamGeom> geom;
+  std::vector<int> units;  // mirror-camera units of the fused projector (mirror_units), or empty
   bool ygantry = false;
   int psf_k = 0;               // 0: no PSF
   std::vector<float> psf_sep;  // [nz][2k]
@@ -52,6 +53,10 @@ void set_tuned_group(int nx, int ny, int nz, int ncam, int group);
 // recorded (the launcher then chooses).
 int tuned_project_slabs(int nx, int ny, int nz, int ncam);
 void set_tuned_project_slabs(int nx, int ny, int nz, int ncam, int slabs);
+// Whether new problems serve mirror cameras (opposite angles) from shared
+// samples (1, the default) or every camera from its own matrix (0).
+void set_mirror_pairs(int on);
+int mirror_pairs();
 
 // Pinned, double-buffered staging of the per-call parameters (camera
 // matrices, separated PSF): copies from pinned memory stay asynchronous,

@@ -98,6 +98,38 @@ bool is_y_gantry(const Cameras& cams) {
   return true;
 }
 
+std::vector<int> mirror_units(const Cameras& cams, int nx, int nz) {
+  const int n = cams.n;
+  const float cx = static_cast<float>((nx - 1) / 2.0), cz = static_cast<float>((nz - 1) / 2.0);
+  std::vector<int> mate(n, -1);
+  std::vector<char> taken(n, 0);
+  bool any = false;
+  const double two_pi = 2.0 * M_PI;
+  auto centred = [&](int c) { return cams.centers[c] == cx && cams.centers[2 * n + c] == cz; };
+  for (int i = 0; i < n; ++i) {
+    if (taken[i] || !centred(i)) continue;
+    for (int j = i + 1; j < n; ++j) {
+      if (taken[j] || !centred(j)) continue;
+      const double d = static_cast<double>(cams.angles[n + j]) - static_cast<double>(cams.angles[n + i]) - M_PI;
+      const double w = d - two_pi * std::nearbyint(d / two_pi);
+      if (std::fabs(w) <= kMirrorTolerance) {
+        mate[i] = j;
+        taken[i] = taken[j] = 1;
+        any = true;
+        break;
+      }
+    }
+  }
+  std::vector<int> units;
+  if (!any || !is_y_gantry(cams)) return units;
+  for (int i = 0; i < n; ++i) {
+    if (taken[i] && mate[i] < 0) continue;  // the second camera of a pair
+    units.push_back(i);
+    units.push_back(mate[i]);
+  }
+  return units;
+}
+
 template <class T>
 std::vector<T> separate_psf_t(const float* psf, int k, int nplanes) {
   std::vector<T> sep(static_cast<size_t>(2 * k) * nplanes);

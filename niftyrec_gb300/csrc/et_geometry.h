@@ -36,6 +36,15 @@ std::vector<CamGeom64> camera_geometry64(const Cameras& cams);
 // theta_z == 0), so that the resampling matrices are exact rotations about y.
 bool is_y_gantry(const Cameras& cams);
 
+// Mirror pairs of y-gantry cameras on an nx x nz grid: cameras i < j whose
+// angles differ by pi (within kMirrorTolerance radians, modulo 2 pi) and
+// whose centres are both the grid centre ((nx-1)/2, (nz-1)/2) sample the
+// same points (camera j's rotated volume is camera i's mirrored in x and z).
+// Returns units {i, j} and {i, -1} (unpaired cameras) in the order of their
+// first camera, two ints per unit; empty when no pair exists.
+constexpr double kMirrorTolerance = 1e-6;
+std::vector<int> mirror_units(const Cameras& cams, int nx, int nz);
+
 // Separated depth-dependent PSF (emission-lib/_et.cpp:194-215): for plane n,
 // row kernel = central row, column kernel = central column / centre value.
 // Device layout: sep[n*2k + i] = row[i], sep[n*2k + k + i] = col[i], the

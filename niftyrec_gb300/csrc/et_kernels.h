@@ -67,6 +67,11 @@ struct YgArgs {
   int back_mode = kBackReference;
   int storage = kStorageF32;  // type of act and mu
   int pslabs = 0;  // projector depth slabs = cluster size (2, 4, 8; 0: chosen by the launcher)
+  // Projector units (device [nunits]): {camera, mirror camera or -1}; a
+  // mirror camera sits at the opposite angle about the grid centre and is
+  // served from the same samples (float32 storage).  Null: unit u = camera u.
+  const int2* units = nullptr;
+  int nunits = 0;
   // backprojector work space (yg_backproject_workspace bytes); the kernels
   // see it as slab sums [ncam][slabs][nx][cy] then scratch [group][nz][nx][cy]
   float* work = nullptr;

@@ -267,6 +267,10 @@ struct TileShape {
   static constexpr int kTapSlots = kW * kOwn;         // footprint slots per stage (see tap_slot)
   static constexpr size_t kSbBytes = sizeof(float4) * 2 * NS * 32;
   static constexpr size_t kTapBytes = sizeof(Tap) * 2 * kTapSlots;
+  // Projector with a mirror camera: the tile region also holds the three
+  // slab-merge buffers (T, P and the mirror camera's P per output column).
+  static constexpr size_t kSbBytesPair = sizeof(float4) * 32 * (2 * NS > 3 * kTXC ? 2 * NS : 3 * kTXC);
+  __host__ __device__ static constexpr size_t sb_bytes(bool pair) { return pair ? kSbBytesPair : kSbBytes; }
 };
 
 // Footprint slot of sampled column c in the tap buffer: the columns one warp
@@ -277,9 +281,12 @@ __device__ __forceinline__ int tap_slot(int c) {
   return (c % kW) * TileShape<R>::kOwn + c / kW;
 }
 
+// Tile, footprints and the separated PSF of nz planes (twice with a mirror
+// camera: its kernels are the mirrored planes, row kernels reversed).
 template <int R>
-__host__ __device__ constexpr size_t tile_smem_bytes(int nz) {
-  return TileShape<R>::kSbBytes + TileShape<R>::kTapBytes + sizeof(float) * static_cast<size_t>(nz) * 2 * (2 * R + 1);
+__host__ __device__ constexpr size_t tile_smem_bytes(int nz, bool pair = false) {
+  return TileShape<R>::sb_bytes(pair) + TileShape<R>::kTapBytes +
+         sizeof(float) * static_cast<size_t>(nz) * 2 * (2 * R + 1) * (pair ? 2 : 1);
 }
 
 // Row pass from the shared tile: outputs i = 0..kTXW-1 of this warp use tile
@@ -325,44 +332,73 @@ __device__ __forceinline__ bool lane_writes(const YgArgs& a, int yb) { return yb
 // V: storage type of activity and mu (float or bfloat16; bfloat16 sums with
 // Kahan).  Ends with a cluster barrier, after which the shared memory may be
 // reused.
-template <int R, bool PSF, bool ATT, class V>
-__device__ __forceinline__ void project_item(const YgArgs& a, int cam, int x0, unsigned char* smem) {
+//
+// Mirror camera (PAIR, mate >= 0): a camera at the opposite angle (theta + pi)
+// about the grid centre samples the same points: its rotated volume is this
+// camera's mirrored in x and z (column x of depth z is its column nx-1-x of
+// depth nz-1-z).  The CTA then serves both from one set of bilinear samples:
+// the mate's row pass uses the PSF plane nz-1-z with the row kernel reversed,
+// its depth sum runs towards this camera, and its slab partial
+//   q = sum_z v'_z exp(-(S - E_z)) = exp(-S) sum_z v'_z exp(E_z)
+// (S the slab's mu sum, E_z the sum before plane z) is accumulated in the
+// forward walk as sum v' exp(E).  A slab whose mu sum exceeds kMateMaxT (or
+// whose sum overflows) is redone for the mate alone by a descending walk with
+// the direct weights.  The mate's slabs merge in the opposite order.
+constexpr float kMateMaxT = 40.0f;
+
+template <int R, bool PSF, bool ATT, class V, bool PAIR = false>
+__device__ __forceinline__ void project_item(const YgArgs& a, int cam, int mate, int x0, unsigned char* smem) {
   using TS = TileShape<R>;
   constexpr bool KAHAN = StorageTraits<V>::kKahan;
+  static_assert(!(PAIR && KAHAN), "mirror cameras are served by the float32 projector");
   const V* __restrict__ act = reinterpret_cast<const V*>(a.act) + a.row0;
   const V* __restrict__ mu = reinterpret_cast<const V*>(a.mu) + a.row0;
   constexpr int NS = TS::NS;
   constexpr int K = 2 * R + 1;
-  float4* sb = reinterpret_cast<float4*>(smem);                       // [2][NS][32]
-  Tap* taps = reinterpret_cast<Tap*>(smem + TS::kSbBytes);             // [2][kTapSlots]
-  float* s_psf = reinterpret_cast<float*>(smem + TS::kSbBytes + TS::kTapBytes);  // [nz][2K]
+  constexpr size_t kSb = TS::sb_bytes(PAIR);
+  float4* sb = reinterpret_cast<float4*>(smem);                    // [2][NS][32]
+  Tap* taps = reinterpret_cast<Tap*>(smem + kSb);                   // [2][kTapSlots]
+  float* s_psf = reinterpret_cast<float*>(smem + kSb + TS::kTapBytes);  // [nz][2K]
+  float* s_psf_m = s_psf + static_cast<size_t>(a.nz) * 2 * K;       // [nz][2K] (mate)
 
   cg::cluster_group cluster = cg::this_cluster();
   const int slab = static_cast<int>(cluster.block_rank());
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int yb = lane * 4;
   const bool yok = lane_rows_ok(a, yb);
+  const bool paired = PAIR && mate >= 0;  // uniform over the cluster
 
   const int nslabs = static_cast<int>(cluster.num_blocks());  // depth slabs = cluster size (2, 4 or 8)
   const int zper = (a.nz + nslabs - 1) / nslabs;
   const int zbeg = slab * zper, zend = min(a.nz, zbeg + zper);
   if (PSF) {  // this slab's planes only
     for (int i = zbeg * 2 * K + threadIdx.x; i < zend * 2 * K; i += blockDim.x) s_psf[i] = __ldg(a.psf + i);
+    if (paired) {
+      for (int i = zbeg * 2 * K + threadIdx.x; i < zend * 2 * K; i += blockDim.x) {
+        const int z = i / (2 * K), j = i % (2 * K);
+        s_psf_m[i] = __ldg(a.psf + (a.nz - 1 - z) * 2 * K + (j < K ? K - 1 - j : j));
+      }
+    }
   }
   const CamRows cr = cam_rows(a.geom[cam].fwd);
 
   float4 T[kTXW], P[kTXW], cT[kTXW], cP[kTXW];  // c*: Kahan compensations (KAHAN only)
+  float4 Q[PAIR ? kTXW : 1];                    // mate's slab partial
 #pragma unroll
   for (int i = 0; i < kTXW; ++i) {
     T[i] = make_float4(0.f, 0.f, 0.f, 0.f);
     P[i] = make_float4(0.f, 0.f, 0.f, 0.f);
     cT[i] = make_float4(0.f, 0.f, 0.f, 0.f);
     cP[i] = make_float4(0.f, 0.f, 0.f, 0.f);
+    if (PAIR) Q[i] = make_float4(0.f, 0.f, 0.f, 0.f);
   }
   __syncthreads();
 
-  for (int z = zbeg; z < zend; ++z) {
-    const int b = z & 1;
+  // One depth step at plane z into tile buffer b.  MODE 0: this camera (and
+  // the mate's forward form); MODE 1: the mate alone, direct weights (walked
+  // from the slab's far end).
+  auto step = [&](int z, int b, auto mode) {
+    constexpr int MODE = decltype(mode)::value;
     float4* sbuf = sb + b * NS * 32;
     Tap* tb = taps + b * TS::kTapSlots;
     // footprints of the columns this warp samples (c = warp + kW * k)
@@ -371,7 +407,7 @@ __device__ __forceinline__ void project_item(const YgArgs& a, int cam, int x0, u
       if (c < NS) {
         const int xp = x0 - R + c;
         tb[tap_slot<R>(c)] = make_tap(xp, z, cr.m00, cr.m02, cr.m03, cr.m20, cr.m22, cr.m23, a.nx, a.nz, a.cy,
-                         xp >= 0 && xp < a.nx);
+                                      xp >= 0 && xp < a.nx);
       }
     }
     __syncwarp();
@@ -381,6 +417,26 @@ __device__ __forceinline__ void project_item(const YgArgs& a, int cam, int x0, u
       if (c < NS) sbuf[c * 32 + lane] = sample4(act, tb[tap_slot<R>(c)], yb, yok);
     }
     __syncthreads();
+    if (PAIR && paired) {
+      auto emit_m = [&](int i, const float4& v) {
+        if (!ATT) {
+          add4(Q[i], v);
+        } else if (MODE == 0) {  // weight exp(E_z): T holds the sum before plane z
+          fma4(Q[i], v, exp_neg4(make_float4(-T[i].x, -T[i].y, -T[i].z, -T[i].w)));
+        } else {  // T runs from the slab's far end, inclusive
+          add4(T[i], sample4(mu, tb[tap_slot<R>(warp * kTXW + i + R)], yb, yok));
+          fma4(Q[i], v, exp_neg4(T[i]));
+        }
+      };
+      if (PSF) {
+        const float* km = s_psf_m + z * 2 * K;
+        rowpass_from_tile<R>(sbuf, warp * kTXW, emit_m, km, km + K, lane, a.ny);
+      } else {
+#pragma unroll
+        for (int i = 0; i < kTXW; ++i) emit_m(i, sbuf[(warp * kTXW + i) * 32 + lane]);
+      }
+    }
+    if (MODE == 1) return;
     auto emit = [&](int i, const float4& v) {
       if (ATT) {
         const float4 m = sample4(mu, tb[tap_slot<R>(warp * kTXW + i + R)], yb, yok);
@@ -402,19 +458,52 @@ __device__ __forceinline__ void project_item(const YgArgs& a, int cam, int x0, u
 #pragma unroll
       for (int i = 0; i < kTXW; ++i) emit(i, sbuf[(warp * kTXW + i) * 32 + lane]);
     }
+  };
+
+  for (int z = zbeg; z < zend; ++z) step(z, z & 1, std::integral_constant<int, 0>());
+
+  if (PAIR && paired && ATT) {
+    bool redo = false;
+#pragma unroll
+    for (int i = 0; i < kTXW; ++i) {
+      redo |= !(T[i].x <= kMateMaxT && T[i].y <= kMateMaxT && T[i].z <= kMateMaxT && T[i].w <= kMateMaxT);
+      redo |= !(isfinite(Q[i].x) && isfinite(Q[i].y) && isfinite(Q[i].z) && isfinite(Q[i].w));
+    }
+    if (__syncthreads_or(redo)) {  // uniform over the CTA
+#pragma unroll
+      for (int i = 0; i < kTXW; ++i) {
+        Q[i] = make_float4(0.f, 0.f, 0.f, 0.f);
+        T[i] = make_float4(0.f, 0.f, 0.f, 0.f);  // ends at the slab sum again
+      }
+      for (int k = 0; k < zend - zbeg; ++k) step(zend - 1 - k, k & 1, std::integral_constant<int, 1>());
+    } else {
+#pragma unroll
+      for (int i = 0; i < kTXW; ++i) Q[i] = mul4(Q[i], exp_neg4(T[i]));
+    }
   }
 
   // cluster merge of the depth slabs (the shared tile is free after this barrier)
   __syncthreads();
   float4* sT = sb;                // [kTXC][32]
   float4* sP = sb + kTXC * 32;    // [kTXC][32]
+  float4* sQ = sb + 2 * kTXC * 32;  // [kTXC][32] (PAIR)
 #pragma unroll
   for (int i = 0; i < kTXW; ++i) {
     sT[(warp * kTXW + i) * 32 + lane] = depth_value4<KAHAN>(T[i], cT[i]);
     sP[(warp * kTXW + i) * 32 + lane] = depth_value4<KAHAN>(P[i], cP[i]);
+    if (PAIR && paired) sQ[(warp * kTXW + i) * 32 + lane] = Q[i];
   }
   cluster.sync();
   const int per_rank = kTXC / nslabs;  // outputs merged by each CTA of the cluster
+  auto store = [&](int c, int x, float4 Pt) {
+    if (a.truncate) {
+      Pt.x = fmaxf(Pt.x, 0.f);
+      Pt.y = fmaxf(Pt.y, 0.f);
+      Pt.z = fmaxf(Pt.z, 0.f);
+      Pt.w = fmaxf(Pt.w, 0.f);
+    }
+    *reinterpret_cast<float4*>(a.out + (static_cast<size_t>(c) * a.nx + x) * a.cy + a.row0 + yb) = Pt;
+  };
 #pragma unroll
   for (int i = 0; i < kTXW; ++i) {
     const int o = warp * kTXW + i;
@@ -432,29 +521,39 @@ __device__ __forceinline__ void project_item(const YgArgs& a, int cam, int x0, u
         add4(Pt, ps);
       }
     }
-    if (a.truncate) {
-      Pt.x = fmaxf(Pt.x, 0.f);
-      Pt.y = fmaxf(Pt.y, 0.f);
-      Pt.z = fmaxf(Pt.z, 0.f);
-      Pt.w = fmaxf(Pt.w, 0.f);
+    store(cam, x, Pt);
+    if (PAIR && paired) {  // the mate's slabs from the far end: its column nx-1-x
+      Pt = make_float4(0.f, 0.f, 0.f, 0.f);
+      Tt = make_float4(0.f, 0.f, 0.f, 0.f);
+      for (int s = nslabs - 1; s >= 0; --s) {
+        const float4 qs = cluster.map_shared_rank(sQ, s)[o * 32 + lane];
+        if (ATT) {
+          fma4(Pt, exp_neg4(Tt), qs);
+          add4(Tt, cluster.map_shared_rank(sT, s)[o * 32 + lane]);
+        } else {
+          add4(Pt, qs);
+        }
+      }
+      store(mate, a.nx - 1 - x, Pt);
     }
-    *reinterpret_cast<float4*>(a.out + (static_cast<size_t>(cam) * a.nx + x) * a.cy + a.row0 + yb) = Pt;
   }
   cluster.sync();  // keep this CTA's shared memory alive until the others have read it
 }
 
 // One work item per cluster of a.pslabs CTAs (the cluster size is set at
-// launch): blockIdx.x / a.pslabs = (camera, x-tile).  CTAS: CTAs per SM the
-// kernel is compiled for -- 3 (80 registers, more warps to hide the gathers'
-// latency) where three tiles fit in shared memory and the storage is
-// float32, else 2 (128 registers; bfloat16 needs them for its Kahan
-// compensations).
-template <int R, bool PSF, bool ATT, class V, int CTAS>
+// launch): blockIdx.x / a.pslabs = (unit, x-tile); a unit is a camera and,
+// with a.units, its mirror camera.  CTAS: CTAs per SM the kernel is compiled
+// for -- 3 (80 registers, more warps to hide the gathers' latency) where
+// three tiles fit in shared memory and the storage is float32, else 2 (128
+// registers; bfloat16 needs them for its Kahan compensations).
+template <int R, bool PSF, bool ATT, class V, int CTAS, bool PAIR>
 __global__ void __launch_bounds__(32 * kW, CTAS) k_project_yg(const YgArgs a) {
   extern __shared__ __align__(16) unsigned char smem[];
   const int ntile = (a.nx + kTXC - 1) / kTXC;
   const int item = blockIdx.x / a.pslabs;
-  project_item<R, PSF, ATT, V>(a, item / ntile, (item % ntile) * kTXC, smem);
+  const int u = item / ntile;
+  const int2 uc = PAIR ? a.units[u] : make_int2(u, -1);
+  project_item<R, PSF, ATT, V, PAIR>(a, uc.x, uc.y, (item % ntile) * kTXC, smem);
 }
 
 // Persistent projector over a batch of volumes: each cluster takes work items
@@ -491,7 +590,7 @@ __global__ void __cluster_dims__(kSlabsP, 1, 1) __launch_bounds__(32 * kW, 2)
     a.ny = d.win[w][1];
     a.out_lo = d.win[w][2];
     a.out_hi = d.win[w][3];
-    project_item<R, PSF, ATT, float>(a, r / ntile, (r % ntile) * kTXC, smem);
+    project_item<R, PSF, ATT, float>(a, r / ntile, -1, (r % ntile) * kTXC, smem);
   }
 }
 
@@ -811,15 +910,19 @@ int launch_project_R(const YgArgs& a_in, cudaStream_t st) {
   YgArgs a = a_in;
   const int ntile = (a.nx + kTXC - 1) / kTXC;
   const bool psf = a.psf != nullptr;
-  const size_t smem = tile_smem_bytes<R>(psf ? a.nz : 0);
+  const bool bf16 = a.storage == kStorageBF16;
+  // mirror cameras are served by the float32 kernels only
+  const bool pair = a.units != nullptr && a.nunits > 0 && !bf16;
+  const int nunits = pair ? a.nunits : a.ncam;
+  const size_t smem = tile_smem_bytes<R>(psf ? a.nz : 0, pair);
   // three CTAs per SM need three tiles (plus 1 KB reserved each) in the 228 KB
   const bool three = 3 * (smem + 1024) <= 228 * 1024;
-  const bool bf16 = a.storage == kStorageBF16;
-  if (a.pslabs != 2 && a.pslabs != 4 && a.pslabs != 8) a.pslabs = project_slabs(a.ncam * ntile, three && !bf16 ? 3 : 2);
+  if (a.pslabs != 2 && a.pslabs != 4 && a.pslabs != 8)
+    a.pslabs = project_slabs(nunits * ntile, three && !bf16 && !pair ? 3 : 2);
   auto go = [&](auto k) {
     cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
     cudaLaunchConfig_t cfg = {};
-    cfg.gridDim = dim3(a.ncam * ntile * a.pslabs);
+    cfg.gridDim = dim3(nunits * ntile * a.pslabs);
     cfg.blockDim = dim3(32 * kW);
     cfg.dynamicSmemBytes = smem;
     cfg.stream = st;
@@ -833,23 +936,29 @@ int launch_project_R(const YgArgs& a_in, cudaStream_t st) {
     NRGB_LAUNCH_SCOPE("k_project_yg", st);
     cudaLaunchKernelEx(&cfg, k, a);
   };
-  auto pick = [&](auto v, auto ctas) {
+  auto pick = [&](auto v, auto ctas, auto paired) {
     using V = decltype(v);
     constexpr int C = decltype(ctas)::value;
+    constexpr bool P = decltype(paired)::value;
     if (psf) {
-      if (a.mu) go(k_project_yg<R, true, true, V, C>);
-      else go(k_project_yg<R, true, false, V, C>);
+      if (a.mu) go(k_project_yg<R, true, true, V, C, P>);
+      else go(k_project_yg<R, true, false, V, C, P>);
     } else {
-      if (a.mu) go(k_project_yg<0, false, true, V, C>);
-      else go(k_project_yg<0, false, false, V, C>);
+      if (a.mu) go(k_project_yg<0, false, true, V, C, P>);
+      else go(k_project_yg<0, false, false, V, C, P>);
     }
   };
+  using Off = std::false_type;
+  using On = std::true_type;
+  // the mirror-camera item needs the 128-register budget of two CTAs per SM
   if (bf16)
-    pick(__nv_bfloat16(), std::integral_constant<int, 2>());
+    pick(__nv_bfloat16(), std::integral_constant<int, 2>(), Off());
+  else if (pair)
+    pick(0.0f, std::integral_constant<int, 2>(), On());
   else if (three)
-    pick(0.0f, std::integral_constant<int, 3>());
+    pick(0.0f, std::integral_constant<int, 3>(), Off());
   else
-    pick(0.0f, std::integral_constant<int, 2>());
+    pick(0.0f, std::integral_constant<int, 2>(), Off());
   return cudaGetLastError() == cudaSuccess ? kOk : kErrKernel;
 }
 

@@ -33,11 +33,16 @@ def main(argv=None):
     ap.add_argument("--bf16", action="store_true", help="activity and mu stored in bfloat16")
     ap.add_argument("--slope", type=float, default=0.02, help="PSF sigma = 0.5 + slope * depth")
     ap.add_argument("--group", type=int, default=0, help="backprojector cameras per scratch group (0: tuned)")
+    ap.add_argument("--slabs", type=int, default=0, help="projector depth slabs 2/4/8 (0: tuned)")
+    ap.add_argument("--no-mirror", action="store_true", help="every camera from its own matrix")
     a = ap.parse_args(argv)
 
     L = _lib.load()
     if a.group:
         L.nrgb_set_backproject_group(a.n, a.n, a.n, a.ncam, a.group)
+    if a.slabs:
+        L.nrgb_set_project_slabs(a.n, a.n, a.n, a.ncam, a.slabs)
+    L.nrgb_set_mirror_pairs(0 if a.no_mirror else 1)
     n = a.n
     act = S.ellipsoid_phantom((n, n, n), seed=0)
     mu = S.mu_map((n, n, n), seed=0)
@@ -78,7 +83,8 @@ def main(argv=None):
         run()
     ev[1].record(stream)
     torch.cuda.synchronize()
-    print(f"{a.op} n={n} ncam={a.ncam} psf={a.psf} att={not a.no_att} bf16={a.bf16}: "
+    print(f"{a.op} n={n} ncam={a.ncam} psf={a.psf} att={not a.no_att} bf16={a.bf16} slabs={a.slabs} "
+          f"mirror={not a.no_mirror}: "
           f"{ev[0].elapsed_time(ev[1]) / a.reps:.3f} ms per repetition")
     return 0
 

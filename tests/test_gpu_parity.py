@@ -236,3 +236,39 @@ def test_project_slab_counts(o32, slabs):
     finally:
         L.nrgb_set_project_slabs(*key, 0)
     assert per_plane_rel(s, o32.project(act, cams, psf, mu)) < RTOL
+
+
+@pytest.mark.parametrize("shape,k,att_scale,angles", [
+    ((40, 36, 44), 9, 1.0, None),            # 12 cameras: six mirror pairs
+    ((40, 36, 44), 9, 400.0, None),          # slab mu sums above the mirror form's bound
+    ((24, 150, 24), 5, 1.0, [0, 33, 180, 213, 90, 17]),  # row windows, pairs and singles
+    ((28, 20, 32), 0, 1.0, None),            # no PSF
+])
+def test_mirror_cameras(o32, shape, k, att_scale, angles):
+    """Cameras at opposite angles served from shared samples (the default)
+    match the oracle and the per-camera computation."""
+    from niftyrec_gb300 import _lib
+
+    L = _lib.load()
+    act = S.ellipsoid_phantom(shape, seed=12)
+    mu = (S.mu_map(shape, seed=12) * att_scale).astype(np.float32)
+    psf = S.gaussian_psf(k, shape[2], 0.5, 0.05) if k else None
+    if angles is None:
+        cams = S.cameras_about_y(12, 7.0)
+    else:
+        cams = np.zeros((3, len(angles)), np.float32)
+        cams[1] = np.deg2rad(np.asarray(angles, np.float64)).astype(np.float32)
+    assert L.nrgb_get_mirror_pairs() == 1
+    s = A.project(act, cams, psf, mu)
+    assert A.last_path() == FUSED
+    so = o32.project(act, cams, psf, mu)
+    assert per_plane_rel(s, so) < RTOL
+    L.nrgb_set_mirror_pairs(0)
+    try:
+        s0 = A.project(act, cams, psf, mu)
+    finally:
+        L.nrgb_set_mirror_pairs(1)
+    assert per_plane_rel(s0, so) < RTOL
+    assert per_plane_rel(s, s0) < RTOL
+    for m in (None, mu):  # without attenuation too
+        assert per_plane_rel(A.project(act, cams, psf, m), o32.project(act, cams, psf, m)) < RTOL
