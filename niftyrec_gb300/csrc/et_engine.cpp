@@ -293,7 +293,8 @@ int backproject_device(const Problem& pb, const float* d_sino, const float* d_at
   Carver cv(ws, ws_bytes);
   CamGeom* d_geom;
   float* d_psf;
-  int s = upload_common(pb, cv, &d_geom, &d_psf, stg, st);
+  int2* d_units;
+  int s = upload_common(pb, cv, &d_geom, &d_psf, stg, st, &d_units);
   if (s != kOk) return s;
   if (use_fused(pb)) {
     float* sino_c = cv.take<float>(sino_col_n(pb));
@@ -313,6 +314,8 @@ int backproject_device(const Problem& pb, const float* d_sino, const float* d_at
     a.cy = cy;
     a.ncam = pb.cams.n;
     a.geom = d_geom;
+    a.units = d_units;
+    a.nunits = static_cast<int>(pb.units.size() / 2);
     a.mu = mu_c;
     a.sino = sino_c;
     a.out = out_c;

@@ -67,13 +67,14 @@ struct YgArgs {
   int back_mode = kBackReference;
   int storage = kStorageF32;  // type of act and mu
   int pslabs = 0;  // projector depth slabs = cluster size (2, 4, 8; 0: chosen by the launcher)
-  // Projector units (device [nunits]): {camera, mirror camera or -1}; a
-  // mirror camera sits at the opposite angle about the grid centre and is
-  // served from the same samples (float32 storage).  Null: unit u = camera u.
+  // Units (device [nunits]): {camera, mirror camera or -1}; a mirror camera
+  // sits at the opposite angle about the grid centre and is served from the
+  // same samples by the projector and the reference-mode backprojector
+  // (float32 storage).  Null: unit u = camera u.
   const int2* units = nullptr;
   int nunits = 0;
   // backprojector work space (yg_backproject_workspace bytes); the kernels
-  // see it as slab sums [ncam][slabs][nx][cy] then scratch [group][nz][nx][cy]
+  // see it as carries [ncam][slots][nx][cy] then scratch [group][nz][nx][cy]
   float* work = nullptr;
   float* slab_T = nullptr;
   float* temp = nullptr;
@@ -82,15 +83,16 @@ struct YgArgs {
   // slots; 0: both on the caller's stream with one slot (creates no stream
   // or event).
   int pipelined = 1;
-  // Non-null: transmission carries [ncam][slabs][nx][cy] computed beforehand
+  // Non-null: transmission carries [ncam][slots][nx][cy] computed beforehand
   // (yg_mu_carry) for exactly these cameras; the backprojector then skips
   // that pass and the work space holds only the scratch slot(s).
   const float* carry = nullptr;
 };
-// Slab count of the backprojector's transmission carries.
+// Carry slots per camera of the backprojector's transmission carries (the
+// exclusive prefix of every depth slab, then the column total).
 int yg_carry_slabs();
-// Transmission carries of the rotated mu for a.ncam cameras into out
-// ([ncam][slabs][nx][cy]).
+// Transmission carries of the rotated mu for a.ncam cameras (a.nunits units
+// with a.units) into out ([ncam or nunits][slots][nx][cy]).
 int yg_mu_carry(const YgArgs& a, float* out, cudaStream_t st);
 // True when the fused kernels support this grid / PSF size.
 bool yg_supported(int nx, int ny, int nz, int psf_k);

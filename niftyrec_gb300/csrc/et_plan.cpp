@@ -36,7 +36,7 @@ struct Plan {
   CamGeom* geom_b = nullptr;
   float* psf = nullptr;
   float* mu = nullptr;     // column layout (fused) or nifti copy (general)
-  float* carry = nullptr;  // [ncam][slabs][nx][cy] (fused with attenuation)
+  float* carry = nullptr;  // [ncam][slots][nx][cy] (fused with attenuation)
   float* act_c = nullptr;  // column staging for nifti-layout calls (fused)
   float* sino_c = nullptr;
   float* out_c = nullptr;

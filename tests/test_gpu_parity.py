@@ -239,14 +239,16 @@ def test_project_slab_counts(o32, slabs):
 
 
 @pytest.mark.parametrize("shape,k,att_scale,angles", [
-    ((40, 36, 44), 9, 1.0, None),            # 12 cameras: six mirror pairs
-    ((40, 36, 44), 9, 400.0, None),          # slab mu sums above the mirror form's bound
+    ((40, 36, 40), 9, 1.0, None),            # 12 cameras: six mirror pairs
+    ((40, 36, 40), 9, 400.0, None),          # slab mu sums above the mirror projector's bound
     ((24, 150, 24), 5, 1.0, [0, 33, 180, 213, 90, 17]),  # row windows, pairs and singles
-    ((28, 20, 32), 0, 1.0, None),            # no PSF
+    ((28, 20, 32), 0, 1.0, None),            # no PSF; nz != nx: backprojection centres unpaired
+    ((36, 24, 44), 7, 1.0, None),            # nz != nx
 ])
 def test_mirror_cameras(o32, shape, k, att_scale, angles):
     """Cameras at opposite angles served from shared samples (the default)
-    match the oracle and the per-camera computation."""
+    match the oracle and the per-camera computation, in projection and in
+    reference-mode backprojection."""
     from niftyrec_gb300 import _lib
 
     L = _lib.load()
@@ -272,3 +274,15 @@ def test_mirror_cameras(o32, shape, k, att_scale, angles):
     assert per_plane_rel(s, s0) < RTOL
     for m in (None, mu):  # without attenuation too
         assert per_plane_rel(A.project(act, cams, psf, m), o32.project(act, cams, psf, m)) < RTOL
+    nz = shape[0]
+    for m in (mu, None):
+        b = A.backproject(so, cams, psf, m, nz=nz)
+        assert A.last_path() == FUSED
+        bo = o32.backproject(so, cams, psf, m, nz=nz)
+        assert rel_l2(b, bo) < RTOL
+        L.nrgb_set_mirror_pairs(0)
+        try:
+            b0 = A.backproject(so, cams, psf, m, nz=nz)
+        finally:
+            L.nrgb_set_mirror_pairs(1)
+        assert rel_l2(b, b0) < RTOL
