@@ -55,7 +55,7 @@ def algorithmic_bytes(kernel: str, launches: int, ncam_total: int) -> float:
     """Algorithmic bytes of all launches of one kernel within the timed region."""
     if kernel == "k_project_yg":
         return ncam_total * P_ANGLE
-    if kernel == "k_spread_yg":  # reads mu and the projection plane per angle
+    if kernel in ("k_spread_yg", "k_spread_pair_yg"):  # reads mu and the projection plane per angle
         return ncam_total * (N ** 3 * 4 + N ** 2 * 4)
     if kernel == "k_gather_yg":  # accumulator read-modify-write per angle
         return ncam_total * (N ** 3 * 8)

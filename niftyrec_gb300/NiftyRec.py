@@ -58,7 +58,7 @@ def et_project(activity, cameras, psf=None, attenuation=None, gpu=1, background=
         t_size, t_p = _size(attenuation.shape)
     else:
         t_size, t_p = _size([0, 0, 0])
-    projection = np.zeros([activity.shape[0], activity.shape[1], cams_t.shape[0]], dtype=np.float32)
+    projection = np.empty([activity.shape[0], activity.shape[1], cams_t.shape[0]], dtype=np.float32)
     s_size, s_p = _size(projection.shape)
     status = L.et_array_project(_pf(activity), a_p, _pf(projection), s_p, cameras.ctypes.data_as(P(c_float)), c_p,
                                 _pf(psf), p_p, _pf(attenuation), t_p, float(background),
@@ -85,7 +85,7 @@ def et_backproject(projections, cameras, psf=None, attenuation=None, gpu=1, back
         t_size, t_p = _size(attenuation.shape)
     else:
         t_size, t_p = _size([0, 0, 0])
-    bk = np.zeros([projections.shape[0], projections.shape[1], projections.shape[0]], dtype=np.float32)
+    bk = np.empty([projections.shape[0], projections.shape[1], projections.shape[0]], dtype=np.float32)
     b_size, b_p = _size(bk.shape)
     status = L.et_array_backproject(_pf(projections), s_p, _pf(bk), b_p, cameras.ctypes.data_as(P(c_float)), c_p,
                                     _pf(psf), p_p, _pf(attenuation), t_p, float(background),

@@ -51,7 +51,7 @@ def project(activity, cameras, psf=None, attenuation=None, background=0.0, backg
     ref = act if act is not None else att
     nz, ny, nx = ref.shape
     cs = _cam_size(cams)
-    sino = np.zeros((cs[0], ny, nx), np.float32)
+    sino = np.empty((cs[0], ny, nx), np.float32)  # every element is written
     asz = _ints([nx, ny, nz] if act is not None else [0, 0, 0])
     tsz = _ints([nx, ny, nz] if att is not None else [0, 0, 0])
     psz = _ints(psf.shape[::-1] if psf is not None else [0, 0, 0])
@@ -133,7 +133,7 @@ def backproject(sinogram, cameras, psf=None, attenuation=None, background=0.0, b
     sino, att, psf, cams = _f32(sinogram), _f32(attenuation), _f32(psf), _f32(cameras)
     ncam, ny, nx = sino.shape
     nz = nx if nz is None else nz
-    out = np.zeros((nz, ny, nx), np.float32)
+    out = np.empty((nz, ny, nx), np.float32)  # every element is written
     cs = _cam_size(cams)
     tsz = _ints([nx, ny, nz] if att is not None else [0, 0, 0])
     psz = _ints(psf.shape[::-1] if psf is not None else [0, 0, 0])
@@ -153,7 +153,7 @@ def gradient_attenuation(sinogram, activity, attenuation, cameras, psf=None, bac
     L = load()
     sino, act, att, psf, cams = _f32(sinogram), _f32(activity), _f32(attenuation), _f32(psf), _f32(cameras)
     nz, ny, nx = act.shape
-    out = np.zeros_like(act)
+    out = np.empty_like(act)  # every element is written
     cs = _cam_size(cams)
     psz = _ints(psf.shape[::-1] if psf is not None else [0, 0, 0])
     vs = _ints([nx, ny, nz])
