@@ -91,8 +91,8 @@ struct YgArgs {
 // Carry slots per camera of the backprojector's transmission carries (the
 // exclusive prefix of every depth slab, then the column total).
 int yg_carry_slabs();
-// Transmission carries of the rotated mu for a.ncam cameras (a.nunits units
-// with a.units) into out ([ncam or nunits][slots][nx][cy]).
+// Transmission carries of the rotated mu for a.ncam cameras into out
+// ([ncam][slots][nx][cy]); with a.units only the units' first cameras.
 int yg_mu_carry(const YgArgs& a, float* out, cudaStream_t st);
 // True when the fused kernels support this grid / PSF size.
 bool yg_supported(int nx, int ny, int nz, int psf_k);

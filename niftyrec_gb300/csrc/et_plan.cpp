@@ -49,6 +49,12 @@ struct Plan {
   float* sens = nullptr;  // [n_subsets][volume]
   float* prior_grad = nullptr;  // MRF prior gradient (one volume)
   size_t vol_elems = 0, plane_elems = 0;  // per layout of the OSEM buffers
+  // mirror-camera units of every subset (index n_subsets: all cameras), camera
+  // indexes relative to the subset's first camera; projector and backprojector
+  // geometry each
+  int2* units_p = nullptr;
+  int2* units_b = nullptr;
+  std::vector<int> uoff_p, ucnt_p, uoff_b, ucnt_b;
 };
 
 size_t al(size_t b) { return (b + 255) / 256 * 256; }
@@ -63,6 +69,15 @@ void range(const Plan& p, int subset, int* b, int* e) {
     *b = p.sub_begin[subset];
     *e = p.sub_begin[subset + 1];
   }
+}
+
+// Units of a subset (-1: all cameras) or null.
+void subset_units(const Plan& p, int subset, bool back, YgArgs* a) {
+  const int i = subset < 0 ? p.n_subsets : subset;
+  const std::vector<int>& cnt = back ? p.ucnt_b : p.ucnt_p;
+  if (cnt.empty() || cnt[i] == 0) return;
+  a->units = (back ? p.units_b : p.units_p) + (back ? p.uoff_b : p.uoff_p)[i];
+  a->nunits = cnt[i];
 }
 
 int plan_project(Plan& p, int subset, const float* d_act, float* d_sino, int layout, int truncate, cudaStream_t st) {
@@ -86,6 +101,7 @@ int plan_project(Plan& p, int subset, const float* d_act, float* d_sino, int lay
     a.cy = p.cy;
     a.ncam = n;
     a.geom = p.geom_p + b;
+    subset_units(p, subset, false, &a);
     a.act = act;
     a.mu = p.has_att ? p.mu : nullptr;
     a.out = layout == kLayoutNifti ? p.sino_c : d_sino;
@@ -142,6 +158,7 @@ int plan_backproject(Plan& p, int subset, const float* d_sino, float* d_out, int
     a.cy = p.cy;
     a.ncam = n;
     a.geom = p.geom_b + b;
+    subset_units(p, subset, true, &a);
     a.mu = p.has_att ? p.mu : nullptr;
     a.sino = sino;
     a.out = out;
@@ -246,11 +263,39 @@ int nrgb_plan_create(void** out_plan, const int* size, const float* cameras, con
   p->order = order;
   int max_sub = 0;
   for (int i = 0; i < n_subsets; ++i) max_sub = std::max(max_sub, begin[i + 1] - begin[i]);
+  // mirror units per subset and for all cameras (fused path, mirror pairs on)
+  std::vector<int> hu_p, hu_b;
+  if (p->fused && mirror_pairs()) {
+    auto units_of = [&](const Cameras& all, std::vector<int>& host, std::vector<int>& off, std::vector<int>& cnt) {
+      off.assign(n_subsets + 1, 0);
+      cnt.assign(n_subsets + 1, 0);
+      for (int i = 0; i <= n_subsets; ++i) {
+        const int b = i < n_subsets ? begin[i] : 0, e = i < n_subsets ? begin[i + 1] : ncam;
+        if (e <= b) continue;
+        Cameras sub;
+        sub.n = e - b;
+        sub.angles.resize(3 * static_cast<size_t>(sub.n));
+        sub.centers.resize(3 * static_cast<size_t>(sub.n));
+        for (int a = 0; a < 3; ++a)
+          for (int c = 0; c < sub.n; ++c) {
+            sub.angles[a * sub.n + c] = all.angles[a * ncam + b + c];
+            sub.centers[a * sub.n + c] = all.centers[a * ncam + b + c];
+          }
+        const std::vector<int> u = mirror_units(sub, nx, nz);
+        off[i] = static_cast<int>(host.size() / 2);
+        cnt[i] = static_cast<int>(u.size() / 2);
+        host.insert(host.end(), u.begin(), u.end());
+      }
+    };
+    units_of(p->proj.cams, hu_p, p->uoff_p, p->ucnt_p);
+    units_of(p->back.cams, hu_b, p->uoff_b, p->ucnt_b);
+  }
 
   const size_t nv = static_cast<size_t>(nx) * ny * nz;
   const size_t ncv = static_cast<size_t>(nx) * p->cy * nz;
   const size_t nsc = static_cast<size_t>(nx) * p->cy * ncam;
-  size_t bytes = al(sizeof(CamGeom) * ncam) * 2 + al(sizeof(float) * p->proj.psf_sep.size());
+  size_t bytes = al(sizeof(CamGeom) * ncam) * 2 + al(sizeof(float) * p->proj.psf_sep.size()) +
+                 al(sizeof(int) * hu_p.size()) + al(sizeof(int) * hu_b.size());
   if (p->fused) {
     bytes += al(sizeof(float) * ncv) * (p->has_att ? 4 : 3) + al(sizeof(float) * nsc);
     if (p->has_att) bytes += al(sizeof(float) * static_cast<size_t>(ncam) * yg_carry_slabs() * nx * p->cy);
@@ -277,6 +322,16 @@ int nrgb_plan_create(void** out_plan, const int* size, const float* cameras, con
   if (p->psf)
     cudaMemcpyAsync(p->psf, p->proj.psf_sep.data(), sizeof(float) * p->proj.psf_sep.size(), cudaMemcpyHostToDevice,
                     st);
+  // the host vectors live until the copies have consumed them: pageable
+  // copies return after staging the source
+  if (!hu_p.empty()) {
+    p->units_p = cv.take<int2>(hu_p.size() / 2);
+    cudaMemcpyAsync(p->units_p, hu_p.data(), sizeof(int) * hu_p.size(), cudaMemcpyHostToDevice, st);
+  }
+  if (!hu_b.empty()) {
+    p->units_b = cv.take<int2>(hu_b.size() / 2);
+    cudaMemcpyAsync(p->units_b, hu_b.data(), sizeof(int) * hu_b.size(), cudaMemcpyHostToDevice, st);
+  }
   if (p->fused) {
     if (p->has_att) p->mu = cv.take<float>(ncv);
     p->act_c = cv.take<float>(ncv);

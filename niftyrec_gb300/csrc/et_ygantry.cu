@@ -596,10 +596,11 @@ __global__ void __cluster_dims__(kSlabsP, 1, 1) __launch_bounds__(32 * kW, 2)
 }
 
 // ------------------------------------------------ backprojector: slab carry
-// carry[u][s][x][y] (s < kSlabsB) = sum of the rotated mu over the depth
+// carry[c][s][x][y] (s < kSlabsB) = sum of the rotated mu over the depth
 // slabs before s (exclusive prefix): the transmission a depth slab starts
-// from; carry[u][kSlabsB][x][y] = the whole column's sum.  u is the camera,
-// or with a.units the unit (its first camera's frame).
+// from; carry[c][kSlabsB][x][y] = the whole column's sum.  One block row per
+// camera c, or with a.units per unit (its first camera c; a mirror camera's
+// transmissions are c's read from the other end).
 template <class V>
 __global__ void __launch_bounds__(32 * kSlabsB) k_mu_carry_yg(const YgArgs a) {
   constexpr int C = kCarryCols;
@@ -643,7 +644,7 @@ __global__ void __launch_bounds__(32 * kSlabsB) k_mu_carry_yg(const YgArgs a) {
     if (x >= a.nx) continue;
     float4 pre = make_float4(0.f, 0.f, 0.f, 0.f);
     for (int s = 0; s < warp; ++s) add4(pre, s_sum[s][i][lane]);
-    float* dst = a.slab_T + ((static_cast<size_t>(unit) * kCarrySlots + warp) * a.nx + x) * a.cy + a.row0 + yb;
+    float* dst = a.slab_T + ((static_cast<size_t>(cam) * kCarrySlots + warp) * a.nx + x) * a.cy + a.row0 + yb;
     *reinterpret_cast<float4*>(dst) = pre;
     if (warp == kSlabsB - 1) {  // the column total, one slot further
       add4(pre, s_sum[warp][i][lane]);
@@ -842,7 +843,7 @@ __global__ void __launch_bounds__(32 * kW, 2) k_spread_pair_yg(const YgArgs a, i
     Tr[k] = make_float4(0.f, 0.f, 0.f, 0.f);
     const int xp = x0 - R + warp + kW * k;
     if (ATT && warp + kW * k < NS && xp >= 0 && xp < a.nx && yok) {
-      const float* cp = a.slab_T + ((static_cast<size_t>(unit) * kCarrySlots + slab) * a.nx + xp) * a.cy + a.row0 + yb;
+      const float* cp = a.slab_T + ((static_cast<size_t>(cam) * kCarrySlots + slab) * a.nx + xp) * a.cy + a.row0 + yb;
       Tc[k] = ldg4(cp);
       if (paired) {
         const float4 tot = ldg4(cp + static_cast<size_t>(kSlabsB - slab) * a.nx * a.cy);
@@ -1397,9 +1398,8 @@ Pipe* pipe_for_current_device() {
 int yg_backproject(const YgArgs& a_in, cudaStream_t st) {
   YgArgs a = a_in;
   const int R = a.psf ? (a.psf_k - 1) / 2 : 0;
-  // mirror units: reference mode, float32 mu, carries computed here
-  const bool pair = a.units && a.nunits > 0 && a.back_mode == kBackReference && a.storage != kStorageBF16 &&
-                    !a.carry;
+  // mirror units: reference mode, float32 mu
+  const bool pair = a.units && a.nunits > 0 && a.back_mode == kBackReference && a.storage != kStorageBF16;
   if (!pair) {
     a.units = nullptr;
     a.nunits = 0;
@@ -1417,7 +1417,7 @@ int yg_backproject(const YgArgs& a_in, cudaStream_t st) {
     slot0 = a.work;
   } else {
     a.slab_T = a.work;
-    slot0 = a.work + static_cast<size_t>(nunits) * kCarrySlots * a.nx * a.cy;
+    slot0 = a.work + static_cast<size_t>(a.ncam) * kCarrySlots * a.nx * a.cy;
     int s = yg_mu_carry(a, a.slab_T, st);
     if (s != kOk) return s;
   }
