@@ -316,6 +316,39 @@ __device__ __forceinline__ void rowpass_from_tile(const float4* __restrict__ sbu
   }
 }
 
+// Row passes of two cameras over the same tile (a camera and its mirror
+// camera): each tile column is read once and feeds both sliding windows;
+// output i of camera b is emitted before output i of camera a.
+template <int R, class EmitA, class EmitB>
+__device__ __forceinline__ void rowpass2_from_tile(const float4* __restrict__ sbuf, int base, EmitA emit_a,
+                                                   const float* kra, const float* kca, EmitB emit_b,
+                                                   const float* krb, const float* kcb, int lane, int ny) {
+  constexpr int NJ = kTXW + 2 * R;
+  float4 ua[kTXW], ub[kTXW];
+#pragma unroll
+  for (int q = 0; q < kTXW; ++q) {
+    ua[q] = make_float4(0.f, 0.f, 0.f, 0.f);
+    ub[q] = make_float4(0.f, 0.f, 0.f, 0.f);
+  }
+#pragma unroll
+  for (int j = 0; j < NJ; ++j) {
+    const float4 r = sbuf[(base + j) * 32 + lane];
+#pragma unroll
+    for (int d = 0; d <= 2 * R; ++d) {
+      const int i = j - d;
+      if (i >= 0 && i < kTXW) {
+        axpy4(ua[i], kra[2 * R - d], r);
+        axpy4(ub[i], krb[2 * R - d], r);
+      }
+    }
+    const int i = j - 2 * R;
+    if (i >= 0 && i < kTXW) {
+      emit_b(i, mask_rows(yconv4<R>(ub[i], kcb, lane), 4 * lane, ny));
+      emit_a(i, mask_rows(yconv4<R>(ua[i], kca, lane), 4 * lane, ny));
+    }
+  }
+}
+
 // ---------------------------------------------------------------- projector
 // Row windows: a column holds cy >= ny rows, the kernels see one window of at
 // most 128 rows at a time: rows [row0, row0 + ny) of the columns (row0 a
@@ -418,17 +451,17 @@ __device__ __forceinline__ void project_item(const YgArgs& a, int cam, int mate,
       if (c < NS) sbuf[c * 32 + lane] = sample4(act, tb[tap_slot<R>(c)], yb, yok);
     }
     __syncthreads();
-    if (PAIR && paired) {
-      auto emit_m = [&](int i, const float4& v) {
-        if (!ATT) {
-          add4(Q[i], v);
-        } else if (MODE == 0) {  // weight exp(E_z): T holds the sum before plane z
-          fma4(Q[i], v, exp_neg4(make_float4(-T[i].x, -T[i].y, -T[i].z, -T[i].w)));
-        } else {  // T runs from the slab's far end, inclusive
-          add4(T[i], sample4(mu, tb[tap_slot<R>(warp * kTXW + i + R)], yb, yok));
-          fma4(Q[i], v, exp_neg4(T[i]));
-        }
-      };
+    auto emit_m = [&](int i, const float4& v) {
+      if (!ATT) {
+        add4(Q[i], v);
+      } else if (MODE == 0) {  // weight exp(E_z): T holds the sum before plane z
+        fma4(Q[i], v, exp_neg4(make_float4(-T[i].x, -T[i].y, -T[i].z, -T[i].w)));
+      } else {  // T runs from the slab's far end, inclusive
+        add4(T[i], sample4(mu, tb[tap_slot<R>(warp * kTXW + i + R)], yb, yok));
+        fma4(Q[i], v, exp_neg4(T[i]));
+      }
+    };
+    if (MODE == 1) {
       if (PSF) {
         const float* km = s_psf_m + z * 2 * K;
         rowpass_from_tile<R>(sbuf, warp * kTXW, emit_m, km, km + K, lane, a.ny);
@@ -436,8 +469,8 @@ __device__ __forceinline__ void project_item(const YgArgs& a, int cam, int mate,
 #pragma unroll
         for (int i = 0; i < kTXW; ++i) emit_m(i, sbuf[(warp * kTXW + i) * 32 + lane]);
       }
+      return;
     }
-    if (MODE == 1) return;
     auto emit = [&](int i, const float4& v) {
       if (ATT) {
         const float4 m = sample4(mu, tb[tap_slot<R>(warp * kTXW + i + R)], yb, yok);
@@ -454,10 +487,19 @@ __device__ __forceinline__ void project_item(const YgArgs& a, int cam, int mate,
     };
     if (PSF) {
       const float* kr = s_psf + z * 2 * K;
-      rowpass_from_tile<R>(sbuf, warp * kTXW, emit, kr, kr + K, lane, a.ny);
+      if (PAIR && paired) {
+        const float* km = s_psf_m + z * 2 * K;
+        rowpass2_from_tile<R>(sbuf, warp * kTXW, emit, kr, kr + K, emit_m, km, km + K, lane, a.ny);
+      } else {
+        rowpass_from_tile<R>(sbuf, warp * kTXW, emit, kr, kr + K, lane, a.ny);
+      }
     } else {
 #pragma unroll
-      for (int i = 0; i < kTXW; ++i) emit(i, sbuf[(warp * kTXW + i) * 32 + lane]);
+      for (int i = 0; i < kTXW; ++i) {
+        const float4 v = sbuf[(warp * kTXW + i) * 32 + lane];
+        if (PAIR && paired) emit_m(i, v);
+        emit(i, v);
+      }
     }
   };
 
