@@ -9,6 +9,8 @@
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <map>
+#include <mutex>
 #include <vector>
 
 #include "et_array_interface.h"
@@ -45,6 +47,28 @@ int d2h(float* h, const float* d, size_t n, cudaStream_t st) {
   return cudaMemcpyAsync(h, d, fbytes(n), cudaMemcpyDeviceToHost, st) == cudaSuccess ? kOk : kErrTransferGpu;
 }
 
+// Whether the current device reads pageable host memory through the host's
+// page tables (address translation services, e.g. a Grace-Blackwell
+// NVLink-C2C system): the fused path's layout kernels then read the caller's
+// host arrays directly -- one pass over the link at the rate of a copy, no
+// separate host-to-device copy and the transpose fused into it.
+bool host_memory_readable() {
+  static std::mutex mu;
+  static std::map<int, bool> known;
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) return false;
+  std::lock_guard<std::mutex> lk(mu);
+  auto it = known.find(dev);
+  if (it != known.end()) return it->second;
+  int pma = 0, ats = 0;
+  if (cudaDeviceGetAttribute(&pma, cudaDevAttrPageableMemoryAccess, dev) != cudaSuccess ||
+      cudaDeviceGetAttribute(&ats, cudaDevAttrPageableMemoryAccessUsesHostPageTables, dev) != cudaSuccess) {
+    cudaGetLastError();
+    pma = ats = 0;
+  }
+  return known[dev] = (pma == 1 && ats == 1);
+}
+
 // Project with host buffers (activity and/or attenuation may be null).
 int project_host(const Problem& pb, const float* act, const float* att, float* sino) {
   int s;
@@ -61,9 +85,14 @@ int project_host(const Problem& pb, const float* act, const float* att, float* s
   float* d_sino = cv.take<float>(nsino);
   char* w = cv.take<char>(ws);
   cudaStream_t st = ds.stream;
-  if (act && (s = h2d(d_act, act, nvox, st)) != kOk) return finish(ds, s);
-  if (att && (s = h2d(d_att, att, nvox, st)) != kOk) return finish(ds, s);
   g_last_path = (use_fused(pb) && act) ? 1 : 2;
+  if (g_last_path == 1 && host_memory_readable()) {  // the layout kernels read the host arrays
+    d_act = const_cast<float*>(act);
+    d_att = const_cast<float*>(att);
+  } else {
+    if (act && (s = h2d(d_act, act, nvox, st)) != kOk) return finish(ds, s);
+    if (att && (s = h2d(d_att, att, nvox, st)) != kOk) return finish(ds, s);
+  }
   s = project_device(pb, d_act, d_att, d_sino, w, ws, &ds.staging, st);
   if (s == kOk) s = d2h(sino, d_sino, nsino, st);
   return finish(ds, s);
@@ -84,9 +113,14 @@ int backproject_host(const Problem& pb, const float* sino, const float* att, flo
   float* d_out = cv.take<float>(nvox);
   char* w = cv.take<char>(ws);
   cudaStream_t st = ds.stream;
-  if ((s = h2d(d_sino, sino, nsino, st)) != kOk) return finish(ds, s);
-  if (att && (s = h2d(d_att, att, nvox, st)) != kOk) return finish(ds, s);
   g_last_path = use_fused(pb) ? 1 : 2;
+  if (g_last_path == 1 && host_memory_readable()) {  // the layout kernels read the host arrays
+    d_sino = const_cast<float*>(sino);
+    d_att = const_cast<float*>(att);
+  } else {
+    if ((s = h2d(d_sino, sino, nsino, st)) != kOk) return finish(ds, s);
+    if (att && (s = h2d(d_att, att, nvox, st)) != kOk) return finish(ds, s);
+  }
   s = backproject_device(pb, d_sino, d_att, d_out, w, ws, &ds.staging, st);
   if (s == kOk) s = d2h(out, d_out, nvox, st);
   return finish(ds, s);
