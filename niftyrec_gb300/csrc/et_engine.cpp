@@ -261,6 +261,7 @@ int project_device(const Problem& pb, const float* d_act, const float* d_att, fl
     a.mu = mu_c;
     a.out = sino_c;
     a.psf = d_psf;
+    a.psf_host = pb.psf_k ? pb.psf_sep.data() : nullptr;
     a.psf_k = pb.psf_k;
     a.truncate = pb.truncate;
     if ((s = yg_project(a, st)) != kOk) return s;
@@ -320,6 +321,7 @@ int backproject_device(const Problem& pb, const float* d_sino, const float* d_at
     a.sino = sino_c;
     a.out = out_c;
     a.psf = d_psf;
+    a.psf_host = pb.psf_k ? pb.psf_sep.data() : nullptr;
     a.psf_k = pb.psf_k;
     a.truncate = pb.truncate;
     a.back_mode = pb.back_mode;

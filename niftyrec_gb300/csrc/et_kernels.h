@@ -62,6 +62,7 @@ struct YgArgs {
   const float* sino = nullptr;    // [ncam][nx][cy] (backprojection input)
   float* out = nullptr;           // projector: [ncam][nx][cy]; backprojector: [nz][nx][cy]
   const float* psf = nullptr;     // device [nz][2k] or null
+  const float* psf_host = nullptr;  // host copy of psf (valid during the launching call) or null
   int psf_k = 0;
   int truncate = 0;
   int back_mode = kBackReference;

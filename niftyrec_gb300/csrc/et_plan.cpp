@@ -106,6 +106,7 @@ int plan_project(Plan& p, int subset, const float* d_act, float* d_sino, int lay
     a.mu = p.has_att ? p.mu : nullptr;
     a.out = layout == kLayoutNifti ? p.sino_c : d_sino;
     a.psf = p.psf;
+    a.psf_host = pb.psf_k ? pb.psf_sep.data() : nullptr;
     a.psf_k = pb.psf_k;
     a.truncate = truncate;
     int s = yg_project(a, st);
@@ -163,6 +164,7 @@ int plan_backproject(Plan& p, int subset, const float* d_sino, float* d_out, int
     a.sino = sino;
     a.out = out;
     a.psf = p.psf;
+    a.psf_host = pb.psf_k ? pb.psf_sep.data() : nullptr;
     a.psf_k = pb.psf_k;
     a.truncate = truncate;
     a.group = std::min(pb.group, tuned_group(pb.nx, pb.ny, pb.nz, n));  // by the subset's camera count

@@ -24,6 +24,7 @@
 #include <cuda_bf16.h>
 
 #include <algorithm>
+#include <cstring>
 #include <map>
 #include <mutex>
 #include <type_traits>
@@ -138,8 +139,8 @@ __device__ __forceinline__ float4 mask_rows(float4 v, int yb, int ny) {
 // out[y] = sum_k in[y+k] * kc[R-k], zero outside [0, ny) (rows >= ny are zero
 // pads, rows < 0 come from lanes below 0 and are masked).  Neighbour rows come
 // from lanes l-1, l-2 and l+1, l+2 by shuffles.
-template <int R>
-__device__ __forceinline__ float4 yconv4(const float4& u, const float* kc, int lane) {
+template <int R, class KC>
+__device__ __forceinline__ float4 yconv4(const float4& u, KC kc, int lane) {
   float w[2 * R + 4];
   w[R + 0] = u.x;
   w[R + 1] = u.y;
@@ -252,6 +253,23 @@ __device__ __forceinline__ CamRows cam_rows(const float* m) {
   return c;
 }
 
+// Separated PSF of every plane ([nz][2K]: row kernel, then column kernel)
+// passed as a kernel parameter: the coefficients are read from the constant
+// bank with uniform addresses (no shared-memory copy, no load instruction per
+// use in the row and column passes).  Tables larger than this use the shared
+// memory copy.
+constexpr int kPsfTableFloats = 7680;
+struct PsfTable {
+  float c[kPsfTableFloats];
+};
+
+// A row kernel read backwards (k -> p[2R - k]): a mirror camera's row pass.
+template <int R>
+struct Reversed {
+  const float* p;
+  __device__ __forceinline__ float operator[](int k) const { return p[2 * R - k]; }
+};
+
 // ------------------------------------------------------------ tile engine
 // A CTA of kW warps owns kTXC = kW * kTXW consecutive output columns of one
 // camera and walks one depth slab.  At every depth step the NS = kTXC + 2R
@@ -292,9 +310,9 @@ __host__ __device__ constexpr size_t tile_smem_bytes(int nz, bool pair = false) 
 
 // Row pass from the shared tile: outputs i = 0..kTXW-1 of this warp use tile
 // columns base + i .. base + i + 2R (base = warp * kTXW).
-template <int R, class EmitFn>
-__device__ __forceinline__ void rowpass_from_tile(const float4* __restrict__ sbuf, int base, EmitFn emit,
-                                                  const float* kr, const float* kc, int lane, int ny) {
+template <int R, class EmitFn, class KR, class KC>
+__device__ __forceinline__ void rowpass_from_tile(const float4* __restrict__ sbuf, int base, EmitFn emit, KR kr, KC kc,
+                                                  int lane, int ny) {
   constexpr int K = 2 * R + 1;
   constexpr int NJ = kTXW + 2 * R;
   float4 u[K];
@@ -319,10 +337,9 @@ __device__ __forceinline__ void rowpass_from_tile(const float4* __restrict__ sbu
 // Row passes of two cameras over the same tile (a camera and its mirror
 // camera): each tile column is read once and feeds both sliding windows;
 // output i of camera b is emitted before output i of camera a.
-template <int R, class EmitA, class EmitB>
-__device__ __forceinline__ void rowpass2_from_tile(const float4* __restrict__ sbuf, int base, EmitA emit_a,
-                                                   const float* kra, const float* kca, EmitB emit_b,
-                                                   const float* krb, const float* kcb, int lane, int ny) {
+template <int R, class EmitA, class EmitB, class KRA, class KCA, class KRB, class KCB>
+__device__ __forceinline__ void rowpass2_from_tile(const float4* __restrict__ sbuf, int base, EmitA emit_a, KRA kra,
+                                                   KCA kca, EmitB emit_b, KRB krb, KCB kcb, int lane, int ny) {
   constexpr int NJ = kTXW + 2 * R;
   float4 ua[kTXW], ub[kTXW];
 #pragma unroll
@@ -380,8 +397,9 @@ __device__ __forceinline__ bool lane_writes(const YgArgs& a, int yb) { return yb
 // the direct weights.  The mate's slabs merge in the opposite order.
 constexpr float kMateMaxT = 40.0f;
 
-template <int R, bool PSF, bool ATT, class V, bool PAIR = false>
-__device__ __forceinline__ void project_item(const YgArgs& a, int cam, int mate, int x0, unsigned char* smem) {
+template <int R, bool PSF, bool ATT, class V, bool PAIR = false, bool PTAB = false>
+__device__ __forceinline__ void project_item(const YgArgs& a, int cam, int mate, int x0, unsigned char* smem,
+                                             const float* ptab = nullptr) {
   using TS = TileShape<R>;
   constexpr bool KAHAN = StorageTraits<V>::kKahan;
   static_assert(!(PAIR && KAHAN), "mirror cameras are served by the float32 projector");
@@ -405,7 +423,7 @@ __device__ __forceinline__ void project_item(const YgArgs& a, int cam, int mate,
   const int nslabs = static_cast<int>(cluster.num_blocks());  // depth slabs = cluster size (2, 4 or 8)
   const int zper = (a.nz + nslabs - 1) / nslabs;
   const int zbeg = slab * zper, zend = min(a.nz, zbeg + zper);
-  if (PSF) {  // this slab's planes only
+  if (PSF && !PTAB) {  // this slab's planes only
     for (int i = zbeg * 2 * K + threadIdx.x; i < zend * 2 * K; i += blockDim.x) s_psf[i] = __ldg(a.psf + i);
     if (paired) {
       for (int i = zbeg * 2 * K + threadIdx.x; i < zend * 2 * K; i += blockDim.x) {
@@ -414,6 +432,27 @@ __device__ __forceinline__ void project_item(const YgArgs& a, int cam, int mate,
       }
     }
   }
+  // row and column kernels of plane z for this camera and for the mate
+  // (plane nz-1-z, row kernel reversed)
+  auto mate_pass = [&](const float4* sbuf, int z, auto emit_m) {
+    if constexpr (PTAB) {
+      const float* m = ptab + (a.nz - 1 - z) * 2 * K;
+      rowpass_from_tile<R>(sbuf, warp * kTXW, emit_m, Reversed<R>{m}, m + K, lane, a.ny);
+    } else {
+      const float* m = s_psf_m + z * 2 * K;
+      rowpass_from_tile<R>(sbuf, warp * kTXW, emit_m, m, m + K, lane, a.ny);
+    }
+  };
+  auto both_pass = [&](const float4* sbuf, int z, auto emit, auto emit_m) {
+    const float* kr = (PTAB ? ptab : s_psf) + z * 2 * K;
+    if constexpr (PTAB) {
+      const float* m = ptab + (a.nz - 1 - z) * 2 * K;
+      rowpass2_from_tile<R>(sbuf, warp * kTXW, emit, kr, kr + K, emit_m, Reversed<R>{m}, m + K, lane, a.ny);
+    } else {
+      const float* m = s_psf_m + z * 2 * K;
+      rowpass2_from_tile<R>(sbuf, warp * kTXW, emit, kr, kr + K, emit_m, m, m + K, lane, a.ny);
+    }
+  };
   const CamRows cr = cam_rows(a.geom[cam].fwd);
 
   float4 T[kTXW], P[kTXW], cT[kTXW], cP[kTXW];  // c*: Kahan compensations (KAHAN only)
@@ -463,8 +502,7 @@ __device__ __forceinline__ void project_item(const YgArgs& a, int cam, int mate,
     };
     if (MODE == 1) {
       if (PSF) {
-        const float* km = s_psf_m + z * 2 * K;
-        rowpass_from_tile<R>(sbuf, warp * kTXW, emit_m, km, km + K, lane, a.ny);
+        mate_pass(sbuf, z, emit_m);
       } else {
 #pragma unroll
         for (int i = 0; i < kTXW; ++i) emit_m(i, sbuf[(warp * kTXW + i) * 32 + lane]);
@@ -486,11 +524,10 @@ __device__ __forceinline__ void project_item(const YgArgs& a, int cam, int mate,
       }
     };
     if (PSF) {
-      const float* kr = s_psf + z * 2 * K;
       if (PAIR && paired) {
-        const float* km = s_psf_m + z * 2 * K;
-        rowpass2_from_tile<R>(sbuf, warp * kTXW, emit, kr, kr + K, emit_m, km, km + K, lane, a.ny);
+        both_pass(sbuf, z, emit, emit_m);
       } else {
+        const float* kr = (PTAB ? ptab : s_psf) + z * 2 * K;
         rowpass_from_tile<R>(sbuf, warp * kTXW, emit, kr, kr + K, lane, a.ny);
       }
     } else {
@@ -597,6 +634,17 @@ __global__ void __launch_bounds__(32 * kW, CTAS) k_project_yg(const YgArgs a) {
   const int u = item / ntile;
   const int2 uc = PAIR ? a.units[u] : make_int2(u, -1);
   project_item<R, PSF, ATT, V, PAIR>(a, uc.x, uc.y, (item % ntile) * kTXC, smem);
+}
+
+// The same with the separated PSF in the kernel parameters (PsfTable).
+template <int R, bool ATT, class V, int CTAS, bool PAIR>
+__global__ void __launch_bounds__(32 * kW, CTAS) k_project_ptab_yg(const YgArgs a, const __grid_constant__ PsfTable t) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  const int ntile = (a.nx + kTXC - 1) / kTXC;
+  const int item = blockIdx.x / a.pslabs;
+  const int u = item / ntile;
+  const int2 uc = PAIR ? a.units[u] : make_int2(u, -1);
+  project_item<R, true, ATT, V, PAIR, true>(a, uc.x, uc.y, (item % ntile) * kTXC, smem, t.c);
 }
 
 // Persistent projector over a batch of volumes: each cluster takes work items
@@ -1102,7 +1150,9 @@ int launch_project_R(const YgArgs& a_in, cudaStream_t st) {
   // mirror cameras are served by the float32 kernels only
   const bool pair = a.units != nullptr && a.nunits > 0 && !bf16;
   const int nunits = pair ? a.nunits : a.ncam;
-  const size_t smem = tile_smem_bytes<R>(psf ? a.nz : 0, pair);
+  // the PSF in the kernel parameters when the host copy is given and fits
+  const bool ptab = psf && a.psf_host && static_cast<size_t>(a.nz) * 2 * (2 * R + 1) <= kPsfTableFloats;
+  const size_t smem = tile_smem_bytes<R>(psf && !ptab ? a.nz : 0, pair);
   // three CTAs per SM need three tiles (plus 1 KB reserved each) in the 228 KB
   const bool three = 3 * (smem + 1024) <= 228 * 1024;
   if (a.pslabs != 2 && a.pslabs != 4 && a.pslabs != 8)
@@ -1124,11 +1174,33 @@ int launch_project_R(const YgArgs& a_in, cudaStream_t st) {
     NRGB_LAUNCH_SCOPE("k_project_yg", st);
     cudaLaunchKernelEx(&cfg, k, a);
   };
+  auto go_tab = [&](auto k) {
+    static thread_local PsfTable table;
+    std::memcpy(table.c, a.psf_host, sizeof(float) * a.nz * 2 * (2 * R + 1));
+    cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(nunits * ntile * a.pslabs);
+    cfg.blockDim = dim3(32 * kW);
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = st;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeClusterDimension;
+    attr[0].val.clusterDim.x = a.pslabs;
+    attr[0].val.clusterDim.y = 1;
+    attr[0].val.clusterDim.z = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    NRGB_LAUNCH_SCOPE("k_project_yg", st);
+    cudaLaunchKernelEx(&cfg, k, a, table);
+  };
   auto pick = [&](auto v, auto ctas, auto paired) {
     using V = decltype(v);
     constexpr int C = decltype(ctas)::value;
     constexpr bool P = decltype(paired)::value;
-    if (psf) {
+    if (psf && ptab) {
+      if (a.mu) go_tab(k_project_ptab_yg<R, true, V, C, P>);
+      else go_tab(k_project_ptab_yg<R, false, V, C, P>);
+    } else if (psf) {
       if (a.mu) go(k_project_yg<R, true, true, V, C, P>);
       else go(k_project_yg<R, true, false, V, C, P>);
     } else {
