@@ -20,8 +20,9 @@ BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "lib_et_array_interface.so")
 INCLUDE = os.path.join(os.path.dirname(HERE), "include")
 
-SOURCES = ["et_geometry.cpp", "et_engine.cpp", "et_api.cpp", "et_profile.cpp", "et_general.cu", "et_ygantry.cu", "et_update.cu",
-           "et_noalloc.cu", "et_plan.cpp", "et_fisher.cu"]
+SOURCES = ["et_geometry.cpp", "et_engine.cpp", "et_api.cpp", "et_profile.cpp", "et_general.cu", "et_ygantry.cu",
+           "et_yg_project.cu", "et_yg_proj_r01.cu", "et_yg_proj_r23.cu", "et_yg_proj_r45.cu", "et_yg_proj_r67.cu",
+           "et_yg_back.cu", "et_update.cu", "et_noalloc.cu", "et_plan.cpp", "et_fisher.cu"]
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC,-ffp-contract=off,-fvisibility=hidden",

@@ -2,7 +2,7 @@
 // any background values, any grid.  Volumes in nifti layout.  Each stage is a
 // separate kernel following the reference's float operation order (products
 // and sums rounded separately), so this path reproduces the reference CPU
-// path up to the last bit of expf.  The fused kernels of et_ygantry.cu cover
+// path up to the last bit of expf.  The fused kernels of et_yg_*.cu cover
 // the common gantry case; this path covers everything else.
 #include "et_kernels.h"
 #include "et_profile.h"

@@ -1,5 +1,5 @@
 // Launch-side declarations of the CUDA kernels (device code in et_general.cu,
-// et_ygantry.cu, et_update.cu).
+// et_yg_*.cu / et_yg_*.cuh and et_ygantry.cu, et_update.cu, et_fisher.cu).
 #pragma once
 
 #include <cuda_runtime.h>

@@ -1,0 +1,615 @@
+// Fused y-gantry backprojector: transmission carries, spread (reference and
+// exact-transpose forms, mirror units), inverse-rotation gather and the
+// two-stream pipeline over camera groups.
+#include "et_yg_device.cuh"
+
+namespace nrgb {
+namespace {
+
+// ------------------------------------------------ backprojector: slab carry
+// carry[c][s][x][y] (s < kSlabsB) = sum of the rotated mu over the depth
+// slabs before s (exclusive prefix): the transmission a depth slab starts
+// from; carry[c][kSlabsB][x][y] = the whole column's sum.  One block row per
+// camera c, or with a.units per unit (its first camera c; a mirror camera's
+// transmissions are c's read from the other end).
+template <class V>
+__global__ void __launch_bounds__(32 * kSlabsB) k_mu_carry_yg(const YgArgs a) {
+  constexpr int C = kCarryCols;
+  constexpr bool KAHAN = StorageTraits<V>::kKahan;
+  const V* __restrict__ mu = reinterpret_cast<const V*>(a.mu) + a.row0;
+  __shared__ Tap s_tap[kSlabsB][C];
+  __shared__ float4 s_sum[kSlabsB][C][32];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int nchunk = (a.nx + C - 1) / C;
+  const int unit = blockIdx.x / nchunk;
+  const int cam = a.units ? a.units[unit].x : unit;
+  const int x0 = (blockIdx.x % nchunk) * C;
+  const int yb = lane * 4;
+  const bool yok = lane_rows_ok(a, yb);
+  const CamRows cr = cam_rows(a.geom[cam].fwd);
+  const int zper = (a.nz + kSlabsB - 1) / kSlabsB;
+  const int zbeg = warp * zper, zend = min(a.nz, zbeg + zper);
+  float4 S[C], cS[C];
+#pragma unroll
+  for (int i = 0; i < C; ++i) {
+    S[i] = make_float4(0.f, 0.f, 0.f, 0.f);
+    cS[i] = make_float4(0.f, 0.f, 0.f, 0.f);
+  }
+  for (int z = zbeg; z < zend; ++z) {
+    if (lane < C) {
+      const int xp = x0 + lane;
+      s_tap[warp][lane] = make_tap(xp, z, cr.m00, cr.m02, cr.m03, cr.m20, cr.m22, cr.m23, a.nx, a.nz, a.cy, xp < a.nx);
+    }
+    __syncwarp();
+#pragma unroll
+    for (int i = 0; i < C; ++i) depth_add4<KAHAN>(S[i], cS[i], sample4(mu, s_tap[warp][i], yb, yok));
+    __syncwarp();
+  }
+#pragma unroll
+  for (int i = 0; i < C; ++i) s_sum[warp][i][lane] = depth_value4<KAHAN>(S[i], cS[i]);
+  __syncthreads();
+  if (!yok || !lane_writes(a, yb)) return;
+#pragma unroll
+  for (int i = 0; i < C; ++i) {
+    const int x = x0 + i;
+    if (x >= a.nx) continue;
+    float4 pre = make_float4(0.f, 0.f, 0.f, 0.f);
+    for (int s = 0; s < warp; ++s) add4(pre, s_sum[s][i][lane]);
+    float* dst = a.slab_T + ((static_cast<size_t>(cam) * kCarrySlots + warp) * a.nx + x) * a.cy + a.row0 + yb;
+    *reinterpret_cast<float4*>(dst) = pre;
+    if (warp == kSlabsB - 1) {  // the column total, one slot further
+      add4(pre, s_sum[warp][i][lane]);
+      *reinterpret_cast<float4*>(dst + static_cast<size_t>(a.nx) * a.cy) = pre;
+    }
+  }
+}
+
+// Vector reduction of 4 floats into global memory (sm_90+).
+__device__ __forceinline__ void red4(float* p, const float4& v) {
+  asm volatile("red.global.add.v4.f32 [%0], {%1, %2, %3, %4};" ::"l"(p), "f"(v.x), "f"(v.y), "f"(v.z), "f"(v.w)
+               : "memory");
+}
+
+__device__ __forceinline__ float4 scale4(const float4& v, float w) {
+  return make_float4(v.x * w, v.y * w, v.z * w, v.w * w);
+}
+
+// Transposed bilinear interpolation: add w * v to each corner of footprint t
+// (corners outside the grid have weight 0 and are skipped).
+__device__ __forceinline__ void scatter4(float* __restrict__ base, const Tap& t, int yb, const float4& v) {
+  if (!t.any) return;
+  float* p = base + t.off + yb;
+  if (t.w00 != 0.0f) red4(p, scale4(v, t.w00));
+  if (t.w10 != 0.0f) red4(p + t.dx, scale4(v, t.w10));
+  if (t.w01 != 0.0f) red4(p + t.dz, scale4(v, t.w01));
+  if (t.w11 != 0.0f) red4(p + t.dx + t.dz, scale4(v, t.w11));
+}
+
+// ---------------------------------------- backprojector: spread + PSF
+// temp[g][z][x][y] = PSF_z( s(x', y) * exp(-T_z(x', y)) ) for camera c0+g,
+// T inclusive (emission-lib/_et_line_backproject_attenuated.cpp:24-34), PSF
+// as in the projector.  CTA = (camera, x-tile, depth slab); every sampled
+// column starts its transmission from the slab carry.
+// ADJ: the exact transpose of the projector instead (not in the reference):
+// the PSF taps are flipped (correlation) and each output column is scattered
+// with the projector's own bilinear weights into the accumulator a.out
+// (vector reductions; all cameras in one launch, no scratch).
+// CTAS: CTAs per SM the kernel is compiled for (3 where three tiles fit in
+// shared memory, for the float32 reference spread; else 2).
+template <int R, bool PSF, bool ATT, bool ADJ, class V, int CTAS = 2>
+__global__ void __launch_bounds__(32 * kW, CTAS) k_spread_yg(const YgArgs a, int c0) {
+  using TS = TileShape<R>;
+  constexpr bool KAHAN = StorageTraits<V>::kKahan;
+  const V* __restrict__ mu = reinterpret_cast<const V*>(a.mu) + a.row0;
+  constexpr int NS = TS::NS;
+  constexpr int K = 2 * R + 1;
+  extern __shared__ __align__(16) unsigned char smem[];
+  float4* sb = reinterpret_cast<float4*>(smem);
+  Tap* taps = reinterpret_cast<Tap*>(smem + TS::kSbBytes);
+  float* s_psf = reinterpret_cast<float*>(smem + TS::kSbBytes + TS::kTapBytes);
+
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int ntile = (a.nx + kTXC - 1) / kTXC;
+  const int slab = blockIdx.x % kSlabsB;
+  const int item = blockIdx.x / kSlabsB;
+  const int g = item / ntile;
+  const int cam = c0 + g;
+  const int x0 = (item % ntile) * kTXC;
+  const int yb = lane * 4;
+  const bool yok = lane_rows_ok(a, yb);
+  const int zper = (a.nz + kSlabsB - 1) / kSlabsB;
+  const int zbeg = slab * zper, zend = min(a.nz, zbeg + zper);
+  if (zbeg >= zend) return;  // uniform over the CTA
+  if (PSF) {  // this slab's planes only
+    for (int i = zbeg * 2 * K + threadIdx.x; i < zend * 2 * K; i += blockDim.x) {
+      const int j = i % (2 * K), base = i - j;
+      // transpose of a convolution = correlation: reverse each kernel
+      const int src = !ADJ ? i : (j < K ? base + (K - 1 - j) : base + K + (2 * K - 1 - j));
+      s_psf[i] = __ldg(a.psf + src);
+    }
+  }
+  const CamRows cr = cam_rows(a.geom[cam].fwd);
+  const size_t vol = static_cast<size_t>(a.nz) * a.nx * a.cs;  // one scratch volume
+  float* __restrict__ tmp = ADJ ? a.out + a.row0 : a.temp + vol * g;
+  const float* __restrict__ srow = a.sino + static_cast<size_t>(cam) * a.nx * a.cy + a.row0;
+
+  float4 Tc[TS::kOwn], cTc[TS::kOwn];  // transmission per sampled column (+ Kahan compensation)
+#pragma unroll
+  for (int k = 0; k < TS::kOwn; ++k) {
+    Tc[k] = make_float4(0.f, 0.f, 0.f, 0.f);
+    cTc[k] = make_float4(0.f, 0.f, 0.f, 0.f);
+    const int xp = x0 - R + warp + kW * k;
+    if (ATT && warp + kW * k < NS && xp >= 0 && xp < a.nx && yok)
+      Tc[k] = ldg4(a.slab_T + ((static_cast<size_t>(cam) * kCarrySlots + slab) * a.nx + xp) * a.cy + a.row0 + yb);
+  }
+  __syncthreads();
+
+  for (int z = zbeg; z < zend; ++z) {
+    const int b = z & 1;
+    float4* sbuf = sb + b * NS * 32;
+    Tap* tb = taps + b * TS::kTapSlots;
+    if ((ATT || ADJ) && lane < TS::kOwn) {
+      const int c = warp + kW * lane;
+      if (c < NS) {
+        const int xp = x0 - R + c;
+        tb[tap_slot<R>(c)] = make_tap(xp, z, cr.m00, cr.m02, cr.m03, cr.m20, cr.m22, cr.m23, a.nx, a.nz, a.cy,
+                         xp >= 0 && xp < a.nx);
+      }
+    }
+    __syncwarp();
+#pragma unroll
+    for (int k = 0; k < TS::kOwn; ++k) {
+      const int c = warp + kW * k;
+      if (c < NS) {
+        const int xp = x0 - R + c;
+        float4 s = make_float4(0.f, 0.f, 0.f, 0.f);
+        if (xp >= 0 && xp < a.nx && yok) s = ldg4(srow + static_cast<size_t>(xp) * a.cy + yb);
+        if (ATT) {
+          depth_add4<KAHAN>(Tc[k], cTc[k], sample4(mu, tb[tap_slot<R>(c)], yb, yok));
+          s = mul4(s, exp_neg4(depth_value4<KAHAN>(Tc[k], cTc[k])));
+        }
+        sbuf[c * 32 + lane] = s;
+      }
+    }
+    __syncthreads();
+    auto emit = [&](int i, const float4& v) {
+      const int x = x0 + warp * kTXW + i;
+      if (x >= a.nx || !yok) return;
+      if (ADJ) {
+        // halo rows lack part of their PSF support: their owner window adds them
+        if (lane_writes(a, yb)) scatter4(tmp, tb[tap_slot<R>(warp * kTXW + i + R)], yb, v);
+      } else {
+        *reinterpret_cast<float4*>(tmp + (static_cast<size_t>(z) * a.nx + x) * a.cs + yb) = v;
+      }
+    };
+    if (PSF) {
+      const float* kr = s_psf + z * 2 * K;
+      rowpass_from_tile<R>(sbuf, warp * kTXW, emit, kr, kr + K, lane, a.ny);
+    } else {
+#pragma unroll
+      for (int i = 0; i < kTXW; ++i) emit(i, sbuf[(warp * kTXW + i) * 32 + lane]);
+    }
+  }
+}
+
+// Reference-mode spread of a mirror unit -- camera c and its mate m at the
+// opposite angle about the grid centre -- into ONE scratch volume in c's
+// rotated frame:
+//   U(x', y, z') = PSF_z'[s_c e^{-T}](x') + PSF'_{nz-1-z'}[s_m(nx-1-x') e^{-T'}](x')
+// with T the inclusive mu sum along c's column from its detector side, T'
+// the inclusive sum from the other end (the mate's detector side), and PSF'
+// the mate's plane nz-1-z' with the row kernel reversed.  The mate's inverse
+// matrix is c's mirrored in x and z, so gathering U with c's inverse matrix
+// adds both cameras' terms: one mu scan, one scratch volume and one gather
+// per pair.  A unit without a mate spreads its camera alone.  CTA = (unit,
+// x-tile, depth slab); the PSF planes of the slab only sit in shared memory.
+template <int R, bool PSF, bool ATT>
+__global__ void __launch_bounds__(32 * kW, 2) k_spread_pair_yg(const YgArgs a, int u0) {
+  using TS = TileShape<R>;
+  constexpr int NS = TS::NS;
+  constexpr int K = 2 * R + 1;
+  const float* __restrict__ mu = a.mu + a.row0;
+  extern __shared__ __align__(16) unsigned char smem[];
+  float4* sb = reinterpret_cast<float4*>(smem);                              // [2 stages][2][NS][32]
+  Tap* taps = reinterpret_cast<Tap*>(smem + 2 * TS::kSbBytes);                // [2][kTapSlots]
+  float* s_psf = reinterpret_cast<float*>(smem + 2 * TS::kSbBytes + TS::kTapBytes);  // [zper][2K], mate's next
+
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int ntile = (a.nx + kTXC - 1) / kTXC;
+  const int slab = blockIdx.x % kSlabsB;
+  const int item = blockIdx.x / kSlabsB;
+  const int g = item / ntile;
+  const int unit = u0 + g;
+  const int2 uc = a.units[unit];
+  const int cam = uc.x, mate = uc.y;
+  const bool paired = mate >= 0;  // uniform over the CTA
+  const int x0 = (item % ntile) * kTXC;
+  const int yb = lane * 4;
+  const bool yok = lane_rows_ok(a, yb);
+  const int zper = (a.nz + kSlabsB - 1) / kSlabsB;
+  const int zbeg = slab * zper, zend = min(a.nz, zbeg + zper);
+  if (zbeg >= zend) return;  // uniform over the CTA
+  float* s_psf_m = s_psf + zper * 2 * K;
+  if (PSF) {
+    for (int i = threadIdx.x; i < (zend - zbeg) * 2 * K; i += blockDim.x) {
+      s_psf[i] = __ldg(a.psf + zbeg * 2 * K + i);
+      if (paired) {
+        const int z = zbeg + i / (2 * K), j = i % (2 * K);
+        s_psf_m[i] = __ldg(a.psf + (a.nz - 1 - z) * 2 * K + (j < K ? K - 1 - j : j));
+      }
+    }
+  }
+  const CamRows cr = cam_rows(a.geom[cam].fwd);
+  const size_t vol = static_cast<size_t>(a.nz) * a.nx * a.cs;  // one scratch volume
+  float* __restrict__ tmp = a.temp + vol * g;
+  const float* __restrict__ srow = a.sino + static_cast<size_t>(cam) * a.nx * a.cy + a.row0;
+  const float* __restrict__ mrow = a.sino + static_cast<size_t>(paired ? mate : cam) * a.nx * a.cy + a.row0;
+
+  // transmissions per sampled column: forward (from the slab carry) and, for
+  // the mate, from the far end (column total minus the carry)
+  float4 Tc[TS::kOwn], Tr[TS::kOwn];
+#pragma unroll
+  for (int k = 0; k < TS::kOwn; ++k) {
+    Tc[k] = make_float4(0.f, 0.f, 0.f, 0.f);
+    Tr[k] = make_float4(0.f, 0.f, 0.f, 0.f);
+    const int xp = x0 - R + warp + kW * k;
+    if (ATT && warp + kW * k < NS && xp >= 0 && xp < a.nx && yok) {
+      const float* cp = a.slab_T + ((static_cast<size_t>(cam) * kCarrySlots + slab) * a.nx + xp) * a.cy + a.row0 + yb;
+      Tc[k] = ldg4(cp);
+      if (paired) {
+        const float4 tot = ldg4(cp + static_cast<size_t>(kSlabsB - slab) * a.nx * a.cy);
+        Tr[k] = make_float4(tot.x - Tc[k].x, tot.y - Tc[k].y, tot.z - Tc[k].z, tot.w - Tc[k].w);
+      }
+    }
+  }
+  __syncthreads();
+
+  for (int z = zbeg; z < zend; ++z) {
+    const int b = z & 1;
+    float4* sc = sb + b * 2 * NS * 32;
+    float4* sm = sc + NS * 32;
+    Tap* tb = taps + b * TS::kTapSlots;
+    if (ATT && lane < TS::kOwn) {
+      const int c = warp + kW * lane;
+      if (c < NS) {
+        const int xp = x0 - R + c;
+        tb[tap_slot<R>(c)] = make_tap(xp, z, cr.m00, cr.m02, cr.m03, cr.m20, cr.m22, cr.m23, a.nx, a.nz, a.cy,
+                                      xp >= 0 && xp < a.nx);
+      }
+    }
+    __syncwarp();
+#pragma unroll
+    for (int k = 0; k < TS::kOwn; ++k) {
+      const int c = warp + kW * k;
+      if (c < NS) {
+        const int xp = x0 - R + c;
+        const bool ok = xp >= 0 && xp < a.nx && yok;
+        float4 s = make_float4(0.f, 0.f, 0.f, 0.f), q = s;
+        if (ok) s = ldg4(srow + static_cast<size_t>(xp) * a.cy + yb);
+        if (paired && ok) q = ldg4(mrow + static_cast<size_t>(a.nx - 1 - xp) * a.cy + yb);
+        if (ATT) {
+          const float4 m = sample4(mu, tb[tap_slot<R>(c)], yb, yok);
+          add4(Tc[k], m);
+          s = mul4(s, exp_neg4(Tc[k]));
+          if (paired) {
+            q = mul4(q, exp_neg4(Tr[k]));
+            Tr[k] = make_float4(Tr[k].x - m.x, Tr[k].y - m.y, Tr[k].z - m.z, Tr[k].w - m.w);
+          }
+        }
+        sc[c * 32 + lane] = s;
+        if (paired) sm[c * 32 + lane] = q;
+      }
+    }
+    __syncthreads();
+    float4 acc[kTXW];
+#pragma unroll
+    for (int i = 0; i < kTXW; ++i) acc[i] = make_float4(0.f, 0.f, 0.f, 0.f);
+    auto write = [&](int i, float4 v) {
+      const int x = x0 + warp * kTXW + i;
+      if (x >= a.nx || !yok) return;
+      if (paired) add4(v, acc[i]);
+      *reinterpret_cast<float4*>(tmp + (static_cast<size_t>(z) * a.nx + x) * a.cs + yb) = v;
+    };
+    if (PSF) {
+      if (paired) {
+        const float* km = s_psf_m + (z - zbeg) * 2 * K;
+        rowpass_from_tile<R>(sm, warp * kTXW, [&](int i, const float4& v) { acc[i] = v; }, km, km + K, lane,
+                             a.ny);
+      }
+      const float* kr = s_psf + (z - zbeg) * 2 * K;
+      rowpass_from_tile<R>(sc, warp * kTXW, write, kr, kr + K, lane, a.ny);
+    } else {
+#pragma unroll
+      for (int i = 0; i < kTXW; ++i) {
+        if (paired) acc[i] = sm[(warp * kTXW + i) * 32 + lane];
+        write(i, sc[(warp * kTXW + i) * 32 + lane]);
+      }
+    }
+  }
+}
+
+// ------------------------------------ backprojector: inverse-rotation gather
+// out[Z][X][y] (+)= sum_g bilinear(temp[g], B_g * (X, y, Z)) with B_g the
+// camera's inverse matrix (ZYX order, -theta), emission-lib/_et.cpp:474-497.
+// With a.units, g runs over units and B_g is the unit's first camera's.
+__global__ void __launch_bounds__(32 * kGatherWarps) k_gather_yg(const YgArgs a, int c0, int gcount, int first) {
+  constexpr int C = kGatherCols;
+  extern __shared__ Tap s_gtap[];  // [kGatherWarps][C * group]
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int nchunk = (a.nx + C - 1) / C;
+  const int item = blockIdx.x * kGatherWarps + warp;
+  if (item >= nchunk * a.nz) return;
+  const int Z = item / nchunk;
+  const int X0 = (item % nchunk) * C;
+  const int yb = lane * 4;
+  Tap* tap = s_gtap + warp * C * a.group;
+  for (int e = lane; e < C * gcount; e += 32) {
+    const int g = e / C, X = X0 + e % C;
+    const CamRows cr = cam_rows(a.geom[a.units ? a.units[c0 + g].x : c0 + g].bwd);
+    // footprints in the scratch (column stride cs)
+    tap[e] = make_tap(X, Z, cr.m00, cr.m02, cr.m03, cr.m20, cr.m22, cr.m23, a.nx, a.nz, a.cs, X < a.nx);
+  }
+  __syncwarp();
+  if (!lane_rows_ok(a, yb) || !lane_writes(a, yb)) return;
+  const size_t vol = static_cast<size_t>(a.nz) * a.nx * a.cs;
+  // camera outer, columns inner: neighbouring accumulator columns of one
+  // camera share footprint columns, which then hit in L1
+  float4 acc[C];
+#pragma unroll
+  for (int i = 0; i < C; ++i) acc[i] = make_float4(0.f, 0.f, 0.f, 0.f);
+  for (int g = 0; g < gcount; ++g) {
+    const float* src = a.temp + vol * g;
+#pragma unroll
+    for (int i = 0; i < C; ++i) add4(acc[i], sample4(src, tap[g * C + i], yb, true));
+  }
+#pragma unroll
+  for (int i = 0; i < C; ++i) {
+    const int X = X0 + i;
+    if (X >= a.nx) continue;
+    float4* dst = reinterpret_cast<float4*>(a.out + (static_cast<size_t>(Z) * a.nx + X) * a.cy + a.row0 + yb);
+    if (!first) add4(acc[i], *dst);
+    *dst = acc[i];
+  }
+}
+
+template <int R, bool ADJ>
+int launch_spread_R(const YgArgs& a, int c0, int gcount, cudaStream_t st) {
+  const int ntile = (a.nx + kTXC - 1) / kTXC;
+  const dim3 grid(gcount * ntile * kSlabsB), block(32 * kW);
+  const bool psf = a.psf != nullptr;
+  const size_t smem = tile_smem_bytes<R>(psf ? a.nz : 0);
+  auto go = [&](auto k) {
+    cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
+    NRGB_LAUNCH_SCOPE(ADJ ? "k_adjoint_yg" : "k_spread_yg", st);
+    k<<<grid, block, smem, st>>>(a, c0);
+  };
+  // only mu is sampled from storage here (the sinogram is float32)
+  const bool bf16 = a.storage == kStorageBF16;
+  const bool three = 3 * (smem + 1024) <= 228 * 1024;
+  if (psf) {
+    if (a.mu && bf16) {
+      go(k_spread_yg<R, true, true, ADJ, __nv_bfloat16>);
+    } else if (a.mu) {
+      if constexpr (!ADJ) {
+        if (three)
+          go(k_spread_yg<R, true, true, false, float, 3>);
+        else
+          go(k_spread_yg<R, true, true, false, float>);
+      } else {
+        go(k_spread_yg<R, true, true, true, float>);
+      }
+    } else {
+      go(k_spread_yg<R, true, false, ADJ, float>);
+    }
+  } else {
+    if (a.mu && bf16) go(k_spread_yg<0, false, true, ADJ, __nv_bfloat16>);
+    else if (a.mu) go(k_spread_yg<0, false, true, ADJ, float>);
+    else go(k_spread_yg<0, false, false, ADJ, float>);
+  }
+  return cudaGetLastError() == cudaSuccess ? kOk : kErrKernel;
+}
+
+template <int R>
+int launch_spread_pair_R(const YgArgs& a, int u0, int gcount, cudaStream_t st) {
+  using TS = TileShape<R>;
+  const int ntile = (a.nx + kTXC - 1) / kTXC;
+  const dim3 grid(gcount * ntile * kSlabsB), block(32 * kW);
+  const bool psf = a.psf != nullptr;
+  const int zper = (a.nz + kSlabsB - 1) / kSlabsB;
+  const size_t smem = 2 * TS::kSbBytes + TS::kTapBytes + (psf ? sizeof(float) * 2 * zper * 2 * (2 * R + 1) : 0);
+  auto go = [&](auto k) {
+    cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
+    NRGB_LAUNCH_SCOPE("k_spread_pair_yg", st);
+    k<<<grid, block, smem, st>>>(a, u0);
+  };
+  if (psf) {
+    if (a.mu) go(k_spread_pair_yg<R, true, true>);
+    else go(k_spread_pair_yg<R, true, false>);
+  } else {
+    if (a.mu) go(k_spread_pair_yg<0, false, true>);
+    else go(k_spread_pair_yg<0, false, false>);
+  }
+  return cudaGetLastError() == cudaSuccess ? kOk : kErrKernel;
+}
+
+int spread_pair_by_radius(int R, const YgArgs& a, int u0, int gcount, cudaStream_t st) {
+  switch (R) {
+    case 0: return launch_spread_pair_R<0>(a, u0, gcount, st);
+    case 1: return launch_spread_pair_R<1>(a, u0, gcount, st);
+    case 2: return launch_spread_pair_R<2>(a, u0, gcount, st);
+    case 3: return launch_spread_pair_R<3>(a, u0, gcount, st);
+    case 4: return launch_spread_pair_R<4>(a, u0, gcount, st);
+    case 5: return launch_spread_pair_R<5>(a, u0, gcount, st);
+    case 6: return launch_spread_pair_R<6>(a, u0, gcount, st);
+    case 7: return launch_spread_pair_R<7>(a, u0, gcount, st);
+    default: return kErrParameters;
+  }
+}
+
+template <bool ADJ>
+int spread_by_radius_t(int R, const YgArgs& a, int c0, int gcount, cudaStream_t st) {
+  switch (R) {
+    case 0: return launch_spread_R<0, ADJ>(a, c0, gcount, st);
+    case 1: return launch_spread_R<1, ADJ>(a, c0, gcount, st);
+    case 2: return launch_spread_R<2, ADJ>(a, c0, gcount, st);
+    case 3: return launch_spread_R<3, ADJ>(a, c0, gcount, st);
+    case 4: return launch_spread_R<4, ADJ>(a, c0, gcount, st);
+    case 5: return launch_spread_R<5, ADJ>(a, c0, gcount, st);
+    case 6: return launch_spread_R<6, ADJ>(a, c0, gcount, st);
+    case 7: return launch_spread_R<7, ADJ>(a, c0, gcount, st);
+    default: return kErrParameters;
+  }
+}
+
+int spread_by_radius(int R, const YgArgs& a, int c0, int gcount, cudaStream_t st) {
+  return spread_by_radius_t<false>(R, a, c0, gcount, st);
+}
+
+}  // namespace
+
+size_t yg_backproject_workspace(int nx, int ny, int nz, int ncam, int group, int slots) {
+  const size_t cy = round_up(ny, 4);
+  const size_t vol = static_cast<size_t>(nz) * nx * scratch_rows(ny);  // one window's scratch volume
+  const size_t slabs = static_cast<size_t>(ncam) * kCarrySlots * nx * cy;
+  // with two slots the spread of group g+1 overlaps the gather of group g
+  return sizeof(float) * (slabs + static_cast<size_t>(slots) * vol * std::max(1, std::min(group, ncam)));
+}
+
+int yg_carry_slabs() { return kCarrySlots; }
+
+int yg_mu_carry(const YgArgs& a_in, float* out, cudaStream_t st) {
+  const int nchunk = (a_in.nx + kCarryCols - 1) / kCarryCols;
+  const int n = a_in.units ? a_in.nunits : a_in.ncam;
+  for (const Window& w : row_windows(a_in.ny, 0)) {  // carries need no halo
+    YgArgs a = windowed(a_in, w);
+    a.slab_T = out;
+    NRGB_LAUNCH_SCOPE("k_mu_carry_yg", st);
+    if (a.storage == kStorageBF16)
+      k_mu_carry_yg<__nv_bfloat16><<<n * nchunk, 32 * kSlabsB, 0, st>>>(a);
+    else
+      k_mu_carry_yg<float><<<n * nchunk, 32 * kSlabsB, 0, st>>>(a);
+  }
+  return cudaGetLastError() == cudaSuccess ? kOk : kErrKernel;
+}
+
+namespace {
+
+// Second stream and events of the backprojection pipeline, one set per device.
+struct Pipe {
+  cudaStream_t aux = nullptr;
+  cudaEvent_t fork = nullptr, join = nullptr, spread_done[2] = {nullptr, nullptr},
+              gather_done[2] = {nullptr, nullptr};
+};
+
+Pipe* pipe_for_current_device() {
+  static std::mutex mu;
+  static std::map<int, Pipe> pipes;
+  int dev = 0;
+  cudaGetDevice(&dev);
+  std::lock_guard<std::mutex> lk(mu);
+  Pipe& p = pipes[dev];
+  if (!p.aux) {
+    if (cudaStreamCreateWithFlags(&p.aux, cudaStreamNonBlocking) != cudaSuccess) return nullptr;
+    cudaEvent_t* evs[] = {&p.fork, &p.join, &p.spread_done[0], &p.spread_done[1], &p.gather_done[0],
+                          &p.gather_done[1]};
+    for (cudaEvent_t* e : evs)
+      if (cudaEventCreateWithFlags(e, cudaEventDisableTiming) != cudaSuccess) return nullptr;
+  }
+  return &p;
+}
+
+}  // namespace
+
+// Per row window and camera group: spread on the caller's stream, gather on
+// a second stream; step g (over all windows' groups) uses scratch slot g % 2,
+// so the spread of step g+1 runs while the gather of step g reads the other
+// slot.
+int yg_backproject(const YgArgs& a_in, cudaStream_t st) {
+  YgArgs a = a_in;
+  const int R = a.psf ? (a.psf_k - 1) / 2 : 0;
+  // mirror units: reference mode, float32 mu
+  const bool pair = a.units && a.nunits > 0 && a.back_mode == kBackReference && a.storage != kStorageBF16;
+  if (!pair) {
+    a.units = nullptr;
+    a.nunits = 0;
+  }
+  const int nunits = pair ? a.nunits : a.ncam;  // scratch volumes to spread and gather
+  // even groups of at most a.group units
+  int group = std::max(1, std::min(a.group, nunits));
+  const int ngroups = (nunits + group - 1) / group;
+  group = (nunits + ngroups - 1) / ngroups;
+  // work space: slab carries first (unless given), then the scratch slot(s)
+  const size_t vol = static_cast<size_t>(a.nz) * a.nx * scratch_rows(a.ny);
+  float* slot0;
+  if (a.carry || !a.mu) {  // carries given, or not needed without attenuation
+    a.slab_T = const_cast<float*>(a.carry);
+    slot0 = a.work;
+  } else {
+    a.slab_T = a.work;
+    slot0 = a.work + static_cast<size_t>(a.ncam) * kCarrySlots * a.nx * a.cy;
+    int s = yg_mu_carry(a, a.slab_T, st);
+    if (s != kOk) return s;
+  }
+  a.group = group;
+  auto spread = [&](const YgArgs& b, int c0, int gcount) {
+    return pair ? spread_pair_by_radius(R, b, c0, gcount, st) : spread_by_radius(R, b, c0, gcount, st);
+  };
+  const std::vector<Window> wins = row_windows(a.ny, R);
+  if (a.back_mode == kBackAdjoint) {
+    // transpose of the projector: one launch per window over all cameras,
+    // scattered straight into the zeroed accumulator
+    const size_t full = static_cast<size_t>(a.nz) * a.nx * a.cy;
+    if (cudaMemsetAsync(a.out, 0, sizeof(float) * full, st) != cudaSuccess) return kErrKernel;
+    for (const Window& w : wins) {
+      const int s = spread_by_radius_t<true>(R, windowed(a, w), 0, a.ncam, st);
+      if (s != kOk) return s;
+    }
+    return kOk;
+  }
+  const int nchunk = (a.nx + kGatherCols - 1) / kGatherCols;
+  const int gblocks = (nchunk * a.nz + kGatherWarps - 1) / kGatherWarps;
+  const size_t gsmem = sizeof(Tap) * kGatherWarps * kGatherCols * group;
+  cudaFuncSetAttribute(k_gather_yg, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(gsmem));
+  if (!a.pipelined) {
+    for (const Window& w : wins) {
+      YgArgs b = windowed(a, w);
+      b.temp = slot0;
+      for (int c0 = 0; c0 < nunits; c0 += group) {
+        const int gcount = std::min(group, nunits - c0);
+        int st_ = spread(b, c0, gcount);
+        if (st_ != kOk) return st_;
+        NRGB_LAUNCH_SCOPE("k_gather_yg", st);
+        k_gather_yg<<<gblocks, 32 * kGatherWarps, gsmem, st>>>(b, c0, gcount, c0 == 0 ? 1 : 0);
+      }
+    }
+    return cudaGetLastError() == cudaSuccess ? kOk : kErrKernel;
+  }
+  Pipe* pp = pipe_for_current_device();
+  if (!pp) return kErrUnspecified;
+  cudaEventRecord(pp->fork, st);
+  cudaStreamWaitEvent(pp->aux, pp->fork, 0);
+  int gi = 0;
+  for (const Window& w : wins) {
+    YgArgs b = windowed(a, w);
+    for (int c0 = 0; c0 < nunits; c0 += group, ++gi) {
+      const int gcount = std::min(group, nunits - c0);
+      const int slot = gi & 1;
+      b.temp = slot0 + vol * group * slot;
+      if (gi >= 2) cudaStreamWaitEvent(st, pp->gather_done[slot], 0);
+      int st_ = spread(b, c0, gcount);
+      if (st_ != kOk) return st_;
+      cudaEventRecord(pp->spread_done[slot], st);
+      cudaStreamWaitEvent(pp->aux, pp->spread_done[slot], 0);
+      {
+        NRGB_LAUNCH_SCOPE("k_gather_yg", pp->aux);
+        k_gather_yg<<<gblocks, 32 * kGatherWarps, gsmem, pp->aux>>>(b, c0, gcount, c0 == 0 ? 1 : 0);
+      }
+      cudaEventRecord(pp->gather_done[slot], pp->aux);
+    }
+  }
+  cudaEventRecord(pp->join, pp->aux);
+  cudaStreamWaitEvent(st, pp->join, 0);
+  return cudaGetLastError() == cudaSuccess ? kOk : kErrKernel;
+}
+
+}  // namespace nrgb

@@ -1,0 +1,675 @@
+// Device building blocks of the fused y-gantry kernels (shared by the
+// projector, backprojector and layout translation units): the column layout,
+// bilinear footprints, the tile engine with its row and column passes, the
+// projector's work item, and the row windows of tall volumes.
+//
+// Fused kernels for cameras that rotate about the gantry axis (nifti y):
+// theta_x = theta_z = 0, so the resampling matrix is an exact rotation in the
+// (x, z) plane and y maps to itself.  Every detector row y then samples the
+// SAME bilinear footprint in the (x, z) plane, so the device layout puts y
+// fastest ("column layout" [z][x][cy]) and one warp handles whole columns:
+// lane l owns y = 4l..4l+3 (float4), the footprint of an (x, z) column is
+// computed once and every gather is a coalesced 16-byte-per-lane column load.
+//
+// Projector (emission-lib/_et.cpp:218-281): per camera and depth plane z,
+//   rotate (bilinear gather of activity and mu), per-plane separable PSF
+//   (row pass along x in a register sliding window over a shared tile, column
+//   pass along y with warp shuffles), attenuated depth scan T += mu;
+//   p += v * exp(-T).  No rotated volume is written anywhere: a thread-block
+//   cluster owns (camera, 32-column x-tile), its CTAs own depth slabs and
+//   merge (T, p) through distributed shared memory.
+// Backprojector, reference mode (emission-lib/_et.cpp:415-499):
+//   (1) per-slab transmission carries of the rotated mu, (2) per camera
+//   group: spread s*exp(-T) + PSF in the rotated frame into an L2-sized
+//   scratch, (3) inverse-rotation gather of the group into the accumulator.
+#pragma once
+
+#include "et_kernels.h"
+#include "et_profile.h"
+
+#include <cooperative_groups.h>
+#include <cuda_bf16.h>
+
+#include <algorithm>
+#include <cstring>
+#include <map>
+#include <mutex>
+#include <type_traits>
+#include <vector>
+
+namespace nrgb {
+
+namespace {
+
+namespace cg = cooperative_groups;
+
+constexpr int kW = 8;             // warps per CTA of the tile engine
+constexpr int kTXW = 4;           // output columns per warp
+constexpr int kTXC = kW * kTXW;   // output columns per CTA
+constexpr int kSlabsP = 4;        // depth slabs (= cluster size) of the batched projector
+constexpr int kSlabsB = 16;       // backprojector depth slabs
+constexpr int kCarrySlots = kSlabsB + 1;  // carries per camera: slab prefixes, column total
+constexpr int kCarryCols = 64 / kSlabsB;  // columns per CTA of the carry pass (32 KB of slab sums)
+constexpr int kGatherWarps = 4;   // warps per CTA of the inverse-rotation gather
+constexpr int kGatherCols = 2;    // accumulator columns per warp in the gather
+constexpr unsigned kFull = 0xffffffffu;
+
+__device__ __forceinline__ float fm(float a, float b) { return __fmul_rn(a, b); }
+__device__ __forceinline__ float fa(float a, float b) { return __fadd_rn(a, b); }
+
+// Bilinear footprint of one sampled column.  Corner (a, c) sits at
+// off + a*dx + c*dz; corners outside the grid get weight 0 and a clamped
+// (valid) address, so loads never leave the volume.
+struct __align__(16) Tap {
+  int off, dx, dz, any;
+  float w00, w10, w01, w11;
+};
+
+// Footprint of rotated column (xp, zp) under rows (m00, m02, m03) -> x and
+// (m20, m22, m23) -> z.  Position arithmetic follows
+// reg-lib/_reg_affineTransformation.cpp:116-132 (the y terms are exact zeros
+// for a y-gantry), floor/relative/basis follow reg-lib/_reg_resampling.cpp:347-364.
+__device__ __forceinline__ Tap make_tap(int xp, int zp, float m00, float m02, float m03, float m20, float m22,
+                                        float m23, int nx, int nz, int cy, bool col_valid) {
+  const float fx = static_cast<float>(xp), fz = static_cast<float>(zp);
+  const float px = fa(fa(fm(m00, fx), fm(m02, fz)), m03);
+  const float pz = fa(fa(fm(m20, fx), fm(m22, fz)), m23);
+  const int xs = static_cast<int>(floorf(px));
+  const int zs = static_cast<int>(floorf(pz));
+  float rx = __fsub_rn(px, static_cast<float>(xs));
+  float rz = __fsub_rn(pz, static_cast<float>(zs));
+  if (rx < 0.0f) rx = 0.0f;
+  if (rz < 0.0f) rz = 0.0f;
+  const float wx0 = __fsub_rn(1.0f, rx), wx1 = rx, wz0 = __fsub_rn(1.0f, rz), wz1 = rz;
+  const bool x0 = col_valid && xs >= 0 && xs < nx;
+  const bool x1 = col_valid && xs + 1 >= 0 && xs + 1 < nx;
+  const bool z0 = col_valid && zs >= 0 && zs < nz;
+  const bool z1 = col_valid && zs + 1 >= 0 && zs + 1 < nz;
+  Tap t;
+  const int xb = x0 ? xs : (x1 ? xs + 1 : 0);
+  const int zb = z0 ? zs : (z1 ? zs + 1 : 0);
+  t.off = (zb * nx + xb) * cy;
+  t.dx = (x0 && x1) ? cy : 0;
+  t.dz = (z0 && z1) ? nx * cy : 0;
+  t.w00 = (x0 && z0) ? wx0 * wz0 : 0.0f;
+  t.w10 = (x1 && z0) ? wx1 * wz0 : 0.0f;
+  t.w01 = (x0 && z1) ? wx0 * wz1 : 0.0f;
+  t.w11 = (x1 && z1) ? wx1 * wz1 : 0.0f;
+  t.any = (x0 || x1) && (z0 || z1);
+  return t;
+}
+
+__device__ __forceinline__ float4 ldg4(const float* p) { return __ldg(reinterpret_cast<const float4*>(p)); }
+
+// Four consecutive rows of a bfloat16 column (8 bytes, 8-byte aligned since
+// cy and the lane's first row are multiples of 4), widened to float32: a
+// bfloat16 is the high half of the float32 with the same value.
+__device__ __forceinline__ float4 ldg4(const __nv_bfloat16* p) {
+  const uint2 u = __ldg(reinterpret_cast<const uint2*>(p));
+  return make_float4(__uint_as_float(u.x << 16), __uint_as_float(u.x & 0xffff0000u), __uint_as_float(u.y << 16),
+                     __uint_as_float(u.y & 0xffff0000u));
+}
+
+template <class V>
+__device__ __forceinline__ float4 sample4(const V* __restrict__ base, const Tap& t, int yb, bool yok) {
+  float4 r = make_float4(0.f, 0.f, 0.f, 0.f);
+  if (!t.any || !yok) return r;
+  const V* p = base + t.off + yb;
+  const float4 a = ldg4(p), b = ldg4(p + t.dx), c = ldg4(p + t.dz), d = ldg4(p + t.dx + t.dz);
+  r.x = fmaf(d.x, t.w11, fmaf(c.x, t.w01, fmaf(b.x, t.w10, a.x * t.w00)));
+  r.y = fmaf(d.y, t.w11, fmaf(c.y, t.w01, fmaf(b.y, t.w10, a.y * t.w00)));
+  r.z = fmaf(d.z, t.w11, fmaf(c.z, t.w01, fmaf(b.z, t.w10, a.z * t.w00)));
+  r.w = fmaf(d.w, t.w11, fmaf(c.w, t.w01, fmaf(b.w, t.w10, a.w * t.w00)));
+  return r;
+}
+
+__device__ __forceinline__ float comp(const float4& v, int c) { return c == 0 ? v.x : c == 1 ? v.y : c == 2 ? v.z : v.w; }
+
+__device__ __forceinline__ void axpy4(float4& acc, float k, const float4& v) {
+  acc.x = fmaf(k, v.x, acc.x);
+  acc.y = fmaf(k, v.y, acc.y);
+  acc.z = fmaf(k, v.z, acc.z);
+  acc.w = fmaf(k, v.w, acc.w);
+}
+
+// Rows y >= ny are zero pads of the column layout; the column pass must not
+// leak into them (the reference's column pass only produces rows < ny).
+__device__ __forceinline__ float4 mask_rows(float4 v, int yb, int ny) {
+  if (yb + 0 >= ny) v.x = 0.0f;
+  if (yb + 1 >= ny) v.y = 0.0f;
+  if (yb + 2 >= ny) v.z = 0.0f;
+  if (yb + 3 >= ny) v.w = 0.0f;
+  return v;
+}
+
+// Column (y) pass of the per-plane convolution for the 4 rows a lane owns:
+// out[y] = sum_k in[y+k] * kc[R-k], zero outside [0, ny) (rows >= ny are zero
+// pads, rows < 0 come from lanes below 0 and are masked).  Neighbour rows come
+// from lanes l-1, l-2 and l+1, l+2 by shuffles.
+template <int R, class KC>
+__device__ __forceinline__ float4 yconv4(const float4& u, KC kc, int lane) {
+  float w[2 * R + 4];
+  w[R + 0] = u.x;
+  w[R + 1] = u.y;
+  w[R + 2] = u.z;
+  w[R + 3] = u.w;
+#pragma unroll
+  for (int t = 1; t <= R; ++t) {
+    const int dl = (t + 3) / 4;
+    const float s = __shfl_up_sync(kFull, comp(u, 4 * dl - t), dl);
+    w[R - t] = (lane >= dl) ? s : 0.0f;
+  }
+#pragma unroll
+  for (int t = 1; t <= R; ++t) {
+    const int dl = (t + 3) / 4;
+    const float s = __shfl_down_sync(kFull, comp(u, t + 3 - 4 * dl), dl);
+    w[R + 3 + t] = (lane + dl < 32) ? s : 0.0f;
+  }
+  float4 o = make_float4(0.f, 0.f, 0.f, 0.f);
+#pragma unroll
+  for (int k = -R; k <= R; ++k) {
+    const float kk = kc[R - k];
+    o.x = fmaf(w[R + 0 + k], kk, o.x);
+    o.y = fmaf(w[R + 1 + k], kk, o.y);
+    o.z = fmaf(w[R + 2 + k], kk, o.z);
+    o.w = fmaf(w[R + 3 + k], kk, o.w);
+  }
+  return o;
+}
+
+__device__ __forceinline__ float4 exp_neg4(const float4& t) {
+  return make_float4(__expf(-t.x), __expf(-t.y), __expf(-t.z), __expf(-t.w));
+}
+
+__device__ __forceinline__ void add4(float4& a, const float4& b) {
+  a.x += b.x;
+  a.y += b.y;
+  a.z += b.z;
+  a.w += b.w;
+}
+
+__device__ __forceinline__ void fma4(float4& acc, const float4& a, const float4& b) {
+  acc.x = fmaf(a.x, b.x, acc.x);
+  acc.y = fmaf(a.y, b.y, acc.y);
+  acc.z = fmaf(a.z, b.z, acc.z);
+  acc.w = fmaf(a.w, b.w, acc.w);
+}
+
+__device__ __forceinline__ float4 mul4(const float4& a, const float4& b) {
+  return make_float4(a.x * b.x, a.y * b.y, a.z * b.z, a.w * b.w);
+}
+
+// Compensated summation (Kahan, CACM 8(1):40, 1965): s + (-c) tracks the
+// exact sum of the added terms far better than s alone; c holds the rounding
+// excess of the previous additions.  Each operation rounds separately.
+__device__ __forceinline__ void kahan_add(float& s, float& c, float v) {
+  const float y = __fsub_rn(v, c);
+  const float t = __fadd_rn(s, y);
+  c = __fsub_rn(__fsub_rn(t, s), y);
+  s = t;
+}
+
+__device__ __forceinline__ void kahan_add4(float4& s, float4& c, const float4& v) {
+  kahan_add(s.x, c.x, v.x);
+  kahan_add(s.y, c.y, v.y);
+  kahan_add(s.z, c.z, v.z);
+  kahan_add(s.w, c.w, v.w);
+}
+
+// Compensated value of a Kahan pair.
+__device__ __forceinline__ float4 kahan_value4(const float4& s, const float4& c) {
+  return make_float4(__fsub_rn(s.x, c.x), __fsub_rn(s.y, c.y), __fsub_rn(s.z, c.z), __fsub_rn(s.w, c.w));
+}
+
+// Depth sum s += v: plain float32 (the reference's order) or compensated.
+template <bool KAHAN>
+__device__ __forceinline__ void depth_add4(float4& s, float4& c, const float4& v) {
+  if (KAHAN)
+    kahan_add4(s, c, v);
+  else
+    add4(s, v);
+}
+
+template <bool KAHAN>
+__device__ __forceinline__ float4 depth_value4(const float4& s, const float4& c) {
+  return KAHAN ? kahan_value4(s, c) : s;
+}
+
+// Storage type of the sampled volumes; bfloat16 storage sums with Kahan.
+template <class V>
+struct StorageTraits {
+  static constexpr bool kKahan = false;
+};
+template <>
+struct StorageTraits<__nv_bfloat16> {
+  static constexpr bool kKahan = true;
+};
+
+struct CamRows {
+  float m00, m02, m03, m20, m22, m23;
+};
+
+__device__ __forceinline__ CamRows cam_rows(const float* m) {
+  CamRows c;
+  c.m00 = __ldg(m + 0);
+  c.m02 = __ldg(m + 2);
+  c.m03 = __ldg(m + 3);
+  c.m20 = __ldg(m + 8);
+  c.m22 = __ldg(m + 10);
+  c.m23 = __ldg(m + 11);
+  return c;
+}
+
+// Separated PSF of every plane ([nz][2K]: row kernel, then column kernel)
+// passed as a kernel parameter: the coefficients are read from the constant
+// bank with uniform addresses (no shared-memory copy, no load instruction per
+// use in the row and column passes).  Tables larger than this use the shared
+// memory copy.
+constexpr int kPsfTableFloats = 7680;
+struct PsfTable {
+  float c[kPsfTableFloats];
+};
+
+// A row kernel read backwards (k -> p[2R - k]): a mirror camera's row pass.
+template <int R>
+struct Reversed {
+  const float* p;
+  __device__ __forceinline__ float operator[](int k) const { return p[2 * R - k]; }
+};
+
+// ------------------------------------------------------------ tile engine
+// A CTA of kW warps owns kTXC = kW * kTXW consecutive output columns of one
+// camera and walks one depth slab.  At every depth step the NS = kTXC + 2R
+// sampled columns (outputs plus the PSF row halo) are produced once per CTA
+// -- column c by warp c % kW -- into a double-buffered shared tile; after one
+// barrier each warp runs the row pass (register sliding window over its
+// kTXW + 2R tile columns), the column pass and its consumer for its kTXW
+// outputs.  Writes of step z+1 go to the other buffer, so one barrier per
+// step suffices.
+template <int R>
+struct TileShape {
+  static constexpr int NS = kTXC + 2 * R;            // sampled columns per CTA
+  static constexpr int kOwn = (NS + kW - 1) / kW;    // sampled columns per warp (max)
+  static constexpr int kTapSlots = kW * kOwn;         // footprint slots per stage (see tap_slot)
+  static constexpr size_t kSbBytes = sizeof(float4) * 2 * NS * 32;
+  static constexpr size_t kTapBytes = sizeof(Tap) * 2 * kTapSlots;
+  // Projector with a mirror camera: the tile region also holds the three
+  // slab-merge buffers (T, P and the mirror camera's P per output column).
+  static constexpr size_t kSbBytesPair = sizeof(float4) * 32 * (2 * NS > 3 * kTXC ? 2 * NS : 3 * kTXC);
+  __host__ __device__ static constexpr size_t sb_bytes(bool pair) { return pair ? kSbBytesPair : kSbBytes; }
+};
+
+// Footprint slot of sampled column c in the tap buffer: the columns one warp
+// computes (c = warp + kW * k) sit next to each other, so the footprint
+// stores of a warp do not collide in shared-memory banks.
+template <int R>
+__device__ __forceinline__ int tap_slot(int c) {
+  return (c % kW) * TileShape<R>::kOwn + c / kW;
+}
+
+// Tile, footprints and the separated PSF of nz planes (twice with a mirror
+// camera: its kernels are the mirrored planes, row kernels reversed).
+template <int R>
+__host__ __device__ constexpr size_t tile_smem_bytes(int nz, bool pair = false) {
+  return TileShape<R>::sb_bytes(pair) + TileShape<R>::kTapBytes +
+         sizeof(float) * static_cast<size_t>(nz) * 2 * (2 * R + 1) * (pair ? 2 : 1);
+}
+
+// Row pass from the shared tile: outputs i = 0..kTXW-1 of this warp use tile
+// columns base + i .. base + i + 2R (base = warp * kTXW).
+template <int R, class EmitFn, class KR, class KC>
+__device__ __forceinline__ void rowpass_from_tile(const float4* __restrict__ sbuf, int base, EmitFn emit, KR kr, KC kc,
+                                                  int lane, int ny) {
+  constexpr int K = 2 * R + 1;
+  constexpr int NJ = kTXW + 2 * R;
+  float4 u[K];
+#pragma unroll
+  for (int q = 0; q < K; ++q) u[q] = make_float4(0.f, 0.f, 0.f, 0.f);
+#pragma unroll
+  for (int j = 0; j < NJ; ++j) {
+    const float4 r = sbuf[(base + j) * 32 + lane];
+#pragma unroll
+    for (int d = 0; d < K; ++d) {
+      const int i = j - d;
+      if (i >= 0 && i < kTXW) axpy4(u[i % K], kr[2 * R - d], r);
+    }
+    const int i = j - 2 * R;
+    if (i >= 0 && i < kTXW) {
+      emit(i, mask_rows(yconv4<R>(u[i % K], kc, lane), 4 * lane, ny));
+      u[i % K] = make_float4(0.f, 0.f, 0.f, 0.f);
+    }
+  }
+}
+
+// Row passes of two cameras over the same tile (a camera and its mirror
+// camera): each tile column is read once and feeds both sliding windows;
+// output i of camera b is emitted before output i of camera a.
+template <int R, class EmitA, class EmitB, class KRA, class KCA, class KRB, class KCB>
+__device__ __forceinline__ void rowpass2_from_tile(const float4* __restrict__ sbuf, int base, EmitA emit_a, KRA kra,
+                                                   KCA kca, EmitB emit_b, KRB krb, KCB kcb, int lane, int ny) {
+  constexpr int NJ = kTXW + 2 * R;
+  float4 ua[kTXW], ub[kTXW];
+#pragma unroll
+  for (int q = 0; q < kTXW; ++q) {
+    ua[q] = make_float4(0.f, 0.f, 0.f, 0.f);
+    ub[q] = make_float4(0.f, 0.f, 0.f, 0.f);
+  }
+#pragma unroll
+  for (int j = 0; j < NJ; ++j) {
+    const float4 r = sbuf[(base + j) * 32 + lane];
+#pragma unroll
+    for (int d = 0; d <= 2 * R; ++d) {
+      const int i = j - d;
+      if (i >= 0 && i < kTXW) {
+        axpy4(ua[i], kra[2 * R - d], r);
+        axpy4(ub[i], krb[2 * R - d], r);
+      }
+    }
+    const int i = j - 2 * R;
+    if (i >= 0 && i < kTXW) {
+      emit_b(i, mask_rows(yconv4<R>(ub[i], kcb, lane), 4 * lane, ny));
+      emit_a(i, mask_rows(yconv4<R>(ua[i], kca, lane), 4 * lane, ny));
+    }
+  }
+}
+
+// ---------------------------------------------------------------- projector
+// Row windows: a column holds cy >= ny rows, the kernels see one window of at
+// most 128 rows at a time: rows [row0, row0 + ny) of the columns (row0 a
+// multiple of 4, so lane loads stay aligned), valid output rows [out_lo,
+// out_hi) relative to row0.  Rows past a window's end read as zero (lanes past
+// round_up(ny, 4) sample nothing; the rows inside the last lane are the zero
+// pads of the column layout at the volume's end, the only place a window
+// ends off a multiple of 4).
+__device__ __forceinline__ bool lane_rows_ok(const YgArgs& a, int yb) { return yb < ((a.ny + 3) & ~3); }
+__device__ __forceinline__ bool lane_writes(const YgArgs& a, int yb) { return yb >= a.out_lo && yb < a.out_hi; }
+
+// One projector work item: camera `cam`, output columns x0 .. x0 + kTXC - 1;
+// the CTAs of the cluster walk the depth slabs and merge (T, p) through
+// distributed shared memory: p = p0 + exp(-T0) p1 + exp(-T0-T1) p2 + ...
+// V: storage type of activity and mu (float or bfloat16; bfloat16 sums with
+// Kahan).  Ends with a cluster barrier, after which the shared memory may be
+// reused.
+//
+// Mirror camera (PAIR, mate >= 0): a camera at the opposite angle (theta + pi)
+// about the grid centre samples the same points: its rotated volume is this
+// camera's mirrored in x and z (column x of depth z is its column nx-1-x of
+// depth nz-1-z).  The CTA then serves both from one set of bilinear samples:
+// the mate's row pass uses the PSF plane nz-1-z with the row kernel reversed,
+// its depth sum runs towards this camera, and its slab partial
+//   q = sum_z v'_z exp(-(S - E_z)) = exp(-S) sum_z v'_z exp(E_z)
+// (S the slab's mu sum, E_z the sum before plane z) is accumulated in the
+// forward walk as sum v' exp(E).  A slab whose mu sum exceeds kMateMaxT (or
+// whose sum overflows) is redone for the mate alone by a descending walk with
+// the direct weights.  The mate's slabs merge in the opposite order.
+constexpr float kMateMaxT = 40.0f;
+
+template <int R, bool PSF, bool ATT, class V, bool PAIR = false, bool PTAB = false>
+__device__ __forceinline__ void project_item(const YgArgs& a, int cam, int mate, int x0, unsigned char* smem,
+                                             const float* ptab = nullptr) {
+  using TS = TileShape<R>;
+  constexpr bool KAHAN = StorageTraits<V>::kKahan;
+  static_assert(!(PAIR && KAHAN), "mirror cameras are served by the float32 projector");
+  const V* __restrict__ act = reinterpret_cast<const V*>(a.act) + a.row0;
+  const V* __restrict__ mu = reinterpret_cast<const V*>(a.mu) + a.row0;
+  constexpr int NS = TS::NS;
+  constexpr int K = 2 * R + 1;
+  constexpr size_t kSb = TS::sb_bytes(PAIR);
+  float4* sb = reinterpret_cast<float4*>(smem);                    // [2][NS][32]
+  Tap* taps = reinterpret_cast<Tap*>(smem + kSb);                   // [2][kTapSlots]
+  float* s_psf = reinterpret_cast<float*>(smem + kSb + TS::kTapBytes);  // [nz][2K]
+  float* s_psf_m = s_psf + static_cast<size_t>(a.nz) * 2 * K;       // [nz][2K] (mate)
+
+  cg::cluster_group cluster = cg::this_cluster();
+  const int slab = static_cast<int>(cluster.block_rank());
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int yb = lane * 4;
+  const bool yok = lane_rows_ok(a, yb);
+  const bool paired = PAIR && mate >= 0;  // uniform over the cluster
+
+  const int nslabs = static_cast<int>(cluster.num_blocks());  // depth slabs = cluster size (2, 4 or 8)
+  const int zper = (a.nz + nslabs - 1) / nslabs;
+  const int zbeg = slab * zper, zend = min(a.nz, zbeg + zper);
+  if (PSF && !PTAB) {  // this slab's planes only
+    for (int i = zbeg * 2 * K + threadIdx.x; i < zend * 2 * K; i += blockDim.x) s_psf[i] = __ldg(a.psf + i);
+    if (paired) {
+      for (int i = zbeg * 2 * K + threadIdx.x; i < zend * 2 * K; i += blockDim.x) {
+        const int z = i / (2 * K), j = i % (2 * K);
+        s_psf_m[i] = __ldg(a.psf + (a.nz - 1 - z) * 2 * K + (j < K ? K - 1 - j : j));
+      }
+    }
+  }
+  // row and column kernels of plane z for this camera and for the mate
+  // (plane nz-1-z, row kernel reversed)
+  auto mate_pass = [&](const float4* sbuf, int z, auto emit_m) {
+    if constexpr (PTAB) {
+      const float* m = ptab + (a.nz - 1 - z) * 2 * K;
+      rowpass_from_tile<R>(sbuf, warp * kTXW, emit_m, Reversed<R>{m}, m + K, lane, a.ny);
+    } else {
+      const float* m = s_psf_m + z * 2 * K;
+      rowpass_from_tile<R>(sbuf, warp * kTXW, emit_m, m, m + K, lane, a.ny);
+    }
+  };
+  auto both_pass = [&](const float4* sbuf, int z, auto emit, auto emit_m) {
+    const float* kr = (PTAB ? ptab : s_psf) + z * 2 * K;
+    if constexpr (PTAB) {
+      const float* m = ptab + (a.nz - 1 - z) * 2 * K;
+      rowpass2_from_tile<R>(sbuf, warp * kTXW, emit, kr, kr + K, emit_m, Reversed<R>{m}, m + K, lane, a.ny);
+    } else {
+      const float* m = s_psf_m + z * 2 * K;
+      rowpass2_from_tile<R>(sbuf, warp * kTXW, emit, kr, kr + K, emit_m, m, m + K, lane, a.ny);
+    }
+  };
+  const CamRows cr = cam_rows(a.geom[cam].fwd);
+
+  float4 T[kTXW], P[kTXW], cT[kTXW], cP[kTXW];  // c*: Kahan compensations (KAHAN only)
+  float4 Q[PAIR ? kTXW : 1];                    // mate's slab partial
+#pragma unroll
+  for (int i = 0; i < kTXW; ++i) {
+    T[i] = make_float4(0.f, 0.f, 0.f, 0.f);
+    P[i] = make_float4(0.f, 0.f, 0.f, 0.f);
+    cT[i] = make_float4(0.f, 0.f, 0.f, 0.f);
+    cP[i] = make_float4(0.f, 0.f, 0.f, 0.f);
+    if (PAIR) Q[i] = make_float4(0.f, 0.f, 0.f, 0.f);
+  }
+  __syncthreads();
+
+  // One depth step at plane z into tile buffer b.  MODE 0: this camera (and
+  // the mate's forward form); MODE 1: the mate alone, direct weights (walked
+  // from the slab's far end).
+  auto step = [&](int z, int b, auto mode) {
+    constexpr int MODE = decltype(mode)::value;
+    float4* sbuf = sb + b * NS * 32;
+    Tap* tb = taps + b * TS::kTapSlots;
+    // footprints of the columns this warp samples (c = warp + kW * k)
+    if (lane < TS::kOwn) {
+      const int c = warp + kW * lane;
+      if (c < NS) {
+        const int xp = x0 - R + c;
+        tb[tap_slot<R>(c)] = make_tap(xp, z, cr.m00, cr.m02, cr.m03, cr.m20, cr.m22, cr.m23, a.nx, a.nz, a.cy,
+                                      xp >= 0 && xp < a.nx);
+      }
+    }
+    __syncwarp();
+#pragma unroll
+    for (int k = 0; k < TS::kOwn; ++k) {
+      const int c = warp + kW * k;
+      if (c < NS) sbuf[c * 32 + lane] = sample4(act, tb[tap_slot<R>(c)], yb, yok);
+    }
+    __syncthreads();
+    auto emit_m = [&](int i, const float4& v) {
+      if (!ATT) {
+        add4(Q[i], v);
+      } else if (MODE == 0) {  // weight exp(E_z): T holds the sum before plane z
+        fma4(Q[i], v, exp_neg4(make_float4(-T[i].x, -T[i].y, -T[i].z, -T[i].w)));
+      } else {  // T runs from the slab's far end, inclusive
+        add4(T[i], sample4(mu, tb[tap_slot<R>(warp * kTXW + i + R)], yb, yok));
+        fma4(Q[i], v, exp_neg4(T[i]));
+      }
+    };
+    if (MODE == 1) {
+      if (PSF) {
+        mate_pass(sbuf, z, emit_m);
+      } else {
+#pragma unroll
+        for (int i = 0; i < kTXW; ++i) emit_m(i, sbuf[(warp * kTXW + i) * 32 + lane]);
+      }
+      return;
+    }
+    auto emit = [&](int i, const float4& v) {
+      if (ATT) {
+        const float4 m = sample4(mu, tb[tap_slot<R>(warp * kTXW + i + R)], yb, yok);
+        if (KAHAN) {
+          kahan_add4(T[i], cT[i], m);
+          kahan_add4(P[i], cP[i], mul4(v, exp_neg4(kahan_value4(T[i], cT[i]))));
+        } else {
+          add4(T[i], m);
+          fma4(P[i], v, exp_neg4(T[i]));
+        }
+      } else {
+        depth_add4<KAHAN>(P[i], cP[i], v);
+      }
+    };
+    if (PSF) {
+      if (PAIR && paired) {
+        both_pass(sbuf, z, emit, emit_m);
+      } else {
+        const float* kr = (PTAB ? ptab : s_psf) + z * 2 * K;
+        rowpass_from_tile<R>(sbuf, warp * kTXW, emit, kr, kr + K, lane, a.ny);
+      }
+    } else {
+#pragma unroll
+      for (int i = 0; i < kTXW; ++i) {
+        const float4 v = sbuf[(warp * kTXW + i) * 32 + lane];
+        if (PAIR && paired) emit_m(i, v);
+        emit(i, v);
+      }
+    }
+  };
+
+  for (int z = zbeg; z < zend; ++z) step(z, z & 1, std::integral_constant<int, 0>());
+
+  if (PAIR && paired && ATT) {
+    bool redo = false;
+#pragma unroll
+    for (int i = 0; i < kTXW; ++i) {
+      redo |= !(T[i].x <= kMateMaxT && T[i].y <= kMateMaxT && T[i].z <= kMateMaxT && T[i].w <= kMateMaxT);
+      redo |= !(isfinite(Q[i].x) && isfinite(Q[i].y) && isfinite(Q[i].z) && isfinite(Q[i].w));
+    }
+    if (__syncthreads_or(redo)) {  // uniform over the CTA
+#pragma unroll
+      for (int i = 0; i < kTXW; ++i) {
+        Q[i] = make_float4(0.f, 0.f, 0.f, 0.f);
+        T[i] = make_float4(0.f, 0.f, 0.f, 0.f);  // ends at the slab sum again
+      }
+      for (int k = 0; k < zend - zbeg; ++k) step(zend - 1 - k, k & 1, std::integral_constant<int, 1>());
+    } else {
+#pragma unroll
+      for (int i = 0; i < kTXW; ++i) Q[i] = mul4(Q[i], exp_neg4(T[i]));
+    }
+  }
+
+  // cluster merge of the depth slabs (the shared tile is free after this barrier)
+  __syncthreads();
+  float4* sT = sb;                // [kTXC][32]
+  float4* sP = sb + kTXC * 32;    // [kTXC][32]
+  float4* sQ = sb + 2 * kTXC * 32;  // [kTXC][32] (PAIR)
+#pragma unroll
+  for (int i = 0; i < kTXW; ++i) {
+    sT[(warp * kTXW + i) * 32 + lane] = depth_value4<KAHAN>(T[i], cT[i]);
+    sP[(warp * kTXW + i) * 32 + lane] = depth_value4<KAHAN>(P[i], cP[i]);
+    if (PAIR && paired) sQ[(warp * kTXW + i) * 32 + lane] = Q[i];
+  }
+  cluster.sync();
+  const int per_rank = kTXC / nslabs;  // outputs merged by each CTA of the cluster
+  auto store = [&](int c, int x, float4 Pt) {
+    if (a.truncate) {
+      Pt.x = fmaxf(Pt.x, 0.f);
+      Pt.y = fmaxf(Pt.y, 0.f);
+      Pt.z = fmaxf(Pt.z, 0.f);
+      Pt.w = fmaxf(Pt.w, 0.f);
+    }
+    *reinterpret_cast<float4*>(a.out + (static_cast<size_t>(c) * a.nx + x) * a.cy + a.row0 + yb) = Pt;
+  };
+#pragma unroll
+  for (int i = 0; i < kTXW; ++i) {
+    const int o = warp * kTXW + i;
+    const int x = x0 + o;
+    if (o / per_rank != slab || x >= a.nx || !yok || !lane_writes(a, yb)) continue;
+    float4 Pt = make_float4(0.f, 0.f, 0.f, 0.f), Tt = make_float4(0.f, 0.f, 0.f, 0.f);
+    for (int s = 0; s < nslabs; ++s) {
+      const float4* rT = cluster.map_shared_rank(sT, s);
+      const float4* rP = cluster.map_shared_rank(sP, s);
+      const float4 ps = rP[o * 32 + lane];
+      if (ATT) {
+        fma4(Pt, exp_neg4(Tt), ps);
+        add4(Tt, rT[o * 32 + lane]);
+      } else {
+        add4(Pt, ps);
+      }
+    }
+    store(cam, x, Pt);
+    if (PAIR && paired) {  // the mate's slabs from the far end: its column nx-1-x
+      Pt = make_float4(0.f, 0.f, 0.f, 0.f);
+      Tt = make_float4(0.f, 0.f, 0.f, 0.f);
+      for (int s = nslabs - 1; s >= 0; --s) {
+        const float4 qs = cluster.map_shared_rank(sQ, s)[o * 32 + lane];
+        if (ATT) {
+          fma4(Pt, exp_neg4(Tt), qs);
+          add4(Tt, cluster.map_shared_rank(sT, s)[o * 32 + lane]);
+        } else {
+          add4(Pt, qs);
+        }
+      }
+      store(mate, a.nx - 1 - x, Pt);
+    }
+  }
+  cluster.sync();  // keep this CTA's shared memory alive until the others have read it
+}
+
+constexpr int kWindowRows = 128;  // rows one warp covers (32 lanes x 4)
+
+// Row windows of a volume for a PSF halo: window starts and valid ranges are
+// multiples of 4 (the halo is rounded up), every row is valid in exactly one
+// window, and a valid row's whole PSF support lies inside its window or past
+// the volume's edge.  Y-gantry rotations keep y, so a window computes its
+// valid rows with exactly the arithmetic of a single pass.
+struct Window {
+  int row0, rows, lo, hi;  // rows [row0, row0 + rows); valid [row0 + lo, row0 + hi)
+};
+
+std::vector<Window> row_windows(int ny, int halo) {
+  const int h = (halo + 3) & ~3;
+  std::vector<Window> w;
+  if (ny <= kWindowRows) {
+    w.push_back({0, ny, 0, ny});
+    return w;
+  }
+  int out0 = 0;
+  while (out0 < ny) {
+    const int in0 = std::max(0, out0 - h);
+    if (in0 + kWindowRows >= ny) {
+      w.push_back({in0, ny - in0, out0 - in0, ny - in0});
+      break;
+    }
+    const int out1 = in0 + kWindowRows - h;
+    w.push_back({in0, kWindowRows, out0 - in0, out1 - in0});
+    out0 = out1;
+  }
+  return w;
+}
+
+YgArgs windowed(const YgArgs& a, const Window& w) {
+  YgArgs b = a;
+  b.row0 = w.row0;
+  b.ny = w.rows;
+  b.out_lo = w.lo;
+  b.out_hi = w.hi;
+  b.cs = round_up(w.rows, 4);
+  return b;
+}
+
+int scratch_rows(int ny) { return round_up(std::min(ny, kWindowRows), 4); }
+
+}  // namespace
+}  // namespace nrgb
