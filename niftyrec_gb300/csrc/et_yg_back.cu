@@ -96,8 +96,10 @@ __device__ __forceinline__ void scatter4(float* __restrict__ base, const Tap& t,
 // (vector reductions; all cameras in one launch, no scratch).
 // CTAS: CTAs per SM the kernel is compiled for (3 where three tiles fit in
 // shared memory, for the float32 reference spread; else 2).
-template <int R, bool PSF, bool ATT, bool ADJ, class V, int CTAS = 2>
-__global__ void __launch_bounds__(32 * kW, CTAS) k_spread_yg(const YgArgs a, int c0) {
+// PTAB: the separated PSF comes from the kernel-parameter table `ptab`
+// ([nz][2K]) instead of a shared-memory copy of the slab's planes.
+template <int R, bool PSF, bool ATT, bool ADJ, class V, bool PTAB>
+__device__ __forceinline__ void spread_body(const YgArgs& a, int c0, const float* ptab) {
   using TS = TileShape<R>;
   constexpr bool KAHAN = StorageTraits<V>::kKahan;
   const V* __restrict__ mu = reinterpret_cast<const V*>(a.mu) + a.row0;
@@ -120,7 +122,7 @@ __global__ void __launch_bounds__(32 * kW, CTAS) k_spread_yg(const YgArgs a, int
   const int zper = (a.nz + kSlabsB - 1) / kSlabsB;
   const int zbeg = slab * zper, zend = min(a.nz, zbeg + zper);
   if (zbeg >= zend) return;  // uniform over the CTA
-  if (PSF) {  // this slab's planes only
+  if (PSF && !PTAB) {  // this slab's planes only
     for (int i = zbeg * 2 * K + threadIdx.x; i < zend * 2 * K; i += blockDim.x) {
       const int j = i % (2 * K), base = i - j;
       // transpose of a convolution = correlation: reverse each kernel
@@ -183,13 +185,29 @@ __global__ void __launch_bounds__(32 * kW, CTAS) k_spread_yg(const YgArgs a, int
       }
     };
     if (PSF) {
-      const float* kr = s_psf + z * 2 * K;
-      rowpass_from_tile<R>(sbuf, warp * kTXW, emit, kr, kr + K, lane, a.ny);
+      if constexpr (PTAB && ADJ) {  // transpose of a convolution = correlation: both kernels reversed
+        const float* kr = ptab + z * 2 * K;
+        rowpass_from_tile<R>(sbuf, warp * kTXW, emit, Reversed<R>{kr}, Reversed<R>{kr + K}, lane, a.ny);
+      } else {
+        const float* kr = (PTAB ? ptab : s_psf) + z * 2 * K;
+        rowpass_from_tile<R>(sbuf, warp * kTXW, emit, kr, kr + K, lane, a.ny);
+      }
     } else {
 #pragma unroll
       for (int i = 0; i < kTXW; ++i) emit(i, sbuf[(warp * kTXW + i) * 32 + lane]);
     }
   }
+}
+
+template <int R, bool PSF, bool ATT, bool ADJ, class V, int CTAS = 2>
+__global__ void __launch_bounds__(32 * kW, CTAS) k_spread_yg(const YgArgs a, int c0) {
+  spread_body<R, PSF, ATT, ADJ, V, false>(a, c0, nullptr);
+}
+
+template <int R, bool ATT, bool ADJ, class V, int CTAS = 2>
+__global__ void __launch_bounds__(32 * kW, CTAS)
+    k_spread_ptab_yg(const YgArgs a, int c0, const __grid_constant__ PsfTable t) {
+  spread_body<R, true, ATT, ADJ, V, true>(a, c0, t.c);
 }
 
 // Reference-mode spread of a mirror unit -- camera c and its mate m at the
@@ -203,8 +221,8 @@ __global__ void __launch_bounds__(32 * kW, CTAS) k_spread_yg(const YgArgs a, int
 // adds both cameras' terms: one mu scan, one scratch volume and one gather
 // per pair.  A unit without a mate spreads its camera alone.  CTA = (unit,
 // x-tile, depth slab); the PSF planes of the slab only sit in shared memory.
-template <int R, bool PSF, bool ATT>
-__global__ void __launch_bounds__(32 * kW, 2) k_spread_pair_yg(const YgArgs a, int u0) {
+template <int R, bool PSF, bool ATT, bool PTAB>
+__device__ __forceinline__ void spread_pair_body(const YgArgs& a, int u0, const float* ptab) {
   using TS = TileShape<R>;
   constexpr int NS = TS::NS;
   constexpr int K = 2 * R + 1;
@@ -230,7 +248,7 @@ __global__ void __launch_bounds__(32 * kW, 2) k_spread_pair_yg(const YgArgs a, i
   const int zbeg = slab * zper, zend = min(a.nz, zbeg + zper);
   if (zbeg >= zend) return;  // uniform over the CTA
   float* s_psf_m = s_psf + zper * 2 * K;
-  if (PSF) {
+  if (PSF && !PTAB) {
     for (int i = threadIdx.x; i < (zend - zbeg) * 2 * K; i += blockDim.x) {
       s_psf[i] = __ldg(a.psf + zbeg * 2 * K + i);
       if (paired) {
@@ -311,12 +329,17 @@ __global__ void __launch_bounds__(32 * kW, 2) k_spread_pair_yg(const YgArgs a, i
       *reinterpret_cast<float4*>(tmp + (static_cast<size_t>(z) * a.nx + x) * a.cs + yb) = v;
     };
     if (PSF) {
+      auto keep = [&](int i, const float4& v) { acc[i] = v; };
       if (paired) {
-        const float* km = s_psf_m + (z - zbeg) * 2 * K;
-        rowpass_from_tile<R>(sm, warp * kTXW, [&](int i, const float4& v) { acc[i] = v; }, km, km + K, lane,
-                             a.ny);
+        if constexpr (PTAB) {
+          const float* km = ptab + (a.nz - 1 - z) * 2 * K;
+          rowpass_from_tile<R>(sm, warp * kTXW, keep, Reversed<R>{km}, km + K, lane, a.ny);
+        } else {
+          const float* km = s_psf_m + (z - zbeg) * 2 * K;
+          rowpass_from_tile<R>(sm, warp * kTXW, keep, km, km + K, lane, a.ny);
+        }
       }
-      const float* kr = s_psf + (z - zbeg) * 2 * K;
+      const float* kr = PTAB ? ptab + z * 2 * K : s_psf + (z - zbeg) * 2 * K;
       rowpass_from_tile<R>(sc, warp * kTXW, write, kr, kr + K, lane, a.ny);
     } else {
 #pragma unroll
@@ -326,6 +349,17 @@ __global__ void __launch_bounds__(32 * kW, 2) k_spread_pair_yg(const YgArgs a, i
       }
     }
   }
+}
+
+template <int R, bool PSF, bool ATT>
+__global__ void __launch_bounds__(32 * kW, 2) k_spread_pair_yg(const YgArgs a, int u0) {
+  spread_pair_body<R, PSF, ATT, false>(a, u0, nullptr);
+}
+
+template <int R, bool ATT>
+__global__ void __launch_bounds__(32 * kW, 2)
+    k_spread_pair_ptab_yg(const YgArgs a, int u0, const __grid_constant__ PsfTable t) {
+  spread_pair_body<R, true, ATT, true>(a, u0, t.c);
 }
 
 // ------------------------------------ backprojector: inverse-rotation gather
@@ -372,21 +406,52 @@ __global__ void __launch_bounds__(32 * kGatherWarps) k_gather_yg(const YgArgs a,
   }
 }
 
+// The separated PSF of a.nz planes as a kernel-parameter table, or null when
+// it is not available on the host or does not fit.
+template <int R>
+const PsfTable* psf_table(const YgArgs& a) {
+  if (!a.psf || !a.psf_host || static_cast<size_t>(a.nz) * 2 * (2 * R + 1) > kPsfTableFloats) return nullptr;
+  static thread_local PsfTable table;
+  std::memcpy(table.c, a.psf_host, sizeof(float) * a.nz * 2 * (2 * R + 1));
+  return &table;
+}
+
 template <int R, bool ADJ>
 int launch_spread_R(const YgArgs& a, int c0, int gcount, cudaStream_t st) {
   const int ntile = (a.nx + kTXC - 1) / kTXC;
   const dim3 grid(gcount * ntile * kSlabsB), block(32 * kW);
   const bool psf = a.psf != nullptr;
-  const size_t smem = tile_smem_bytes<R>(psf ? a.nz : 0);
+  const PsfTable* tab = psf_table<R>(a);
+  const size_t smem = tile_smem_bytes<R>(psf && !tab ? a.nz : 0);
   auto go = [&](auto k) {
     cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
     NRGB_LAUNCH_SCOPE(ADJ ? "k_adjoint_yg" : "k_spread_yg", st);
     k<<<grid, block, smem, st>>>(a, c0);
   };
+  auto go_tab = [&](auto k) {
+    cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
+    NRGB_LAUNCH_SCOPE(ADJ ? "k_adjoint_yg" : "k_spread_yg", st);
+    k<<<grid, block, smem, st>>>(a, c0, *tab);
+  };
   // only mu is sampled from storage here (the sinogram is float32)
   const bool bf16 = a.storage == kStorageBF16;
   const bool three = 3 * (smem + 1024) <= 228 * 1024;
-  if (psf) {
+  if (psf && tab) {
+    if (a.mu && bf16) {
+      go_tab(k_spread_ptab_yg<R, true, ADJ, __nv_bfloat16>);
+    } else if (a.mu) {
+      if constexpr (!ADJ) {
+        if (three)
+          go_tab(k_spread_ptab_yg<R, true, false, float, 3>);
+        else
+          go_tab(k_spread_ptab_yg<R, true, false, float>);
+      } else {
+        go_tab(k_spread_ptab_yg<R, true, true, float>);
+      }
+    } else {
+      go_tab(k_spread_ptab_yg<R, false, ADJ, float>);
+    }
+  } else if (psf) {
     if (a.mu && bf16) {
       go(k_spread_yg<R, true, true, ADJ, __nv_bfloat16>);
     } else if (a.mu) {
@@ -416,13 +481,23 @@ int launch_spread_pair_R(const YgArgs& a, int u0, int gcount, cudaStream_t st) {
   const dim3 grid(gcount * ntile * kSlabsB), block(32 * kW);
   const bool psf = a.psf != nullptr;
   const int zper = (a.nz + kSlabsB - 1) / kSlabsB;
-  const size_t smem = 2 * TS::kSbBytes + TS::kTapBytes + (psf ? sizeof(float) * 2 * zper * 2 * (2 * R + 1) : 0);
+  const PsfTable* tab = psf_table<R>(a);
+  const size_t smem =
+      2 * TS::kSbBytes + TS::kTapBytes + (psf && !tab ? sizeof(float) * 2 * zper * 2 * (2 * R + 1) : 0);
   auto go = [&](auto k) {
     cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
     NRGB_LAUNCH_SCOPE("k_spread_pair_yg", st);
     k<<<grid, block, smem, st>>>(a, u0);
   };
-  if (psf) {
+  auto go_tab = [&](auto k) {
+    cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
+    NRGB_LAUNCH_SCOPE("k_spread_pair_yg", st);
+    k<<<grid, block, smem, st>>>(a, u0, *tab);
+  };
+  if (psf && tab) {
+    if (a.mu) go_tab(k_spread_pair_ptab_yg<R, true>);
+    else go_tab(k_spread_pair_ptab_yg<R, false>);
+  } else if (psf) {
     if (a.mu) go(k_spread_pair_yg<R, true, true>);
     else go(k_spread_pair_yg<R, true, false>);
   } else {
