@@ -293,10 +293,13 @@ struct TileShape {
   static constexpr int kTapSlots = kW * kOwn;         // footprint slots per stage (see tap_slot)
   static constexpr size_t kSbBytes = sizeof(float4) * 2 * NS * 32;
   static constexpr size_t kTapBytes = sizeof(Tap) * 2 * kTapSlots;
-  // Projector with a mirror camera: the tile region also holds the three
-  // slab-merge buffers (T, P and the mirror camera's P per output column).
-  static constexpr size_t kSbBytesPair = sizeof(float4) * 32 * (2 * NS > 3 * kTXC ? 2 * NS : 3 * kTXC);
-  __host__ __device__ static constexpr size_t sb_bytes(bool pair) { return pair ? kSbBytesPair : kSbBytes; }
+  // Projector: 2 x steps tile buffers (steps depth planes sampled per
+  // barrier); the region also holds the slab-merge buffers after the walk (T
+  // and P per output column, and with a mirror camera its P).
+  __host__ __device__ static constexpr size_t sb_bytes(bool pair, int steps = 1) {
+    return sizeof(float4) * 32 * (2 * steps * NS > (pair ? 3 : 2) * kTXC ? 2 * steps * NS : (pair ? 3 : 2) * kTXC);
+  }
+  __host__ __device__ static constexpr size_t tap_bytes(int steps = 1) { return sizeof(Tap) * 2 * steps * kTapSlots; }
 };
 
 // Footprint slot of sampled column c in the tap buffer: the columns one warp
@@ -310,8 +313,8 @@ __device__ __forceinline__ int tap_slot(int c) {
 // Tile, footprints and the separated PSF of nz planes (twice with a mirror
 // camera: its kernels are the mirrored planes, row kernels reversed).
 template <int R>
-__host__ __device__ constexpr size_t tile_smem_bytes(int nz, bool pair = false) {
-  return TileShape<R>::sb_bytes(pair) + TileShape<R>::kTapBytes +
+__host__ __device__ constexpr size_t tile_smem_bytes(int nz, bool pair = false, int steps = 1) {
+  return TileShape<R>::sb_bytes(pair, steps) + TileShape<R>::tap_bytes(steps) +
          sizeof(float) * static_cast<size_t>(nz) * 2 * (2 * R + 1) * (pair ? 2 : 1);
 }
 
@@ -404,7 +407,11 @@ __device__ __forceinline__ bool lane_writes(const YgArgs& a, int yb) { return yb
 // the direct weights.  The mate's slabs merge in the opposite order.
 constexpr float kMateMaxT = 40.0f;
 
-template <int R, bool PSF, bool ATT, class V, bool PAIR = false, bool PTAB = false>
+//
+// STEPS: depth planes sampled per barrier (2 x STEPS tile buffers).  Two
+// planes per barrier measured no faster on GB300 (128^3 x 120: 0.676 against
+// 0.674 ms; 256^3 x 180: 11.9 against 11.2 ms), so the kernels use one.
+template <int R, bool PSF, bool ATT, class V, bool PAIR = false, bool PTAB = false, int STEPS = 1>
 __device__ __forceinline__ void project_item(const YgArgs& a, int cam, int mate, int x0, unsigned char* smem,
                                              const float* ptab = nullptr) {
   using TS = TileShape<R>;
@@ -414,10 +421,10 @@ __device__ __forceinline__ void project_item(const YgArgs& a, int cam, int mate,
   const V* __restrict__ mu = reinterpret_cast<const V*>(a.mu) + a.row0;
   constexpr int NS = TS::NS;
   constexpr int K = 2 * R + 1;
-  constexpr size_t kSb = TS::sb_bytes(PAIR);
-  float4* sb = reinterpret_cast<float4*>(smem);                    // [2][NS][32]
-  Tap* taps = reinterpret_cast<Tap*>(smem + kSb);                   // [2][kTapSlots]
-  float* s_psf = reinterpret_cast<float*>(smem + kSb + TS::kTapBytes);  // [nz][2K]
+  constexpr size_t kSb = TS::sb_bytes(PAIR, STEPS);
+  float4* sb = reinterpret_cast<float4*>(smem);                    // [2 * STEPS][NS][32]
+  Tap* taps = reinterpret_cast<Tap*>(smem + kSb);                   // [2 * STEPS][kTapSlots]
+  float* s_psf = reinterpret_cast<float*>(smem + kSb + TS::tap_bytes(STEPS));  // [nz][2K]
   float* s_psf_m = s_psf + static_cast<size_t>(a.nz) * 2 * K;       // [nz][2K] (mate)
 
   cg::cluster_group cluster = cg::this_cluster();
@@ -474,11 +481,12 @@ __device__ __forceinline__ void project_item(const YgArgs& a, int cam, int mate,
   }
   __syncthreads();
 
-  // One depth step at plane z into tile buffer b.  MODE 0: this camera (and
-  // the mate's forward form); MODE 1: the mate alone, direct weights (walked
-  // from the slab's far end).
-  auto step = [&](int z, int b, auto mode) {
-    constexpr int MODE = decltype(mode)::value;
+  // A depth step at plane z through tile buffer b: produce (footprints and
+  // samples of the NS columns), then, after a barrier, consume (row and
+  // column passes, depth sums).  MODE 0: this camera (and the mate's forward
+  // form); MODE 1: the mate alone, direct weights (walked from the slab's
+  // far end).
+  auto produce = [&](int z, int b) {
     float4* sbuf = sb + b * NS * 32;
     Tap* tb = taps + b * TS::kTapSlots;
     // footprints of the columns this warp samples (c = warp + kW * k)
@@ -496,7 +504,11 @@ __device__ __forceinline__ void project_item(const YgArgs& a, int cam, int mate,
       const int c = warp + kW * k;
       if (c < NS) sbuf[c * 32 + lane] = sample4(act, tb[tap_slot<R>(c)], yb, yok);
     }
-    __syncthreads();
+  };
+  auto consume = [&](int z, int b, auto mode) {
+    constexpr int MODE = decltype(mode)::value;
+    const float4* sbuf = sb + b * NS * 32;
+    const Tap* tb = taps + b * TS::kTapSlots;
     auto emit_m = [&](int i, const float4& v) {
       if (!ATT) {
         add4(Q[i], v);
@@ -547,7 +559,23 @@ __device__ __forceinline__ void project_item(const YgArgs& a, int cam, int mate,
     }
   };
 
-  for (int z = zbeg; z < zend; ++z) step(z, z & 1, std::integral_constant<int, 0>());
+  // walk: STEPS planes per barrier; iteration j uses buffers (j & 1) * STEPS + s,
+  // rewritten at iteration j + 2 after the barrier of iteration j + 1
+  auto walk = [&](auto mode) {
+    constexpr int MODE = decltype(mode)::value;
+    const int n = zend - zbeg;
+    for (int k = 0; k < n; k += STEPS) {
+      const int base = ((k / STEPS) & 1) * STEPS;
+#pragma unroll
+      for (int s = 0; s < STEPS; ++s)
+        if (k + s < n) produce(MODE == 0 ? zbeg + k + s : zend - 1 - k - s, base + s);
+      __syncthreads();
+#pragma unroll
+      for (int s = 0; s < STEPS; ++s)
+        if (k + s < n) consume(MODE == 0 ? zbeg + k + s : zend - 1 - k - s, base + s, mode);
+    }
+  };
+  walk(std::integral_constant<int, 0>());
 
   if (PAIR && paired && ATT) {
     bool redo = false;
@@ -562,7 +590,7 @@ __device__ __forceinline__ void project_item(const YgArgs& a, int cam, int mate,
         Q[i] = make_float4(0.f, 0.f, 0.f, 0.f);
         T[i] = make_float4(0.f, 0.f, 0.f, 0.f);  // ends at the slab sum again
       }
-      for (int k = 0; k < zend - zbeg; ++k) step(zend - 1 - k, k & 1, std::integral_constant<int, 1>());
+      walk(std::integral_constant<int, 1>());
     } else {
 #pragma unroll
       for (int i = 0; i < kTXW; ++i) Q[i] = mul4(Q[i], exp_neg4(T[i]));
