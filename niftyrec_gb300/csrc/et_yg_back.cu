@@ -319,33 +319,37 @@ __device__ __forceinline__ void spread_pair_body(const YgArgs& a, int u0, const 
       }
     }
     __syncthreads();
-    float4 acc[kTXW];
-#pragma unroll
-    for (int i = 0; i < kTXW; ++i) acc[i] = make_float4(0.f, 0.f, 0.f, 0.f);
-    auto write = [&](int i, float4 v) {
+    auto write = [&](int i, const float4& v) {
       const int x = x0 + warp * kTXW + i;
       if (x >= a.nx || !yok) return;
-      if (paired) add4(v, acc[i]);
       *reinterpret_cast<float4*>(tmp + (static_cast<size_t>(z) * a.nx + x) * a.cs + yb) = v;
     };
+    float4 pend;  // the mate's term of the output being written
+    auto keep = [&](int i, const float4& v) { pend = v; };
+    auto write_sum = [&](int i, float4 v) {
+      add4(v, pend);
+      write(i, v);
+    };
     if (PSF) {
-      auto keep = [&](int i, const float4& v) { acc[i] = v; };
-      if (paired) {
+      const float* kr = PTAB ? ptab + z * 2 * K : s_psf + (z - zbeg) * 2 * K;
+      if (paired) {  // both row passes in one sweep over the two tiles
         if constexpr (PTAB) {
           const float* km = ptab + (a.nz - 1 - z) * 2 * K;
-          rowpass_from_tile<R>(sm, warp * kTXW, keep, Reversed<R>{km}, km + K, lane, a.ny);
+          rowpass2_from_tiles<R>(sc, sm, warp * kTXW, write_sum, kr, kr + K, keep, Reversed<R>{km}, km + K, lane,
+                                 a.ny);
         } else {
           const float* km = s_psf_m + (z - zbeg) * 2 * K;
-          rowpass_from_tile<R>(sm, warp * kTXW, keep, km, km + K, lane, a.ny);
+          rowpass2_from_tiles<R>(sc, sm, warp * kTXW, write_sum, kr, kr + K, keep, km, km + K, lane, a.ny);
         }
+      } else {
+        rowpass_from_tile<R>(sc, warp * kTXW, write, kr, kr + K, lane, a.ny);
       }
-      const float* kr = PTAB ? ptab + z * 2 * K : s_psf + (z - zbeg) * 2 * K;
-      rowpass_from_tile<R>(sc, warp * kTXW, write, kr, kr + K, lane, a.ny);
     } else {
 #pragma unroll
       for (int i = 0; i < kTXW; ++i) {
-        if (paired) acc[i] = sm[(warp * kTXW + i) * 32 + lane];
-        write(i, sc[(warp * kTXW + i) * 32 + lane]);
+        float4 v = sc[(warp * kTXW + i) * 32 + lane];
+        if (paired) add4(v, sm[(warp * kTXW + i) * 32 + lane]);
+        write(i, v);
       }
     }
   }

@@ -344,12 +344,14 @@ __device__ __forceinline__ void rowpass_from_tile(const float4* __restrict__ sbu
   }
 }
 
-// Row passes of two cameras over the same tile (a camera and its mirror
-// camera): each tile column is read once and feeds both sliding windows;
-// output i of camera b is emitted before output i of camera a.
+// Row passes of two cameras in one sweep: over the same tile (a camera and
+// its mirror camera in the projector: each tile column is read once and feeds
+// both sliding windows) or over two tiles (the mirror-unit spread); output i
+// of camera b is emitted before output i of camera a.
 template <int R, class EmitA, class EmitB, class KRA, class KCA, class KRB, class KCB>
-__device__ __forceinline__ void rowpass2_from_tile(const float4* __restrict__ sbuf, int base, EmitA emit_a, KRA kra,
-                                                   KCA kca, EmitB emit_b, KRB krb, KCB kcb, int lane, int ny) {
+__device__ __forceinline__ void rowpass2_from_tiles(const float4* __restrict__ sa, const float4* __restrict__ sbt,
+                                                    int base, EmitA emit_a, KRA kra, KCA kca, EmitB emit_b, KRB krb,
+                                                    KCB kcb, int lane, int ny) {
   constexpr int NJ = kTXW + 2 * R;
   float4 ua[kTXW], ub[kTXW];
 #pragma unroll
@@ -359,13 +361,14 @@ __device__ __forceinline__ void rowpass2_from_tile(const float4* __restrict__ sb
   }
 #pragma unroll
   for (int j = 0; j < NJ; ++j) {
-    const float4 r = sbuf[(base + j) * 32 + lane];
+    const float4 r = sa[(base + j) * 32 + lane];
+    const float4 rb = sbt == sa ? r : sbt[(base + j) * 32 + lane];
 #pragma unroll
     for (int d = 0; d <= 2 * R; ++d) {
       const int i = j - d;
       if (i >= 0 && i < kTXW) {
         axpy4(ua[i], kra[2 * R - d], r);
-        axpy4(ub[i], krb[2 * R - d], r);
+        axpy4(ub[i], krb[2 * R - d], rb);
       }
     }
     const int i = j - 2 * R;
@@ -374,6 +377,12 @@ __device__ __forceinline__ void rowpass2_from_tile(const float4* __restrict__ sb
       emit_a(i, mask_rows(yconv4<R>(ua[i], kca, lane), 4 * lane, ny));
     }
   }
+}
+
+template <int R, class EmitA, class EmitB, class KRA, class KCA, class KRB, class KCB>
+__device__ __forceinline__ void rowpass2_from_tile(const float4* __restrict__ sbuf, int base, EmitA emit_a, KRA kra,
+                                                   KCA kca, EmitB emit_b, KRB krb, KCB kcb, int lane, int ny) {
+  rowpass2_from_tiles<R>(sbuf, sbuf, base, emit_a, kra, kca, emit_b, krb, kcb, lane, ny);
 }
 
 // ---------------------------------------------------------------- projector
