@@ -221,7 +221,13 @@ __global__ void __launch_bounds__(32 * kW, CTAS)
 // adds both cameras' terms: one mu scan, one scratch volume and one gather
 // per pair.  A unit without a mate spreads its camera alone.  CTA = (unit,
 // x-tile, depth slab); the PSF planes of the slab only sit in shared memory.
-template <int R, bool PSF, bool ATT, bool PTAB>
+//
+// ADJ: the exact transpose of the mirror-unit projector instead: both terms in
+// c's frame go through the transposed PSF (camera: both kernels reversed;
+// mate: row kernel forward, column kernel reversed) and, summed, are
+// scattered with c's bilinear weights into the accumulator a.out (the mate's
+// footprint of its mirrored column is c's).
+template <int R, bool PSF, bool ATT, bool ADJ, bool PTAB>
 __device__ __forceinline__ void spread_pair_body(const YgArgs& a, int u0, const float* ptab) {
   using TS = TileShape<R>;
   constexpr int NS = TS::NS;
@@ -249,17 +255,20 @@ __device__ __forceinline__ void spread_pair_body(const YgArgs& a, int u0, const 
   if (zbeg >= zend) return;  // uniform over the CTA
   float* s_psf_m = s_psf + zper * 2 * K;
   if (PSF && !PTAB) {
+    // reversed index of a row (j < K) or column (j >= K) kernel entry
+    auto rev = [&](int j) { return j < K ? K - 1 - j : 3 * K - 1 - j; };
     for (int i = threadIdx.x; i < (zend - zbeg) * 2 * K; i += blockDim.x) {
-      s_psf[i] = __ldg(a.psf + zbeg * 2 * K + i);
-      if (paired) {
-        const int z = zbeg + i / (2 * K), j = i % (2 * K);
-        s_psf_m[i] = __ldg(a.psf + (a.nz - 1 - z) * 2 * K + (j < K ? K - 1 - j : j));
+      const int z = zbeg + i / (2 * K), j = i % (2 * K);
+      s_psf[i] = __ldg(a.psf + z * 2 * K + (ADJ ? rev(j) : j));
+      if (paired) {  // mate: reference row reversed; transpose column reversed
+        const int jm = (j < K) != ADJ ? rev(j) : j;
+        s_psf_m[i] = __ldg(a.psf + (a.nz - 1 - z) * 2 * K + jm);
       }
     }
   }
   const CamRows cr = cam_rows(a.geom[cam].fwd);
   const size_t vol = static_cast<size_t>(a.nz) * a.nx * a.cs;  // one scratch volume
-  float* __restrict__ tmp = a.temp + vol * g;
+  float* __restrict__ tmp = ADJ ? a.out + a.row0 : a.temp + vol * g;
   const float* __restrict__ srow = a.sino + static_cast<size_t>(cam) * a.nx * a.cy + a.row0;
   const float* __restrict__ mrow = a.sino + static_cast<size_t>(paired ? mate : cam) * a.nx * a.cy + a.row0;
 
@@ -287,7 +296,7 @@ __device__ __forceinline__ void spread_pair_body(const YgArgs& a, int u0, const 
     float4* sc = sb + b * 2 * NS * 32;
     float4* sm = sc + NS * 32;
     Tap* tb = taps + b * TS::kTapSlots;
-    if (ATT && lane < TS::kOwn) {
+    if ((ATT || ADJ) && lane < TS::kOwn) {
       const int c = warp + kW * lane;
       if (c < NS) {
         const int xp = x0 - R + c;
@@ -322,7 +331,12 @@ __device__ __forceinline__ void spread_pair_body(const YgArgs& a, int u0, const 
     auto write = [&](int i, const float4& v) {
       const int x = x0 + warp * kTXW + i;
       if (x >= a.nx || !yok) return;
-      *reinterpret_cast<float4*>(tmp + (static_cast<size_t>(z) * a.nx + x) * a.cs + yb) = v;
+      if (ADJ) {
+        // halo rows lack part of their PSF support: their owner window adds them
+        if (lane_writes(a, yb)) scatter4(tmp, tb[tap_slot<R>(warp * kTXW + i + R)], yb, v);
+      } else {
+        *reinterpret_cast<float4*>(tmp + (static_cast<size_t>(z) * a.nx + x) * a.cs + yb) = v;
+      }
     };
     float4 pend;  // the mate's term of the output being written
     auto keep = [&](int i, const float4& v) { pend = v; };
@@ -333,7 +347,11 @@ __device__ __forceinline__ void spread_pair_body(const YgArgs& a, int u0, const 
     if (PSF) {
       const float* kr = PTAB ? ptab + z * 2 * K : s_psf + (z - zbeg) * 2 * K;
       if (paired) {  // both row passes in one sweep over the two tiles
-        if constexpr (PTAB) {
+        if constexpr (PTAB && ADJ) {
+          const float* km = ptab + (a.nz - 1 - z) * 2 * K;
+          rowpass2_from_tiles<R>(sc, sm, warp * kTXW, write_sum, Reversed<R>{kr}, Reversed<R>{kr + K}, keep, km,
+                                 Reversed<R>{km + K}, lane, a.ny);
+        } else if constexpr (PTAB) {
           const float* km = ptab + (a.nz - 1 - z) * 2 * K;
           rowpass2_from_tiles<R>(sc, sm, warp * kTXW, write_sum, kr, kr + K, keep, Reversed<R>{km}, km + K, lane,
                                  a.ny);
@@ -341,6 +359,8 @@ __device__ __forceinline__ void spread_pair_body(const YgArgs& a, int u0, const 
           const float* km = s_psf_m + (z - zbeg) * 2 * K;
           rowpass2_from_tiles<R>(sc, sm, warp * kTXW, write_sum, kr, kr + K, keep, km, km + K, lane, a.ny);
         }
+      } else if constexpr (PTAB && ADJ) {
+        rowpass_from_tile<R>(sc, warp * kTXW, write, Reversed<R>{kr}, Reversed<R>{kr + K}, lane, a.ny);
       } else {
         rowpass_from_tile<R>(sc, warp * kTXW, write, kr, kr + K, lane, a.ny);
       }
@@ -355,15 +375,15 @@ __device__ __forceinline__ void spread_pair_body(const YgArgs& a, int u0, const 
   }
 }
 
-template <int R, bool PSF, bool ATT>
+template <int R, bool PSF, bool ATT, bool ADJ>
 __global__ void __launch_bounds__(32 * kW, 2) k_spread_pair_yg(const YgArgs a, int u0) {
-  spread_pair_body<R, PSF, ATT, false>(a, u0, nullptr);
+  spread_pair_body<R, PSF, ATT, ADJ, false>(a, u0, nullptr);
 }
 
-template <int R, bool ATT>
+template <int R, bool ATT, bool ADJ>
 __global__ void __launch_bounds__(32 * kW, 2)
     k_spread_pair_ptab_yg(const YgArgs a, int u0, const __grid_constant__ PsfTable t) {
-  spread_pair_body<R, true, ATT, true>(a, u0, t.c);
+  spread_pair_body<R, true, ATT, ADJ, true>(a, u0, t.c);
 }
 
 // ------------------------------------ backprojector: inverse-rotation gather
@@ -478,7 +498,7 @@ int launch_spread_R(const YgArgs& a, int c0, int gcount, cudaStream_t st) {
   return cudaGetLastError() == cudaSuccess ? kOk : kErrKernel;
 }
 
-template <int R>
+template <int R, bool ADJ>
 int launch_spread_pair_R(const YgArgs& a, int u0, int gcount, cudaStream_t st) {
   using TS = TileShape<R>;
   const int ntile = (a.nx + kTXC - 1) / kTXC;
@@ -490,37 +510,38 @@ int launch_spread_pair_R(const YgArgs& a, int u0, int gcount, cudaStream_t st) {
       2 * TS::kSbBytes + TS::kTapBytes + (psf && !tab ? sizeof(float) * 2 * zper * 2 * (2 * R + 1) : 0);
   auto go = [&](auto k) {
     cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
-    NRGB_LAUNCH_SCOPE("k_spread_pair_yg", st);
+    NRGB_LAUNCH_SCOPE(ADJ ? "k_adjoint_pair_yg" : "k_spread_pair_yg", st);
     k<<<grid, block, smem, st>>>(a, u0);
   };
   auto go_tab = [&](auto k) {
     cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
-    NRGB_LAUNCH_SCOPE("k_spread_pair_yg", st);
+    NRGB_LAUNCH_SCOPE(ADJ ? "k_adjoint_pair_yg" : "k_spread_pair_yg", st);
     k<<<grid, block, smem, st>>>(a, u0, *tab);
   };
   if (psf && tab) {
-    if (a.mu) go_tab(k_spread_pair_ptab_yg<R, true>);
-    else go_tab(k_spread_pair_ptab_yg<R, false>);
+    if (a.mu) go_tab(k_spread_pair_ptab_yg<R, true, ADJ>);
+    else go_tab(k_spread_pair_ptab_yg<R, false, ADJ>);
   } else if (psf) {
-    if (a.mu) go(k_spread_pair_yg<R, true, true>);
-    else go(k_spread_pair_yg<R, true, false>);
+    if (a.mu) go(k_spread_pair_yg<R, true, true, ADJ>);
+    else go(k_spread_pair_yg<R, true, false, ADJ>);
   } else {
-    if (a.mu) go(k_spread_pair_yg<0, false, true>);
-    else go(k_spread_pair_yg<0, false, false>);
+    if (a.mu) go(k_spread_pair_yg<0, false, true, ADJ>);
+    else go(k_spread_pair_yg<0, false, false, ADJ>);
   }
   return cudaGetLastError() == cudaSuccess ? kOk : kErrKernel;
 }
 
+template <bool ADJ>
 int spread_pair_by_radius(int R, const YgArgs& a, int u0, int gcount, cudaStream_t st) {
   switch (R) {
-    case 0: return launch_spread_pair_R<0>(a, u0, gcount, st);
-    case 1: return launch_spread_pair_R<1>(a, u0, gcount, st);
-    case 2: return launch_spread_pair_R<2>(a, u0, gcount, st);
-    case 3: return launch_spread_pair_R<3>(a, u0, gcount, st);
-    case 4: return launch_spread_pair_R<4>(a, u0, gcount, st);
-    case 5: return launch_spread_pair_R<5>(a, u0, gcount, st);
-    case 6: return launch_spread_pair_R<6>(a, u0, gcount, st);
-    case 7: return launch_spread_pair_R<7>(a, u0, gcount, st);
+    case 0: return launch_spread_pair_R<0, ADJ>(a, u0, gcount, st);
+    case 1: return launch_spread_pair_R<1, ADJ>(a, u0, gcount, st);
+    case 2: return launch_spread_pair_R<2, ADJ>(a, u0, gcount, st);
+    case 3: return launch_spread_pair_R<3, ADJ>(a, u0, gcount, st);
+    case 4: return launch_spread_pair_R<4, ADJ>(a, u0, gcount, st);
+    case 5: return launch_spread_pair_R<5, ADJ>(a, u0, gcount, st);
+    case 6: return launch_spread_pair_R<6, ADJ>(a, u0, gcount, st);
+    case 7: return launch_spread_pair_R<7, ADJ>(a, u0, gcount, st);
     default: return kErrParameters;
   }
 }
@@ -606,8 +627,8 @@ Pipe* pipe_for_current_device() {
 int yg_backproject(const YgArgs& a_in, cudaStream_t st) {
   YgArgs a = a_in;
   const int R = a.psf ? (a.psf_k - 1) / 2 : 0;
-  // mirror units: reference mode, float32 mu
-  const bool pair = a.units && a.nunits > 0 && a.back_mode == kBackReference && a.storage != kStorageBF16;
+  // mirror units: float32 mu
+  const bool pair = a.units && a.nunits > 0 && a.storage != kStorageBF16;
   if (!pair) {
     a.units = nullptr;
     a.nunits = 0;
@@ -631,7 +652,7 @@ int yg_backproject(const YgArgs& a_in, cudaStream_t st) {
   }
   a.group = group;
   auto spread = [&](const YgArgs& b, int c0, int gcount) {
-    return pair ? spread_pair_by_radius(R, b, c0, gcount, st) : spread_by_radius(R, b, c0, gcount, st);
+    return pair ? spread_pair_by_radius<false>(R, b, c0, gcount, st) : spread_by_radius(R, b, c0, gcount, st);
   };
   const std::vector<Window> wins = row_windows(a.ny, R);
   if (a.back_mode == kBackAdjoint) {
@@ -640,7 +661,8 @@ int yg_backproject(const YgArgs& a_in, cudaStream_t st) {
     const size_t full = static_cast<size_t>(a.nz) * a.nx * a.cy;
     if (cudaMemsetAsync(a.out, 0, sizeof(float) * full, st) != cudaSuccess) return kErrKernel;
     for (const Window& w : wins) {
-      const int s = spread_by_radius_t<true>(R, windowed(a, w), 0, a.ncam, st);
+      const int s = pair ? spread_pair_by_radius<true>(R, windowed(a, w), 0, nunits, st)
+                         : spread_by_radius_t<true>(R, windowed(a, w), 0, a.ncam, st);
       if (s != kOk) return s;
     }
     return kOk;

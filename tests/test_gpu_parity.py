@@ -286,3 +286,10 @@ def test_mirror_cameras(o32, shape, k, att_scale, angles):
         finally:
             L.nrgb_set_mirror_pairs(1)
         assert rel_l2(b, b0) < RTOL
+    # the exact-transpose backprojector (mode 1) serves mirror units too
+    torch = pytest.importorskip("torch")
+    from niftyrec_gb300.autograd import backproject_raw
+
+    bt = backproject_raw(torch.from_numpy(so).cuda(), torch.from_numpy(mu).cuda(), cams, psf, nz=nz, mode=1)
+    bto = o32.backproject(so, cams, psf, mu, truncate=0, adjoint=True, nz=nz)
+    assert rel_l2(bt.cpu().numpy(), bto) < RTOL
