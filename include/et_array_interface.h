@@ -317,8 +317,9 @@ int nrgb_set_backproject_group(int nx, int ny, int nz, int ncam, int group);
 int nrgb_get_backproject_group(int nx, int ny, int nz, int ncam);
 /* Tuning table of the fused projector (no counterpart in the reference):
  * depth slabs per (camera, x-tile) item -- the thread-block cluster size, 2,
- * 4 or 8 -- for a problem shape; 0 (the initial state) lets the launcher take
- * the fewest slabs that give four waves of thread blocks.
+ * 4, 8 or 16 (a non-portable cluster size: 8 where it cannot be resident) --
+ * for a problem shape; 0 (the initial state) lets the launcher take the
+ * fewest slabs that give four waves of thread blocks.
  * niftyrec_gb300.autotune measures the candidates and records the fastest. */
 int nrgb_set_project_slabs(int nx, int ny, int nz, int ncam, int slabs);
 int nrgb_get_project_slabs(int nx, int ny, int nz, int ncam);

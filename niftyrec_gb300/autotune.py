@@ -6,7 +6,7 @@
   gather of group g).  The best group size trades L2 residency of the scratch
   against launch count and per-launch parallelism.
 * Projector depth slabs.  Each (camera, x-tile) item of the projector is
-  split into 2, 4 or 8 depth slabs, one thread block each, merged through
+  split into 2, 4, 8 or 16 depth slabs, one thread block each, merged through
   distributed shared memory inside a thread-block cluster of that size.  More
   slabs mean more thread blocks in flight (better latency hiding on small
   grids) and a longer merge.
@@ -29,7 +29,7 @@ import os
 import numpy as np
 
 CANDIDATES = (8, 16, 24, 32, 40, 48, 64)
-SLAB_CANDIDATES = (2, 4, 8)
+SLAB_CANDIDATES = (2, 4, 8, 16)
 CACHE = os.path.join(os.path.expanduser("~"), ".cache", "niftyrec_gb300", "tune.json")
 
 

@@ -1071,10 +1071,10 @@ int nrgb_set_backproject_group(int nx, int ny, int nz, int ncam, int group) {
 
 int nrgb_get_backproject_group(int nx, int ny, int nz, int ncam) { return tuned_group(nx, ny, nz, ncam); }
 
-// Tuning table of the fused projector: depth slabs (cluster size 2, 4, 8;
-// 0 removes the entry) for the shape (nx, ny, nz, n_cameras).
+// Tuning table of the fused projector: depth slabs (cluster size 2, 4, 8,
+// 16; 0 removes the entry) for the shape (nx, ny, nz, n_cameras).
 int nrgb_set_project_slabs(int nx, int ny, int nz, int ncam, int slabs) {
-  if (slabs != 0 && slabs != 2 && slabs != 4 && slabs != 8) return kErrParameters;
+  if (slabs != 0 && slabs != 2 && slabs != 4 && slabs != 8 && slabs != 16) return kErrParameters;
   set_tuned_project_slabs(nx, ny, nz, ncam, slabs);
   return kOk;
 }

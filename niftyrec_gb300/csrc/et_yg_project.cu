@@ -8,16 +8,18 @@ template <int R>
 int launch_project_R(const YgArgs& a, cudaStream_t st);  // et_yg_project_kernels.cuh
 
 // ------------------------------------------------------------- dispatch
-// Depth slabs (cluster size) of the projector: the fewest of 2, 4, 8 that
-// give at least four waves of CTAs (fewer slabs merge less; more slabs fill
-// the GPU for small problems).  Measured on GB300: 128^3 x 120 cameras 4
-// (0.84 ms; 2: 0.87, 8: 0.87), 256^3 x 180: 2 (15.9 ms; 4: 16.7),
-// 64^3 x 60: 8 (0.149 ms; 4: 0.158).
-int project_slabs(int items, int ctas_per_sm) {
+// Depth slabs (cluster size) of the projector: the fewest of 2, 4, 8 (16
+// with at least 8 planes per slab) that give at least four waves of CTAs
+// (fewer slabs merge less; more slabs fill the GPU for small problems, e.g.
+// the 15-camera subsets of an OSEM step).  Measured on GB300 without mirror
+// units: 128^3 x 120 cameras 4 (0.84 ms; 2: 0.87, 8: 0.87), 256^3 x 180: 2
+// (15.9 ms; 4: 16.7), 64^3 x 60: 8 (0.149 ms; 4: 0.158).
+int project_slabs(int items, int ctas_per_sm, int nz) {
   const int slots = 152 * ctas_per_sm;
-  for (int s = 2; s < 8; s *= 2)
+  const int most = nz >= 128 ? 16 : 8;
+  for (int s = 2; s < most; s *= 2)
     if (items * s >= 4 * slots) return s;
-  return 8;
+  return most;
 }
 
 namespace {

@@ -8,8 +8,8 @@
 namespace nrgb {
 
 // Depth slabs (cluster size) of the projector for `items` cluster work items
-// at `ctas_per_sm` CTAs per SM (et_yg_project.cu).
-int project_slabs(int items, int ctas_per_sm);
+// at `ctas_per_sm` CTAs per SM and nz depth planes (et_yg_project.cu).
+int project_slabs(int items, int ctas_per_sm, int nz);
 
 namespace {
 
@@ -58,43 +58,42 @@ int launch_project_R(const YgArgs& a_in, cudaStream_t st) {
   const size_t smem = tile_smem_bytes<R>(psf && !ptab ? a.nz : 0, pair);
   // three CTAs per SM need three tiles (plus 1 KB reserved each) in the 228 KB
   const bool three = 3 * (smem + 1024) <= 228 * 1024;
-  if (a.pslabs != 2 && a.pslabs != 4 && a.pslabs != 8)
-    a.pslabs = project_slabs(nunits * ntile, three && !bf16 && !pair ? 3 : 2);
-  auto go = [&](auto k) {
+  if (a.pslabs != 2 && a.pslabs != 4 && a.pslabs != 8 && a.pslabs != 16)
+    a.pslabs = project_slabs(nunits * ntile, three && !bf16 && !pair ? 3 : 2, a.nz);
+  // one cluster of a.pslabs CTAs per (unit, x-tile); 16 is a non-portable
+  // cluster size: it falls back to 8 where the kernel cannot be resident so
+  auto launch = [&](auto k, auto&&... extra) {
     cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
     cudaLaunchConfig_t cfg = {};
-    cfg.gridDim = dim3(nunits * ntile * a.pslabs);
     cfg.blockDim = dim3(32 * kW);
     cfg.dynamicSmemBytes = smem;
     cfg.stream = st;
     cudaLaunchAttribute attr[1];
     attr[0].id = cudaLaunchAttributeClusterDimension;
-    attr[0].val.clusterDim.x = a.pslabs;
     attr[0].val.clusterDim.y = 1;
     attr[0].val.clusterDim.z = 1;
     cfg.attrs = attr;
     cfg.numAttrs = 1;
+    if (a.pslabs == 16) {
+      int clusters = 0;
+      cfg.gridDim = dim3(nunits * ntile * 16);
+      attr[0].val.clusterDim.x = 16;
+      if (cudaFuncSetAttribute(k, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) != cudaSuccess ||
+          cudaOccupancyMaxActiveClusters(&clusters, k, &cfg) != cudaSuccess || clusters < 1) {
+        cudaGetLastError();
+        a.pslabs = 8;
+      }
+    }
+    cfg.gridDim = dim3(nunits * ntile * a.pslabs);
+    attr[0].val.clusterDim.x = a.pslabs;
     NRGB_LAUNCH_SCOPE("k_project_yg", st);
-    cudaLaunchKernelEx(&cfg, k, a);
+    cudaLaunchKernelEx(&cfg, k, a, extra...);
   };
+  auto go = [&](auto k) { launch(k); };
   auto go_tab = [&](auto k) {
     static thread_local PsfTable table;
     std::memcpy(table.c, a.psf_host, sizeof(float) * a.nz * 2 * (2 * R + 1));
-    cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
-    cudaLaunchConfig_t cfg = {};
-    cfg.gridDim = dim3(nunits * ntile * a.pslabs);
-    cfg.blockDim = dim3(32 * kW);
-    cfg.dynamicSmemBytes = smem;
-    cfg.stream = st;
-    cudaLaunchAttribute attr[1];
-    attr[0].id = cudaLaunchAttributeClusterDimension;
-    attr[0].val.clusterDim.x = a.pslabs;
-    attr[0].val.clusterDim.y = 1;
-    attr[0].val.clusterDim.z = 1;
-    cfg.attrs = attr;
-    cfg.numAttrs = 1;
-    NRGB_LAUNCH_SCOPE("k_project_yg", st);
-    cudaLaunchKernelEx(&cfg, k, a, table);
+    launch(k, table);
   };
   auto pick = [&](auto v, auto ctas, auto paired) {
     using V = decltype(v);

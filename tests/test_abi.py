@@ -81,12 +81,12 @@ def test_tuning_tables(lib):
     """The host-side tuning tables: set, read back, reject bad values, clear."""
     shape = (40, 44, 36, 7)
     assert lib.nrgb_get_project_slabs(*shape) == 0
-    for s in (2, 4, 8):
+    for s in (2, 4, 8, 16):
         assert lib.nrgb_set_project_slabs(*shape, s) == 0
         assert lib.nrgb_get_project_slabs(*shape) == s
-    for bad in (1, 3, 16, -2):
+    for bad in (1, 3, 32, -2):
         assert lib.nrgb_set_project_slabs(*shape, bad) == 2
-    assert lib.nrgb_get_project_slabs(*shape) == 8
+    assert lib.nrgb_get_project_slabs(*shape) == 16
     assert lib.nrgb_set_project_slabs(*shape, 0) == 0
     assert lib.nrgb_get_project_slabs(*shape) == 0
     g0 = lib.nrgb_get_backproject_group(*shape)

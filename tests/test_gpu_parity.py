@@ -216,7 +216,7 @@ def test_fisher_grid_golden(golden, o32):
     assert getattr(e.value, "status", None) == 2
 
 
-@pytest.mark.parametrize("slabs", [2, 4, 8])
+@pytest.mark.parametrize("slabs", [2, 4, 8, 16])
 def test_project_slab_counts(o32, slabs):
     """Every depth-slab count of the projector (cluster size, from the tuning
     table) gives the oracle's projection; the entry is removed afterwards."""
