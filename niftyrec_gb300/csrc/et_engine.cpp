@@ -289,6 +289,38 @@ int project_device(const Problem& pb, const float* d_act, const float* d_att, fl
   return check(general_project(g, st));
 }
 
+namespace {
+
+// A second stream per device on which a backprojection converts its
+// sinogram while the transmission carries run on the caller's stream.
+struct SideStream {
+  std::mutex mu;
+  cudaStream_t stream = nullptr;
+  cudaEvent_t fork = nullptr, done = nullptr;
+};
+
+SideStream* side_for_current_device() {
+  static std::mutex mu;
+  static std::map<int, std::unique_ptr<SideStream>> sides;
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) return nullptr;
+  std::lock_guard<std::mutex> lk(mu);
+  std::unique_ptr<SideStream>& p = sides[dev];
+  if (!p) {
+    auto q = std::make_unique<SideStream>();
+    if (cudaStreamCreateWithFlags(&q->stream, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaEventCreateWithFlags(&q->fork, cudaEventDisableTiming) != cudaSuccess ||
+        cudaEventCreateWithFlags(&q->done, cudaEventDisableTiming) != cudaSuccess) {
+      cudaGetLastError();
+      return nullptr;
+    }
+    p = std::move(q);
+  }
+  return p.get();
+}
+
+}  // namespace
+
 int backproject_device(const Problem& pb, const float* d_sino, const float* d_att, float* d_out, char* ws,
                        size_t ws_bytes, Staging* stg, cudaStream_t st) {
   Carver cv(ws, ws_bytes);
@@ -305,9 +337,23 @@ int backproject_device(const Problem& pb, const float* d_sino, const float* d_at
     float* slab = cv.take<float>(yg_backproject_workspace(pb.nx, pb.ny, pb.nz, pb.cams.n, group) / sizeof(float));
     if (!sino_c || !out_c || !slab || (d_att && !mu_c)) return kErrAllocGpu;
     const int cy = round_up(pb.ny, 4);
-    if ((s = to_column(d_sino, sino_c, pb.nx, pb.ny, cy, pb.cams.n, st)) != kOk) return s;
-    if (d_att && (s = stage_column(pb, d_att, mu_c, cy, pb.nz, st)) != kOk) return s;
+    // with attenuation the sinogram is converted on a side stream while the
+    // carries (which need only mu) run on st
+    SideStream* side = d_att ? side_for_current_device() : nullptr;
+    std::unique_lock<std::mutex> side_lock;
+    if (side) {
+      side_lock = std::unique_lock<std::mutex>(side->mu);
+      if ((s = stage_column(pb, d_att, mu_c, cy, pb.nz, st)) != kOk) return s;
+      cudaEventRecord(side->fork, st);
+      cudaStreamWaitEvent(side->stream, side->fork, 0);
+      if ((s = to_column(d_sino, sino_c, pb.nx, pb.ny, cy, pb.cams.n, side->stream)) != kOk) return s;
+      cudaEventRecord(side->done, side->stream);
+    } else {
+      if ((s = to_column(d_sino, sino_c, pb.nx, pb.ny, cy, pb.cams.n, st)) != kOk) return s;
+      if (d_att && (s = stage_column(pb, d_att, mu_c, cy, pb.nz, st)) != kOk) return s;
+    }
     YgArgs a;
+    a.sino_ready = side ? side->done : nullptr;
     a.storage = pb.storage;
     a.nx = pb.nx;
     a.ny = pb.ny;

@@ -84,6 +84,10 @@ struct YgArgs {
   // slots; 0: both on the caller's stream with one slot (creates no stream
   // or event).
   int pipelined = 1;
+  // Backprojector: non-null when the caller produces a.sino on another
+  // stream; this event (a cudaEvent_t) marks its completion and is waited
+  // for after the transmission carries are launched, which overlap it.
+  void* sino_ready = nullptr;
   // Non-null: transmission carries [ncam][slots][nx][cy] computed beforehand
   // (yg_mu_carry) for exactly these cameras; the backprojector then skips
   // that pass and the work space holds only the scratch slot(s).

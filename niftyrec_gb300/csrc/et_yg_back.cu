@@ -650,6 +650,7 @@ int yg_backproject(const YgArgs& a_in, cudaStream_t st) {
     int s = yg_mu_carry(a, a.slab_T, st);
     if (s != kOk) return s;
   }
+  if (a.sino_ready) cudaStreamWaitEvent(st, static_cast<cudaEvent_t>(a.sino_ready), 0);
   a.group = group;
   auto spread = [&](const YgArgs& b, int c0, int gcount) {
     return pair ? spread_pair_by_radius<false>(R, b, c0, gcount, st) : spread_by_radius(R, b, c0, gcount, st);
