@@ -344,9 +344,22 @@ long long nrgb_launch_count(void);
 int nrgb_profile_enable(int on);
 int nrgb_profile_summary(char *buf, int len);
 
+/* NIfTI-1 single-file images (no counterpart in the reference library; its
+ * command-line tool reads and writes them with nifti1_io, apps/command_line_tools/
+ * rec_spect.cpp:447-606).  .nii.gz needs zlib at build time
+ * (nrgb_nifti_gzip_supported).  nrgb_nifti_info: dims = {ndim, dim1..dim7};
+ * nrgb_nifti_read: every voxel as float32 (integer and real datatypes, either
+ * byte order, scl_slope applied), n_voxels must match; nrgb_nifti_write:
+ * float32 image of dims = {ndim, dim1..dimN}.  Status 2 on any failure. */
+int nrgb_nifti_info(const char *path, int *dims);
+int nrgb_nifti_read(const char *path, float *data, long long n_voxels);
+int nrgb_nifti_write(const char *path, const float *data, const int *dims);
+int nrgb_nifti_gzip_supported(void);
+
 #if defined(__GNUC__)
 #pragma GCC visibility pop
 #endif
+
 
 #ifdef __cplusplus
 }

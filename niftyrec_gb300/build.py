@@ -22,7 +22,8 @@ INCLUDE = os.path.join(os.path.dirname(HERE), "include")
 
 SOURCES = ["et_geometry.cpp", "et_engine.cpp", "et_api.cpp", "et_profile.cpp", "et_general.cu", "et_ygantry.cu",
            "et_yg_project.cu", "et_yg_proj_r01.cu", "et_yg_proj_r23.cu", "et_yg_proj_r45.cu", "et_yg_proj_r67.cu",
-           "et_yg_back.cu", "et_update.cu", "et_noalloc.cu", "et_plan.cpp", "et_fisher.cu"]
+           "et_yg_back.cu", "et_update.cu", "et_noalloc.cu", "et_plan.cpp", "et_fisher.cu", "et_nifti.cpp"]
+TOOL = os.path.join(HERE, "rec_spect")  # command-line reconstruction (csrc/rec_spect.cpp)
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC,-ffp-contract=off,-fvisibility=hidden",
@@ -33,6 +34,15 @@ def _nvcc() -> str:
     cuda = os.environ.get("CUDA_HOME", "/usr/local/cuda")
     path = os.path.join(cuda, "bin", "nvcc")
     return path if os.path.exists(path) else (shutil.which("nvcc") or "nvcc")
+
+
+def _zlib() -> bool:
+    """zlib headers and a linkable library (for .nii.gz)."""
+    import glob
+
+    if not os.path.exists("/usr/include/zlib.h"):
+        return False
+    return bool(glob.glob("/usr/lib*/libz.so") + glob.glob("/usr/lib*/*/libz.so") + glob.glob("/lib*/*/libz.so"))
 
 
 def _stale(target: str, deps) -> bool:
@@ -53,7 +63,8 @@ def _compile(src: str, verbose: bool) -> str:
     obj = os.path.join(BUILD, os.path.splitext(src)[0] + ".o")
     path = os.path.join(CSRC, src)
     if _stale(obj, [path, __file__] + _headers()):
-        cmd = [_nvcc()] + ARCH + NVCC_FLAGS + ["-c", path, "-o", obj]
+        cmd = [_nvcc()] + ARCH + NVCC_FLAGS + (["-DNRGB_ZLIB"] if src == "et_nifti.cpp" and _zlib() else []) + [
+            "-c", path, "-o", obj]
         if src.endswith(".cu") and verbose:
             cmd += ["-Xptxas", "-v"]
         r = subprocess.run(cmd, capture_output=True, text=True)
@@ -75,10 +86,18 @@ def build(force: bool = False, verbose: bool = False) -> str:
     if force or _stale(LIB, objs):
         cuda = os.environ.get("CUDA_HOME", "/usr/local/cuda")
         cmd = [_nvcc()] + ARCH + ["-shared", "-cudart", "shared", "-o", LIB] + objs + [
-            "-Xlinker", "-rpath," + os.path.join(cuda, "lib64")]
+            "-Xlinker", "-rpath," + os.path.join(cuda, "lib64")] + (["-lz"] if _zlib() else [])
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:
             raise RuntimeError(f"link failed:\n{r.stdout}\n{r.stderr}")
+    tool_src = os.path.join(CSRC, "rec_spect.cpp")
+    if force or _stale(TOOL, [LIB, tool_src] + _headers()):
+        cxx = shutil.which("g++") or "g++"
+        cmd = [cxx, "-O2", "-std=c++17", "-I" + INCLUDE, tool_src, "-o", TOOL, "-L" + HERE,
+               "-l:lib_et_array_interface.so", "-Wl,-rpath,$ORIGIN"]
+        r = subprocess.run(cmd, capture_output=True, text=True)
+        if r.returncode != 0:
+            raise RuntimeError(f"rec_spect build failed:\n{r.stdout}\n{r.stderr}")
     return LIB
 
 
