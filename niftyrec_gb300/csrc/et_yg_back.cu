@@ -13,7 +13,7 @@ namespace {
 // camera c, or with a.units per unit (its first camera c; a mirror camera's
 // transmissions are c's read from the other end).
 template <class V>
-__global__ void __launch_bounds__(32 * kSlabsB) k_mu_carry_yg(const YgArgs a) {
+__global__ void __launch_bounds__(32 * kSlabsB) k_mu_carry_yg(const YgArgs a, int u0) {
   constexpr int C = kCarryCols;
   constexpr bool KAHAN = StorageTraits<V>::kKahan;
   const V* __restrict__ mu = reinterpret_cast<const V*>(a.mu) + a.row0;
@@ -21,7 +21,7 @@ __global__ void __launch_bounds__(32 * kSlabsB) k_mu_carry_yg(const YgArgs a) {
   __shared__ float4 s_sum[kSlabsB][C][32];
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int nchunk = (a.nx + C - 1) / C;
-  const int unit = blockIdx.x / nchunk;
+  const int unit = u0 + blockIdx.x / nchunk;
   const int cam = a.units ? a.units[unit].x : unit;
   const int x0 = (blockIdx.x % nchunk) * C;
   const int yb = lane * 4;
@@ -577,19 +577,27 @@ size_t yg_backproject_workspace(int nx, int ny, int nz, int ncam, int group, int
 
 int yg_carry_slabs() { return kCarrySlots; }
 
-int yg_mu_carry(const YgArgs& a_in, float* out, cudaStream_t st) {
+namespace {
+
+// Carries of units (or cameras) [u0, u0 + n).
+int mu_carry_range(const YgArgs& a_in, float* out, int u0, int n, cudaStream_t st) {
   const int nchunk = (a_in.nx + kCarryCols - 1) / kCarryCols;
-  const int n = a_in.units ? a_in.nunits : a_in.ncam;
   for (const Window& w : row_windows(a_in.ny, 0)) {  // carries need no halo
     YgArgs a = windowed(a_in, w);
     a.slab_T = out;
     NRGB_LAUNCH_SCOPE("k_mu_carry_yg", st);
     if (a.storage == kStorageBF16)
-      k_mu_carry_yg<__nv_bfloat16><<<n * nchunk, 32 * kSlabsB, 0, st>>>(a);
+      k_mu_carry_yg<__nv_bfloat16><<<n * nchunk, 32 * kSlabsB, 0, st>>>(a, u0);
     else
-      k_mu_carry_yg<float><<<n * nchunk, 32 * kSlabsB, 0, st>>>(a);
+      k_mu_carry_yg<float><<<n * nchunk, 32 * kSlabsB, 0, st>>>(a, u0);
   }
   return cudaGetLastError() == cudaSuccess ? kOk : kErrKernel;
+}
+
+}  // namespace
+
+int yg_mu_carry(const YgArgs& a, float* out, cudaStream_t st) {
+  return mu_carry_range(a, out, 0, a.units ? a.nunits : a.ncam, st);
 }
 
 namespace {
@@ -598,7 +606,7 @@ namespace {
 struct Pipe {
   cudaStream_t aux = nullptr;
   cudaEvent_t fork = nullptr, join = nullptr, spread_done[2] = {nullptr, nullptr},
-              gather_done[2] = {nullptr, nullptr};
+              gather_done[2] = {nullptr, nullptr}, carry_done = nullptr;
 };
 
 Pipe* pipe_for_current_device() {
@@ -638,9 +646,12 @@ int yg_backproject(const YgArgs& a_in, cudaStream_t st) {
   int group = std::max(1, std::min(a.group, nunits));
   const int ngroups = (nunits + group - 1) / group;
   group = (nunits + ngroups - 1) / ngroups;
+  const std::vector<Window> wins = row_windows(a.ny, R);
   // work space: slab carries first (unless given), then the scratch slot(s)
   const size_t vol = static_cast<size_t>(a.nz) * a.nx * scratch_rows(a.ny);
   float* slot0;
+  // carries of every unit first (computing group g+1's carries on the gather
+  // stream while group g spreads measured no faster on GB300)
   if (a.carry || !a.mu) {  // carries given, or not needed without attenuation
     a.slab_T = const_cast<float*>(a.carry);
     slot0 = a.work;
@@ -655,7 +666,6 @@ int yg_backproject(const YgArgs& a_in, cudaStream_t st) {
   auto spread = [&](const YgArgs& b, int c0, int gcount) {
     return pair ? spread_pair_by_radius<false>(R, b, c0, gcount, st) : spread_by_radius(R, b, c0, gcount, st);
   };
-  const std::vector<Window> wins = row_windows(a.ny, R);
   if (a.back_mode == kBackAdjoint) {
     // transpose of the projector: one launch per window over all cameras,
     // scattered straight into the zeroed accumulator

@@ -135,6 +135,7 @@ __device__ __forceinline__ void axpy4(float4& acc, float k, const float4& v) {
 // Rows y >= ny are zero pads of the column layout; the column pass must not
 // leak into them (the reference's column pass only produces rows < ny).
 __device__ __forceinline__ float4 mask_rows(float4 v, int yb, int ny) {
+  if (yb + 3 < ny) return v;  // every lane of a full window
   if (yb + 0 >= ny) v.x = 0.0f;
   if (yb + 1 >= ny) v.y = 0.0f;
   if (yb + 2 >= ny) v.z = 0.0f;
