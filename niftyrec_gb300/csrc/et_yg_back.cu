@@ -606,7 +606,7 @@ namespace {
 struct Pipe {
   cudaStream_t aux = nullptr;
   cudaEvent_t fork = nullptr, join = nullptr, spread_done[2] = {nullptr, nullptr},
-              gather_done[2] = {nullptr, nullptr}, carry_done = nullptr;
+              gather_done[2] = {nullptr, nullptr};
 };
 
 Pipe* pipe_for_current_device() {
