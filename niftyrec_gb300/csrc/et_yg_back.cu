@@ -602,8 +602,11 @@ int yg_mu_carry(const YgArgs& a, float* out, cudaStream_t st) {
 
 namespace {
 
-// Second stream and events of the backprojection pipeline, one set per device.
+// Second stream and events of the backprojection pipeline, one set per
+// device; `mu` makes each call's event records and waits one sequence (calls
+// from several host threads, e.g. plans on their own streams).
 struct Pipe {
+  std::mutex mu;
   cudaStream_t aux = nullptr;
   cudaEvent_t fork = nullptr, join = nullptr, spread_done[2] = {nullptr, nullptr},
               gather_done[2] = {nullptr, nullptr};
@@ -698,6 +701,7 @@ int yg_backproject(const YgArgs& a_in, cudaStream_t st) {
   }
   Pipe* pp = pipe_for_current_device();
   if (!pp) return kErrUnspecified;
+  std::lock_guard<std::mutex> pipe_lock(pp->mu);
   cudaEventRecord(pp->fork, st);
   cudaStreamWaitEvent(pp->aux, pp->fork, 0);
   int gi = 0;
