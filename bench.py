@@ -377,9 +377,23 @@ def osem_compare(act, mu, psf, cams, dev, n_subsets=8, iterations=3):
     e1.record(stream)
     torch.cuda.synchronize(dev)
     eager_ms = e0.elapsed_time(e1) / iterations
+    # the same iteration with opposite cameras in the same subset (mirror units)
+    from niftyrec_gb300.plan import opposed_subsets
+
+    plan2 = Plan((N, N, N), cams, psf, torch.from_numpy(mu).to(dev), subsets=opposed_subsets(NCAM, n_subsets))
+    plan2.osem(y, iterations=1, layout="column", graph=True)
+    g2 = plan2._graph[0]
+    torch.cuda.synchronize(dev)
+    e0.record(stream)
+    for _ in range(iterations):
+        g2.replay()
+    e1.record(stream)
+    torch.cuda.synchronize(dev)
+    opposed_ms = e0.elapsed_time(e1) / iterations
     return {"workload": f"OSEM iteration, 128^3, {NCAM} angles, {n_subsets} interleaved subsets, PSF 11x11, mu",
             "per_call_iteration_ms": round(per_call, 3), "plan_eager_iteration_ms": round(eager_ms, 3),
-            "plan_graph_iteration_ms": round(graph_ms, 3), "speedup_graph_vs_per_call": round(per_call / graph_ms, 2)}
+            "plan_graph_iteration_ms": round(graph_ms, 3), "speedup_graph_vs_per_call": round(per_call / graph_ms, 2),
+            "plan_graph_opposed_subsets_iteration_ms": round(opposed_ms, 3)}
 
 
 # ------------------------------------------------------------ batched OSEM

@@ -31,6 +31,17 @@ def interleaved_subsets(n_cameras, n_subsets):
     return np.arange(n_cameras, dtype=np.int32) % n_subsets
 
 
+def opposed_subsets(n_cameras, n_subsets):
+    """Subset id per camera for cameras evenly spaced over 360 degrees, with
+    camera k and its opposite k + n/2 in the same subset (interleaved over the
+    first half-turn: subset (k mod n/2) % n_subsets).  The library then serves
+    each opposite pair from one set of samples (mirror units); an odd camera
+    count falls back to interleaved subsets."""
+    if n_cameras % 2:
+        return interleaved_subsets(n_cameras, n_subsets)
+    return (np.arange(n_cameras, dtype=np.int32) % (n_cameras // 2)) % n_subsets
+
+
 class Plan:
     def __init__(self, shape, cameras, psf=None, attenuation=None, subsets=None, background=0.0,
                  background_attenuation=0.0, n_subsets=None):

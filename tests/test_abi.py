@@ -94,3 +94,14 @@ def test_tuning_tables(lib):
     assert lib.nrgb_get_backproject_group(*shape) == 5
     assert lib.nrgb_set_backproject_group(*shape, 0) == 0
     assert lib.nrgb_get_backproject_group(*shape) == g0
+
+
+def test_opposed_subsets():
+    from niftyrec_gb300.plan import interleaved_subsets, opposed_subsets
+
+    s = opposed_subsets(120, 8)
+    assert s.shape == (120,) and s.min() == 0 and s.max() == 7
+    assert (s[:60] == s[60:]).all()  # camera k and k + 60 share a subset
+    counts = np.bincount(s)
+    assert counts.max() - counts.min() <= 2
+    np.testing.assert_array_equal(opposed_subsets(9, 3), interleaved_subsets(9, 3))
