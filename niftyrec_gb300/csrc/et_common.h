@@ -64,4 +64,8 @@ enum Storage : int { kStorageF32 = 0, kStorageBF16 = 1 };
 
 inline int round_up(int v, int m) { return (v + m - 1) / m * m; }
 
+// Streaming multiprocessors of the current device (queried once per device;
+// 152 on GB300), for grids sized in waves.
+int sm_count();
+
 }  // namespace nrgb

@@ -13,6 +13,22 @@
 
 namespace nrgb {
 
+int sm_count() {
+  static std::mutex mu;
+  static std::map<int, int> counts;
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) return 152;
+  std::lock_guard<std::mutex> lk(mu);
+  auto it = counts.find(dev);
+  if (it != counts.end()) return it->second;
+  int n = 0;
+  if (cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || n < 1) {
+    cudaGetLastError();
+    n = 152;
+  }
+  return counts[dev] = n;
+}
+
 // ------------------------------------------------------------ tuning table
 // Cameras per backprojection scratch group, keyed by (nx, ny, nz, ncam); a
 // key of zeros is the default.  Filled by nrgb_tune_set (the autotuner in

@@ -321,7 +321,8 @@ __global__ void k_dmu_scan(const float* __restrict__ v, const float* __restrict_
 
 int grid_for(size_t n, int block) {
   const size_t g = (n + block - 1) / block;
-  return static_cast<int>(g < 152 * 64 ? g : 152 * 64);
+  const int cap = sm_count() * 64;
+  return static_cast<int>(g < cap ? g : cap);
 }
 
 template <class T>

@@ -1,6 +1,6 @@
 // Elementwise kernels of the OSEM / MLEM step and small helpers.  All are
 // HBM-streaming: float4 vectorised where the buffer allows it, grid-stride
-// loops over a grid sized to a few waves of the 152 SMs.
+// loops over a grid sized to a few waves of the SMs (152 on GB300).
 #include "et_kernels.h"
 #include "et_profile.h"
 
@@ -12,7 +12,7 @@ constexpr int kBlock = 256;
 
 int grid_for(size_t n) {
   const size_t g = (n + kBlock - 1) / kBlock;
-  const size_t cap = 152 * 16;
+  const size_t cap = static_cast<size_t>(sm_count()) * 16;
   return static_cast<int>(g < cap ? (g == 0 ? 1 : g) : cap);
 }
 

@@ -15,7 +15,7 @@ int launch_project_R(const YgArgs& a, cudaStream_t st);  // et_yg_project_kernel
 // units: 128^3 x 120 cameras 4 (0.84 ms; 2: 0.87, 8: 0.87), 256^3 x 180: 2
 // (15.9 ms; 4: 16.7), 64^3 x 60: 8 (0.149 ms; 4: 0.158).
 int project_slabs(int items, int ctas_per_sm, int nz) {
-  const int slots = 152 * ctas_per_sm;
+  const int slots = sm_count() * ctas_per_sm;
   const int most = nz >= 128 ? 16 : 8;
   for (int s = 2; s < most; s *= 2)
     if (items * s >= 4 * slots) return s;
@@ -77,7 +77,7 @@ int project_by_radius(int R, const YgArgs& a, cudaStream_t st) {
 }
 
 // Persistent grid: two CTAs per SM, whole clusters.
-constexpr int kBatchClusters = 152 * 2 / kSlabsP;
+int batch_clusters() { return sm_count() * 2 / kSlabsP; }
 
 template <int R, bool PSF>
 int launch_project_batch_R(const BatchStepDesc* d, const BatchSel& sel, bool att, int max_nz, int* counter,
@@ -86,7 +86,7 @@ int launch_project_batch_R(const BatchStepDesc* d, const BatchSel& sel, bool att
   auto go = [&](auto k) {
     cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
     NRGB_LAUNCH_SCOPE("k_project_batch_yg", st);
-    k<<<kBatchClusters * kSlabsP, 32 * kW, smem, st>>>(d, sel, counter);
+    k<<<batch_clusters() * kSlabsP, 32 * kW, smem, st>>>(d, sel, counter);
   };
   if (att)
     go(k_project_batch_yg<R, PSF, true>);

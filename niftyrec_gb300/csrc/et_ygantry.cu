@@ -140,7 +140,7 @@ int to_column_rows_bf16(const float* src_f32, const void* src_bf16, void* dst, i
 
 int to_bf16(const float* src, void* dst, size_t n, cudaStream_t st) {
   if (n == 0) return kOk;
-  const int grid = static_cast<int>(std::min<size_t>((n + 255) / 256, 152 * 16));
+  const int grid = static_cast<int>(std::min<size_t>((n + 255) / 256, static_cast<size_t>(sm_count()) * 16));
   NRGB_LAUNCH_SCOPE("k_to_bf16", st);
   k_to_bf16<<<grid, 256, 0, st>>>(src, static_cast<__nv_bfloat16*>(dst), n);
   return cudaGetLastError() == cudaSuccess ? kOk : kErrKernel;
@@ -148,7 +148,7 @@ int to_bf16(const float* src, void* dst, size_t n, cudaStream_t st) {
 
 int from_bf16(const void* src, float* dst, size_t n, cudaStream_t st) {
   if (n == 0) return kOk;
-  const int grid = static_cast<int>(std::min<size_t>((n + 255) / 256, 152 * 16));
+  const int grid = static_cast<int>(std::min<size_t>((n + 255) / 256, static_cast<size_t>(sm_count()) * 16));
   NRGB_LAUNCH_SCOPE("k_from_bf16", st);
   k_from_bf16<<<grid, 256, 0, st>>>(static_cast<const __nv_bfloat16*>(src), dst, n);
   return cudaGetLastError() == cudaSuccess ? kOk : kErrKernel;
