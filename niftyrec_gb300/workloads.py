@@ -3,6 +3,8 @@ line (e.g. under a profiler) through the device-pointer C-ABI:
 
     python -m niftyrec_gb300.workloads pair --n 128 --ncam 120 --psf 11 --reps 2
     python -m niftyrec_gb300.workloads project --n 64 --ncam 60 --psf 0 --no-att
+    python -m niftyrec_gb300.workloads osem --subsets 8 --reps 1     # plan OSEM iterations
+    python -m niftyrec_gb300.workloads batch --volumes 8 --reps 1    # batched OSEM steps
 
 Inputs are the seeded synthetic phantom, mu map and depth-dependent Gaussian
 PSF of niftyrec_gb300.synthetic; cameras rotate about the gantry axis in
@@ -23,7 +25,9 @@ def main(argv=None):
     from . import synthetic as S
 
     ap = argparse.ArgumentParser()
-    ap.add_argument("op", choices=["project", "backproject", "pair"])
+    ap.add_argument("op", choices=["project", "backproject", "pair", "osem", "batch"])
+    ap.add_argument("--subsets", type=int, default=8, help="osem: interleaved subsets")
+    ap.add_argument("--volumes", type=int, default=8, help="batch: volumes of the batched workload")
     ap.add_argument("--n", type=int, default=128)
     ap.add_argument("--ncam", type=int, default=120)
     ap.add_argument("--psf", type=int, default=11, help="PSF width (0: none)")
@@ -62,7 +66,37 @@ def main(argv=None):
     mu_p = vp(t_mu.data_ptr()) if t_mu is not None else None
     stream = torch.cuda.current_stream(dev)
 
-    def run():
+    if a.op == "osem":
+        from .plan import Plan
+
+        plan = Plan((n, n, n), cams, psf, t_mu, subsets=a.subsets)
+        counts = torch.from_numpy(S.poisson_counts(act_proj(L, act, mu, cams, psf), 50, seed=1)).to(dev)
+        state = {}
+
+        def run_osem():
+            state["x"] = plan.osem(counts, iterations=1, activity=state.get("x"))
+        run = run_osem
+    elif a.op == "batch":
+        from .batch import Batch, config_volumes
+        from .plan import Plan
+
+        vols, ys = [], []
+        for c in config_volumes(a.volumes):
+            shape = c["shape"]
+            va, vm = S.ellipsoid_phantom(shape, seed=c["seed"]), S.mu_map(shape, seed=c["seed"])
+            vp_ = S.gaussian_psf(a.psf or 11, shape[2], 0.5, c["slope"])
+            vc = S.cameras_about_y(c["ncam"], 0.0, 360.0 / c["ncam"])
+            vols.append(Plan(shape, vc, vp_, torch.from_numpy(vm).to(dev), subsets=c["subsets"]))
+            ys.append(torch.from_numpy(S.poisson_counts(act_proj(L, va, vm, vc, vp_), 50, seed=c["seed"])).to(dev))
+        batch = Batch(vols)
+
+        def run_batch():
+            batch.osem(ys, iterations=1)
+        run = run_batch
+    else:
+        run = None
+
+    def run_pair():
         sp = vp(stream.cuda_stream)
         if a.op in ("project", "pair"):
             fn = L.nrgb_project_device_bf16 if a.bf16 else L.nrgb_project_device
@@ -74,6 +108,9 @@ def main(argv=None):
             st = fn(vp(t_sino.data_ptr()), mu_p, size, vp(t_bk.data_ptr()), cams.ctypes.data_as(vp), csize, psf_p,
                     psize, 0.0, 0.0, 1, a.mode, sp)
             assert st == 0, st
+
+    if run is None:
+        run = run_pair
 
     run()
     torch.cuda.synchronize()
@@ -87,6 +124,13 @@ def main(argv=None):
           f"mirror={not a.no_mirror}: "
           f"{ev[0].elapsed_time(ev[1]) / a.reps:.3f} ms per repetition")
     return 0
+
+
+def act_proj(L, act, mu, cams, psf):
+    """Projection of a host activity through the host-buffer C-ABI (counts for the OSEM workloads)."""
+    from . import array_api as A
+
+    return A.project(act, cams, psf, mu)
 
 
 if __name__ == "__main__":
