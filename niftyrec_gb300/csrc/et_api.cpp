@@ -1031,11 +1031,11 @@ int nrgb_attenuation_grad_device(const float* d_grad_sinogram, const float* d_ac
   DeviceState& ds = current_device_state(&s);
   if (s != kOk) return s;
   std::lock_guard<std::mutex> lk(ds.mu);
-  const size_t ws = gradient_workspace(pb);
+  const size_t ws = dmu_workspace(pb);
   if ((s = ensure_arena(ds, ws)) != kOk) return s;
   cudaStream_t st = static_cast<cudaStream_t>(stream);
   cudaStreamWaitEvent(st, ds.last_use, 0);
-  g_last_path = 2;
+  g_last_path = use_fused(pb) ? 1 : 2;
   s = dmu_device(pb, d_grad_sinogram, d_activity, d_attenuation, d_out, ds.arena, ds.arena_bytes, &ds.staging, st);
   cudaEventRecord(ds.last_use, st);
   return s;

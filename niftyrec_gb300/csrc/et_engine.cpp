@@ -445,6 +445,12 @@ int project_partial_device(const Problem& pb, const float* d_act, const float* d
   return check(general_project_partial(g, d_bg_image, d_partial, do_rotate, st));
 }
 
+size_t dmu_workspace(const Problem& pb) {
+  if (use_fused(pb) && pb.storage == kStorageF32)
+    return common_bytes(pb) + sizeof(float) * (3 * col_n(pb) + sino_col_n(pb)) + 4 * 256;
+  return gradient_workspace(pb);
+}
+
 int dmu_device(const Problem& pb, const float* d_g, const float* d_act, const float* d_att, float* d_out, char* ws,
                size_t ws_bytes, Staging* stg, cudaStream_t st) {
   Carver cv(ws, ws_bytes);
@@ -452,6 +458,33 @@ int dmu_device(const Problem& pb, const float* d_g, const float* d_act, const fl
   float* d_psf;
   int s = upload_common(pb, cv, &d_geom, &d_psf, stg, st);
   if (s != kOk) return s;
+  if (use_fused(pb) && pb.storage == kStorageF32) {
+    const int cy = round_up(pb.ny, 4);
+    float* act_c = cv.take<float>(col_n(pb));
+    float* mu_c = cv.take<float>(col_n(pb));
+    float* out_c = cv.take<float>(col_n(pb));
+    float* g_c = cv.take<float>(sino_col_n(pb));
+    if (!act_c || !mu_c || !out_c || !g_c) return kErrAllocGpu;
+    if ((s = to_column(d_act, act_c, pb.nx, pb.ny, cy, pb.nz, st)) != kOk) return s;
+    if ((s = to_column(d_att, mu_c, pb.nx, pb.ny, cy, pb.nz, st)) != kOk) return s;
+    if ((s = to_column(d_g, g_c, pb.nx, pb.ny, cy, pb.cams.n, st)) != kOk) return s;
+    YgArgs a;
+    a.nx = pb.nx;
+    a.ny = pb.ny;
+    a.nz = pb.nz;
+    a.cy = cy;
+    a.ncam = pb.cams.n;
+    a.geom = d_geom;
+    a.act = act_c;
+    a.mu = mu_c;
+    a.sino = g_c;
+    a.out = out_c;
+    a.psf = d_psf;
+    a.psf_host = pb.psf_k ? pb.psf_sep.data() : nullptr;
+    a.psf_k = pb.psf_k;
+    if ((s = yg_dmu(a, st)) != kOk) return s;
+    return check(from_column(out_c, d_out, pb.nx, pb.ny, cy, pb.nz, 0, st));
+  }
   GeneralArgs g;
   g.nx = pb.nx;
   g.ny = pb.ny;

@@ -130,8 +130,9 @@ int project_device64(const Problem& pb, const double* d_act, const double* d_att
                      size_t ws_bytes, cudaStream_t st);
 int backproject_device64(const Problem& pb, const double* d_sino, const double* d_att, double* d_out, char* ws,
                          size_t ws_bytes, cudaStream_t st);
-// Exact d/dmu of sum(g * project(act, mu)) (g = d_sino); work space as
-// gradient_workspace.
+// Exact d/dmu of sum(g * project(act, mu)) (g = d_sino); work space
+// dmu_workspace.  Gantry cameras without backgrounds run the fused kernel.
+size_t dmu_workspace(const Problem& pb);
 int dmu_device(const Problem& pb, const float* d_g, const float* d_act, const float* d_att, float* d_out, char* ws,
                size_t ws_bytes, Staging* stg, cudaStream_t st);
 

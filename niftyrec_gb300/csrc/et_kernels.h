@@ -105,6 +105,10 @@ bool yg_supported(int nx, int ny, int nz, int psf_k);
 // scratch volumes of `group` cameras each).
 size_t yg_backproject_workspace(int nx, int ny, int nz, int ncam, int group, int slots = 2);
 int yg_project(const YgArgs& a, cudaStream_t st);
+// Gradient of sum(g * project(act, mu)) with respect to mu for gantry cameras
+// (column layouts: a.act, a.mu; a.sino = g [ncam][nx][cy]; a.out = the
+// gradient [nz][nx][cy], zeroed here); no backgrounds.
+int yg_dmu(const YgArgs& a, cudaStream_t st);
 int yg_backproject(const YgArgs& a, cudaStream_t st);
 
 // ---- batches of volumes (one OSEM subset step of many plans at once) ----

@@ -386,6 +386,27 @@ __device__ __forceinline__ void rowpass2_from_tile(const float4* __restrict__ sb
   rowpass2_from_tiles<R>(sbuf, sbuf, base, emit_a, kra, kca, emit_b, krb, kcb, lane, ny);
 }
 
+// Vector reduction of 4 floats into global memory (sm_90+).
+__device__ __forceinline__ void red4(float* p, const float4& v) {
+  asm volatile("red.global.add.v4.f32 [%0], {%1, %2, %3, %4};" ::"l"(p), "f"(v.x), "f"(v.y), "f"(v.z), "f"(v.w)
+               : "memory");
+}
+
+__device__ __forceinline__ float4 scale4(const float4& v, float w) {
+  return make_float4(v.x * w, v.y * w, v.z * w, v.w * w);
+}
+
+// Transposed bilinear interpolation: add w * v to each corner of footprint t
+// (corners outside the grid have weight 0 and are skipped).
+__device__ __forceinline__ void scatter4(float* __restrict__ base, const Tap& t, int yb, const float4& v) {
+  if (!t.any) return;
+  float* p = base + t.off + yb;
+  if (t.w00 != 0.0f) red4(p, scale4(v, t.w00));
+  if (t.w10 != 0.0f) red4(p + t.dx, scale4(v, t.w10));
+  if (t.w01 != 0.0f) red4(p + t.dz, scale4(v, t.w01));
+  if (t.w11 != 0.0f) red4(p + t.dx + t.dz, scale4(v, t.w11));
+}
+
 // ---------------------------------------------------------------- projector
 // Row windows: a column holds cy >= ny rows, the kernels see one window of at
 // most 128 rows at a time: rows [row0, row0 + ny) of the columns (row0 a

@@ -151,3 +151,27 @@ def test_reference_attenuation_gradient_direction():
            - A.gradient_attenuation(np.ones_like(ratio), act, mu, cams, None, truncate_negative_values=0))
     cos = float(np.sum(exact * ref) / (np.linalg.norm(exact) * np.linalg.norm(ref)))
     assert cos > 0.98, cos
+
+
+@pytest.mark.parametrize("shape,k", [((24, 24, 24), 5), ((20, 140, 28), 7), ((24, 20, 24), 0)])
+def test_fused_dmu_matches_general_path(shape, k):
+    """The fused y-gantry d/dmu kernel (clusters of depth slabs, two walks)
+    against the general-orientation kernels: the same cameras with theta_z =
+    1e-9 rad (a rotation far below float resolution) take the general path."""
+    from niftyrec_gb300 import _lib
+    from niftyrec_gb300.autograd import attenuation_grad_raw
+
+    L = _lib.load()
+    act = S.ellipsoid_phantom(shape, seed=52)
+    mu = S.mu_map(shape, seed=52)
+    psf = S.gaussian_psf(k, shape[2], 0.5, 0.05) if k else None
+    cams = np.zeros((3, 10), np.float32)
+    cams[1] = np.deg2rad(7.0 + 36.0 * np.arange(10)).astype(np.float32)
+    g = cuda(np.random.default_rng(3).uniform(0.5, 1.5, (10, shape[1], shape[2])))
+    fused = attenuation_grad_raw(g, cuda(act), cuda(mu), cams, psf).cpu().numpy()
+    assert L.nrgb_last_path() == 1
+    tilted = cams.copy()
+    tilted[2] = 1e-9
+    general = attenuation_grad_raw(g, cuda(act), cuda(mu), tilted, psf).cpu().numpy()
+    assert L.nrgb_last_path() == 2
+    assert np.linalg.norm(fused - general) / np.linalg.norm(general) < 1e-5
