@@ -24,7 +24,7 @@ namespace {
 bool all_zero3(const int* s) { return s[0] == 0 && s[1] == 0 && s[2] == 0; }
 
 // Diagnostics: which path the last call of this thread took.
-thread_local int g_last_path = 0;  // 1 = fused y-gantry kernels, 2 = general path
+thread_local int g_last_path = 0;  // 1 = fused gantry kernels (about y, or x with x and y exchanged), 2 = general path
 
 size_t fbytes(size_t n) { return n * sizeof(float); }
 
@@ -85,8 +85,8 @@ int project_host(const Problem& pb, const float* act, const float* att, float* s
   float* d_sino = cv.take<float>(nsino);
   char* w = cv.take<char>(ws);
   cudaStream_t st = ds.stream;
-  g_last_path = (use_fused(pb) && act) ? 1 : 2;
-  if (g_last_path == 1 && host_memory_readable()) {  // the layout kernels read the host arrays
+  g_last_path = ((use_fused(pb) || use_fused_x(pb)) && act) ? 1 : 2;
+  if (use_fused(pb) && act && host_memory_readable()) {  // the layout kernels read the host arrays
     d_act = const_cast<float*>(act);
     d_att = const_cast<float*>(att);
   } else {
@@ -113,8 +113,8 @@ int backproject_host(const Problem& pb, const float* sino, const float* att, flo
   float* d_out = cv.take<float>(nvox);
   char* w = cv.take<char>(ws);
   cudaStream_t st = ds.stream;
-  g_last_path = use_fused(pb) ? 1 : 2;
-  if (g_last_path == 1 && host_memory_readable()) {  // the layout kernels read the host arrays
+  g_last_path = (use_fused(pb) || use_fused_x(pb)) ? 1 : 2;
+  if (use_fused(pb) && host_memory_readable()) {  // the layout kernels read the host arrays
     d_sino = const_cast<float*>(sino);
     d_att = const_cast<float*>(att);
   } else {
@@ -178,7 +178,7 @@ int osem_step_host(const Problem& pb, float* act, const float* ysub, const float
   if ((s = h2d(d_y, ysub, nsino, st)) != kOk) return finish(ds, s);
   Problem p1 = pb;
   p1.truncate = 1;
-  g_last_path = use_fused(p1) ? 1 : 2;
+  g_last_path = (use_fused(p1) || use_fused_x(p1)) ? 1 : 2;
   if ((s = project_device(p1, d_act, d_att, d_p, w, ws, &ds.staging, st)) != kOk) return finish(ds, s);
   if ((s = osem_ratio(d_y, d_p, nsino, eps, st)) != kOk) return finish(ds, s);
   if ((s = backproject_device(p1, d_p, d_att, d_num, w, ws, &ds.staging, st)) != kOk) return finish(ds, s);
@@ -741,7 +741,7 @@ int et_array_fisher_grid(float* activity_ptr, int* activity_size, float* cameras
   cudaStream_t st = ds.stream;
   if ((s = h2d(d_act, activity_ptr, nvox, st)) != kOk) return finish(ds, s);
   if (d_att && (s = h2d(d_att, attenuation, nvox, st)) != kOk) return finish(ds, s);
-  g_last_path = use_fused(pb) ? 1 : 2;
+  g_last_path = (use_fused(pb) || use_fused_x(pb)) ? 1 : 2;
   if ((s = project_device(pb, d_act, d_att, d_sino, w, ws, &ds.staging, st)) != kOk) return finish(ds, s);
   s = fisher_from_projection(ds, cv, d_sino, nx, ny, nz, cc, xyz, n, psf, psf_size[0], psf_size[1], psf_size[2],
                              fisher_ptr, fisher_prior_ptr, st);
@@ -872,7 +872,7 @@ int project_device_call(const float* d_activity, const float* d_attenuation, con
   if ((s = ensure_arena(ds, ws)) != kOk) return s;
   cudaStream_t st = static_cast<cudaStream_t>(stream);
   cudaStreamWaitEvent(st, ds.last_use, 0);
-  g_last_path = (use_fused(pb) && d_activity) ? 1 : 2;
+  g_last_path = ((use_fused(pb) || use_fused_x(pb)) && d_activity) ? 1 : 2;
   s = project_device(pb, d_activity, d_attenuation, d_sinogram, ds.arena, ds.arena_bytes, &ds.staging, st);
   cudaEventRecord(ds.last_use, st);
   return s;
@@ -903,7 +903,7 @@ int backproject_device_call(const float* d_sinogram, const float* d_attenuation,
   if ((s = ensure_arena(ds, ws)) != kOk) return s;
   cudaStream_t st = static_cast<cudaStream_t>(stream);
   cudaStreamWaitEvent(st, ds.last_use, 0);
-  g_last_path = use_fused(pb) ? 1 : 2;
+  g_last_path = (use_fused(pb) || use_fused_x(pb)) ? 1 : 2;
   s = backproject_device(pb, d_sinogram, d_attenuation, d_out, ds.arena, ds.arena_bytes, &ds.staging, st);
   cudaEventRecord(ds.last_use, st);
   return s;
@@ -1035,7 +1035,7 @@ int nrgb_attenuation_grad_device(const float* d_grad_sinogram, const float* d_ac
   if ((s = ensure_arena(ds, ws)) != kOk) return s;
   cudaStream_t st = static_cast<cudaStream_t>(stream);
   cudaStreamWaitEvent(st, ds.last_use, 0);
-  g_last_path = use_fused(pb) ? 1 : 2;
+  g_last_path = (use_fused(pb) || use_fused_x(pb)) ? 1 : 2;
   s = dmu_device(pb, d_grad_sinogram, d_activity, d_attenuation, d_out, ds.arena, ds.arena_bytes, &ds.staging, st);
   cudaEventRecord(ds.last_use, st);
   return s;

@@ -3,6 +3,8 @@
 #include "et_engine.h"
 
 #include <algorithm>
+#include <cstdint>
+#include <initializer_list>
 #include <atomic>
 #include <cstring>
 #include <map>
@@ -102,6 +104,12 @@ int make_problem(int nx, int ny, int nz, const Cameras& cams, const float* psf, 
   pb.geom = camera_geometry(cams);
   pb.ygantry = is_y_gantry(cams);
   if (pb.ygantry && mirror_pairs()) pb.units = mirror_units(cams, nx, nz);
+  if (!pb.ygantry && nx % 4 == 0 && is_x_gantry(cams)) {
+    pb.xgantry = true;
+    pb.geom_x.resize(pb.geom.size());
+    for (size_t c = 0; c < pb.geom.size(); ++c) pb.geom_x[c] = swap_xy(pb.geom[c]);
+    if (mirror_pairs()) pb.units_x = mirror_units(cams, ny, nz, 0);
+  }
   pb.bg = bg;
   pb.bg_att = bg_att;
   pb.truncate = truncate;
@@ -115,6 +123,14 @@ int make_problem(int nx, int ny, int nz, const Cameras& cams, const float* psf, 
     pb.psf_k = kx;
     pb.psf_sep = separate_psf(psf, kx, nz);
     pb.psf_host = psf;
+    if (pb.xgantry) {  // row and column kernels exchanged
+      pb.psf_sep_x.resize(pb.psf_sep.size());
+      for (int n = 0; n < nz; ++n)
+        for (int i = 0; i < kx; ++i) {
+          pb.psf_sep_x[static_cast<size_t>(2 * kx) * n + i] = pb.psf_sep[static_cast<size_t>(2 * kx) * n + kx + i];
+          pb.psf_sep_x[static_cast<size_t>(2 * kx) * n + kx + i] = pb.psf_sep[static_cast<size_t>(2 * kx) * n + i];
+        }
+    }
   }
   *out = std::move(pb);
   return kOk;
@@ -122,6 +138,10 @@ int make_problem(int nx, int ny, int nz, const Cameras& cams, const float* psf, 
 
 bool use_fused(const Problem& pb) {
   return pb.ygantry && pb.bg == 0.0f && pb.bg_att == 0.0f && yg_supported(pb.nx, pb.ny, pb.nz, pb.psf_k);
+}
+
+bool use_fused_x(const Problem& pb) {
+  return pb.xgantry && pb.bg == 0.0f && pb.bg_att == 0.0f && yg_supported(pb.ny, pb.nx, pb.nz, pb.psf_k);
 }
 
 namespace {
@@ -132,28 +152,63 @@ size_t sino_col_n(const Problem& pb) { return static_cast<size_t>(pb.nx) * round
 constexpr size_t kSlack = 8 * 256;
 
 size_t common_bytes(const Problem& pb) {
-  return sizeof(CamGeom) * pb.cams.n + sizeof(float) * pb.psf_sep.size() + sizeof(int) * pb.units.size() + kSlack;
+  return sizeof(CamGeom) * pb.cams.n + sizeof(float) * pb.psf_sep.size() +
+         sizeof(int) * std::max(pb.units.size(), pb.units_x.size()) + kSlack;
+}
+
+// The x-gantry form reads and writes the caller's nifti buffers directly with
+// vector loads: 16-byte aligned float32 (8-byte bfloat16) buffers only.
+bool aligned_for_x(const Problem& pb, std::initializer_list<const void*> ptrs) {
+  const uintptr_t mask = pb.storage == kStorageBF16 ? 7 : 15;
+  for (const void* p : ptrs)
+    if (p && (reinterpret_cast<uintptr_t>(p) & mask)) return false;
+  return true;
+}
+
+// Gantry-kernel arguments of an x-gantry problem on nifti buffers: engine x
+// is nifti y, engine rows are nifti x (column stride nx).
+YgArgs x_args(const Problem& pb, const CamGeom* d_geom, const float* d_psf, const int2* d_units) {
+  YgArgs a;
+  a.storage = pb.storage;
+  a.pslabs = pb.pslabs;
+  a.nx = pb.ny;
+  a.ny = pb.nx;
+  a.nz = pb.nz;
+  a.cy = pb.nx;
+  a.ncam = pb.cams.n;
+  a.geom = d_geom;
+  a.units = d_units;
+  a.nunits = static_cast<int>(pb.units_x.size() / 2);
+  a.psf = d_psf;
+  a.psf_host = pb.psf_k ? pb.psf_sep_x.data() : nullptr;
+  a.psf_k = pb.psf_k;
+  a.truncate = pb.truncate;
+  return a;
 }
 
 // Uploads camera matrices, the separated PSF and the mirror-camera units
 // through the pinned staging slot that is not in flight (waiting for its
 // previous copy if needed).
+// engine_x: the x-gantry forms (geom_x, psf_sep_x, units_x).
 int upload_common(const Problem& pb, Carver& cv, CamGeom** d_geom, float** d_psf, Staging* stg, cudaStream_t st,
-                  int2** d_units = nullptr) {
+                  int2** d_units = nullptr, bool engine_x = false) {
+  const std::vector<CamGeom>& geom = engine_x ? pb.geom_x : pb.geom;
+  const std::vector<float>& psf_sep = engine_x ? pb.psf_sep_x : pb.psf_sep;
+  const std::vector<int>& units = engine_x ? pb.units_x : pb.units;
   *d_geom = cv.take<CamGeom>(pb.cams.n);
   *d_psf = nullptr;
   if (!*d_geom) return kErrAllocGpu;
   if (pb.psf_k) {
-    *d_psf = cv.take<float>(pb.psf_sep.size());
+    *d_psf = cv.take<float>(psf_sep.size());
     if (!*d_psf) return kErrAllocGpu;
   }
-  const size_t ubytes = d_units ? sizeof(int) * pb.units.size() : 0;
+  const size_t ubytes = d_units ? sizeof(int) * units.size() : 0;
   if (d_units) {
     *d_units = nullptr;
-    if (ubytes && !(*d_units = cv.take<int2>(pb.units.size() / 2))) return kErrAllocGpu;
+    if (ubytes && !(*d_units = cv.take<int2>(units.size() / 2))) return kErrAllocGpu;
   }
   const size_t gbytes = sizeof(CamGeom) * pb.cams.n;
-  const size_t pbytes = sizeof(float) * pb.psf_sep.size();
+  const size_t pbytes = sizeof(float) * psf_sep.size();
   const int slot = stg->slot;
   stg->slot ^= 1;
   if (stg->done[slot]) {
@@ -173,13 +228,13 @@ int upload_common(const Problem& pb, Carver& cv, CamGeom** d_geom, float** d_psf
     stg->bytes[slot] = want;
   }
   char* h = stg->pinned[slot];
-  std::memcpy(h, pb.geom.data(), gbytes);
-  if (pbytes) std::memcpy(h + gbytes, pb.psf_sep.data(), pbytes);
+  std::memcpy(h, geom.data(), gbytes);
+  if (pbytes) std::memcpy(h + gbytes, psf_sep.data(), pbytes);
   if (cudaMemcpyAsync(*d_geom, h, gbytes, cudaMemcpyHostToDevice, st) != cudaSuccess) return kErrTransferGpu;
   if (pbytes && cudaMemcpyAsync(*d_psf, h + gbytes, pbytes, cudaMemcpyHostToDevice, st) != cudaSuccess)
     return kErrTransferGpu;
   if (ubytes) {
-    std::memcpy(h + gbytes + pbytes, pb.units.data(), ubytes);
+    std::memcpy(h + gbytes + pbytes, units.data(), ubytes);
     if (cudaMemcpyAsync(*d_units, h + gbytes + pbytes, ubytes, cudaMemcpyHostToDevice, st) != cudaSuccess)
       return kErrTransferGpu;
   }
@@ -214,6 +269,7 @@ int widen_inputs(const Problem& pb, Carver& cv, const float** act, const float**
 
 size_t project_workspace(const Problem& pb, bool has_act, bool has_att) {
   size_t b = common_bytes(pb);
+  if (use_fused_x(pb) && has_act) return b + vol_n(pb) * 3 * sizeof(float) + widen_bytes(pb);  // or general
   if (use_fused(pb) && has_act)
     b += sizeof(float) * (col_n(pb) * (has_att ? 2 : 1) + sino_col_n(pb));
   else
@@ -223,6 +279,9 @@ size_t project_workspace(const Problem& pb, bool has_act, bool has_att) {
 
 size_t backproject_workspace(const Problem& pb, bool has_att) {
   size_t b = common_bytes(pb);
+  if (use_fused_x(pb))  // the fused form's scratch, or the general path's volumes
+    return b + std::max(yg_backproject_workspace(pb.ny, pb.nx, pb.nz, pb.cams.n, pb.group) + kSlack,
+                        sizeof(float) * vol_n(pb) * 3 + widen_bytes(pb));
   if (use_fused(pb))
     b += sizeof(float) * (col_n(pb) * (has_att ? 2 : 1) + sino_col_n(pb)) +
          yg_backproject_workspace(pb.nx, pb.ny, pb.nz, pb.cams.n, pb.group) + kSlack;
@@ -248,6 +307,19 @@ int stage_column(const Problem& pb, const float* src, float* dst, int cy, int pl
 
 int project_device(const Problem& pb, const float* d_act, const float* d_att, float* d_sino, char* ws,
                    size_t ws_bytes, Staging* stg, cudaStream_t st) {
+  if (use_fused_x(pb) && d_act && aligned_for_x(pb, {d_act, d_att, d_sino})) {
+    Carver cx(ws, ws_bytes);
+    CamGeom* d_geom;
+    float* d_psf;
+    int2* d_units;
+    int s = upload_common(pb, cx, &d_geom, &d_psf, stg, st, &d_units, true);
+    if (s != kOk) return s;
+    YgArgs a = x_args(pb, d_geom, d_psf, d_units);
+    a.act = d_act;
+    a.mu = d_att;
+    a.out = d_sino;
+    return check(yg_project(a, st));
+  }
   Carver cv(ws, ws_bytes);
   CamGeom* d_geom;
   float* d_psf;
@@ -339,6 +411,25 @@ SideStream* side_for_current_device() {
 
 int backproject_device(const Problem& pb, const float* d_sino, const float* d_att, float* d_out, char* ws,
                        size_t ws_bytes, Staging* stg, cudaStream_t st) {
+  if (use_fused_x(pb) && aligned_for_x(pb, {d_sino, d_att, d_out})) {
+    Carver cx(ws, ws_bytes);
+    CamGeom* d_geom;
+    float* d_psf;
+    int2* d_units;
+    int s = upload_common(pb, cx, &d_geom, &d_psf, stg, st, &d_units, true);
+    if (s != kOk) return s;
+    YgArgs a = x_args(pb, d_geom, d_psf, d_units);
+    a.mu = d_att;
+    a.sino = d_sino;
+    a.out = d_out;
+    a.back_mode = pb.back_mode;
+    a.group = std::max(1, std::min(pb.group, pb.cams.n));
+    a.work = cx.take<float>(yg_backproject_workspace(pb.ny, pb.nx, pb.nz, pb.cams.n, a.group) / sizeof(float));
+    if (!a.work) return kErrAllocGpu;
+    if ((s = yg_backproject(a, st)) != kOk) return s;
+    if (pb.truncate) launch_truncate(d_out, vol_n(pb), st);
+    return check(kOk);
+  }
   Carver cv(ws, ws_bytes);
   CamGeom* d_geom;
   float* d_psf;
@@ -446,6 +537,7 @@ int project_partial_device(const Problem& pb, const float* d_act, const float* d
 }
 
 size_t dmu_workspace(const Problem& pb) {
+  if (use_fused_x(pb) && pb.storage == kStorageF32) return gradient_workspace(pb);  // fused needs less
   if (use_fused(pb) && pb.storage == kStorageF32)
     return common_bytes(pb) + sizeof(float) * (3 * col_n(pb) + sino_col_n(pb)) + 4 * 256;
   return gradient_workspace(pb);
@@ -453,6 +545,21 @@ size_t dmu_workspace(const Problem& pb) {
 
 int dmu_device(const Problem& pb, const float* d_g, const float* d_act, const float* d_att, float* d_out, char* ws,
                size_t ws_bytes, Staging* stg, cudaStream_t st) {
+  if (use_fused_x(pb) && pb.storage == kStorageF32 && aligned_for_x(pb, {d_g, d_act, d_att, d_out})) {
+    Carver cx(ws, ws_bytes);
+    CamGeom* d_geom;
+    float* d_psf;
+    int s = upload_common(pb, cx, &d_geom, &d_psf, stg, st, nullptr, true);
+    if (s != kOk) return s;
+    YgArgs a = x_args(pb, d_geom, d_psf, nullptr);
+    a.units = nullptr;
+    a.nunits = 0;
+    a.act = d_act;
+    a.mu = d_att;
+    a.sino = d_g;
+    a.out = d_out;
+    return check(yg_dmu(a, st));
+  }
   Carver cv(ws, ws_bytes);
   CamGeom* d_geom;
   float* d_psf;

@@ -19,6 +19,13 @@ struct Problem {
   std::vector<CamGeom> geom;
   std::vector<int> units;  // mirror-camera units of the fused projector (mirror_units), or empty
   bool ygantry = false;
+  // Cameras rotating about x with nx a multiple of 4: the gantry kernels run
+  // on the nifti arrays directly with x and y exchanged (engine geometry,
+  // separated PSF with row and column kernels exchanged, mirror units).
+  bool xgantry = false;
+  std::vector<CamGeom> geom_x;
+  std::vector<float> psf_sep_x;
+  std::vector<int> units_x;
   int psf_k = 0;               // 0: no PSF
   std::vector<float> psf_sep;  // [nz][2k]
   const float* psf_host = nullptr;  // the caller's PSF, valid during the call only
@@ -44,6 +51,9 @@ int make_problem(int nx, int ny, int nz, const Cameras& cams, const float* psf, 
 // Whether the fused y-gantry kernels handle this problem (any ny: volumes
 // taller than 128 rows run in row windows inside the kernels' launchers).
 bool use_fused(const Problem& pb);
+// Whether the gantry kernels handle this problem with x and y exchanged
+// (cameras about x; the direct device and host-buffer entry points).
+bool use_fused_x(const Problem& pb);
 
 // Cameras per backprojection scratch group for a problem shape (tuning table;
 // all-zero shape = default for shapes without an entry).

@@ -98,19 +98,41 @@ bool is_y_gantry(const Cameras& cams) {
   return true;
 }
 
-std::vector<int> mirror_units(const Cameras& cams, int nx, int nz) {
+bool is_x_gantry(const Cameras& cams) {
+  for (int c = 0; c < cams.n; ++c)
+    if (cams.angles[cams.n + c] != 0.0f || cams.angles[2 * cams.n + c] != 0.0f) return false;
+  return true;
+}
+
+CamGeom swap_xy(const CamGeom& g) {
+  static const int sigma[3] = {1, 0, 2};
+  CamGeom o;
+  for (int r = 0; r < 3; ++r) {
+    for (int c = 0; c < 3; ++c) {
+      o.fwd[4 * r + c] = g.fwd[4 * sigma[r] + sigma[c]];
+      o.bwd[4 * r + c] = g.bwd[4 * sigma[r] + sigma[c]];
+    }
+    o.fwd[4 * r + 3] = g.fwd[4 * sigma[r] + 3];
+    o.bwd[4 * r + 3] = g.bwd[4 * sigma[r] + 3];
+  }
+  return o;
+}
+
+std::vector<int> mirror_units(const Cameras& cams, int nx, int nz, int axis) {
   const int n = cams.n;
+  const int lateral = axis == 0 ? 1 : 0;  // the rotated in-plane axis other than z
   const float cx = static_cast<float>((nx - 1) / 2.0), cz = static_cast<float>((nz - 1) / 2.0);
   std::vector<int> mate(n, -1);
   std::vector<char> taken(n, 0);
   bool any = false;
   const double two_pi = 2.0 * M_PI;
-  auto centred = [&](int c) { return cams.centers[c] == cx && cams.centers[2 * n + c] == cz; };
+  auto centred = [&](int c) { return cams.centers[lateral * n + c] == cx && cams.centers[2 * n + c] == cz; };
+  const float* theta = cams.angles.data() + static_cast<size_t>(axis) * n;
   for (int i = 0; i < n; ++i) {
     if (taken[i] || !centred(i)) continue;
     for (int j = i + 1; j < n; ++j) {
       if (taken[j] || !centred(j)) continue;
-      const double d = static_cast<double>(cams.angles[n + j]) - static_cast<double>(cams.angles[n + i]) - M_PI;
+      const double d = static_cast<double>(theta[j]) - static_cast<double>(theta[i]) - M_PI;
       const double w = d - two_pi * std::nearbyint(d / two_pi);
       if (std::fabs(w) <= kMirrorTolerance) {
         mate[i] = j;
@@ -121,7 +143,7 @@ std::vector<int> mirror_units(const Cameras& cams, int nx, int nz) {
     }
   }
   std::vector<int> units;
-  if (!any || !is_y_gantry(cams)) return units;
+  if (!any || !(axis == 0 ? is_x_gantry(cams) : is_y_gantry(cams))) return units;
   for (int i = 0; i < n; ++i) {
     if (taken[i] && mate[i] < 0) continue;  // the second camera of a pair
     units.push_back(i);

@@ -42,8 +42,18 @@ bool is_y_gantry(const Cameras& cams);
 // same points (camera j's rotated volume is camera i's mirrored in x and z).
 // Returns units {i, j} and {i, -1} (unpaired cameras) in the order of their
 // first camera, two ints per unit; empty when no pair exists.
+// axis 1 (gantry about y, the default) or 0 (gantry about x: nx is then the
+// y extent and the angles and centres are the x-rotation's and y's).
 constexpr double kMirrorTolerance = 1e-6;
-std::vector<int> mirror_units(const Cameras& cams, int nx, int nz);
+std::vector<int> mirror_units(const Cameras& cams, int nx, int nz, int axis = 1);
+
+// True when every camera rotates about the x axis only (theta_y == theta_z ==
+// 0).  Such cameras run on the gantry kernels with x and y exchanged: the
+// nifti volume [z][y][x] is then their column layout (x fastest), and
+// swap_xy gives the matrices in those coordinates (rows and columns of x and
+// y exchanged: the same float values, so the same sampling positions).
+bool is_x_gantry(const Cameras& cams);
+CamGeom swap_xy(const CamGeom& g);
 
 // Separated depth-dependent PSF (emission-lib/_et.cpp:194-215): for plane n,
 // row kernel = central row, column kernel = central column / centre value.
