@@ -264,6 +264,8 @@ def run_ours(args):
     ms_adj, _, _ = timed(max(3, args.steps // 2), mode=1)
     adjoint = world * 1000.0 / reduce_max(sum(ms_adj) / len(ms_adj), world)
 
+    grad = None if args.no_grad else grad_compare(L, t_act, t_mu, t_sino, t_bk, cams, psf, stream, flush, dev)
+
     # end to end through the reference-facing C-ABI with host buffers
     y = t_sino.cpu().numpy()
     A.project(act, cams, psf, mu)
@@ -319,6 +321,8 @@ def run_ours(args):
         "gpu_launches": int(launches),
         "clocks": clocks,
     }
+    if grad:
+        out["attenuation_gradient"] = grad
     if not args.no_osem:
         out["osem"] = osem_compare(act, mu, psf, cams, dev)
     if not args.no_batch:
@@ -331,6 +335,63 @@ def run_ours(args):
         import torch.distributed as dist
 
         dist.destroy_process_group()
+
+
+# --------------------------------------------------- attenuation gradient
+def grad_compare(L, t_act, t_mu, t_sino, t_out, cams, psf, stream, flush, dev, reps=3):
+    """The reference attenuation gradient (et_array_gradient_attenuation
+    semantics) on device buffers at the bench workload: the gantry kernels
+    against the general-orientation path (the same cameras tilted by 1e-9 rad
+    about z, which leaves the gantry form)."""
+    import torch
+
+    vp = ctypes.c_void_p
+    size = (ctypes.c_int * 3)(N, N, N)
+    psize = (ctypes.c_int * 3)(K, K, N)
+    psf_c = np.ascontiguousarray(psf, np.float32)
+    gantry = np.zeros((3, NCAM), np.float32)
+    gantry[1] = cams
+    tilted = gantry.copy()
+    tilted[2] = 1e-9
+
+    def run(cm):
+        cs = (ctypes.c_int * 2)(cm.shape[1], cm.shape[0])
+        st = L.nrgb_gradient_attenuation_device(vp(t_sino.data_ptr()), vp(t_act.data_ptr()), vp(t_mu.data_ptr()),
+                                                size, vp(t_out.data_ptr()), cm.ctypes.data_as(vp), cs,
+                                                psf_c.ctypes.data_as(vp), psize, 0.0, 0.0, 0, vp(stream.cuda_stream))
+        if st:
+            raise RuntimeError(f"nrgb_gradient_attenuation_device status {st}")
+        return L.nrgb_last_path()
+
+    def timed(cm, n):
+        ms = []
+        for _ in range(n):
+            flush.zero_()
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record(stream)
+            run(cm)
+            b.record(stream)
+            torch.cuda.synchronize(dev)
+            ms.append(a.elapsed_time(b))
+        return statistics.median(ms)
+
+    paths = (run(gantry), run(tilted))
+    torch.cuda.synchronize(dev)
+    fused_ms = timed(gantry, reps)
+    L.nrgb_profile_enable(1)
+    run(gantry)
+    torch.cuda.synchronize(dev)
+    buf = ctypes.create_string_buffer(1 << 16)
+    L.nrgb_profile_summary(buf, len(buf))
+    L.nrgb_profile_enable(0)
+    kernels = {}
+    for line in buf.value.decode().splitlines():
+        name, cnt, ms = line.split()
+        kernels[name] = {"launches": int(cnt), "ms_total": round(float(ms), 3)}
+    general_ms = timed(tilted, 2)
+    return {"workload": "et_array_gradient_attenuation semantics, 128^3, 120 angles, PSF 11x11, mu, device buffers",
+            "paths": list(paths), "fused_ms": round(fused_ms, 3), "general_ms": round(general_ms, 3),
+            "speedup": round(general_ms / fused_ms, 2), "fused_kernels": kernels}
 
 
 # ------------------------------------------------------------------- OSEM
@@ -579,6 +640,7 @@ def main():
     ap.add_argument("--cpu-angles", type=int, default=24)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-osem", action="store_true")
+    ap.add_argument("--no-grad", action="store_true")
     ap.add_argument("--no-batch", action="store_true")
     args = ap.parse_args()
     if args.warmup < 3:

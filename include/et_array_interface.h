@@ -214,6 +214,16 @@ int nrgb_attenuation_grad_device(const float *d_grad_sinogram, const float *d_ac
                                  const float *psf, const int *psf_size, float background,
                                  float background_attenuation, void *stream);
 
+/* et_array_gradient_attenuation (emission-lib/_et_array_interface.h:48, the
+ * GPU semantics of emission-lib/_et.cpp:1679-1924) on device buffers in nifti
+ * order, enqueued on `stream` (a cudaStream_t or null): size = {nx, ny, nz},
+ * d_sinogram [ncam][ny][nx].  No counterpart in the reference (which takes
+ * host arrays only). */
+int nrgb_gradient_attenuation_device(const float *d_sinogram, const float *d_activity, const float *d_attenuation,
+                                     const int *size, float *d_out, const float *cameras, const int *cameras_size,
+                                     const float *psf, const int *psf_size, float background,
+                                     float background_attenuation, int truncate, void *stream);
+
 /* Backprojection that allocates nothing.  No counterpart in the reference.
  * For callers that cannot call cudaMalloc: code inside a CUDA-graph capture,
  * processes whose device memory is held by a framework's allocator, real-time

@@ -62,6 +62,7 @@ PROTOTYPES = {
     "nrgb_backproject_device_bf16": (_I, [_P, _P, _PI, _P, _P, _PI, _P, _PI, _F, _F, _I, _I, _P]),
     "nrgb_backproject_device_noalloc":(_I, [_P, _P, _PI, _P, _P, _PI, _P, _PI, _F, _F, _I, _P]),
     "nrgb_attenuation_grad_device": (_I, [_P, _P, _P, _PI, _P, _P, _PI, _P, _PI, _F, _F, _P]),
+    "nrgb_gradient_attenuation_device": (_I, [_P, _P, _P, _PI, _P, _P, _PI, _P, _PI, _F, _F, _I, _P]),
     "nrgb_project_device_f64": (_I, [_P, _P, _PI, _P, _P, _PI, _P, _PI, ctypes.c_double, ctypes.c_double, _I, _P]),
     "nrgb_backproject_device_f64": (_I, [_P, _P, _PI, _P, _P, _PI, _P, _PI, ctypes.c_double, ctypes.c_double, _I,
                                          _P]),

@@ -22,7 +22,7 @@ INCLUDE = os.path.join(os.path.dirname(HERE), "include")
 
 SOURCES = ["et_geometry.cpp", "et_engine.cpp", "et_api.cpp", "et_profile.cpp", "et_general.cu", "et_ygantry.cu",
            "et_yg_project.cu", "et_yg_proj_r01.cu", "et_yg_proj_r23.cu", "et_yg_proj_r45.cu", "et_yg_proj_r67.cu",
-           "et_yg_back.cu", "et_yg_dmu.cu", "et_update.cu", "et_noalloc.cu", "et_plan.cpp", "et_fisher.cu", "et_nifti.cpp"]
+           "et_yg_back.cu", "et_yg_dmu.cu", "et_yg_grad.cu", "et_update.cu", "et_noalloc.cu", "et_plan.cpp", "et_fisher.cu", "et_nifti.cpp"]
 TOOL = os.path.join(HERE, "rec_spect")  # command-line reconstruction (csrc/rec_spect.cpp)
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]

@@ -142,10 +142,17 @@ int gradient_host(const Problem& pb, const float* sino, const float* act, const 
   float* d_out = cv.take<float>(nvox);
   char* w = cv.take<char>(ws);
   cudaStream_t st = ds.stream;
-  if ((s = h2d(d_sino, sino, nsino, st)) != kOk) return finish(ds, s);
-  if ((s = h2d(d_act, act, nvox, st)) != kOk) return finish(ds, s);
-  if ((s = h2d(d_att, att, nvox, st)) != kOk) return finish(ds, s);
-  g_last_path = 2;
+  const bool fused = (use_fused(pb) || use_fused_x(pb)) && pb.storage == kStorageF32;
+  g_last_path = fused ? 1 : 2;
+  if (fused && use_fused(pb) && host_memory_readable()) {  // the layout kernels read the host arrays
+    d_sino = const_cast<float*>(sino);
+    d_act = const_cast<float*>(act);
+    d_att = const_cast<float*>(att);
+  } else {
+    if ((s = h2d(d_sino, sino, nsino, st)) != kOk) return finish(ds, s);
+    if ((s = h2d(d_act, act, nvox, st)) != kOk) return finish(ds, s);
+    if ((s = h2d(d_att, att, nvox, st)) != kOk) return finish(ds, s);
+  }
   s = gradient_device(pb, d_sino, d_act, d_att, d_out, w, ws, &ds.staging, st);
   if (s == kOk) s = d2h(out, d_out, nvox, st);
   return finish(ds, s);
@@ -1037,6 +1044,33 @@ int nrgb_attenuation_grad_device(const float* d_grad_sinogram, const float* d_ac
   cudaStreamWaitEvent(st, ds.last_use, 0);
   g_last_path = (use_fused(pb) || use_fused_x(pb)) ? 1 : 2;
   s = dmu_device(pb, d_grad_sinogram, d_activity, d_attenuation, d_out, ds.arena, ds.arena_bytes, &ds.staging, st);
+  cudaEventRecord(ds.last_use, st);
+  return s;
+}
+
+// et_array_gradient_attenuation on device buffers (nifti order, float32),
+// enqueued on `stream`.
+int nrgb_gradient_attenuation_device(const float* d_sinogram, const float* d_activity, const float* d_attenuation,
+                                     const int* size, float* d_out, const float* cameras, const int* cameras_size,
+                                     const float* psf, const int* psf_size, float background,
+                                     float background_attenuation, int truncate, void* stream) {
+  if (!size || !cameras || !cameras_size || !d_sinogram || !d_activity || !d_attenuation || !d_out)
+    return kErrParameters;
+  Cameras cc;
+  int s = expand_cameras(cameras, cameras_size[0], cameras_size[1], size, &cc);
+  if (s != kOk) return s;
+  Problem pb;
+  s = make_problem(size[0], size[1], size[2], cc, psf, psf_size, background, background_attenuation, truncate, &pb);
+  if (s != kOk) return s;
+  DeviceState& ds = current_device_state(&s);
+  if (s != kOk) return s;
+  std::lock_guard<std::mutex> lk(ds.mu);
+  const size_t ws = gradient_workspace(pb);
+  if ((s = ensure_arena(ds, ws)) != kOk) return s;
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  cudaStreamWaitEvent(st, ds.last_use, 0);
+  g_last_path = (use_fused(pb) || use_fused_x(pb)) && pb.storage == kStorageF32 ? 1 : 2;
+  s = gradient_device(pb, d_sinogram, d_activity, d_attenuation, d_out, ds.arena, ds.arena_bytes, &ds.staging, st);
   cudaEventRecord(ds.last_use, st);
   return s;
 }

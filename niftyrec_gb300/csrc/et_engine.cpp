@@ -290,7 +290,22 @@ size_t backproject_workspace(const Problem& pb, bool has_att) {
   return b;
 }
 
-size_t gradient_workspace(const Problem& pb) { return common_bytes(pb) + sizeof(float) * vol_n(pb) * 3; }
+namespace {
+// The general-orientation path's three work volumes.
+size_t general3_workspace(const Problem& pb) { return common_bytes(pb) + sizeof(float) * vol_n(pb) * 3; }
+int grad_group(const Problem& pb) { return std::max(1, std::min(pb.group, pb.cams.n)); }
+}  // namespace
+
+size_t gradient_workspace(const Problem& pb) {
+  if (pb.storage != kStorageF32) return general3_workspace(pb);
+  if (use_fused_x(pb))  // the fused form's scratch, or the general path's volumes
+    return std::max(general3_workspace(pb),
+                    common_bytes(pb) + yg_gradient_workspace(pb.ny, pb.nx, pb.nz, pb.cams.n, grad_group(pb)) + kSlack);
+  if (use_fused(pb))
+    return common_bytes(pb) + sizeof(float) * (3 * col_n(pb) + sino_col_n(pb)) +
+           yg_gradient_workspace(pb.nx, pb.ny, pb.nz, pb.cams.n, grad_group(pb)) + kSlack;
+  return general3_workspace(pb);
+}
 
 namespace {
 
@@ -537,10 +552,10 @@ int project_partial_device(const Problem& pb, const float* d_act, const float* d
 }
 
 size_t dmu_workspace(const Problem& pb) {
-  if (use_fused_x(pb) && pb.storage == kStorageF32) return gradient_workspace(pb);  // fused needs less
+  if (use_fused_x(pb) && pb.storage == kStorageF32) return general3_workspace(pb);  // fused needs less
   if (use_fused(pb) && pb.storage == kStorageF32)
     return common_bytes(pb) + sizeof(float) * (3 * col_n(pb) + sino_col_n(pb)) + 4 * 256;
-  return gradient_workspace(pb);
+  return general3_workspace(pb);
 }
 
 int dmu_device(const Problem& pb, const float* d_g, const float* d_act, const float* d_att, float* d_out, char* ws,
@@ -615,11 +630,65 @@ int dmu_device(const Problem& pb, const float* d_g, const float* d_act, const fl
 
 int gradient_device(const Problem& pb, const float* d_sino, const float* d_act, const float* d_att, float* d_out,
                     char* ws, size_t ws_bytes, Staging* stg, cudaStream_t st) {
+  if (use_fused_x(pb) && pb.storage == kStorageF32 && aligned_for_x(pb, {d_sino, d_act, d_att, d_out})) {
+    Carver cx(ws, ws_bytes);
+    CamGeom* d_geom;
+    float* d_psf;
+    int s = upload_common(pb, cx, &d_geom, &d_psf, stg, st, nullptr, true);
+    if (s != kOk) return s;
+    YgArgs a = x_args(pb, d_geom, d_psf, nullptr);
+    a.units = nullptr;
+    a.nunits = 0;
+    a.gradient = 1;
+    a.act = d_act;
+    a.mu = d_att;
+    a.sino = d_sino;
+    a.out = d_out;
+    a.group = grad_group(pb);
+    a.work = cx.take<float>(yg_gradient_workspace(pb.ny, pb.nx, pb.nz, pb.cams.n, a.group) / sizeof(float));
+    if (!a.work) return kErrAllocGpu;
+    if ((s = yg_backproject(a, st)) != kOk) return s;
+    if (pb.truncate) launch_truncate(d_out, vol_n(pb), st);
+    return check(kOk);
+  }
   Carver cv(ws, ws_bytes);
   CamGeom* d_geom;
   float* d_psf;
   int s = upload_common(pb, cv, &d_geom, &d_psf, stg, st);
   if (s != kOk) return s;
+  if (use_fused(pb) && pb.storage == kStorageF32) {
+    const int cy = round_up(pb.ny, 4);
+    float* act_c = cv.take<float>(col_n(pb));
+    float* mu_c = cv.take<float>(col_n(pb));
+    float* out_c = cv.take<float>(col_n(pb));
+    float* sino_c = cv.take<float>(sino_col_n(pb));
+    const int group = grad_group(pb);
+    float* work = cv.take<float>(yg_gradient_workspace(pb.nx, pb.ny, pb.nz, pb.cams.n, group) / sizeof(float));
+    if (!act_c || !mu_c || !out_c || !sino_c || !work) return kErrAllocGpu;
+    if ((s = to_column(d_act, act_c, pb.nx, pb.ny, cy, pb.nz, st)) != kOk) return s;
+    if ((s = to_column(d_att, mu_c, pb.nx, pb.ny, cy, pb.nz, st)) != kOk) return s;
+    if ((s = to_column(d_sino, sino_c, pb.nx, pb.ny, cy, pb.cams.n, st)) != kOk) return s;
+    YgArgs a;
+    a.nx = pb.nx;
+    a.ny = pb.ny;
+    a.nz = pb.nz;
+    a.cy = cy;
+    a.ncam = pb.cams.n;
+    a.geom = d_geom;
+    a.act = act_c;
+    a.mu = mu_c;
+    a.sino = sino_c;
+    a.out = out_c;
+    a.psf = d_psf;
+    a.psf_host = pb.psf_k ? pb.psf_sep.data() : nullptr;
+    a.psf_k = pb.psf_k;
+    a.pslabs = pb.pslabs;
+    a.gradient = 1;
+    a.group = group;
+    a.work = work;
+    if ((s = yg_backproject(a, st)) != kOk) return s;
+    return check(from_column(out_c, d_out, pb.nx, pb.ny, cy, pb.nz, pb.truncate, st));
+  }
   GeneralArgs g;
   g.nx = pb.nx;
   g.ny = pb.ny;

@@ -92,6 +92,10 @@ struct YgArgs {
   // (yg_mu_carry) for exactly these cameras; the backprojector then skips
   // that pass and the work space holds only the scratch slot(s).
   const float* carry = nullptr;
+  // Non-zero: yg_backproject spreads the reference's attenuation gradient
+  // instead (a.act and a.mu sampled, a.sino the camera planes; no carries,
+  // no mirror units), then gathers it like the reference-mode backprojection.
+  int gradient = 0;
 };
 // Carry slots per camera of the backprojector's transmission carries (the
 // exclusive prefix of every depth slab, then the column total).
@@ -110,6 +114,12 @@ int yg_project(const YgArgs& a, cudaStream_t st);
 // gradient [nz][nx][cy], zeroed here); no backgrounds.
 int yg_dmu(const YgArgs& a, cudaStream_t st);
 int yg_backproject(const YgArgs& a, cudaStream_t st);
+// Spread of the reference attenuation gradient for cameras [c0, c0 + gcount)
+// into the scratch volumes a.temp (one row window: a.row0, a.ny, a.cs).
+int yg_grad_spread(const YgArgs& a, int c0, int gcount, cudaStream_t st);
+// Bytes of work space of the fused attenuation gradient (`slots` scratch
+// volumes of `group` cameras each; no carries).
+size_t yg_gradient_workspace(int nx, int ny, int nz, int ncam, int group, int slots = 2);
 
 // ---- batches of volumes (one OSEM subset step of many plans at once) ----
 constexpr int kMaxBatch = 64;    // volumes per batched launch

@@ -554,6 +554,11 @@ size_t yg_backproject_workspace(int nx, int ny, int nz, int ncam, int group, int
   return sizeof(float) * (slabs + static_cast<size_t>(slots) * vol * std::max(1, std::min(group, ncam)));
 }
 
+size_t yg_gradient_workspace(int nx, int ny, int nz, int ncam, int group, int slots) {
+  const size_t vol = static_cast<size_t>(nz) * nx * scratch_rows(ny);
+  return sizeof(float) * static_cast<size_t>(slots) * vol * std::max(1, std::min(group, ncam));
+}
+
 int yg_carry_slabs() { return kCarrySlots; }
 
 namespace {
@@ -618,7 +623,7 @@ int yg_backproject(const YgArgs& a_in, cudaStream_t st) {
   YgArgs a = a_in;
   const int R = a.psf ? (a.psf_k - 1) / 2 : 0;
   // mirror units: float32 mu
-  const bool pair = a.units && a.nunits > 0 && a.storage != kStorageBF16;
+  const bool pair = !a.gradient && a.units && a.nunits > 0 && a.storage != kStorageBF16;
   if (!pair) {
     a.units = nullptr;
     a.nunits = 0;
@@ -634,7 +639,7 @@ int yg_backproject(const YgArgs& a_in, cudaStream_t st) {
   float* slot0;
   // carries of every unit first (computing group g+1's carries on the gather
   // stream while group g spreads measured no faster on GB300)
-  if (a.carry || !a.mu) {  // carries given, or not needed without attenuation
+  if (a.gradient || a.carry || !a.mu) {  // carries given, or not needed
     a.slab_T = const_cast<float*>(a.carry);
     slot0 = a.work;
   } else {
@@ -646,9 +651,10 @@ int yg_backproject(const YgArgs& a_in, cudaStream_t st) {
   if (a.sino_ready) cudaStreamWaitEvent(st, static_cast<cudaEvent_t>(a.sino_ready), 0);
   a.group = group;
   auto spread = [&](const YgArgs& b, int c0, int gcount) {
+    if (a.gradient) return yg_grad_spread(b, c0, gcount, st);
     return pair ? spread_pair_by_radius<false>(R, b, c0, gcount, st) : spread_by_radius(R, b, c0, gcount, st);
   };
-  if (a.back_mode == kBackAdjoint) {
+  if (a.back_mode == kBackAdjoint && !a.gradient) {
     // transpose of the projector: one launch per window over all cameras,
     // scattered straight into the zeroed accumulator
     const size_t full = static_cast<size_t>(a.nz) * a.nx * a.cy;

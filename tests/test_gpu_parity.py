@@ -156,8 +156,45 @@ def test_gradient_attenuation_matches_restated_reference(o32):
     cams = S.cameras_about_y(6, 2.0)
     y = S.poisson_counts(o32.project(act, cams, psf, mu), 50)
     g = A.gradient_attenuation(y, act, mu, cams, psf)
+    assert A.last_path() == FUSED
     go = o32.gradient_attenuation(y, act, mu, cams, psf)
     assert rel_l2(g, go) < RTOL
+
+
+@pytest.mark.parametrize("shape,k,ncam,truncate", [
+    ((20, 150, 20), 7, 5, 0),    # row windows (ny > 128)
+    ((28, 36, 44), 15, 7, 1),    # radius 7, truncation of negative values
+    ((16, 20, 24), 0, 4, 0),     # no PSF
+    ((260, 8, 264), 15, 2, 0),   # PSF too large for the kernel-parameter table
+])
+def test_fused_gradient_attenuation(o32, shape, k, ncam, truncate):
+    """The reference attenuation gradient on the gantry kernels (sampled
+    activity and mu, suffix sums across depth slabs, PSF, inverse-rotation
+    gather) against the oracle, with signed sinogram weights."""
+    act = S.ellipsoid_phantom(shape, seed=71)
+    mu = S.mu_map(shape, seed=71)
+    psf = S.gaussian_psf(k, shape[2]) if k else None
+    cams = S.cameras_about_y(ncam, 7.0)
+    y = np.random.default_rng(71).uniform(-0.5, 1.5, (ncam, shape[1], shape[2])).astype(np.float32)
+    g = A.gradient_attenuation(y, act, mu, cams, psf, truncate_negative_values=truncate)
+    assert A.last_path() == FUSED
+    go = o32.gradient_attenuation(y, act, mu, cams, psf, truncate=truncate)
+    assert rel_l2(g, go) < RTOL
+
+
+def test_fused_gradient_attenuation_x_gantry(o32):
+    """Cameras rotating about x: the gradient runs on the gantry kernels with
+    x and y exchanged."""
+    shape = (20, 28, 24)
+    act = S.ellipsoid_phantom(shape, seed=72)
+    mu = S.mu_map(shape, seed=72)
+    psf = S.gaussian_psf(5, shape[2], 0.5, 0.05)
+    cams = np.zeros((3, 6), np.float32)
+    cams[0] = np.deg2rad(3.0 + 60.0 * np.arange(6)).astype(np.float32)
+    y = np.random.default_rng(72).uniform(0.0, 2.0, (6, shape[1], shape[2])).astype(np.float32)
+    g = A.gradient_attenuation(y, act, mu, cams, psf)
+    assert A.last_path() == FUSED
+    assert rel_l2(g, o32.gradient_attenuation(y, act, mu, cams, psf)) < RTOL
 
 
 def test_known_answer_angle0_is_depth_sum():
