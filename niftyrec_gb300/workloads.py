@@ -5,6 +5,7 @@ line (e.g. under a profiler) through the device-pointer C-ABI:
     python -m niftyrec_gb300.workloads project --n 64 --ncam 60 --psf 0 --no-att
     python -m niftyrec_gb300.workloads osem --subsets 8 --reps 1     # plan OSEM iterations
     python -m niftyrec_gb300.workloads batch --volumes 8 --reps 1    # batched OSEM steps
+    python -m niftyrec_gb300.workloads gradient --ncam 40 --reps 1   # et_array_gradient_attenuation
 
 Inputs are the seeded synthetic phantom, mu map and depth-dependent Gaussian
 PSF of niftyrec_gb300.synthetic; cameras rotate about the gantry axis in
@@ -25,7 +26,7 @@ def main(argv=None):
     from . import synthetic as S
 
     ap = argparse.ArgumentParser()
-    ap.add_argument("op", choices=["project", "backproject", "pair", "osem", "batch"])
+    ap.add_argument("op", choices=["project", "backproject", "pair", "osem", "batch", "gradient"])
     ap.add_argument("--subsets", type=int, default=8, help="osem: interleaved subsets")
     ap.add_argument("--volumes", type=int, default=8, help="batch: volumes of the batched workload")
     ap.add_argument("--n", type=int, default=128)
@@ -93,6 +94,19 @@ def main(argv=None):
         def run_batch():
             batch.osem(ys, iterations=1)
         run = run_batch
+    elif a.op == "gradient":  # the reference attenuation gradient of the projection (float32, mu required)
+        if a.bf16 or t_mu is None:
+            raise SystemExit("gradient: float32 activity and mu required")
+        st = L.nrgb_project_device(vp(t_act.data_ptr()), mu_p, size, vp(t_sino.data_ptr()), cams.ctypes.data_as(vp),
+                                   csize, psf_p, psize, 0.0, 0.0, 1, vp(stream.cuda_stream))
+        assert st == 0, st
+
+        def run_gradient():
+            st = L.nrgb_gradient_attenuation_device(vp(t_sino.data_ptr()), vp(t_act.data_ptr()), mu_p, size,
+                                                    vp(t_bk.data_ptr()), cams.ctypes.data_as(vp), csize, psf_p,
+                                                    psize, 0.0, 0.0, 0, vp(stream.cuda_stream))
+            assert st == 0, st
+        run = run_gradient
     else:
         run = None
 
