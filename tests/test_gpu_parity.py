@@ -197,6 +197,45 @@ def test_fused_gradient_attenuation_x_gantry(o32):
     assert rel_l2(g, o32.gradient_attenuation(y, act, mu, cams, psf)) < RTOL
 
 
+def close(a, b, tol=RTOL):
+    """Relative L2 error below tol, or both (near) zero."""
+    nb = float(np.linalg.norm(np.asarray(b, np.float64)))
+    if nb == 0.0:
+        return float(np.abs(a).max(initial=0.0)) <= 1e-12
+    return rel_l2(a, b) < tol
+
+
+@pytest.mark.parametrize("shape,k,ncam", [((1, 1, 1), 0, 1), ((2, 3, 5), 3, 2), ((3, 12, 16), 3, 4),
+                                          ((1, 7, 9), 5, 3), ((5, 1, 6), 0, 2), ((3, 5, 4), 5, 5)])
+def test_tiny_and_ragged_volumes(o32, shape, k, ncam):
+    """One-voxel, one-plane and one-row volumes, PSFs wider than the volume,
+    odd sizes, more depth slabs than planes and an opposite-angle pair:
+    projection, both backprojectors and the attenuation gradient against the
+    oracle."""
+    torch = pytest.importorskip("torch")
+    from niftyrec_gb300.autograd import backproject_raw
+
+    rng = np.random.default_rng(sum(shape) + k)
+    act = rng.uniform(0.5, 2.0, shape).astype(np.float32)
+    mu = rng.uniform(0.0, 0.1, shape).astype(np.float32)
+    psf = S.gaussian_psf(k, shape[2]) if k else None
+    cams = S.cameras_about_y(ncam, 7.0)
+    nz = shape[0]
+    s = A.project(act, cams, psf, mu)
+    assert A.last_path() == FUSED
+    so = o32.project(act, cams, psf, mu)
+    assert close(s, so)
+    b = A.backproject(so, cams, psf, mu, nz=nz)
+    assert A.last_path() == FUSED
+    assert close(b, o32.backproject(so, cams, psf, mu, nz=nz))
+    bt = backproject_raw(torch.from_numpy(so).cuda(), torch.from_numpy(mu).cuda(), cams, psf, nz=nz, mode=1)
+    assert close(bt.cpu().numpy(), o32.backproject(so, cams, psf, mu, truncate=0, adjoint=True, nz=nz))
+    y = rng.uniform(-0.5, 1.5, so.shape).astype(np.float32)
+    g = A.gradient_attenuation(y, act, mu, cams, psf)
+    assert A.last_path() == FUSED
+    assert close(g, o32.gradient_attenuation(y, act, mu, cams, psf))
+
+
 def test_known_answer_angle0_is_depth_sum():
     vol = S.ellipsoid_phantom((32, 32, 32), seed=8)
     s = A.project(vol, np.zeros(1, np.float32))
