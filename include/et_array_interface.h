@@ -349,10 +349,14 @@ int nrgb_get_mirror_pairs(void);
  * brackets every launch with CUDA events on its stream (0 turns it off; both
  * clear the record); nrgb_profile_summary writes one "name launches total_ms"
  * line per kernel into buf, waiting for the recorded events, and returns the
- * size it needs. */
+ * size it needs.  nrgb_profile_only(name) restricts the timing to launches of
+ * that kernel name (null or "" times every launch): the events between
+ * launches cost a few microseconds each on the GPU, so a throughput run times
+ * one kernel only. */
 long long nrgb_launch_count(void);
 int nrgb_profile_enable(int on);
 int nrgb_profile_summary(char *buf, int len);
+int nrgb_profile_only(const char *name);
 
 /* NIfTI-1 single-file images (no counterpart in the reference library; its
  * command-line tool reads and writes them with nifti1_io, apps/command_line_tools/

@@ -101,6 +101,7 @@ PROTOTYPES = {
     "nrgb_launch_count": (ctypes.c_longlong, []),
     "nrgb_profile_enable": (_I, [_I]),
     "nrgb_profile_summary": (_I, [ctypes.c_char_p, _I]),
+    "nrgb_profile_only": (_I, [ctypes.c_char_p]),
 }
 
 _lib = None

@@ -17,6 +17,7 @@ namespace {
 std::atomic<long long> g_launches{0};
 std::atomic<bool> g_timing{false};
 std::mutex g_mu;
+std::string g_only;  // time only launches of this name (empty: all)
 
 struct Entry {
   const char* name;
@@ -43,6 +44,7 @@ void count_launch() { g_launches.fetch_add(1, std::memory_order_relaxed); }
 int prof_begin(const char* name, cudaStream_t st) {
   if (!g_timing.load(std::memory_order_relaxed)) return -1;
   std::lock_guard<std::mutex> lk(g_mu);
+  if (!g_only.empty() && g_only != name) return -1;
   Entry e{name, get_event(), get_event()};
   cudaEventRecord(e.a, st);
   g_entries.push_back(e);
@@ -71,6 +73,13 @@ int nrgb_profile_enable(int on) {
   }
   nrgb::g_entries.clear();
   nrgb::g_timing.store(on != 0);
+  return 0;
+}
+
+// Restrict the event timing to launches named `name` (null or "": all).
+int nrgb_profile_only(const char* name) {
+  std::lock_guard<std::mutex> lk(nrgb::g_mu);
+  nrgb::g_only = name ? name : "";
   return 0;
 }
 
