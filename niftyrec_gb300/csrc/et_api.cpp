@@ -554,7 +554,7 @@ int et_array_gradient_attenuation(float* sino, int* sino_size, float* activity, 
   return gradient_host(pb, sino, activity, attenuation, gradient);
 }
 
-// The spelling used in the project's spec description.
+// Alias with the words in the other order (et_array_attenuation_gradient).
 int et_array_attenuation_gradient(float* sino, int* sino_size, float* activity, int* activity_size, float* gradient,
                                   int* gradient_size, float* cameras, int* cameras_size, float* psf, int* psf_size,
                                   float* attenuation, int* attenuation_size, float background,
