@@ -1,6 +1,6 @@
 /*
  * et_oracle.c -- CPU restatement of NiftyRec's rotation-based SPECT emission
- * path, used ONLY as test infrastructure: the checker that the CUDA product
+ * path, used ONLY as test infrastructure: the oracle that the CUDA product
  * path is compared against, and the "port" CPU baseline of bench.py.  Nothing
  * in the shipped library links or calls this file.
  *

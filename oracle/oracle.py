@@ -1,4 +1,4 @@
-"""ctypes front end of the two CPU checkers.  Test infrastructure only.
+"""ctypes front end of the two CPU oracles.  Test infrastructure only.
 
 * ``Restated`` -- the oracle's own C restatement (``et_oracle.c``), float
   (``"f32"``, follows the reference's float arithmetic) or double (``"f64"``,
