@@ -123,6 +123,7 @@ __device__ __forceinline__ void spread_body(const YgArgs& a, int c0, const float
     if (ATT && warp + kW * k < NS && xp >= 0 && xp < a.nx && yok)
       Tc[k] = ldg4(a.slab_T + ((static_cast<size_t>(cam) * kCarrySlots + slab) * a.nx + xp) * a.cy + a.row0 + yb);
   }
+  ybuf_zero_pads();
   __syncthreads();
 
   for (int z = zbeg; z < zend; ++z) {
@@ -268,6 +269,7 @@ __device__ __forceinline__ void spread_pair_body(const YgArgs& a, int u0, const 
       }
     }
   }
+  ybuf_zero_pads();
   __syncthreads();
 
   for (int z = zbeg; z < zend; ++z) {

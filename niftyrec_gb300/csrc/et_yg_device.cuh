@@ -178,6 +178,57 @@ __device__ __forceinline__ float4 yconv4(const float4& u, KC kc, int lane) {
   return o;
 }
 
+// Column pass through shared memory: each lane stores its 4 rows in its
+// warp's row buffer and reads the neighbour rows back with 16-byte loads (one
+// store and 2 ceil(R/4) loads in place of 2R shuffles and 2R selects).  Two
+// buffers per warp alternate, so one warp barrier per call orders a store
+// after the loads of the call before the previous one.  Rows outside the
+// warp's 128 read zero pads, written by ybuf_zero_pads before a kernel's
+// first row pass.
+constexpr int kYPad = 2;  // pad chunks (4 rows each) on either side: R <= 8
+__shared__ __align__(16) float4 s_ybuf[kW][2][32 + 2 * kYPad];
+
+__device__ __forceinline__ void ybuf_zero_pads() {
+  for (int i = threadIdx.x; i < kW * 2 * 2 * kYPad; i += blockDim.x) {
+    const int w = i / (4 * kYPad), r = i % (4 * kYPad);
+    const int b = r / (2 * kYPad), q = r % (2 * kYPad);
+    s_ybuf[w][b][q < kYPad ? q : 32 + q] = make_float4(0.f, 0.f, 0.f, 0.f);
+  }
+}
+
+template <int R, class KC>
+__device__ __forceinline__ float4 yconv4s(const float4& u, KC kc, int lane, int b) {
+  if constexpr (R == 0) {
+    return yconv4<0>(u, kc, lane);
+  } else {
+    constexpr int C = (R + 3) / 4;
+    static_assert(C <= kYPad, "row-buffer pads");
+    float4* row = &s_ybuf[threadIdx.x >> 5][b][kYPad];
+    row[lane] = u;
+    __syncwarp();
+    float w[2 * R + 4];
+#pragma unroll
+    for (int c = -C; c <= C; ++c) {
+      const float4 v = c == 0 ? u : row[lane + c];
+#pragma unroll
+      for (int q = 0; q < 4; ++q) {
+        const int rel = 4 * c + q;
+        if (rel >= -R && rel <= 3 + R) w[R + rel] = comp(v, q);
+      }
+    }
+    float4 o = make_float4(0.f, 0.f, 0.f, 0.f);
+#pragma unroll
+    for (int k = -R; k <= R; ++k) {
+      const float kk = kc[R - k];
+      o.x = fmaf(w[R + 0 + k], kk, o.x);
+      o.y = fmaf(w[R + 1 + k], kk, o.y);
+      o.z = fmaf(w[R + 2 + k], kk, o.z);
+      o.w = fmaf(w[R + 3 + k], kk, o.w);
+    }
+    return o;
+  }
+}
+
 __device__ __forceinline__ float4 exp_neg4(const float4& t) {
   return make_float4(__expf(-t.x), __expf(-t.y), __expf(-t.z), __expf(-t.w));
 }
@@ -339,7 +390,7 @@ __device__ __forceinline__ void rowpass_from_tile(const float4* __restrict__ sbu
     }
     const int i = j - 2 * R;
     if (i >= 0 && i < kTXW) {
-      emit(i, mask_rows(yconv4<R>(u[i % K], kc, lane), 4 * lane, ny));
+      emit(i, mask_rows(yconv4s<R>(u[i % K], kc, lane, i & 1), 4 * lane, ny));
       u[i % K] = make_float4(0.f, 0.f, 0.f, 0.f);
     }
   }
@@ -374,8 +425,8 @@ __device__ __forceinline__ void rowpass2_from_tiles(const float4* __restrict__ s
     }
     const int i = j - 2 * R;
     if (i >= 0 && i < kTXW) {
-      emit_b(i, mask_rows(yconv4<R>(ub[i], kcb, lane), 4 * lane, ny));
-      emit_a(i, mask_rows(yconv4<R>(ua[i], kca, lane), 4 * lane, ny));
+      emit_b(i, mask_rows(yconv4s<R>(ub[i], kcb, lane, 0), 4 * lane, ny));
+      emit_a(i, mask_rows(yconv4s<R>(ua[i], kca, lane, 1), 4 * lane, ny));
     }
   }
 }
@@ -510,6 +561,7 @@ __device__ __forceinline__ void project_item(const YgArgs& a, int cam, int mate,
     cP[i] = make_float4(0.f, 0.f, 0.f, 0.f);
     if (PAIR) Q[i] = make_float4(0.f, 0.f, 0.f, 0.f);
   }
+  ybuf_zero_pads();
   __syncthreads();
 
   // A depth step at plane z through tile buffer b: produce (footprints and

@@ -48,6 +48,7 @@ __device__ __forceinline__ void dmu_item(const YgArgs& a, int cam, int x0, unsig
     T[i] = make_float4(0.f, 0.f, 0.f, 0.f);
     P[i] = make_float4(0.f, 0.f, 0.f, 0.f);
   }
+  ybuf_zero_pads();
   __syncthreads();
 
   auto produce = [&](int z, int b) {

@@ -70,6 +70,8 @@ __device__ __forceinline__ void grad_item(const YgArgs& a, int cam, int g, int x
     return tb;
   };
 
+  ybuf_zero_pads();  // ordered before walk 2 by the cluster barriers
+
   // walk 1: the slab's transmission and partial per sampled column
   float4 T[OWN], P[OWN];
 #pragma unroll
