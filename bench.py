@@ -60,6 +60,8 @@ def algorithmic_bytes(kernel: str, launches: int, ncam_total: int) -> float:
         return ncam_total * (N ** 3 * 4 + N ** 2 * 4)
     if kernel == "k_gather_yg":  # accumulator read-modify-write per angle
         return ncam_total * (N ** 3 * 8)
+    if kernel == "k_mu_carry_yg":  # reads mu per angle
+        return ncam_total * (N ** 3 * 4)
     return float("nan")
 
 
@@ -294,24 +296,29 @@ def run_ours(args):
     h2d = act.nbytes + mu.nbytes + y.nbytes + mu.nbytes + 2 * params
     d2h = y.nbytes + act.nbytes
 
-    # roofline of the dominant kernel (the largest total of the per-kernel pass),
-    # timed in the timed region when it is the projector
+    # rooflines of the kernels with algorithmic bytes: the projector timed in the
+    # timed region, the others in the per-kernel pass; `roofline` is the
+    # dominant kernel's (the largest total of the per-kernel pass)
     peak, peak_kind = measured_peak()
+    rooflines = {}
+    for name in (prof or {}):
+        src, steps_src = (prof_dom, args.steps) if name in (prof_dom or {}) else (prof, max(3, args.steps // 2))
+        cnt, tot_ms = src[name]
+        alg = algorithmic_bytes(name, cnt, NCAM * steps_src)
+        if alg != alg or cnt == 0:  # NaN: no algorithmic-byte model for this kernel
+            continue
+        per_launch_bytes = alg / cnt
+        avg_s = tot_ms / cnt / 1e3
+        achieved = per_launch_bytes / avg_s / 1e9
+        rooflines[name] = {"bound": "hbm", "kernel": name, "achieved": round(achieved, 1), "peak": peak,
+                           "unit": "GB/s", "frac": round(achieved / peak, 4), "peak_source": peak_kind,
+                           "bytes_per_launch": per_launch_bytes, "avg_launch_ms": round(avg_s * 1e3, 4),
+                           "timed_in": "timed region" if src is prof_dom else "per-kernel pass",
+                           "traffic": committed_traffic(name)}
     roof = None
     if prof:
         dom = max(prof, key=lambda k: prof[k][1])
-        src, steps_src = (prof_dom, args.steps) if dom in (prof_dom or {}) else (prof, max(3, args.steps // 2))
-        cnt, tot_ms = src[dom]
-        alg = algorithmic_bytes(dom, cnt, NCAM * steps_src)
-        if alg == alg:  # not NaN
-            per_launch_bytes = alg / cnt
-            avg_s = tot_ms / cnt / 1e3
-            achieved = per_launch_bytes / avg_s / 1e9
-            roof = {"bound": "hbm", "kernel": dom, "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
-                    "frac": round(achieved / peak, 4), "peak_source": peak_kind,
-                    "bytes_per_launch": per_launch_bytes, "avg_launch_ms": round(avg_s * 1e3, 4),
-                    "timed_in": "timed region" if src is prof_dom else "per-kernel pass",
-                    "traffic": committed_traffic(dom)}
+        roof = rooflines.get(dom)
     kernels = {k: {"launches": v[0], "ms_total": round(v[1], 3)} for k, v in (prof or {}).items()}
 
     out = {
@@ -327,6 +334,7 @@ def run_ours(args):
         "pair_hbm": {"bytes_per_pair": PAIR_BYTES, "achieved_gbs": round(PAIR_BYTES * value / world / 1e9, 1),
                      "frac_of_peak": round(PAIR_BYTES * value / world / 1e9 / peak, 4), "peak_source": peak_kind},
         "roofline": roof,
+        "rooflines": rooflines,
         "kernels": kernels,
         "kernels_pass": {"ms_per_step": round(sum(ms_prof) / len(ms_prof), 4),
                          "note": "separate pass with CUDA events around every launch"},

@@ -14,7 +14,8 @@
 // Projector (emission-lib/_et.cpp:218-281): per camera and depth plane z,
 //   rotate (bilinear gather of activity and mu), per-plane separable PSF
 //   (row pass along x in a register sliding window over a shared tile, column
-//   pass along y with warp shuffles), attenuated depth scan T += mu;
+//   pass along y through a per-warp shared row buffer), attenuated depth scan
+//   T += mu;
 //   p += v * exp(-T).  No rotated volume is written anywhere: a thread-block
 //   cluster owns (camera, 32-column x-tile), its CTAs own depth slabs and
 //   merge (T, p) through distributed shared memory.
@@ -146,7 +147,8 @@ __device__ __forceinline__ float4 mask_rows(float4 v, int yb, int ny) {
 // Column (y) pass of the per-plane convolution for the 4 rows a lane owns:
 // out[y] = sum_k in[y+k] * kc[R-k], zero outside [0, ny) (rows >= ny are zero
 // pads, rows < 0 come from lanes below 0 and are masked).  Neighbour rows come
-// from lanes l-1, l-2 and l+1, l+2 by shuffles.
+// from lanes l-1, l-2 and l+1, l+2 by shuffles (the form for R = 0; larger
+// radii use yconv4s below).
 template <int R, class KC>
 __device__ __forceinline__ float4 yconv4(const float4& u, KC kc, int lane) {
   float w[2 * R + 4];
