@@ -440,7 +440,7 @@ int launch_spread_R(const YgArgs& a, int c0, int gcount, cudaStream_t st) {
   };
   // only mu is sampled from storage here (the sinogram is float32)
   const bool bf16 = a.storage == kStorageBF16;
-  const bool three = 3 * (smem + 1024) <= 228 * 1024;
+  const bool three = 3 * (smem + kYBufBytes + 1024) <= 228 * 1024;
   if (psf && tab) {
     if (a.mu && bf16) {
       go_tab(k_spread_ptab_yg<R, true, ADJ, __nv_bfloat16>);

@@ -189,6 +189,7 @@ __device__ __forceinline__ float4 yconv4(const float4& u, KC kc, int lane) {
 // first row pass.
 constexpr int kYPad = 2;  // pad chunks (4 rows each) on either side: R <= 8
 __shared__ __align__(16) float4 s_ybuf[kW][2][32 + 2 * kYPad];
+constexpr size_t kYBufBytes = sizeof(float4) * kW * 2 * (32 + 2 * kYPad);  // static, per CTA
 
 __device__ __forceinline__ void ybuf_zero_pads() {
   for (int i = threadIdx.x; i < kW * 2 * 2 * kYPad; i += blockDim.x) {

@@ -178,6 +178,7 @@ int launch_dmu_R(const YgArgs& a_in, cudaStream_t st) {
         break;
       }
   }
+  bool launch_err = false;
   auto launch = [&](auto k, auto&&... extra) {
     cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
     cudaLaunchConfig_t cfg = {};
@@ -193,7 +194,7 @@ int launch_dmu_R(const YgArgs& a_in, cudaStream_t st) {
     cfg.attrs = attr;
     cfg.numAttrs = 1;
     NRGB_LAUNCH_SCOPE("k_dmu_yg", st);
-    cudaLaunchKernelEx(&cfg, k, a, extra...);
+    if (cudaLaunchKernelEx(&cfg, k, a, extra...) != cudaSuccess) launch_err = true;
   };
   if (ptab) {
     static thread_local PsfTable table;
@@ -204,7 +205,7 @@ int launch_dmu_R(const YgArgs& a_in, cudaStream_t st) {
   } else {
     launch(k_dmu_yg<0, false>);
   }
-  return cudaGetLastError() == cudaSuccess ? kOk : kErrKernel;
+  return cudaGetLastError() == cudaSuccess && !launch_err ? kOk : kErrKernel;
 }
 
 int dmu_by_radius(int R, const YgArgs& a, cudaStream_t st) {

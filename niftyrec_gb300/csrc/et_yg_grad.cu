@@ -194,6 +194,7 @@ int launch_grad_R(const YgArgs& a_in, int c0, int gcount, cudaStream_t st) {
         break;
       }
   }
+  bool launch_err = false;
   auto launch = [&](auto k, auto&&... extra) {
     cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
     cudaLaunchConfig_t cfg = {};
@@ -209,7 +210,7 @@ int launch_grad_R(const YgArgs& a_in, int c0, int gcount, cudaStream_t st) {
     cfg.attrs = attr;
     cfg.numAttrs = 1;
     NRGB_LAUNCH_SCOPE("k_grad_spread_yg", st);
-    cudaLaunchKernelEx(&cfg, k, a, c0, extra...);
+    if (cudaLaunchKernelEx(&cfg, k, a, c0, extra...) != cudaSuccess) launch_err = true;
   };
   if (ptab) {
     static thread_local PsfTable table;
@@ -220,7 +221,7 @@ int launch_grad_R(const YgArgs& a_in, int c0, int gcount, cudaStream_t st) {
   } else {
     launch(k_grad_spread_yg<0, false>);
   }
-  return cudaGetLastError() == cudaSuccess ? kOk : kErrKernel;
+  return cudaGetLastError() == cudaSuccess && !launch_err ? kOk : kErrKernel;
 }
 
 }  // namespace

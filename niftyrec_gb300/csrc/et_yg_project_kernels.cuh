@@ -57,11 +57,12 @@ int launch_project_R(const YgArgs& a_in, cudaStream_t st) {
   const bool ptab = psf && a.psf_host && static_cast<size_t>(a.nz) * 2 * (2 * R + 1) <= kPsfTableFloats;
   const size_t smem = tile_smem_bytes<R>(psf && !ptab ? a.nz : 0, pair);
   // three CTAs per SM need three tiles (plus 1 KB reserved each) in the 228 KB
-  const bool three = 3 * (smem + 1024) <= 228 * 1024;
+  const bool three = 3 * (smem + kYBufBytes + 1024) <= 228 * 1024;
   if (a.pslabs != 2 && a.pslabs != 4 && a.pslabs != 8 && a.pslabs != 16)
     a.pslabs = project_slabs(nunits * ntile, three && !bf16 && !pair ? 3 : 2, a.nz);
   // one cluster of a.pslabs CTAs per (unit, x-tile); 16 is a non-portable
   // cluster size: it falls back to 8 where the kernel cannot be resident so
+  bool launch_err = false;
   auto launch = [&](auto k, auto&&... extra) {
     cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
     cudaLaunchConfig_t cfg = {};
@@ -87,7 +88,7 @@ int launch_project_R(const YgArgs& a_in, cudaStream_t st) {
     cfg.gridDim = dim3(nunits * ntile * a.pslabs);
     attr[0].val.clusterDim.x = a.pslabs;
     NRGB_LAUNCH_SCOPE("k_project_yg", st);
-    cudaLaunchKernelEx(&cfg, k, a, extra...);
+    if (cudaLaunchKernelEx(&cfg, k, a, extra...) != cudaSuccess) launch_err = true;
   };
   auto go = [&](auto k) { launch(k); };
   auto go_tab = [&](auto k) {
@@ -121,7 +122,7 @@ int launch_project_R(const YgArgs& a_in, cudaStream_t st) {
     pick(0.0f, std::integral_constant<int, 3>(), Off());
   else
     pick(0.0f, std::integral_constant<int, 2>(), Off());
-  return cudaGetLastError() == cudaSuccess ? kOk : kErrKernel;
+  return cudaGetLastError() == cudaSuccess && !launch_err ? kOk : kErrKernel;
 }
 
 }  // namespace nrgb
