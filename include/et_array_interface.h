@@ -343,6 +343,16 @@ int nrgb_get_project_slabs(int nx, int ny, int nz, int ncam);
  * from its own matrix, as the reference.  Applies to calls made afterwards. */
 int nrgb_set_mirror_pairs(int on);
 int nrgb_get_mirror_pairs(void);
+/* Host-side introspection (no counterpart in the reference; no GPU needed).
+ * nrgb_mirror_units: the {camera, mate} pairs (mate -1 when unpaired) the
+ * fused kernels form for this camera table and volume size {nx, ny, nz};
+ * *n_units = 0 when every camera runs on its own.  nrgb_row_windows: the row
+ * windows {first row, rows, first valid row, end of valid rows} of ny rows for
+ * a PSF of width psf_k (0: none).  Both return status 2 when the output
+ * cannot hold the result (the count is still written). */
+int nrgb_mirror_units(const float *cameras, const int *cameras_size, const int *size, int *out_units, int max_units,
+                      int *n_units);
+int nrgb_row_windows(int ny, int psf_k, int *out, int max_windows, int *n_windows);
 
 /* Instrumentation (no counterpart in the reference).  nrgb_launch_count: CUDA
  * kernels this library launched since it was loaded.  nrgb_profile_enable(1)

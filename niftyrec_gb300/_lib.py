@@ -102,6 +102,8 @@ PROTOTYPES = {
     "nrgb_profile_enable": (_I, [_I]),
     "nrgb_profile_summary": (_I, [ctypes.c_char_p, _I]),
     "nrgb_profile_only": (_I, [ctypes.c_char_p]),
+    "nrgb_mirror_units": (_I, [_P, _PI, _PI, _PI, _I, _PI]),
+    "nrgb_row_windows": (_I, [_I, _I, _PI, _I, _PI]),
 }
 
 _lib = None

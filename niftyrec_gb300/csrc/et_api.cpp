@@ -1125,6 +1125,42 @@ int nrgb_set_mirror_pairs(int on) {
 
 int nrgb_get_mirror_pairs(void) { return mirror_pairs(); }
 
+// The mirror units the fused kernels would form for these cameras and this
+// volume (host only): {camera, mate} pairs, mate -1 when unpaired, in the
+// cameras' order; *n_units = 0 when every camera runs on its own (no
+// opposite-angle pairs about the grid centre, cameras off the gantry forms,
+// or nrgb_set_mirror_pairs(0)).
+int nrgb_mirror_units(const float* cameras, const int* cameras_size, const int* size, int* out_units, int max_units,
+                      int* n_units) {
+  if (!cameras || !cameras_size || !size || !n_units || max_units < 0 || (max_units > 0 && !out_units))
+    return kErrParameters;
+  Cameras cc;
+  int s = expand_cameras(cameras, cameras_size[0], cameras_size[1], size, &cc);
+  if (s != kOk) return s;
+  Problem pb;
+  if ((s = make_problem(size[0], size[1], size[2], cc, nullptr, nullptr, 0.0f, 0.0f, 0, &pb)) != kOk) return s;
+  const std::vector<int>& u = pb.xgantry ? pb.units_x : pb.units;
+  const int n = static_cast<int>(u.size() / 2);
+  *n_units = n;
+  if (n > max_units) return kErrParameters;
+  std::copy(u.begin(), u.end(), out_units);
+  return kOk;
+}
+
+// Row windows of the fused kernels for ny rows and a PSF of width psf_k (0:
+// none), host only: {first row, rows, first valid row, end of valid rows}
+// per window (valid rows relative to the first row).
+int nrgb_row_windows(int ny, int psf_k, int* out, int max_windows, int* n_windows) {
+  if (ny < 1 || psf_k < 0 || !n_windows || max_windows < 0 || (max_windows > 0 && !out)) return kErrParameters;
+  std::vector<int> w(4 * static_cast<size_t>(ny + 1));
+  const int n = yg_row_windows(ny, psf_k, w.data(), ny + 1);
+  if (n < 0) return kErrParameters;
+  *n_windows = n;
+  if (n > max_windows) return kErrParameters;
+  std::copy(w.begin(), w.begin() + 4 * n, out);
+  return kOk;
+}
+
 // 1 when the last call of this thread ran the fused y-gantry kernels, 2 when
 // it ran the general-orientation path, 0 before any call.
 int nrgb_last_path(void) { return g_last_path; }

@@ -105,3 +105,79 @@ def test_opposed_subsets():
     counts = np.bincount(s)
     assert counts.max() - counts.min() <= 2
     np.testing.assert_array_equal(opposed_subsets(9, 3), interleaved_subsets(9, 3))
+
+
+def _windows(lib, ny, k):
+    out = (ctypes.c_int * (4 * (ny + 1)))()
+    n = ctypes.c_int(0)
+    assert lib.nrgb_row_windows(ny, k, out, ny + 1, ctypes.byref(n)) == 0
+    return [tuple(out[4 * i:4 * i + 4]) for i in range(n.value)]
+
+
+@pytest.mark.parametrize("k", [0, 1, 3, 5, 11, 15])
+def test_row_windows_partition_rows(lib, k):
+    """Row windows of the fused kernels: at most 128 rows, starts and valid
+    ranges on multiples of 4 (except at the volume's end), valid ranges
+    partition [0, ny) in order, and every valid row's PSF support lies inside
+    its window or past the volume's edge."""
+    r = (k - 1) // 2 if k else 0
+    for ny in list(range(1, 300)) + [511, 512, 513, 1000]:
+        wins = _windows(lib, ny, k)
+        assert wins
+        expect = 0
+        for row0, rows, lo, hi in wins:
+            assert row0 % 4 == 0 and 0 < rows <= 128 and row0 + rows <= ny
+            assert 0 <= lo < hi <= rows
+            assert row0 + lo == expect
+            assert (row0 + lo) % 4 == 0 and ((row0 + hi) % 4 == 0 or row0 + hi == ny)
+            for y in (row0 + lo, row0 + hi - 1):
+                assert max(0, y - r) >= row0 and min(ny - 1, y + r) < row0 + rows, (ny, k, y)
+            expect = row0 + hi
+        assert expect == ny
+    if k == 15:
+        assert [w[3] - w[2] for w in _windows(lib, 256, 15)] == [120, 112, 24]
+    out, n = (ctypes.c_int * 4)(), ctypes.c_int(0)
+    assert lib.nrgb_row_windows(300, k, out, 1, ctypes.byref(n)) == 2 and n.value > 1  # too small an output
+    assert lib.nrgb_row_windows(0, k, out, 1, ctypes.byref(n)) == 2
+
+
+def _units(lib, cams, size):
+    cams = np.ascontiguousarray(cams, np.float32)
+    cs = (ctypes.c_int * 2)(*((cams.shape[0], 1) if cams.ndim == 1 else (cams.shape[1], cams.shape[0])))
+    out = (ctypes.c_int * (2 * 4096))()
+    n = ctypes.c_int(0)
+    st = lib.nrgb_mirror_units(cams.ctypes.data_as(ctypes.c_void_p), cs, (ctypes.c_int * 3)(*size), out, 4096,
+                               ctypes.byref(n))
+    assert st == 0
+    return [tuple(out[2 * i:2 * i + 2]) for i in range(n.value)]
+
+
+def test_mirror_units_of_camera_tables(lib):
+    """Cameras at opposite angles about the grid centre pair up; odd counts
+    leave cameras unpaired; tilted or off-centre cameras and the switch off
+    form no units; cameras about x pair on the x-gantry form."""
+    from niftyrec_gb300 import synthetic as S
+
+    size = (32, 24, 32)
+    u = _units(lib, S.cameras_about_y(120, 0.0, 3.0)[1], size)
+    assert u == [(k, k + 60) for k in range(60)]
+    u = _units(lib, S.cameras_about_y(7, 10.0), size)  # 360/7 deg steps: no opposite pairs
+    assert u == []
+    cams = S.cameras_about_y(5, 0.0, 45.0)  # 0, 45, 90, 135, 180 deg
+    u = _units(lib, cams, size)
+    assert u == [(0, 4), (1, -1), (2, -1), (3, -1)]
+    tilted = S.cameras_about_y(4, 0.0)
+    tilted[2] = 1e-3
+    assert _units(lib, tilted, size) == []
+    six = np.zeros((6, 4), np.float32)
+    six[1] = np.deg2rad([0, 180, 90, 270])
+    six[3:] = 5.0  # centres away from the grid centre
+    assert _units(lib, six, size) == []
+    about_x = np.zeros((3, 4), np.float32)
+    about_x[0] = np.deg2rad([0, 90, 180, 270])
+    assert _units(lib, about_x, size) == [(0, 2), (1, 3)]
+    assert lib.nrgb_set_mirror_pairs(0) == 0
+    try:
+        assert _units(lib, S.cameras_about_y(120, 0.0, 3.0)[1], size) == []
+    finally:
+        lib.nrgb_set_mirror_pairs(1)
