@@ -2,6 +2,7 @@
 // rounded separately, as in the reference's x86-64 float code.
 #include "et_geometry.h"
 
+#include <algorithm>
 #include <cmath>
 #include <cstring>
 
@@ -128,18 +129,38 @@ std::vector<int> mirror_units(const Cameras& cams, int nx, int nz, int axis) {
   const double two_pi = 2.0 * M_PI;
   auto centred = [&](int c) { return cams.centers[lateral * n + c] == cx && cams.centers[2 * n + c] == cz; };
   const float* theta = cams.angles.data() + static_cast<size_t>(axis) * n;
+  auto opposite = [&](int i, int j) {
+    const double d = static_cast<double>(theta[j]) - static_cast<double>(theta[i]) - M_PI;
+    return std::fabs(d - two_pi * std::nearbyint(d / two_pi)) <= kMirrorTolerance;
+  };
+  auto reduce = [&](double a) { return a - two_pi * std::floor(a / two_pi); };
+  // centred cameras by angle in [0, 2 pi): each camera looks up the cameras
+  // near its opposite angle instead of testing every later camera
+  std::vector<std::pair<double, int>> by_angle;
+  for (int c = 0; c < n; ++c)
+    if (centred(c)) by_angle.emplace_back(reduce(theta[c]), c);
+  std::sort(by_angle.begin(), by_angle.end());
+  const double reach = kMirrorTolerance + 1e-9;  // covers the rounding of the reduction
   for (int i = 0; i < n; ++i) {
     if (taken[i] || !centred(i)) continue;
-    for (int j = i + 1; j < n; ++j) {
-      if (taken[j] || !centred(j)) continue;
-      const double d = static_cast<double>(theta[j]) - static_cast<double>(theta[i]) - M_PI;
-      const double w = d - two_pi * std::nearbyint(d / two_pi);
-      if (std::fabs(w) <= kMirrorTolerance) {
-        mate[i] = j;
-        taken[i] = taken[j] = 1;
-        any = true;
-        break;
+    // the first later camera (by index) that is free and opposite, as a scan
+    // over all later cameras would find it
+    int best = -1;
+    auto scan = [&](double lo, double hi) {
+      for (auto it = std::lower_bound(by_angle.begin(), by_angle.end(), std::make_pair(lo, -1));
+           it != by_angle.end() && it->first <= hi; ++it) {
+        const int j = it->second;
+        if (j > i && !taken[j] && (best < 0 || j < best) && opposite(i, j)) best = j;
       }
+    };
+    const double target = reduce(static_cast<double>(theta[i]) + M_PI);
+    scan(target - reach, target + reach);
+    if (target - reach < 0.0) scan(target - reach + two_pi, two_pi);
+    if (target + reach >= two_pi) scan(0.0, target + reach - two_pi);
+    if (best >= 0) {
+      mate[i] = best;
+      taken[i] = taken[best] = 1;
+      any = true;
     }
   }
   std::vector<int> units;

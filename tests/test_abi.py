@@ -181,3 +181,46 @@ def test_mirror_units_of_camera_tables(lib):
         assert _units(lib, S.cameras_about_y(120, 0.0, 3.0)[1], size) == []
     finally:
         lib.nrgb_set_mirror_pairs(1)
+
+
+def _greedy_units(theta, centred):
+    """Restatement of the pairing rule: camera i (in order) takes the first
+    later free camera whose angle differs by pi within 1e-6 rad (modulo 2 pi)."""
+    n = len(theta)
+    mate, taken = [-1] * n, [False] * n
+    for i in range(n):
+        if taken[i] or not centred[i]:
+            continue
+        for j in range(i + 1, n):
+            if taken[j] or not centred[j]:
+                continue
+            d = float(theta[j]) - float(theta[i]) - np.pi
+            if abs(d - 2 * np.pi * round(d / (2 * np.pi))) <= 1e-6:
+                mate[i], taken[i], taken[j] = j, True, True
+                break
+    if not any(taken):
+        return []
+    return [(i, mate[i]) for i in range(n) if not (taken[i] and mate[i] < 0)]
+
+
+@pytest.mark.parametrize("seed", range(6))
+def test_mirror_units_match_greedy_rule(lib, seed):
+    """The angle-sorted lookup pairs exactly like a scan over all later
+    cameras: repeated angles, pairs across the 0 / 2 pi seam, differences just
+    inside and just outside the tolerance, off-centre cameras."""
+    rng = np.random.default_rng(seed)
+    n = int(rng.integers(2, 400))
+    base = rng.choice(np.deg2rad(np.arange(0.0, 360.0, 1.5)), n)
+    jitter = rng.choice([0.0, 0.0, 4e-7, -9e-7, 3e-6, 2 * np.pi, -2 * np.pi], n)
+    theta = (base + jitter).astype(np.float32)
+    theta[: n // 10] = np.float32(np.pi) * rng.choice([1.0, -1.0, 3.0], n // 10).astype(np.float32)
+    six = np.zeros((6, n), np.float32)
+    six[1] = theta
+    size = (40, 20, 40)
+    six[3] = (size[0] - 1) / 2.0
+    six[4] = (size[1] - 1) / 2.0
+    six[5] = (size[2] - 1) / 2.0
+    off = rng.random(n) < 0.1
+    six[5, off] += 1.0
+    got = _units(lib, six, size)
+    assert got == _greedy_units(theta, ~off)
