@@ -54,6 +54,17 @@ def _cam_size(cameras: np.ndarray):
     return [cameras.shape[1], cameras.shape[0]]
 
 
+def _psf_size(psf, nz):
+    """PSF size in the reference's order; a PSF with fewer planes than the
+    volume's depth would be read past its end by the restated convolution
+    (as by the reference), so it is refused here."""
+    if psf is None:
+        return [0, 0, 0]
+    if psf.shape[0] < nz:
+        raise ValueError(f"PSF has {psf.shape[0]} planes, the volume {nz}")
+    return list(psf.shape[::-1])
+
+
 class Restated:
     """The C restatement, float or double."""
 
@@ -101,7 +112,7 @@ class Restated:
         sino = np.zeros((cs[0], ny, nx), dtype=self.dtype)
         asz = _ints([nx, ny, nz] if act is not None else [0, 0, 0])
         tsz = _ints([nx, ny, nz] if att is not None else [0, 0, 0])
-        psz = _ints(list(psf.shape[::-1]) if psf is not None else [0, 0, 0])
+        psz = _ints(_psf_size(psf, nz))
         st = self._f("spect_project")(_ptr(act), _ptr(asz), _ptr(sino), _ptr(_ints([nx, ny, cs[0]])),
                                       _ptr(cams), _ptr(_ints(cs)), _ptr(psf), _ptr(psz), _ptr(att), _ptr(tsz),
                                       self.real(bg), self.real(bg_att), _I(truncate))
@@ -120,7 +131,7 @@ class Restated:
         out = np.zeros((nz, ny, nx), dtype=self.dtype)
         cs = _cam_size(cams)
         tsz = _ints([nx, ny, nz] if att is not None else [0, 0, 0])
-        psz = _ints(list(psf.shape[::-1]) if psf is not None else [0, 0, 0])
+        psz = _ints(_psf_size(psf, nz))
         st = self._f("spect_backproject")(_ptr(sino), _ptr(_ints([nx, ny, ncam])), _ptr(out), _ptr(_ints([nx, ny, nz])),
                                           _ptr(cams), _ptr(_ints(cs)), _ptr(psf), _ptr(psz), _ptr(att), _ptr(tsz),
                                           self.real(bg), self.real(bg_att), _I(truncate), _I(1 if adjoint else 0))
@@ -143,7 +154,7 @@ class Restated:
         part = np.zeros((cs[0], nz, ny, nx), dtype=self.dtype)
         asz = _ints([nx, ny, nz] if act is not None else [0, 0, 0])
         tsz = _ints([nx, ny, nz] if att is not None else [0, 0, 0])
-        psz = _ints(list(psf.shape[::-1]) if psf is not None else [0, 0, 0])
+        psz = _ints(_psf_size(psf, nz))
         st = self._f("spect_project_partial")(_ptr(act), _ptr(asz), _ptr(sino), _ptr(part), _ptr(cams),
                                               _ptr(_ints(cs)), _ptr(psf), _ptr(psz), _ptr(att), _ptr(tsz),
                                               self.real(bg), _ptr(bgi), self.real(bg_att), _I(truncate), _I(rotate))
@@ -160,7 +171,7 @@ class Restated:
         pr = np.zeros((n, n), dtype=self.dtype) if prior else None
         tsz = _ints([nx, ny, nz] if att is not None else [0, 0, 0])
         st = self._f("spect_fisher_grid")(_ptr(act), _ptr(_ints([nx, ny, nz])), _ptr(cams), _ptr(_ints(cs)), _ptr(psf),
-                                          _ptr(_ints(list(psf.shape[::-1]))), _ptr(grid), _ptr(fisher), _ptr(pr),
+                                          _ptr(_ints(_psf_size(psf, nz))), _ptr(grid), _ptr(fisher), _ptr(pr),
                                           _I(n), _ptr(att), _ptr(tsz), self.real(bg), self.real(bg_att))
         if st:
             raise RuntimeError(f"oracle fisher_grid status {st}")
@@ -176,7 +187,7 @@ class Restated:
         ncam = sino.shape[0]
         out = np.zeros_like(act)
         cs = _cam_size(cams)
-        psz = _ints(list(psf.shape[::-1]) if psf is not None else [0, 0, 0])
+        psz = _ints(_psf_size(psf, nz))
         st = self._f("spect_gradient_attenuation")(_ptr(sino), _ptr(_ints([nx, ny, ncam])), _ptr(act),
                                                    _ptr(_ints([nx, ny, nz])), _ptr(out), _ptr(_ints([nx, ny, nz])),
                                                    _ptr(cams), _ptr(_ints(cs)), _ptr(psf), _ptr(psz), _ptr(att),
@@ -194,6 +205,7 @@ class Restated:
         nz, ny, nx = act.shape
         ncam = sino.shape[0]
         idx = _ints(idx)
+        _psf_size(psf, act.shape[0])  # refuses a PSF with fewer planes than nz
         kx, ky = (psf.shape[2], psf.shape[1]) if psf is not None else (0, 0)
         self._f("osem_step_subset")(_ptr(act), _I(nx), _I(ny), _ptr(sino), _I(ncam), _ptr(cams), _ptr(idx),
                                     _I(len(idx)), _ptr(att), _ptr(psf), _I(kx), _I(ky), self.real(bg),
@@ -228,7 +240,7 @@ class Reference:
         cs = _cam_size(cams)
         sino = np.zeros((cs[0], ny, nx), dtype=np.float32)
         tsz = _ints([nx, ny, nz] if att is not None else [0, 0, 0])
-        psz = _ints(list(psf.shape[::-1]) if psf is not None else [0, 0, 0])
+        psz = _ints(_psf_size(psf, nz))
         fn = self.lib.SPECT_project_parallelholes
         fn.restype = _I
         st = fn(_ptr(act), _ptr(_ints([nx, ny, nz])), _ptr(sino), _ptr(_ints([nx, ny, cs[0]])), _ptr(cams),
@@ -246,7 +258,7 @@ class Reference:
         out = np.zeros((nz, ny, nx), dtype=np.float32)
         cs = _cam_size(cams)
         tsz = _ints([nx, ny, nz] if att is not None else [0, 0, 0])
-        psz = _ints(list(psf.shape[::-1]) if psf is not None else [0, 0, 0])
+        psz = _ints(_psf_size(psf, nz))
         fn = self.lib.SPECT_backproject_parallelholes
         fn.restype = _I
         st = fn(_ptr(sino), _ptr(_ints([nx, ny, ncam])), _ptr(out), _ptr(_ints([nx, ny, nz])), _ptr(cams),
@@ -262,6 +274,7 @@ class Reference:
         sino, att, psf, cams = self._f32(sino), self._f32(att), self._f32(psf), self._f32(cameras3)
         nz, ny, nx = act.shape
         ncam = sino.shape[0]
+        _psf_size(psf, act.shape[0])  # refuses a PSF with fewer planes than nz
         kx, ky = (psf.shape[2], psf.shape[1]) if psf is not None else (0, 0)
         fn = self.lib.et_array_mlem_step
         fn.restype = _I
@@ -282,7 +295,7 @@ class Reference:
         fn = self.lib.et_array_fisher_grid
         fn.restype = _I
         st = fn(_ptr(act), _ptr(_ints([nx, ny, nz])), _ptr(cams), _ptr(_ints(cs)), _ptr(psf),
-                _ptr(_ints(list(psf.shape[::-1]))), _ptr(grid), _ptr(fisher), _ptr(pr), _ptr(_ints([n, n])), _ptr(att),
+                _ptr(_ints(_psf_size(psf, nz))), _ptr(grid), _ptr(fisher), _ptr(pr), _ptr(_ints([n, n])), _ptr(att),
                 _ptr(tsz), ctypes.c_float(0.0), ctypes.c_float(bg), ctypes.c_float(bg_att), _I(0))
         if st:
             raise RuntimeError(f"reference fisher_grid status {st}")

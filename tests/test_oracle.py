@@ -98,6 +98,49 @@ def test_constant_mu_beer_lambert(o32):
     np.testing.assert_allclose(s[0], expect, rtol=1e-5)
 
 
+def test_gradient_known_answer_angle0(o32):
+    """The attenuation gradient at angle 0 without PSF is the sinogram times
+    the depth suffix sum of a * exp(-T) (T the inclusive depth sum of mu),
+    emission-lib_gpu/_et_attenuation_gradient_gpu_kernels.cu:24-39 with an
+    identity rotation; with a PSF every plane of it is convolved (row, then
+    column), and a camera at 90 degrees sees the same sums along x."""
+    rng = np.random.default_rng(12)
+    shape = (8, 7, 9)  # nz <= nx: the PSF has nx planes
+    act = rng.uniform(0.5, 2.0, shape).astype(np.float32)
+    mu = rng.uniform(0.0, 0.2, shape).astype(np.float32)
+    s = rng.uniform(-1.0, 1.0, (1,) + shape[1:]).astype(np.float32)
+    g = o32.gradient_attenuation(s, act, mu, np.zeros(1, np.float32))
+    a, m = act.astype(np.float64), mu.astype(np.float64)
+    w = a * np.exp(-np.cumsum(m, axis=0))
+    expect = s[0].astype(np.float64) * np.cumsum(w[::-1], axis=0)[::-1]
+    np.testing.assert_allclose(g, expect, rtol=2e-5, atol=1e-6)
+    # separable PSF: each plane z of the suffix volume convolved with plane z's kernels
+    psf = S.gaussian_psf(3, shape[2], 0.6, 0.1)
+    gp = o32.gradient_attenuation(s, act, mu, np.zeros(1, np.float32), psf)
+    conv = np.empty_like(expect)
+    for z in range(shape[0]):
+        k = psf[z].astype(np.float64)
+        kr, kc = k[1, :], k[:, 1] / k[1, 1]
+        row = np.zeros_like(expect[z])
+        for d in (-1, 0, 1):  # true convolution along x: out[x] = sum_d in[x + d] * kr[1 - d]
+            src = np.roll(expect[z], -d, axis=1)
+            if d > 0:
+                src[:, -d:] = 0
+            if d < 0:
+                src[:, :-d] = 0
+            row += src * kr[1 - d]
+        col = np.zeros_like(row)
+        for d in (-1, 0, 1):
+            src = np.roll(row, -d, axis=0)
+            if d > 0:
+                src[-d:, :] = 0
+            if d < 0:
+                src[:-d, :] = 0
+            col += src * kc[1 - d]
+        conv[z] = col
+    np.testing.assert_allclose(gp, conv, rtol=5e-5, atol=1e-5)
+
+
 @pytest.mark.skipif(not Reference.available, reason="compiled reference not present")
 def test_against_compiled_reference_fresh_inputs(o32):
     R = Reference()
