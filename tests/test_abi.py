@@ -224,3 +224,25 @@ def test_mirror_units_match_greedy_rule(lib, seed):
     six[5, off] += 1.0
     got = _units(lib, six, size)
     assert got == _greedy_units(theta, ~off)
+
+
+def test_autotune_cache_round_trip(lib, tmp_path):
+    """Tuning results recorded in the JSON cache are applied to the library's
+    tables by load_cache in a later process; a broken cache file is ignored."""
+    from niftyrec_gb300 import autotune as AT
+
+    path = str(tmp_path / "tune.json")
+    key = AT._key(44, 40, 36, 9)
+    AT._record(path, key, {"group": 6})
+    AT._record(path, key, {"slabs": 4, "slabs_ms": {"4": 0.1}})
+    cache = AT.load_cache(path)
+    assert cache[key]["group"] == 6 and cache[key]["slabs"] == 4
+    try:
+        assert lib.nrgb_get_backproject_group(44, 40, 36, 9) == 6
+        assert lib.nrgb_get_project_slabs(44, 40, 36, 9) == 4
+    finally:
+        lib.nrgb_set_backproject_group(44, 40, 36, 9, 0)
+        lib.nrgb_set_project_slabs(44, 40, 36, 9, 0)
+    (tmp_path / "bad.json").write_text("{not json")
+    assert AT.load_cache(str(tmp_path / "bad.json")) == {}
+    assert AT.load_cache(str(tmp_path / "missing.json")) == {}
