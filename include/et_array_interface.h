@@ -11,7 +11,8 @@
  *
  * Status codes (emission-lib/_et_common.h:40-48): 0 success, 1 unspecified,
  * 2 parameters, 3 kernel, 4 allocgpu, 5 alloccpu, 6 transfergpu,
- * 7 nogpubuilt, 8 nogpuinstalled; 9 (new) a bounded device-side wait expired.
+ * 7 nogpubuilt, 8 nogpuinstalled; 10 (new) the problem does not fit the fixed
+ * scratch of nrgb_backproject_device_noalloc.  9 is not used.
  */
 #ifndef NIFTYREC_GB300_ET_ARRAY_INTERFACE_H
 #define NIFTYREC_GB300_ET_ARRAY_INTERFACE_H
@@ -225,17 +226,24 @@ int nrgb_gradient_attenuation_device(const float *d_sinogram, const float *d_act
                                      float background_attenuation, int truncate, void *stream);
 
 /* Backprojection that allocates nothing.  No counterpart in the reference.
- * For callers that cannot call cudaMalloc: code inside a CUDA-graph capture,
- * processes whose device memory is held by a framework's allocator, real-time
- * loops that must not enter the driver's allocator.  Same arguments and result
- * as nrgb_backproject_device with mode 0; every temporary lives in a fixed
- * 64 MiB __device__ array of this library (held by every GPU that loads it,
- * until the process exits), camera matrices and PSF are built in fixed host
- * arrays.  Problems whose work space does not fit (e.g. 128^3 x 120 cameras)
- * return status 10; use nrgb_backproject_device for those.  The first call on
- * a device looks up the array's device address (cudaGetSymbolAddress): make
- * that first call before any stream capture.  All calls share the array and
- * it keeps the last call's contents; calls that overlap on the GPU (two
+ * For callers that cannot call cudaMalloc: a plug-in inside a host
+ * application whose framework allocator already holds the GPU's memory (a
+ * cudaMalloc there fails or forces the host to free its cache), or a
+ * real-time reconstruction loop that must not enter the driver's allocator
+ * (unbounded latency, possible device-wide synchronisation).  Same arguments
+ * and result (within float32 rounding) as nrgb_backproject_device with mode 0;
+ * cameras about the gantry axis y run the same fused kernels, every other
+ * camera (also cameras about x, which nrgb_backproject_device serves with the
+ * fused kernels) runs the general-orientation kernels.  Every temporary lives
+ * in a fixed 64 MiB __device__ array of this library (held by every GPU that
+ * loads it, until the process exits); camera matrices and the separated PSF
+ * are stored into it by kernels that carry them in their launch parameters.
+ * Problems whose work space does not fit (e.g. 128^3 x 120 cameras) return
+ * status 10; use nrgb_backproject_device for those.  The first call on a
+ * device looks up the array's device address (cudaGetSymbolAddress), once per
+ * device with that device current; make that first call before any stream
+ * capture.  All calls share the array and it keeps the last call's contents
+ * (every call overwrites what it reads); calls that overlap on the GPU (two
  * streams, two threads) race on it, so serialise them.  No cudaMalloc,
  * cudaFree or allocating library routine is called (with the launch profiler
  * off, its default). */

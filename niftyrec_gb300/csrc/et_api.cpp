@@ -28,6 +28,12 @@ thread_local int g_last_path = 0;  // 1 = fused gantry kernels (about y, or x wi
 
 size_t fbytes(size_t n) { return n * sizeof(float); }
 
+}  // namespace
+
+void nrgb::set_last_path(int path) { g_last_path = path; }
+
+namespace {
+
 int finish(DeviceState& ds, int status) {
   cudaEventRecord(ds.last_use, ds.stream);
   const cudaError_t e = cudaStreamSynchronize(ds.stream);
@@ -393,7 +399,7 @@ const char* kMessages[] = {
     "niftyrec: host/GPU transfer failed",
     "niftyrec: built without GPU support",
     "niftyrec: no GPU installed",
-    "niftyrec: a bounded device-side wait expired",
+    "niftyrec: status 9 is not used",
     "niftyrec: the problem needs more work space than the 64 MiB fixed scratch of "
     "nrgb_backproject_device_noalloc (use nrgb_backproject_device, or fewer cameras / a smaller grid)",
 };

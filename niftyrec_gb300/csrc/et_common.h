@@ -10,9 +10,9 @@
 namespace nrgb {
 
 // Status codes.  0..8 keep the values of the reference
-// (emission-lib/_et_common.h:40-48); 9 and 10 are new: 9 a bounded
-// device-side wait expired and the kernel returned early; 10 the problem does
-// not fit the fixed scratch of the no-allocation backprojection entry point.
+// (emission-lib/_et_common.h:40-48); 10 is new: the problem does not fit the
+// fixed scratch of the no-allocation backprojection entry point.  9 is not
+// used (no kernel of this library waits on another block or device).
 enum Status : int {
   kOk = 0,
   kErrUnspecified = 1,
@@ -23,7 +23,6 @@ enum Status : int {
   kErrTransferGpu = 6,
   kErrNoGpuBuilt = 7,
   kErrNoGpuInstalled = 8,
-  kErrTimeout = 9,
   kErrScratchTooSmall = 10,
 };
 

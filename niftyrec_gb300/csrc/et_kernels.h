@@ -215,4 +215,8 @@ int sum_fp64(const float* a, const float* b, size_t n, double* out, cudaStream_t
 // out[i] = value
 int fill(float* out, size_t n, float value, cudaStream_t st);
 
+// Records which path the calling thread's last call took (read back by
+// nrgb_last_path; defined in et_api.cpp): 1 fused gantry kernels, 2 general.
+void set_last_path(int path);
+
 }  // namespace nrgb

@@ -1,19 +1,25 @@
 // Backprojection entry point that allocates nothing.
 //
-// Who needs it: callers that cannot call cudaMalloc -- code running inside a
-// CUDA-graph capture (allocation is not a capturable operation), hosts whose
-// device memory is fully pre-reserved by a framework allocator, or real-time
-// reconstruction loops that must not hit the driver allocator.  They pass
+// Who needs it: callers that cannot call cudaMalloc -- a plug-in running
+// inside a host application whose framework allocator has already reserved
+// the GPU's memory (a cudaMalloc there fails or evicts the host's cache), or a
+// real-time reconstruction loop that must not enter the driver's allocator
+// (its latency is unbounded and it may synchronise the device).  They pass
 // their own input and output buffers; every temporary lives in one file-scope
 // __device__ array of fixed size (kNoAllocScratchBytes), which each GPU that
 // loads this library holds until the process exits.
 //
-// It runs the same kernels as nrgb_backproject_device (fused gantry kernels or
-// the general-orientation path), single-stream, with camera-group scratch
+// It runs the same kernels as nrgb_backproject_device (the fused kernels for
+// cameras about the gantry axis y, the general-orientation kernels for every
+// other camera -- including cameras about x, which nrgb_backproject_device
+// serves with the fused kernels), single-stream, with camera-group scratch
 // sized to what fits in the array.  Camera matrices and the separated PSF are
-// built in fixed host arrays and copied with plain cudaMemcpyAsync.
+// built on the host and stored into the array by small kernels that carry the
+// values in their launch parameters, so no host memory is read after the call
+// returns.
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <cmath>
 #include <cstring>
 #include <mutex>
@@ -30,6 +36,30 @@ constexpr size_t kNoAllocScratchBytes = static_cast<size_t>(64) << 20;  // 64 Mi
 constexpr int kMaxDevices = 64;
 constexpr int kMaxCams = 4096;
 constexpr int kMaxPsfFloats = 2048 * 30;  // nz * 2k for nz <= 2048, k <= 15
+
+// Words carried by value in one store launch (kernel parameters hold up to
+// 32 KB).
+constexpr int kWordsPerLaunch = 7936;
+struct Words {
+  unsigned int w[kWordsPerLaunch];
+};
+
+__global__ void k_store_words(unsigned int* __restrict__ dst, const __grid_constant__ Words src, int n) {
+  for (int i = threadIdx.x; i < n; i += blockDim.x) dst[i] = src.w[i];
+}
+
+// Copies `bytes` (a multiple of 4) of host data into device memory through
+// launch parameters.
+int store_by_value(void* dst, const void* src, size_t bytes, cudaStream_t st) {
+  static thread_local Words chunk;
+  const size_t n = bytes / sizeof(unsigned int);
+  for (size_t i = 0; i < n; i += kWordsPerLaunch) {
+    const int m = static_cast<int>(std::min<size_t>(kWordsPerLaunch, n - i));
+    std::memcpy(chunk.w, static_cast<const unsigned int*>(src) + i, sizeof(unsigned int) * m);
+    k_store_words<<<1, 256, 0, st>>>(static_cast<unsigned int*>(dst) + i, chunk, m);
+  }
+  return cudaGetLastError() == cudaSuccess ? kOk : kErrTransferGpu;
+}
 
 // The scratch.  In host code this name is only a handle: its device address
 // comes from cudaGetSymbolAddress, once per device.
@@ -77,8 +107,9 @@ extern "C" int nrgb_backproject_device_noalloc(const float* d_sinogram, const fl
   const int ncam = cameras_size[0], ncols = cameras_size[1];
   if (nx <= 0 || ny <= 0 || nz <= 0 || ncam <= 0 || !(ncols == 1 || ncols == 3 || ncols == 6)) return kErrParameters;
   if (ncam > kMaxCams) return kErrScratchTooSmall;
+  if (psf && !psf_size) return kErrParameters;
   int k = 0;
-  if (psf && psf_size && !(psf_size[0] == 0 && psf_size[1] == 0 && psf_size[2] == 0)) {
+  if (psf && !(psf_size[0] == 0 && psf_size[1] == 0 && psf_size[2] == 0)) {
     k = psf_size[0];
     if (k % 2 != 1 || psf_size[1] != k || psf_size[2] < nz) return kErrParameters;
     if (static_cast<size_t>(nz) * 2 * k > static_cast<size_t>(kMaxPsfFloats)) return kErrScratchTooSmall;
@@ -147,11 +178,10 @@ extern "C" int nrgb_backproject_device_noalloc(const float* d_sinogram, const fl
   p += geom_b;
   float* d_psf = k ? reinterpret_cast<float*>(p) : nullptr;
   p += psf_b;
-  if (cudaMemcpyAsync(d_geom, g_geom, sizeof(CamGeom) * ncam, cudaMemcpyHostToDevice, st) != cudaSuccess)
-    return kErrTransferGpu;
-  if (k && cudaMemcpyAsync(d_psf, g_psf_sep, sizeof(float) * static_cast<size_t>(nz) * 2 * k,
-                           cudaMemcpyHostToDevice, st) != cudaSuccess)
-    return kErrTransferGpu;
+  if ((s = store_by_value(d_geom, g_geom, sizeof(CamGeom) * ncam, st)) != kOk) return s;
+  if (k && (s = store_by_value(d_psf, g_psf_sep, sizeof(float) * static_cast<size_t>(nz) * 2 * k, st)) != kOk)
+    return s;
+  set_last_path(fused ? 1 : 2);
 
   if (fused) {
     float* sino_c = reinterpret_cast<float*>(p);

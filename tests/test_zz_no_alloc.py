@@ -1,6 +1,7 @@
 """nrgb_backproject_device_noalloc -- the backprojection for callers that
-cannot allocate device memory (inside a CUDA-graph capture, under a
-framework-owned allocator) -- called through the C-ABI and checked against the
+cannot allocate device memory (a plug-in whose host application's allocator
+already holds the GPU's memory, a real-time loop that must not enter the
+driver's allocator) -- called through the C-ABI and checked against the
 allocating entry point nrgb_backproject_device on two calls in a row, with the
 same relative-L2 tolerance as the other parity tests.  Collected last on
 purpose; it also passes alone in a fresh process."""
@@ -66,9 +67,26 @@ def test_noalloc_matches_allocating_entry_point_twice(case):
         assert st == 0, st
         st = _run(L.nrgb_backproject_device_noalloc, sino, mu, out, n, cams, ncols, psf, stream, False)
         assert st == 0, st
+        assert L.nrgb_last_path() == (1 if case == "gantry_psf_att" else 2)
         torch.cuda.synchronize(dev)
         assert torch.isfinite(out).all()
         assert _rel(out, ref) < RTOL
+
+
+def test_noalloc_rejects_psf_without_size():
+    torch = pytest.importorskip("torch")
+    L = _lib.load()
+    dev = torch.device("cuda", 0)
+    n = (16, 16, 16)
+    cams = np.ascontiguousarray(S.cameras_about_y(4)[1])
+    psf = S.gaussian_psf(3, 16)
+    sino = torch.zeros((4, 16, 16), dtype=torch.float32, device=dev)
+    out = torch.zeros((16, 16, 16), dtype=torch.float32, device=dev)
+    st = L.nrgb_backproject_device_noalloc(vp(sino.data_ptr()), None, (ctypes.c_int * 3)(*n), vp(out.data_ptr()),
+                                           cams.ctypes.data_as(vp), (ctypes.c_int * 2)(4, 1),
+                                           psf.ctypes.data_as(vp), None, 0.0, 0.0, 1,
+                                           vp(torch.cuda.current_stream(dev).cuda_stream))
+    assert st == 2
 
 
 def test_noalloc_rejects_problems_beyond_its_scratch():
