@@ -82,6 +82,25 @@ def measured_peak():
         return 6800.0, "fallback"
 
 
+def cpu_model() -> str:
+    """Host CPU model name (lscpu / /proc/cpuinfo), for the CPU baselines."""
+    try:
+        out = subprocess.run(["lscpu"], capture_output=True, text=True, timeout=10).stdout
+        for line in out.splitlines():
+            if line.strip().startswith("Model name:"):
+                return line.split(":", 1)[1].strip()
+    except Exception:
+        pass
+    try:
+        with open("/proc/cpuinfo") as f:
+            for line in f:
+                if line.lower().startswith("model name"):
+                    return line.split(":", 1)[1].strip()
+    except Exception:
+        pass
+    return "unknown"
+
+
 def committed_traffic(kernel: str):
     """dram bytes per launch of `kernel` from the committed ncu summary, or None."""
     for fn in sorted(os.listdir(os.path.join(ROOT, "profiles"))) if os.path.isdir(os.path.join(ROOT, "profiles")) else []:
@@ -345,6 +364,11 @@ def run_ours(args):
     }
     if grad:
         out["attenuation_gradient"] = grad
+    out["error_vs_fp64"] = fp64_errors(act, mu, psf, cams, dev)
+    if not args.no_config1:
+        out["config1"] = config1_leg(dev, flush, stream, args, cpu=rank == 0 and world == 1 and not args.no_cpu_baseline)
+    if not args.no_config5:
+        out["config5"] = config5_leg(dev, flush, stream, args, cpu=rank == 0 and world == 1 and not args.no_cpu_baseline)
     if not args.no_osem:
         out["osem"] = osem_compare(act, mu, psf, cams, dev)
     if not args.no_batch:
@@ -414,6 +438,310 @@ def grad_compare(L, t_act, t_mu, t_sino, t_out, cams, psf, stream, flush, dev, r
     return {"workload": "et_array_gradient_attenuation semantics, 128^3, 120 angles, PSF 11x11, mu, device buffers",
             "paths": list(paths), "fused_ms": round(fused_ms, 3), "general_ms": round(general_ms, 3),
             "speedup": round(general_ms / fused_ms, 2), "fused_kernels": kernels}
+
+
+# ------------------------------------------------------- error vs float64
+def fp64_errors(act, mu, psf, cams, dev):
+    """Relative L2 error of the timed pair's float32 results against the
+    float64 GPU run of the reference algorithm (computed once, outside the
+    timed region): the projection, and the backprojection of that projection."""
+    import torch
+
+    from niftyrec_gb300 import precision as pr
+
+    a32, m32 = torch.from_numpy(act).to(dev), torch.from_numpy(mu).to(dev)
+    p32 = pr.project(a32, m32, cams, psf, truncate=True)
+    p64 = pr.project(a32.double(), m32.double(), cams, psf, truncate=True)
+    b32 = pr.backproject(p32, m32, cams, psf, nz=N, truncate=True)
+    b64 = pr.backproject(p32.double(), m32.double(), cams, psf, nz=N, truncate=True)
+    ep, wp = pr.rel_error(p32, p64)
+    eb, wb = pr.rel_error(b32, b64)
+    return {"projection_rel_l2": ep, "projection_worst_plane": wp, "backprojection_rel_l2": eb,
+            "backprojection_worst_plane": wb,
+            "reference": "float64 GPU run of the reference algorithm (general-orientation kernels in double)"}
+
+
+def _time_ms(fn, flush, stream, reps):
+    """Mean device time of fn() over reps runs (CUDA events on the stream, L2
+    flushed before each run)."""
+    import torch
+
+    ms = []
+    for _ in range(reps):
+        flush.zero_()
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        fn()
+        b.record(stream)
+        ms.append((a, b))
+    torch.cuda.synchronize()
+    return sum(a.elapsed_time(b) for a, b in ms) / reps
+
+
+# ------------------------------------------------- config 1: 64^3 x 60 MLEM
+C1_N, C1_NCAM = 64, 60
+# per angle: projector N^3*4 + N^2*4, each backprojector 2*N^3*4 + N^2*4; one
+# projection and two backprojections per MLEM iteration
+C1_BYTES = C1_NCAM * ((C1_N ** 3 * 4 + C1_N ** 2 * 4) + 2 * (2 * C1_N ** 3 * 4 + C1_N ** 2 * 4))  # 317,521,920
+
+
+def config1_workload():
+    from niftyrec_gb300 import synthetic as S
+    from niftyrec_gb300.array_api import make_cameras
+
+    act = S.ellipsoid_phantom((C1_N,) * 3, seed=0)
+    cams3 = np.ascontiguousarray(make_cameras(0.0, 354.0, C1_NCAM, 1), np.float32)  # [3, 60]
+    return act, cams3
+
+
+def config1_leg(dev, flush, stream, args, cpu=True):
+    """Plain SPECT MLEM at 64^3 x 60 cameras (0..354 degrees, no PSF, no mu;
+    counts Poisson(100 A x), seed 1): device-resident MLEM iterations/s with
+    et_array_mlem_step's work (one projection, two backprojections, ratio and
+    update) through the device entry points, the same through
+    et_array_mlem_step with host buffers (e2e), a plan whose normaliser is
+    computed once (graph-replayed), error of one step against float64, and the
+    CPU reference step."""
+    import torch
+
+    from niftyrec_gb300 import _lib
+    from niftyrec_gb300 import array_api as A
+    from niftyrec_gb300 import precision as pr
+    from niftyrec_gb300 import synthetic as S
+    from niftyrec_gb300.plan import Plan
+
+    L = _lib.load()
+    n, ncam = C1_N, C1_NCAM
+    act, cams3 = config1_workload()
+    y = S.poisson_counts(A.project(act, cams3), 100, seed=1)
+    vp = ctypes.c_void_p
+    size = (ctypes.c_int * 3)(n, n, n)
+    csize = (ctypes.c_int * 2)(ncam, 3)
+    nopsf = (ctypes.c_int * 3)(0, 0, 0)
+    t_y = torch.from_numpy(y).to(dev)
+    t_x = torch.ones((n, n, n), dtype=torch.float32, device=dev)
+    t_p = torch.empty((ncam, n, n), dtype=torch.float32, device=dev)
+    t_ones = torch.ones((ncam, n, n), dtype=torch.float32, device=dev)
+    t_num = torch.empty((n, n, n), dtype=torch.float32, device=dev)
+    t_den = torch.empty((n, n, n), dtype=torch.float32, device=dev)
+    cp = cams3.ctypes.data_as(vp)
+    launches = [0]
+
+    def iteration():
+        sp = vp(stream.cuda_stream)
+        n0 = L.nrgb_launch_count()
+        st = [L.nrgb_project_device(vp(t_x.data_ptr()), None, size, vp(t_p.data_ptr()), cp, csize, None, nopsf,
+                                    0.0, 0.0, 1, sp),
+              L.nrgb_osem_ratio_device(vp(t_y.data_ptr()), vp(t_p.data_ptr()), t_p.numel(), 1e-6, sp),
+              L.nrgb_backproject_device(vp(t_p.data_ptr()), None, size, vp(t_num.data_ptr()), cp, csize, None,
+                                        nopsf, 0.0, 0.0, 1, 0, sp),
+              L.nrgb_backproject_device(vp(t_ones.data_ptr()), None, size, vp(t_den.data_ptr()), cp, csize, None,
+                                        nopsf, 0.0, 0.0, 1, 0, sp),
+              L.nrgb_osem_update_device(vp(t_x.data_ptr()), vp(t_num.data_ptr()), vp(t_den.data_ptr()),
+                                        t_x.numel(), 1e-6, sp)]
+        launches[0] = L.nrgb_launch_count() - n0
+        if any(st):
+            raise RuntimeError(f"config-1 MLEM iteration status {st}")
+
+    for _ in range(args.warmup):
+        iteration()
+    t_x.fill_(1.0)
+    reps = max(5, args.steps)
+    ms = _time_ms(iteration, flush, stream, reps)
+    peak, peak_kind = measured_peak()
+    achieved = C1_BYTES / (ms / 1e3) / 1e9
+
+    # e2e: et_array_mlem_step with host buffers (copies inside the timed region)
+    x = np.ones((n, n, n), np.float32)
+    A.mlem_step(x, y, cams3)
+    e2e_t = []
+    for _ in range(reps):
+        t0 = time.perf_counter()
+        x = A.mlem_step(x, y, cams3)
+        e2e_t.append(time.perf_counter() - t0)
+
+    # a plan (normaliser computed once, the iteration captured as a CUDA graph)
+    plan = Plan((n, n, n), cams3[1].copy(), None, None, subsets=1)
+    plan.osem(t_y, iterations=1, layout="column", graph=True)
+    g = plan._graph[0]
+    plan_ms = _time_ms(g.replay, flush, stream, reps)
+
+    # error of one step against the float64 run (float32 vs float64 MLEM from ones)
+    x32 = pr.osem(t_y, cams3, None, None, 1, 1, storage="float32")
+    x64 = pr.osem(t_y, cams3, None, None, 1, 1, storage="float64")
+    err = pr.rel_error(x32, x64)[0]
+
+    out = {"workload": "plain SPECT MLEM, 64^3 activity (seeded ellipsoid phantom), 60 cameras 0..354 deg about "
+                       "the gantry axis, no PSF, no mu, counts Poisson(100 A x) seed 1",
+           "metric": "MLEM iterations/s (1 projection + 2 backprojections)", "unit": "iterations/s",
+           "value": round(1000.0 / ms, 2), "ms_per_iteration": round(ms, 4), "gpu_launches_per_iteration":
+               launches[0],
+           "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
+                        "frac": round(achieved / peak, 4), "peak_source": peak_kind, "bytes_per_iteration": C1_BYTES,
+                        "note": "whole iteration (several kernels); the volumes fit in L2, flushed before every "
+                                "iteration"},
+           "e2e": {"value": round(1.0 / statistics.median(e2e_t), 2), "unit": "iterations/s",
+                   "api": "et_array_mlem_step", "h2d_bytes_per_step": int(x.nbytes + y.nbytes),
+                   "d2h_bytes_per_step": int(x.nbytes)},
+           "plan_graph": {"value": round(1000.0 / plan_ms, 2), "unit": "iterations/s",
+                          "note": "normaliser B^T 1 computed once per plan (one projection and one backprojection "
+                                  "per iteration), iteration replayed as a CUDA graph"},
+           "error_vs_fp64": {"mlem_step_rel_l2": err}}
+    if cpu:
+        from oracle.oracle import Reference, Restated
+
+        impl, kind = (Reference(), "reference") if Reference.available else (Restated("f32"), "port")
+        x0 = np.ones((n, n, n), np.float32)
+        t0 = time.perf_counter()
+        k = 0
+        while True:
+            if kind == "reference":
+                impl.mlem_step(x0, y, cams3)
+            else:
+                impl.osem_step(x0, y, cams3, list(range(ncam)))
+            k += 1
+            if time.perf_counter() - t0 > 4.0:
+                break
+        dt = (time.perf_counter() - t0) / k
+        out["cpu_baseline"] = {"value": round(1.0 / dt, 4), "unit": "iterations/s", "cores": 1, "kind": kind,
+                               "cpu_model": cpu_model(), "sample": f"{k} full MLEM iteration(s), {dt:.2f} s each"}
+    return out
+
+
+# ------------------------------- config 5: 256^3 x 180, PSF 15, BF16 vs FP32
+C5_N, C5_NCAM, C5_K, C5_SLOPE = 256, 180, 15, 0.015
+
+
+def _c5_bytes(s_vol):
+    """Algorithmic bytes of one pair: per angle the projector reads activity and
+    mu (s_vol bytes each) and writes a float32 plane; the backprojector reads
+    mu, read-modify-writes the float32 accumulator and reads a plane."""
+    n3, n2 = C5_N ** 3, C5_N ** 2
+    return C5_NCAM * ((n3 * 2 * s_vol + n2 * 4) + (n3 * (s_vol + 8) + n2 * 4))
+
+
+def config5_workload():
+    from niftyrec_gb300 import synthetic as S
+
+    n = C5_N
+    act = S.ellipsoid_phantom((n, n, n), seed=0)
+    mu = S.mu_map((n, n, n), seed=0)
+    psf = S.gaussian_psf(C5_K, n, 0.5, C5_SLOPE)
+    cams = S.cameras_about_y(C5_NCAM, 0.0, 2.0)[1].copy()
+    return act, mu, psf, cams
+
+
+def config5_leg(dev, flush, stream, args, cpu=True):
+    """Precision at scale: one project + backproject pair of 256^3 x 180
+    cameras, PSF 15 (sigma = 0.5 + 0.015 z), mu, with float32 storage and with
+    bfloat16 activity / mu (float32 accumulation, Kahan depth sums); pairs/s,
+    HBM fraction of each against its algorithmic bytes, and the error of each
+    result against the float64 GPU run."""
+    import torch
+
+    from niftyrec_gb300 import _lib
+    from niftyrec_gb300 import precision as pr
+
+    L = _lib.load()
+    n, ncam, k = C5_N, C5_NCAM, C5_K
+    act, mu, psf, cams = config5_workload()
+    vp = ctypes.c_void_p
+    size = (ctypes.c_int * 3)(n, n, n)
+    csize = (ctypes.c_int * 2)(ncam, 1)
+    psize = (ctypes.c_int * 3)(k, k, n)
+    cp = np.ascontiguousarray(cams, np.float32)
+    pp = np.ascontiguousarray(psf, np.float32)
+    a32, m32 = torch.from_numpy(act).to(dev), torch.from_numpy(mu).to(dev)
+    a16, m16 = a32.to(torch.bfloat16), m32.to(torch.bfloat16)
+    sino = torch.empty((ncam, n, n), dtype=torch.float32, device=dev)
+    bk = torch.empty((n, n, n), dtype=torch.float32, device=dev)
+
+    def pair(bf16):
+        sp = vp(stream.cuda_stream)
+        fp = L.nrgb_project_device_bf16 if bf16 else L.nrgb_project_device
+        fb = L.nrgb_backproject_device_bf16 if bf16 else L.nrgb_backproject_device
+        a, m = (a16, m16) if bf16 else (a32, m32)
+        st = fp(vp(a.data_ptr()), vp(m.data_ptr()), size, vp(sino.data_ptr()), cp.ctypes.data_as(vp), csize,
+                pp.ctypes.data_as(vp), psize, 0.0, 0.0, 1, sp)
+        st2 = fb(vp(sino.data_ptr()), vp(m.data_ptr()), size, vp(bk.data_ptr()), cp.ctypes.data_as(vp), csize,
+                 pp.ctypes.data_as(vp), psize, 0.0, 0.0, 1, 0, sp)
+        if st or st2:
+            raise RuntimeError(f"config-5 pair status {st} {st2}")
+
+    peak, peak_kind = measured_peak()
+    reps = max(3, args.steps // 3)
+    res = {}
+    for name, bf16, sv in (("float32", False, 4), ("bfloat16", True, 2)):
+        for _ in range(2):
+            pair(bf16)
+        ms = _time_ms(lambda: pair(bf16), flush, stream, reps)
+        byts = _c5_bytes(sv)
+        ach = byts / (ms / 1e3) / 1e9
+        res[name] = {"pairs_per_s": round(1000.0 / ms, 3), "ms_per_pair": round(ms, 3),
+                     "roofline": {"bound": "hbm", "achieved": round(ach, 1), "peak": peak, "unit": "GB/s",
+                                  "frac": round(ach / peak, 4), "peak_source": peak_kind, "bytes_per_pair": byts}}
+    # errors against float64 (outside the timed region)
+    p64 = pr.project(a32.double(), m32.double(), cams, psf, truncate=True)
+    b64 = pr.backproject(p64, m32.double(), cams, psf, nz=n, truncate=True)
+    s32 = p64.float()
+    for name, (a, m) in (("float32", (a32, m32)), ("bfloat16", (a16, m16))):
+        p = pr.project(a, m, cams, psf, truncate=True)
+        b = pr.backproject(s32, m, cams, psf, nz=n, truncate=True)
+        ep, wp = pr.rel_error(p, p64)
+        eb, wb = pr.rel_error(b, b64)
+        res[name]["error_vs_fp64"] = {"projection_rel_l2": ep, "projection_worst_plane": wp,
+                                      "backprojection_rel_l2": eb, "backprojection_worst_plane": wb}
+        del p, b
+    del p64, b64, s32
+    out = {"workload": "256^3 activity + mu (seeded ellipsoid phantom, mu map), PSF 15x15 sigma=0.5+0.015*z, "
+                       "180 angles x 2 deg, project + reference backproject; float32 vs bfloat16 storage",
+           "unit": "pairs/s", **res,
+           "bf16_speedup": round(res["bfloat16"]["pairs_per_s"] / res["float32"]["pairs_per_s"], 3)}
+    if cpu:
+        out["cpu_baseline"] = cpu_pair_sample("config5", 16)
+    return out
+
+
+def _pool_init(which, kind):
+    global _W
+    from oracle.oracle import Reference, Restated
+
+    wl = workload(0) if which == "headline" else config5_workload()
+    _W = (Reference() if kind == "reference" else Restated("f32"),) + tuple(wl)
+
+
+def _pool_noop(_):
+    return 0
+
+
+def _pool_pair(angle_idx):
+    impl, act, mu, psf, cams = _W
+    sub = cams[list(angle_idx)]
+    s = impl.project(act, sub, psf, mu)
+    return float(np.sum(impl.backproject(s, sub, psf, mu)))
+
+
+def cpu_pair_sample(which, n_angles, workers=None):
+    """Project + backproject of n_angles cameras of a workload on all host
+    cores (one process per share of the angles), scaled to pairs/s."""
+    import multiprocessing as mp
+
+    from oracle.oracle import Reference
+
+    kind = "reference" if Reference.available else "port"
+    workers = workers or os.cpu_count() or 1
+    ncam = NCAM if which == "headline" else C5_NCAM
+    idx = list(range(n_angles))
+    chunks = [idx[w::workers] for w in range(workers) if idx[w::workers]]
+    with mp.get_context("spawn").Pool(len(chunks), initializer=_pool_init, initargs=(which, kind)) as pool:
+        pool.map(_pool_noop, range(len(chunks)))
+        t0 = time.perf_counter()
+        pool.map(_pool_pair, chunks)
+        dt = time.perf_counter() - t0
+    return {"value": round(n_angles / ncam / dt, 6), "unit": "pairs/s", "cores": len(chunks), "kind": kind,
+            "cpu_model": cpu_model(),
+            "sample": f"{n_angles} of {ncam} angles projected and backprojected over {len(chunks)} processes, "
+                      f"{dt:.1f} s, scaled to one pair"}
 
 
 # ------------------------------------------------------------------- OSEM
@@ -589,6 +917,7 @@ def cpu_baseline(act, mu, psf, cams, n_angles):
     impl.backproject(s, sub, psf, mu)
     dt = time.perf_counter() - t0
     return {"value": round(n_angles / NCAM / dt, 6), "unit": UNIT, "cores": 1, "kind": kind,
+            "cpu_model": cpu_model(),
             "sample": f"{n_angles} of {NCAM} angles projected and backprojected (128^3, PSF 11x11, mu), "
                       f"{dt:.1f} s, scaled to one pair"}
 
@@ -647,10 +976,159 @@ def run_reference(args):
                    "psf": [K, K, N]},
         "impl": "reference",
         "cpu_baseline": {"value": round(value, 6), "unit": UNIT, "cores": workers, "kind": kind,
+                         "cpu_model": cpu_model(),
                          "sample": f"{per_step} of {NCAM} angles per step over {workers} processes"},
         "e2e": {"value": round(value, 6), "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
+    if not args.no_config1:
+        out["config1"] = cpu_mlem_all_cores(kind, workers, iterations=max(2, min(args.steps, 5)))
+    if not args.no_config5:
+        out["config5"] = {"workload": "256^3 activity + mu, PSF 15x15 sigma=0.5+0.015*z, 180 angles x 2 deg, "
+                                      "project + reference backproject, float32",
+                          "cpu_baseline": cpu_pair_sample("config5", 2 * workers, workers)}
     print(json.dumps(out), flush=True)
+
+
+def _mlem_init(kind):
+    global _W
+    from oracle.oracle import Reference, Restated
+
+    act, cams3 = config1_workload()
+    impl = Reference() if kind == "reference" else Restated("f32")
+    y = np.clip(impl.project(act, cams3), 0, None).astype(np.float64) * 100.0
+    y = np.random.default_rng(1).poisson(y).astype(np.float32)
+    _W = (impl, cams3, y)
+
+
+def _mlem_part(task):
+    """Numerator and normaliser of one share of the cameras (the reference's
+    MLEM step restricted to them: emission-lib/_et_array_interface.cpp:1080-1131)."""
+    idx, x = task
+    impl, cams3, y = _W
+    sub = np.ascontiguousarray(cams3[:, idx])
+    p = impl.project(x, sub)
+    ys = y[idx]
+    r = np.where(p < 1e-6, ys / np.float32(1e-6), ys / np.where(p < 1e-6, 1, p)).astype(np.float32)
+    num = impl.backproject(r, sub, nz=x.shape[0])
+    den = impl.backproject(np.ones_like(r), sub, nz=x.shape[0])
+    return num, den
+
+
+def cpu_mlem_all_cores(kind, workers, iterations):
+    """Config 1 (64^3 x 60, plain MLEM) on all host cores: every iteration
+    splits the cameras over the processes and sums their numerators and
+    normalisers before the update."""
+    import multiprocessing as mp
+
+    idx = list(range(C1_NCAM))
+    chunks = [idx[w::workers] for w in range(workers) if idx[w::workers]]
+    x = np.ones((C1_N,) * 3, np.float32)
+    with mp.get_context("spawn").Pool(len(chunks), initializer=_mlem_init, initargs=(kind,)) as pool:
+        pool.map(_pool_noop, range(len(chunks)))
+        t0 = time.perf_counter()
+        for _ in range(iterations):
+            parts = pool.map(_mlem_part, [(c, x) for c in chunks])
+            num = np.sum([p[0] for p in parts], axis=0)
+            den = np.sum([p[1] for p in parts], axis=0)
+            x = (x * num / np.maximum(den, np.float32(1e-6))).astype(np.float32)
+        dt = (time.perf_counter() - t0) / iterations
+    return {"workload": "plain SPECT MLEM, 64^3, 60 cameras 0..354 deg, no PSF, no mu",
+            "metric": "MLEM iterations/s (1 projection + 2 backprojections)", "unit": "iterations/s",
+            "cpu_baseline": {"value": round(1.0 / dt, 4), "unit": "iterations/s", "cores": len(chunks),
+                             "kind": kind, "cpu_model": cpu_model(),
+                             "sample": f"{iterations} MLEM iterations, cameras split over {len(chunks)} processes"}}
+
+
+# ------------------------------------------------- angle-sharded OSEM mode
+def headline_sharded_workload():
+    """The headline volume with counts Poisson(50 A x) (seed 1) from this
+    rank's GPU projector; every rank draws the same counts."""
+    from niftyrec_gb300 import array_api as A
+    from niftyrec_gb300 import synthetic as S
+
+    act, mu, psf, cams = workload(0)
+    y = S.poisson_counts(A.project(act, cams, psf, mu), 50, seed=1)
+    return act, mu, psf, cams, y
+
+
+def run_sharded(args, make_operator=None, make_workload=None, device=None, out=None):
+    """OSEM whose every subset's cameras are dealt over the ranks (one
+    all_reduce of the numerator volume per subset step; niftyrec_gb300.sharded).
+    Default: the headline workload (128^3 x 120, PSF 11, mu) with 8 interleaved
+    subsets on CUDA with NCCL; make_operator / make_workload / device replace
+    the GPU operator, the workload and the device (CPU ranks over gloo in the
+    tests).  Rank 0 prints one JSON line (and stores it in `out` if given)."""
+    import torch
+    import torch.distributed as dist
+
+    from niftyrec_gb300 import sharded as SH
+
+    world, rank, local = dist_env()
+    cuda = make_operator is None
+    if cuda:
+        torch.cuda.set_device(local)
+        device = torch.device("cuda", local)
+    device = device or torch.device("cpu")
+    if world > 1 and not dist.is_initialized():
+        dist.init_process_group("nccl" if cuda else "gloo", init_method="env://")
+    sync = (lambda: torch.cuda.synchronize(device)) if cuda else (lambda: None)
+    act, mu, psf, cams, y = (make_workload or headline_sharded_workload)()
+    n_subsets = args.subsets
+    ncam = cams.shape[-1]
+    shape = act.shape
+    ids, sids = SH.camera_shares(np.arange(ncam) % n_subsets, rank, world)
+    if make_operator is None:
+        cams3 = np.zeros((3, ncam), np.float32)
+        cams3[1] = cams if cams.ndim == 1 else cams[1]
+        op = SH.PlanOperator(shape, cams3, ids, sids, n_subsets, psf, torch.from_numpy(mu).to(device))
+    else:
+        op = make_operator(cams, ids, sids, n_subsets, psf, mu)
+    counts = SH.split_counts(torch.from_numpy(y).to(device), ids, sids, n_subsets)
+    rec = SH.ShardedOSEM(op, counts, n_subsets, rank=rank, world=world, sync=sync)
+    x = torch.ones(shape, dtype=torch.float32, device=device)
+    for _ in range(args.warmup):
+        rec.run(x, 1)
+    x.fill_(1.0)
+
+    def reduce_max_dev(v):
+        if world == 1:
+            return v
+        t = torch.tensor([v], dtype=torch.float64, device=device)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        return float(t.item())
+
+    if world > 1:
+        dist.barrier()
+    sync()
+    t0 = time.perf_counter()
+    rec.run(x, args.steps)
+    sync()
+    dt = time.perf_counter() - t0
+    if world > 1:
+        dist.barrier()
+    dt = reduce_max_dev(dt)
+    # a second pass with the collectives timed on their own (device synchronised around each)
+    rec.timing_collectives = True
+    rec.collective_seconds = 0.0
+    rec.run(x.clone(), 1)
+    coll_ms = reduce_max_dev(rec.collective_seconds / max(1, n_subsets) * 1e3)
+    line = {"metric": f"OSEM iterations/s, angle-sharded over {world} rank(s) ({shape[2]}x{shape[1]}x{shape[0]}, "
+                      f"{ncam} angles, {n_subsets} subsets)", "value": round(args.steps / dt, 4),
+            "unit": "iterations/s", "n_gpus": world if cuda else 0, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": round(dt / args.steps * 1e3, 4), "higher_is_better": True, "scaling": "strong",
+            "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded ellipsoid phantom, mu map, Gaussian PSF)",
+            "mode": "sharded", "backend": (dist.get_backend() if world > 1 else "none"),
+            "config": {"workload": "angle-sharded OSEM", "volume": list(shape[::-1]), "angles": ncam,
+                       "subsets": n_subsets, "parallelism": f"angles{world}"},
+            "cameras_this_rank": int(len(ids)),
+            "collectives_per_iteration": n_subsets if world > 1 else 0,
+            "allreduce_ms_per_step": round(coll_ms, 4) if world > 1 else 0.0,
+            "allreduce_bytes_per_step": int(np.prod(shape) * 4) if world > 1 else 0}
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+        if out is not None:
+            out.update(line)
+    return x
 
 
 def main():
@@ -664,11 +1142,18 @@ def main():
     ap.add_argument("--no-osem", action="store_true")
     ap.add_argument("--no-grad", action="store_true")
     ap.add_argument("--no-batch", action="store_true")
+    ap.add_argument("--no-config1", action="store_true")
+    ap.add_argument("--no-config5", action="store_true")
+    ap.add_argument("--sharded", action="store_true",
+                    help="angle-sharded OSEM over the ranks (one all_reduce per subset step) instead of the pair")
+    ap.add_argument("--subsets", type=int, default=8)
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
     if args.impl == "reference":
         run_reference(args)
+    elif args.sharded:
+        run_sharded(args)
     else:
         run_ours(args)
 

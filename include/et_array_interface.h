@@ -225,6 +225,26 @@ int nrgb_gradient_attenuation_device(const float *d_sinogram, const float *d_act
                                      const float *psf, const int *psf_size, float background,
                                      float background_attenuation, int truncate, void *stream);
 
+/* Projection and backprojection in one call (addition; the sequence the
+ * reference's et_array_osem_step / et_array_mlem_step run inside one step,
+ * emission-lib/_et_array_interface.cpp:1017-1035, of the et_project /
+ * et_backproject pair emission-lib/_et.cpp:122 and :312).  Projects
+ * d_activity into d_sinogram exactly as nrgb_project_device, then backprojects
+ * d_backproject_input -- or, when it is null, the projection just written --
+ * into d_backprojection exactly as nrgb_backproject_device (mode 0 reference,
+ * 1 exact transpose), with the same cameras, PSF, mu, backgrounds and
+ * truncation.  For cameras about the gantry axis the volumes are laid out
+ * once for both halves, the projector leaves the backprojector's
+ * transmission carries (per depth slab mu prefix sums) and the projection
+ * feeds the backprojector without another layout pass; results equal the two
+ * calls' within float32 rounding.  Device buffers in nifti order; returns once
+ * the work is enqueued on `stream`. */
+int nrgb_project_backproject_device(const float *d_activity, const float *d_attenuation, const int *size,
+                                    float *d_sinogram, const float *d_backproject_input, float *d_backprojection,
+                                    const float *cameras, const int *cameras_size, const float *psf,
+                                    const int *psf_size, float background, float background_attenuation,
+                                    int truncate, int mode, void *stream);
+
 /* Backprojection that allocates nothing.  No counterpart in the reference.
  * For callers that cannot call cudaMalloc: a plug-in inside a host
  * application whose framework allocator already holds the GPU's memory (a

@@ -922,9 +922,48 @@ int backproject_device_call(const float* d_sinogram, const float* d_attenuation,
   return s;
 }
 
+int pair_device_call(const float* d_activity, const float* d_attenuation, const int* size, float* d_sinogram,
+                     const float* d_backproject_input, float* d_backprojection, const float* cameras,
+                     const int* cameras_size, const float* psf, const int* psf_size, float background,
+                     float background_attenuation, int truncate, int mode, void* stream) {
+  if (!size || !cameras || !cameras_size || !d_activity || !d_sinogram || !d_backprojection ||
+      (mode != kBackReference && mode != kBackAdjoint))
+    return kErrParameters;
+  Cameras cc;
+  int s = expand_cameras(cameras, cameras_size[0], cameras_size[1], size, &cc);
+  if (s != kOk) return s;
+  Problem pb;
+  s = make_problem(size[0], size[1], size[2], cc, psf, psf_size, background, background_attenuation, truncate, &pb);
+  if (s != kOk) return s;
+  pb.back_mode = mode;
+  DeviceState& ds = current_device_state(&s);
+  if (s != kOk) return s;
+  std::lock_guard<std::mutex> lk(ds.mu);
+  const size_t ws = pair_workspace(pb, d_attenuation != nullptr, d_backproject_input != nullptr);
+  if ((s = ensure_arena(ds, ws)) != kOk) return s;
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  cudaStreamWaitEvent(st, ds.last_use, 0);
+  g_last_path = (use_fused(pb) || use_fused_x(pb)) ? 1 : 2;
+  s = pair_device(pb, d_activity, d_attenuation, d_sinogram, d_backproject_input, d_backprojection, ds.arena,
+                  ds.arena_bytes, &ds.staging, st);
+  cudaEventRecord(ds.last_use, st);
+  return s;
+}
+
 }  // namespace
 
 extern "C" {
+
+// Projection and backprojection in one call (see the header).
+int nrgb_project_backproject_device(const float* d_activity, const float* d_attenuation, const int* size,
+                                    float* d_sinogram, const float* d_backproject_input, float* d_backprojection,
+                                    const float* cameras, const int* cameras_size, const float* psf,
+                                    const int* psf_size, float background, float background_attenuation,
+                                    int truncate, int mode, void* stream) {
+  return pair_device_call(d_activity, d_attenuation, size, d_sinogram, d_backproject_input, d_backprojection,
+                          cameras, cameras_size, psf, psf_size, background, background_attenuation, truncate, mode,
+                          stream);
+}
 
 int nrgb_project_device(const float* d_activity, const float* d_attenuation, const int* size, float* d_sinogram,
                         const float* cameras, const int* cameras_size, const float* psf, const int* psf_size,

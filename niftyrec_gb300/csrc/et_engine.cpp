@@ -520,6 +520,80 @@ int backproject_device(const Problem& pb, const float* d_sino, const float* d_at
   return check(pb.back_mode == kBackAdjoint ? general_adjoint(g, st) : general_backproject(g, st));
 }
 
+size_t pair_workspace(const Problem& pb, bool has_att, bool has_input) {
+  const size_t seq = std::max(project_workspace(pb, true, has_att), backproject_workspace(pb, has_att));
+  if (!use_fused(pb)) return seq;
+  const int group = std::max(1, std::min(pb.group, pb.cams.n));
+  return common_bytes(pb) +
+         sizeof(float) * (col_n(pb) * (has_att ? 3 : 2) + sino_col_n(pb) * (has_input ? 2 : 1)) +
+         yg_backproject_workspace(pb.nx, pb.ny, pb.nz, pb.cams.n, group) + kSlack;
+}
+
+int pair_device(const Problem& pb, const float* d_act, const float* d_att, float* d_sino, const float* d_bk_in,
+                float* d_bk, char* ws, size_t ws_bytes, Staging* stg, cudaStream_t st) {
+  if (!use_fused(pb) || !d_act) {  // the two calls in sequence (stream-ordered reuse of the work space)
+    int s = project_device(pb, d_act, d_att, d_sino, ws, ws_bytes, stg, st);
+    if (s != kOk) return s;
+    return backproject_device(pb, d_bk_in ? d_bk_in : d_sino, d_att, d_bk, ws, ws_bytes, stg, st);
+  }
+  Carver cv(ws, ws_bytes);
+  CamGeom* d_geom;
+  float* d_psf;
+  int2* d_units;
+  int s = upload_common(pb, cv, &d_geom, &d_psf, stg, st, &d_units);
+  if (s != kOk) return s;
+  const int cy = round_up(pb.ny, 4);
+  const int group = std::max(1, std::min(pb.group, pb.cams.n));
+  float* act_c = cv.take<float>(col_n(pb));
+  float* mu_c = d_att ? cv.take<float>(col_n(pb)) : nullptr;
+  float* sino_c = cv.take<float>(sino_col_n(pb));
+  float* in_c = d_bk_in ? cv.take<float>(sino_col_n(pb)) : sino_c;
+  float* out_c = cv.take<float>(col_n(pb));
+  // carries (at most kSlabsB + 1 slots per camera) then the scratch slots
+  float* work = cv.take<float>(yg_backproject_workspace(pb.nx, pb.ny, pb.nz, pb.cams.n, group) / sizeof(float));
+  if (!act_c || !sino_c || !in_c || !out_c || !work || (d_att && !mu_c)) return kErrAllocGpu;
+  const size_t carry_n = static_cast<size_t>(pb.cams.n) * yg_carry_slabs() * pb.nx * cy;
+  if ((s = stage_column(pb, d_act, act_c, cy, pb.nz, st)) != kOk) return s;
+  if (d_att && (s = stage_column(pb, d_att, mu_c, cy, pb.nz, st)) != kOk) return s;
+  YgArgs a;
+  a.storage = pb.storage;
+  a.pslabs = pb.pslabs;
+  a.nx = pb.nx;
+  a.ny = pb.ny;
+  a.nz = pb.nz;
+  a.cy = cy;
+  a.ncam = pb.cams.n;
+  a.geom = d_geom;
+  a.units = d_units;
+  a.nunits = static_cast<int>(pb.units.size() / 2);
+  a.act = act_c;
+  a.mu = mu_c;
+  a.out = sino_c;
+  a.psf = d_psf;
+  a.psf_host = pb.psf_k ? pb.psf_sep.data() : nullptr;
+  a.psf_k = pb.psf_k;
+  a.truncate = pb.truncate;
+  // the projector leaves the carries of its depth slabs for the backprojector
+  a.carry_out = d_att ? work : nullptr;
+  int slabs = 0;
+  if ((s = yg_project(a, st, &slabs)) != kOk) return s;
+  if (d_att && (slabs < 1 || slabs + 1 > yg_carry_slabs())) return kErrKernel;
+  if ((s = from_column(sino_c, d_sino, pb.nx, pb.ny, cy, pb.cams.n, 0, st)) != kOk) return s;
+  if (d_bk_in && (s = to_column(d_bk_in, in_c, pb.nx, pb.ny, cy, pb.cams.n, st)) != kOk) return s;
+  YgArgs b = a;
+  b.carry_out = nullptr;
+  b.act = nullptr;
+  b.sino = in_c;
+  b.out = out_c;
+  b.back_mode = pb.back_mode;
+  b.group = group;
+  b.carry = d_att ? work : nullptr;
+  b.bslabs = d_att ? slabs : b.bslabs;
+  b.work = work + (d_att ? carry_n : 0);
+  if ((s = yg_backproject(b, st)) != kOk) return s;
+  return check(from_column(out_c, d_bk, pb.nx, pb.ny, cy, pb.nz, pb.truncate, st));
+}
+
 size_t partial_workspace(const Problem& pb) { return common_bytes(pb) + sizeof(float) * vol_n(pb) * 3 + 3 * 256; }
 
 int project_partial_device(const Problem& pb, const float* d_act, const float* d_att, const float* d_bg_image,

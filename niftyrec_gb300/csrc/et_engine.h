@@ -126,6 +126,14 @@ int backproject_device(const Problem& pb, const float* d_sino, const float* d_at
                        size_t ws_bytes, Staging* stg, cudaStream_t st);
 int gradient_device(const Problem& pb, const float* d_sino, const float* d_act, const float* d_att, float* d_out,
                     char* ws, size_t ws_bytes, Staging* stg, cudaStream_t st);
+// Projection followed by a backprojection with the same cameras, PSF and mu
+// (d_bk_in, or the projection itself when null), in one sequence: for
+// cameras about the gantry axis the volumes are laid out once, the projector
+// leaves the backprojector's transmission carries, and the projection feeds
+// the backprojector in its column layout.
+size_t pair_workspace(const Problem& pb, bool has_att, bool has_input);
+int pair_device(const Problem& pb, const float* d_act, const float* d_att, float* d_sino, const float* d_bk_in,
+                float* d_bk, char* ws, size_t ws_bytes, Staging* stg, cudaStream_t st);
 // Projection with partial sums (et_project_partial): d_partial receives
 // [ncam][nz][ny][nx]; d_bg_image [ny][nx] or null.
 size_t partial_workspace(const Problem& pb);

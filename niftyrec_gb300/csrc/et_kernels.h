@@ -80,6 +80,13 @@ struct YgArgs {
   float* slab_T = nullptr;
   float* temp = nullptr;
   int group = 16;
+  // Backprojector depth slabs (1..16): carries hold bslabs + 1 slots per
+  // camera (every slab's exclusive prefix, then the column total).
+  int bslabs = 16;
+  // Projector: non-null -> also write the transmission carries of its own
+  // depth slabs ([ncam][pslabs + 1][nx][cy], the layout above with bslabs =
+  // the projector's slab count; with units, at each unit's first camera).
+  float* carry_out = nullptr;
   // 1: spread on the caller's stream, gather on a second stream, two scratch
   // slots; 0: both on the caller's stream with one slot (creates no stream
   // or event).
@@ -108,7 +115,9 @@ bool yg_supported(int nx, int ny, int nz, int psf_k);
 // Bytes of work space yg_backproject needs (slab carries + `slots` camera-group
 // scratch volumes of `group` cameras each).
 size_t yg_backproject_workspace(int nx, int ny, int nz, int ncam, int group, int slots = 2);
-int yg_project(const YgArgs& a, cudaStream_t st);
+// slabs_used (if non-null): the projector's depth slabs (the slab count of
+// the carries written to a.carry_out).
+int yg_project(const YgArgs& a, cudaStream_t st, int* slabs_used = nullptr);
 // Gradient of sum(g * project(act, mu)) with respect to mu for gantry cameras
 // (column layouts: a.act, a.mu; a.sino = g [ncam][nx][cy]; a.out = the
 // gradient [nz][nx][cy], zeroed here); no backgrounds.

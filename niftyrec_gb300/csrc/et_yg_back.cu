@@ -7,11 +7,11 @@ namespace nrgb {
 namespace {
 
 // ------------------------------------------------ backprojector: slab carry
-// carry[c][s][x][y] (s < kSlabsB) = sum of the rotated mu over the depth
+// carry[c][s][x][y] (s < a.bslabs) = sum of the rotated mu over the depth
 // slabs before s (exclusive prefix): the transmission a depth slab starts
-// from; carry[c][kSlabsB][x][y] = the whole column's sum.  One block row per
+// from; carry[c][a.bslabs][x][y] = the whole column's sum.  One block row per
 // camera c, or with a.units per unit (its first camera c; a mirror camera's
-// transmissions are c's read from the other end).
+// transmissions are c's read from the other end); one warp per depth slab.
 template <class V>
 __global__ void __launch_bounds__(32 * kSlabsB) k_mu_carry_yg(const YgArgs a, int u0) {
   constexpr int C = kCarryCols;
@@ -27,7 +27,8 @@ __global__ void __launch_bounds__(32 * kSlabsB) k_mu_carry_yg(const YgArgs a, in
   const int yb = lane * 4;
   const bool yok = lane_rows_ok(a, yb);
   const CamRows cr = cam_rows(a.geom[cam].fwd);
-  const int zper = (a.nz + kSlabsB - 1) / kSlabsB;
+  const int nsl = a.bslabs, slots = nsl + 1;
+  const int zper = (a.nz + nsl - 1) / nsl;
   const int zbeg = warp * zper, zend = min(a.nz, zbeg + zper);
   float4 S[C], cS[C];
 #pragma unroll
@@ -55,9 +56,9 @@ __global__ void __launch_bounds__(32 * kSlabsB) k_mu_carry_yg(const YgArgs a, in
     if (x >= a.nx) continue;
     float4 pre = make_float4(0.f, 0.f, 0.f, 0.f);
     for (int s = 0; s < warp; ++s) add4(pre, s_sum[s][i][lane]);
-    float* dst = a.slab_T + ((static_cast<size_t>(cam) * kCarrySlots + warp) * a.nx + x) * a.cy + a.row0 + yb;
+    float* dst = a.slab_T + ((static_cast<size_t>(cam) * slots + warp) * a.nx + x) * a.cy + a.row0 + yb;
     *reinterpret_cast<float4*>(dst) = pre;
-    if (warp == kSlabsB - 1) {  // the column total, one slot further
+    if (warp == nsl - 1) {  // the column total, one slot further
       add4(pre, s_sum[warp][i][lane]);
       *reinterpret_cast<float4*>(dst + static_cast<size_t>(a.nx) * a.cy) = pre;
     }
@@ -91,14 +92,15 @@ __device__ __forceinline__ void spread_body(const YgArgs& a, int c0, const float
 
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int ntile = (a.nx + kTXC - 1) / kTXC;
-  const int slab = blockIdx.x % kSlabsB;
-  const int item = blockIdx.x / kSlabsB;
+  const int nsl = a.bslabs, slots = nsl + 1;
+  const int slab = blockIdx.x % nsl;
+  const int item = blockIdx.x / nsl;
   const int g = item / ntile;
   const int cam = c0 + g;
   const int x0 = (item % ntile) * kTXC;
   const int yb = lane * 4;
   const bool yok = lane_rows_ok(a, yb);
-  const int zper = (a.nz + kSlabsB - 1) / kSlabsB;
+  const int zper = (a.nz + nsl - 1) / nsl;
   const int zbeg = slab * zper, zend = min(a.nz, zbeg + zper);
   if (zbeg >= zend) return;  // uniform over the CTA
   if (PSF && !PTAB) {  // this slab's planes only
@@ -121,7 +123,7 @@ __device__ __forceinline__ void spread_body(const YgArgs& a, int c0, const float
     cTc[k] = make_float4(0.f, 0.f, 0.f, 0.f);
     const int xp = x0 - R + warp + kW * k;
     if (ATT && warp + kW * k < NS && xp >= 0 && xp < a.nx && yok)
-      Tc[k] = ldg4(a.slab_T + ((static_cast<size_t>(cam) * kCarrySlots + slab) * a.nx + xp) * a.cy + a.row0 + yb);
+      Tc[k] = ldg4(a.slab_T + ((static_cast<size_t>(cam) * slots + slab) * a.nx + xp) * a.cy + a.row0 + yb);
   }
   ybuf_zero_pads();
   __syncthreads();
@@ -220,8 +222,9 @@ __device__ __forceinline__ void spread_pair_body(const YgArgs& a, int u0, const 
 
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int ntile = (a.nx + kTXC - 1) / kTXC;
-  const int slab = blockIdx.x % kSlabsB;
-  const int item = blockIdx.x / kSlabsB;
+  const int nsl = a.bslabs, slots = nsl + 1;
+  const int slab = blockIdx.x % nsl;
+  const int item = blockIdx.x / nsl;
   const int g = item / ntile;
   const int unit = u0 + g;
   const int2 uc = a.units[unit];
@@ -230,7 +233,7 @@ __device__ __forceinline__ void spread_pair_body(const YgArgs& a, int u0, const 
   const int x0 = (item % ntile) * kTXC;
   const int yb = lane * 4;
   const bool yok = lane_rows_ok(a, yb);
-  const int zper = (a.nz + kSlabsB - 1) / kSlabsB;
+  const int zper = (a.nz + nsl - 1) / nsl;
   const int zbeg = slab * zper, zend = min(a.nz, zbeg + zper);
   if (zbeg >= zend) return;  // uniform over the CTA
   float* s_psf_m = s_psf + zper * 2 * K;
@@ -261,10 +264,10 @@ __device__ __forceinline__ void spread_pair_body(const YgArgs& a, int u0, const 
     Tr[k] = make_float4(0.f, 0.f, 0.f, 0.f);
     const int xp = x0 - R + warp + kW * k;
     if (ATT && warp + kW * k < NS && xp >= 0 && xp < a.nx && yok) {
-      const float* cp = a.slab_T + ((static_cast<size_t>(cam) * kCarrySlots + slab) * a.nx + xp) * a.cy + a.row0 + yb;
+      const float* cp = a.slab_T + ((static_cast<size_t>(cam) * slots + slab) * a.nx + xp) * a.cy + a.row0 + yb;
       Tc[k] = ldg4(cp);
       if (paired) {
-        const float4 tot = ldg4(cp + static_cast<size_t>(kSlabsB - slab) * a.nx * a.cy);
+        const float4 tot = ldg4(cp + static_cast<size_t>(nsl - slab) * a.nx * a.cy);
         Tr[k] = make_float4(tot.x - Tc[k].x, tot.y - Tc[k].y, tot.z - Tc[k].z, tot.w - Tc[k].w);
       }
     }
@@ -424,7 +427,7 @@ const PsfTable* psf_table(const YgArgs& a) {
 template <int R, bool ADJ>
 int launch_spread_R(const YgArgs& a, int c0, int gcount, cudaStream_t st) {
   const int ntile = (a.nx + kTXC - 1) / kTXC;
-  const dim3 grid(gcount * ntile * kSlabsB), block(32 * kW);
+  const dim3 grid(gcount * ntile * a.bslabs), block(32 * kW);
   const bool psf = a.psf != nullptr;
   const PsfTable* tab = psf_table<R>(a);
   const size_t smem = tile_smem_bytes<R>(psf && !tab ? a.nz : 0);
@@ -483,9 +486,9 @@ template <int R, bool ADJ>
 int launch_spread_pair_R(const YgArgs& a, int u0, int gcount, cudaStream_t st) {
   using TS = TileShape<R>;
   const int ntile = (a.nx + kTXC - 1) / kTXC;
-  const dim3 grid(gcount * ntile * kSlabsB), block(32 * kW);
+  const dim3 grid(gcount * ntile * a.bslabs), block(32 * kW);
   const bool psf = a.psf != nullptr;
-  const int zper = (a.nz + kSlabsB - 1) / kSlabsB;
+  const int zper = (a.nz + a.bslabs - 1) / a.bslabs;
   const PsfTable* tab = psf_table<R>(a);
   const size_t smem =
       2 * TS::kSbBytes + TS::kTapBytes + (psf && !tab ? sizeof(float) * 2 * zper * 2 * (2 * R + 1) : 0);
@@ -551,7 +554,7 @@ int spread_by_radius(int R, const YgArgs& a, int c0, int gcount, cudaStream_t st
 size_t yg_backproject_workspace(int nx, int ny, int nz, int ncam, int group, int slots) {
   const size_t cy = round_up(ny, 4);
   const size_t vol = static_cast<size_t>(nz) * nx * scratch_rows(ny);  // one window's scratch volume
-  const size_t slabs = static_cast<size_t>(ncam) * kCarrySlots * nx * cy;
+  const size_t slabs = static_cast<size_t>(ncam) * kCarrySlots * nx * cy;  // at most kSlabsB slabs
   // with two slots the spread of group g+1 overlaps the gather of group g
   return sizeof(float) * (slabs + static_cast<size_t>(slots) * vol * std::max(1, std::min(group, ncam)));
 }
@@ -573,9 +576,9 @@ int mu_carry_range(const YgArgs& a_in, float* out, int u0, int n, cudaStream_t s
     a.slab_T = out;
     NRGB_LAUNCH_SCOPE("k_mu_carry_yg", st);
     if (a.storage == kStorageBF16)
-      k_mu_carry_yg<__nv_bfloat16><<<n * nchunk, 32 * kSlabsB, 0, st>>>(a, u0);
+      k_mu_carry_yg<__nv_bfloat16><<<n * nchunk, 32 * a.bslabs, 0, st>>>(a, u0);
     else
-      k_mu_carry_yg<float><<<n * nchunk, 32 * kSlabsB, 0, st>>>(a, u0);
+      k_mu_carry_yg<float><<<n * nchunk, 32 * a.bslabs, 0, st>>>(a, u0);
   }
   return cudaGetLastError() == cudaSuccess ? kOk : kErrKernel;
 }
@@ -623,6 +626,7 @@ Pipe* pipe_for_current_device() {
 // slot.
 int yg_backproject(const YgArgs& a_in, cudaStream_t st) {
   YgArgs a = a_in;
+  if (a.bslabs < 1 || a.bslabs > kSlabsB) return kErrParameters;
   const int R = a.psf ? (a.psf_k - 1) / 2 : 0;
   // mirror units: float32 mu
   const bool pair = !a.gradient && a.units && a.nunits > 0 && a.storage != kStorageBF16;
@@ -646,7 +650,7 @@ int yg_backproject(const YgArgs& a_in, cudaStream_t st) {
     slot0 = a.work;
   } else {
     a.slab_T = a.work;
-    slot0 = a.work + static_cast<size_t>(a.ncam) * kCarrySlots * a.nx * a.cy;
+    slot0 = a.work + static_cast<size_t>(a.ncam) * (a.bslabs + 1) * a.nx * a.cy;
     int s = yg_mu_carry(a, a.slab_T, st);
     if (s != kOk) return s;
   }

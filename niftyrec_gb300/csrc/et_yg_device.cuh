@@ -705,23 +705,30 @@ __device__ __forceinline__ void project_item(const YgArgs& a, int cam, int mate,
     }
     *reinterpret_cast<float4*>(a.out + (static_cast<size_t>(c) * a.nx + x) * a.cy + a.row0 + yb) = Pt;
   };
+  // transmission carries for the backprojector (a.carry_out): the exclusive
+  // prefix of the slab sums at every slab, then the column total
+  float* carry = ATT && a.carry_out ? a.carry_out + a.row0 + yb : nullptr;
+  const size_t cstride = static_cast<size_t>(a.nx) * a.cy;
 #pragma unroll
   for (int i = 0; i < kTXW; ++i) {
     const int o = warp * kTXW + i;
     const int x = x0 + o;
     if (o / per_rank != slab || x >= a.nx || !yok || !lane_writes(a, yb)) continue;
     float4 Pt = make_float4(0.f, 0.f, 0.f, 0.f), Tt = make_float4(0.f, 0.f, 0.f, 0.f);
+    float* cdst = carry ? carry + (static_cast<size_t>(cam) * (nslabs + 1) * a.nx + x) * a.cy : nullptr;
     for (int s = 0; s < nslabs; ++s) {
       const float4* rT = cluster.map_shared_rank(sT, s);
       const float4* rP = cluster.map_shared_rank(sP, s);
       const float4 ps = rP[o * 32 + lane];
       if (ATT) {
+        if (cdst) *reinterpret_cast<float4*>(cdst + s * cstride) = Tt;
         fma4(Pt, exp_neg4(Tt), ps);
         add4(Tt, rT[o * 32 + lane]);
       } else {
         add4(Pt, ps);
       }
     }
+    if (cdst) *reinterpret_cast<float4*>(cdst + nslabs * cstride) = Tt;
     store(cam, x, Pt);
     if (PAIR && paired) {  // the mate's slabs from the far end: its column nx-1-x
       Pt = make_float4(0.f, 0.f, 0.f, 0.f);

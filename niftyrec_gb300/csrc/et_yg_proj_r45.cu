@@ -3,7 +3,7 @@
 
 namespace nrgb {
 
-template int launch_project_R<4>(const YgArgs& a, cudaStream_t st);
-template int launch_project_R<5>(const YgArgs& a, cudaStream_t st);
+template int launch_project_R<4>(const YgArgs& a, cudaStream_t st, int* slabs_used);
+template int launch_project_R<5>(const YgArgs& a, cudaStream_t st, int* slabs_used);
 
 }  // namespace nrgb

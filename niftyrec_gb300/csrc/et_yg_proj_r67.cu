@@ -3,7 +3,7 @@
 
 namespace nrgb {
 
-template int launch_project_R<6>(const YgArgs& a, cudaStream_t st);
-template int launch_project_R<7>(const YgArgs& a, cudaStream_t st);
+template int launch_project_R<6>(const YgArgs& a, cudaStream_t st, int* slabs_used);
+template int launch_project_R<7>(const YgArgs& a, cudaStream_t st, int* slabs_used);
 
 }  // namespace nrgb

@@ -5,7 +5,7 @@
 namespace nrgb {
 
 template <int R>
-int launch_project_R(const YgArgs& a, cudaStream_t st);  // et_yg_project_kernels.cuh
+int launch_project_R(const YgArgs& a, cudaStream_t st, int* slabs_used);  // et_yg_project_kernels.cuh
 
 // ------------------------------------------------------------- dispatch
 // Depth slabs (cluster size) of the projector: the fewest of 2, 4, 8 (16
@@ -62,16 +62,16 @@ __global__ void __cluster_dims__(kSlabsP, 1, 1) __launch_bounds__(32 * kW, 2)
   }
 }
 
-int project_by_radius(int R, const YgArgs& a, cudaStream_t st) {
+int project_by_radius(int R, const YgArgs& a, cudaStream_t st, int* slabs_used) {
   switch (R) {
-    case 0: return launch_project_R<0>(a, st);
-    case 1: return launch_project_R<1>(a, st);
-    case 2: return launch_project_R<2>(a, st);
-    case 3: return launch_project_R<3>(a, st);
-    case 4: return launch_project_R<4>(a, st);
-    case 5: return launch_project_R<5>(a, st);
-    case 6: return launch_project_R<6>(a, st);
-    case 7: return launch_project_R<7>(a, st);
+    case 0: return launch_project_R<0>(a, st, slabs_used);
+    case 1: return launch_project_R<1>(a, st, slabs_used);
+    case 2: return launch_project_R<2>(a, st, slabs_used);
+    case 3: return launch_project_R<3>(a, st, slabs_used);
+    case 4: return launch_project_R<4>(a, st, slabs_used);
+    case 5: return launch_project_R<5>(a, st, slabs_used);
+    case 6: return launch_project_R<6>(a, st, slabs_used);
+    case 7: return launch_project_R<7>(a, st, slabs_used);
     default: return kErrParameters;
   }
 }
@@ -119,11 +119,14 @@ int yg_project_batch(const BatchStepDesc* d_desc, const BatchSel& sel, int psf_k
   return project_batch_by_radius(psf_k, d_desc, sel, att, max_nz, d_counter, st);
 }
 
-int yg_project(const YgArgs& a, cudaStream_t st) {
+int yg_project(const YgArgs& a, cudaStream_t st, int* slabs_used) {
   const int R = a.psf ? (a.psf_k - 1) / 2 : 0;
+  int used = 0;
   for (const Window& w : row_windows(a.ny, R)) {
-    const int s = project_by_radius(R, windowed(a, w), st);
+    const int s = project_by_radius(R, windowed(a, w), st, &used);
     if (s != kOk) return s;
+    // every window launches with the same slab count (same sizes, same kernel)
+    if (slabs_used) *slabs_used = used;
   }
   return kOk;
 }

@@ -43,9 +43,11 @@ __global__ void __launch_bounds__(32 * kW, CTAS) k_project_ptab_yg(const YgArgs 
 }  // namespace
 
 // Launch the per-call projector of PSF radius R (R = 0: no PSF) for one row
-// window; explicitly instantiated in et_yg_proj_r*.cu.
+// window; explicitly instantiated in et_yg_proj_r*.cu.  slabs_used (if
+// non-null) receives the depth-slab count of the launch (the slabs of the
+// carries written to a.carry_out).
 template <int R>
-int launch_project_R(const YgArgs& a_in, cudaStream_t st) {
+int launch_project_R(const YgArgs& a_in, cudaStream_t st, int* slabs_used) {
   YgArgs a = a_in;
   const int ntile = (a.nx + kTXC - 1) / kTXC;
   const bool psf = a.psf != nullptr;
@@ -87,6 +89,7 @@ int launch_project_R(const YgArgs& a_in, cudaStream_t st) {
     }
     cfg.gridDim = dim3(nunits * ntile * a.pslabs);
     attr[0].val.clusterDim.x = a.pslabs;
+    if (slabs_used) *slabs_used = a.pslabs;
     NRGB_LAUNCH_SCOPE("k_project_yg", st);
     if (cudaLaunchKernelEx(&cfg, k, a, extra...) != cudaSuccess) launch_err = true;
   };

@@ -114,13 +114,18 @@ class ShardedOSEM:
     group: torch.distributed group (None: the default group); world == 1
     makes no collective call at all."""
 
-    def __init__(self, operator, counts, n_subsets, rank=0, world=1, group=None, epsilon=1e-6):
+    def __init__(self, operator, counts, n_subsets, rank=0, world=1, group=None, epsilon=1e-6, sync=None):
         self.op = operator
         self.counts = counts
         self.n_subsets = int(n_subsets)
         self.rank, self.world, self.group = rank, world, group
         self.epsilon = float(epsilon)
         self.collectives = 0
+        # collective timing (host clock, the device synchronised on both sides
+        # by `sync`); off unless timing_collectives is set
+        self.sync = sync or (lambda: None)
+        self.timing_collectives = False
+        self.collective_seconds = 0.0
         self.sens = []
         for s in range(self.n_subsets):
             den = self.op.sensitivity(s)
@@ -129,9 +134,17 @@ class ShardedOSEM:
 
     def _sum(self, t):
         if self.world > 1:
+            import time
+
             import torch.distributed as dist
 
+            if self.timing_collectives:
+                self.sync()
+                t0 = time.perf_counter()
             dist.all_reduce(t, op=dist.ReduceOp.SUM, group=self.group)
+            if self.timing_collectives:
+                self.sync()
+                self.collective_seconds += time.perf_counter() - t0
             self.collectives += 1
 
     def step(self, x, subset):

@@ -122,6 +122,53 @@ def test_two_ranks_match_single_process(tmp_path, ncam, n_subsets):
     assert rel < 1e-5, rel
 
 
+def _bench_rank_main(rank, world, port, ncam, n_subsets, iterations, out_dir):
+    """One rank of bench.py's sharded mode, with the oracle operator on CPU."""
+    import json
+    import types
+
+    os.environ.update(MASTER_ADDR="127.0.0.1", MASTER_PORT=str(port), RANK=str(rank), WORLD_SIZE=str(world),
+                      LOCAL_RANK=str(rank))
+    import torch.distributed as dist
+
+    import bench
+
+    args = types.SimpleNamespace(steps=iterations, warmup=1, subsets=n_subsets)
+    line = {}
+    try:
+        x = bench.run_sharded(args, make_operator=OracleOperator, make_workload=lambda: problem(ncam),
+                              device=torch.device("cpu"), out=line)
+        np.save(os.path.join(out_dir, f"x{rank}.npy"), x.numpy())
+        if rank == 0:
+            with open(os.path.join(out_dir, "line.json"), "w") as f:
+                json.dump(line, f)
+    finally:
+        if dist.is_initialized():
+            dist.destroy_process_group()
+
+
+def test_bench_sharded_mode_two_gloo_ranks(tmp_path):
+    """bench.py --sharded, driven with two CPU ranks over gloo: the estimate
+    after K timed iterations is replicated, equals the single-process OSEM, and
+    the JSON line reports one collective per subset step."""
+    import json
+
+    import torch.multiprocessing as mp
+
+    world, ncam, n_subsets, iterations = 2, 12, 3, 2
+    mp.start_processes(_bench_rank_main, args=(world, _free_port(), ncam, n_subsets, iterations, str(tmp_path)),
+                       nprocs=world, start_method="spawn", join=True)
+    x0, x1 = np.load(tmp_path / "x0.npy"), np.load(tmp_path / "x1.npy")
+    np.testing.assert_array_equal(x0, x1)
+    ref = _single_process(ncam, n_subsets, iterations)
+    assert np.linalg.norm(x0 - ref) / np.linalg.norm(ref) < 1e-5
+    line = json.loads((tmp_path / "line.json").read_text())
+    assert line["mode"] == "sharded" and line["backend"] == "gloo"
+    assert line["collectives_per_iteration"] == n_subsets
+    assert line["value"] > 0 and line["allreduce_ms_per_step"] >= 0
+    assert line["allreduce_bytes_per_step"] == int(np.prod(SHAPE)) * 4
+
+
 def test_camera_shares_partition():
     sub = np.arange(30) % 4
     seen = []
