@@ -12,9 +12,11 @@ ranges stand in for a dataset (none is involved).
 
 One JSON line on stdout (rank 0).  `value` is device-resident throughput
 (inputs already in HBM, L2 flushed between steps, CUDA events on the launching
-stream); `e2e` is the same pair through the reference-facing C-ABI with host
-buffers (SPECT_project_parallelholes + SPECT_backproject_parallelholes, all
-host<->device copies inside the timed region).  With --gpus N (torchrun), each
+stream) of nrgb_project_backproject_device, which projects and then
+backprojects the projection in one call (the two separate device calls are
+reported beside it); `e2e` is the same pair through the reference-facing C-ABI
+with host buffers (SPECT_project_parallelholes + SPECT_backproject_parallelholes,
+all host<->device copies inside the timed region).  With --gpus N (torchrun), each
 rank runs its own independent pairs on its own GPU (weak scaling; no
 collective on the data path) and the slowest rank's time is reported.
 """
@@ -221,8 +223,20 @@ def run_ours(args):
     psf_c = np.ascontiguousarray(psf, np.float32)
     vp = ctypes.c_void_p
 
-    def pair(use_psf=True, use_att=True, mode=0):
+    def pair(use_psf=True, use_att=True, mode=0, separate=False):
+        """One pair: nrgb_project_backproject_device (projection, then the
+        backprojection of that projection), or the two separate calls."""
         sp = vp(stream.cuda_stream)
+        if not separate:
+            st = L.nrgb_project_backproject_device(vp(t_act.data_ptr()), vp(t_mu.data_ptr()) if use_att else None,
+                                                   size, vp(t_sino.data_ptr()), None, vp(t_bk.data_ptr()),
+                                                   cams_c.ctypes.data_as(vp), csize,
+                                                   psf_c.ctypes.data_as(vp) if use_psf else None,
+                                                   psize if use_psf else (ctypes.c_int * 3)(0, 0, 0), 0.0, 0.0, 1,
+                                                   mode, sp)
+            if st:
+                raise RuntimeError(f"nrgb_project_backproject_device status {st}")
+            return
         st = L.nrgb_project_device(vp(t_act.data_ptr()), vp(t_mu.data_ptr()) if use_att else None, size,
                                    vp(t_sino.data_ptr()), cams_c.ctypes.data_as(vp), csize,
                                    psf_c.ctypes.data_as(vp) if use_psf else None,
@@ -236,7 +250,7 @@ def run_ours(args):
         if st:
             raise RuntimeError(f"nrgb_backproject_device status {st}")
 
-    def timed(steps, use_psf=True, use_att=True, profile=False, mode=0, only=None):
+    def timed(steps, use_psf=True, use_att=True, profile=False, mode=0, only=None, separate=False):
         """profile: per-kernel CUDA events on the launching stream (`only`: that
         kernel's launches alone; events around every launch add about 0.06 ms
         per pair)."""
@@ -250,7 +264,7 @@ def run_ours(args):
         for a, b in evs:
             flush.zero_()
             a.record(stream)
-            pair(use_psf, use_att, mode)
+            pair(use_psf, use_att, mode, separate)
             b.record(stream)
         torch.cuda.synchronize(dev)
         barrier(world)
@@ -268,10 +282,11 @@ def run_ours(args):
         ms = [a.elapsed_time(b) for a, b in evs]
         return ms, launches, prof
 
-    # warm-up (both variants)
+    # warm-up (every variant)
     for _ in range(args.warmup):
         pair()
         pair(False, False)
+        pair(separate=True)
     torch.cuda.synchronize(dev)
 
     # timed region: full model with clock sampling; CUDA events around the
@@ -284,6 +299,9 @@ def run_ours(args):
     # per-kernel split of the same pair: a second pass with events around every launch
     ms_prof, _, prof = timed(max(3, args.steps // 2), profile=True)
 
+    # the same pair as two separate calls (nrgb_project_device + nrgb_backproject_device)
+    ms_sep, _, _ = timed(max(3, args.steps // 2), separate=True)
+    separate = world * 1000.0 / reduce_max(sum(ms_sep) / len(ms_sep), world)
     # "vs plain": the same pair without PSF and attenuation
     ms_plain, _, _ = timed(max(3, args.steps // 2), use_psf=False, use_att=False)
     plain = world * 1000.0 / reduce_max(sum(ms_plain) / len(ms_plain), world)
@@ -345,6 +363,8 @@ def run_ours(args):
         "config": {"workload": "128^3 activity + mu, PSF 11x11 sigma=0.5+0.02*z, 120 angles x 3 deg, "
                                "project + reference backproject", "volume": [N, N, N], "angles": NCAM,
                    "psf": [K, K, N], "l2": "flushed (256 MB write) before every step", "parallelism": f"replicas{world}"},
+        "api": "nrgb_project_backproject_device (device buffers; projection, then backprojection of it)",
+        "separate_calls_pairs_per_s": round(separate, 3),
         "plain_pairs_per_s": round(plain, 3),
         "adjoint_backprojector_pairs_per_s": round(adjoint, 3),
         "vs_plain": round(value / plain, 4),

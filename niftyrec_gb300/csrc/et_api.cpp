@@ -929,22 +929,29 @@ int pair_device_call(const float* d_activity, const float* d_attenuation, const 
   if (!size || !cameras || !cameras_size || !d_activity || !d_sinogram || !d_backprojection ||
       (mode != kBackReference && mode != kBackAdjoint))
     return kErrParameters;
-  Cameras cc;
+  // camera centres: the projector's from the volume size, the
+  // backprojector's with the reference's {size0, size1, size0} rule
+  Cameras cc, cb;
+  const int csz[3] = {size[0], size[1], size[0]};
   int s = expand_cameras(cameras, cameras_size[0], cameras_size[1], size, &cc);
   if (s != kOk) return s;
-  Problem pb;
+  if ((s = expand_cameras(cameras, cameras_size[0], cameras_size[1], csz, &cb)) != kOk) return s;
+  Problem pb, pbb;
   s = make_problem(size[0], size[1], size[2], cc, psf, psf_size, background, background_attenuation, truncate, &pb);
   if (s != kOk) return s;
-  pb.back_mode = mode;
+  s = make_problem(size[0], size[1], size[2], cb, psf, psf_size, background, background_attenuation, truncate, &pbb);
+  if (s != kOk) return s;
+  pb.back_mode = pbb.back_mode = mode;
   DeviceState& ds = current_device_state(&s);
   if (s != kOk) return s;
   std::lock_guard<std::mutex> lk(ds.mu);
-  const size_t ws = pair_workspace(pb, d_attenuation != nullptr, d_backproject_input != nullptr);
+  const size_t ws = std::max(pair_workspace(pb, d_attenuation != nullptr, d_backproject_input != nullptr),
+                             backproject_workspace(pbb, d_attenuation != nullptr));
   if ((s = ensure_arena(ds, ws)) != kOk) return s;
   cudaStream_t st = static_cast<cudaStream_t>(stream);
   cudaStreamWaitEvent(st, ds.last_use, 0);
   g_last_path = (use_fused(pb) || use_fused_x(pb)) ? 1 : 2;
-  s = pair_device(pb, d_activity, d_attenuation, d_sinogram, d_backproject_input, d_backprojection, ds.arena,
+  s = pair_device(pb, pbb, d_activity, d_attenuation, d_sinogram, d_backproject_input, d_backprojection, ds.arena,
                   ds.arena_bytes, &ds.staging, st);
   cudaEventRecord(ds.last_use, st);
   return s;

@@ -529,12 +529,21 @@ size_t pair_workspace(const Problem& pb, bool has_att, bool has_input) {
          yg_backproject_workspace(pb.nx, pb.ny, pb.nz, pb.cams.n, group) + kSlack;
 }
 
-int pair_device(const Problem& pb, const float* d_act, const float* d_att, float* d_sino, const float* d_bk_in,
-                float* d_bk, char* ws, size_t ws_bytes, Staging* stg, cudaStream_t st) {
-  if (!use_fused(pb) || !d_act) {  // the two calls in sequence (stream-ordered reuse of the work space)
+bool same_geometry(const Problem& a, const Problem& b) {
+  return a.geom.size() == b.geom.size() &&
+         std::memcmp(a.geom.data(), b.geom.data(), sizeof(CamGeom) * a.geom.size()) == 0 && a.units == b.units;
+}
+
+int pair_device(const Problem& pb, const Problem& pb_back, const float* d_act, const float* d_att, float* d_sino,
+                const float* d_bk_in, float* d_bk, char* ws, size_t ws_bytes, Staging* stg, cudaStream_t st) {
+  // The two calls in sequence (stream-ordered reuse of the work space) where
+  // the fused kernels do not apply or the backprojector's cameras sit
+  // elsewhere (the reference centres them at (nx-1)/2 in z, the projector's
+  // at (nz-1)/2).
+  if (!use_fused(pb) || !d_act || !use_fused(pb_back) || !same_geometry(pb, pb_back)) {
     int s = project_device(pb, d_act, d_att, d_sino, ws, ws_bytes, stg, st);
     if (s != kOk) return s;
-    return backproject_device(pb, d_bk_in ? d_bk_in : d_sino, d_att, d_bk, ws, ws_bytes, stg, st);
+    return backproject_device(pb_back, d_bk_in ? d_bk_in : d_sino, d_att, d_bk, ws, ws_bytes, stg, st);
   }
   Carver cv(ws, ws_bytes);
   CamGeom* d_geom;

@@ -132,8 +132,10 @@ int gradient_device(const Problem& pb, const float* d_sino, const float* d_act, 
 // leaves the backprojector's transmission carries, and the projection feeds
 // the backprojector in its column layout.
 size_t pair_workspace(const Problem& pb, bool has_att, bool has_input);
-int pair_device(const Problem& pb, const float* d_act, const float* d_att, float* d_sino, const float* d_bk_in,
-                float* d_bk, char* ws, size_t ws_bytes, Staging* stg, cudaStream_t st);
+// pb: the projection's problem; pb_back: the backprojection's (camera
+// centres from its own size rule).
+int pair_device(const Problem& pb, const Problem& pb_back, const float* d_act, const float* d_att, float* d_sino,
+                const float* d_bk_in, float* d_bk, char* ws, size_t ws_bytes, Staging* stg, cudaStream_t st);
 // Projection with partial sums (et_project_partial): d_partial receives
 // [ncam][nz][ny][nx]; d_bg_image [ny][nx] or null.
 size_t partial_workspace(const Problem& pb);

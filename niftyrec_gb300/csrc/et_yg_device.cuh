@@ -126,6 +126,47 @@ __device__ __forceinline__ float4 sample4(const V* __restrict__ base, const Tap&
 
 __device__ __forceinline__ float comp(const float4& v, int c) { return c == 0 ? v.x : c == 1 ? v.y : c == 2 ? v.z : v.w; }
 
+// Packed float32 pairs (sm_100 and later): two lanes in one 64-bit register
+// pair, multiplied and added by one fma.rn.f32x2 instruction; each lane rounds
+// exactly like fmaf.  The row passes keep their accumulators as pairs (rows
+// 4l, 4l+1 and 4l+2, 4l+3 of a lane), which halves their FMA instructions.
+typedef unsigned long long f32x2;
+
+__device__ __forceinline__ f32x2 pk2(float a, float b) {
+  f32x2 r;
+  asm("mov.b64 %0, {%1, %2};" : "=l"(r) : "f"(a), "f"(b));
+  return r;
+}
+
+__device__ __forceinline__ float2 upk2(f32x2 v) {
+  float2 r;
+  asm("mov.b64 {%0, %1}, %2;" : "=f"(r.x), "=f"(r.y) : "l"(v));
+  return r;
+}
+
+// acc = a * b + acc, lane by lane
+__device__ __forceinline__ void ffma2(f32x2& acc, f32x2 a, f32x2 b) {
+  asm("fma.rn.f32x2 %0, %1, %2, %0;" : "+l"(acc) : "l"(a), "l"(b));
+}
+
+// Four rows as two pairs.
+struct Pair4 {
+  f32x2 lo, hi;
+};
+
+__device__ __forceinline__ Pair4 pair4(const float4& v) { return {pk2(v.x, v.y), pk2(v.z, v.w)}; }
+
+__device__ __forceinline__ float4 unpair4(const Pair4& p) {
+  const float2 a = upk2(p.lo), b = upk2(p.hi);
+  return make_float4(a.x, a.y, b.x, b.y);
+}
+
+// acc += k * v for the 4 rows (k broadcast to both lanes of a pair)
+__device__ __forceinline__ void axpy4p(Pair4& acc, f32x2 kk, const Pair4& v) {
+  ffma2(acc.lo, v.lo, kk);
+  ffma2(acc.hi, v.hi, kk);
+}
+
 __device__ __forceinline__ void axpy4(float4& acc, float k, const float4& v) {
   acc.x = fmaf(k, v.x, acc.x);
   acc.y = fmaf(k, v.y, acc.y);
@@ -399,6 +440,35 @@ __device__ __forceinline__ void rowpass_from_tile(const float4* __restrict__ sbu
   }
 }
 
+// Packed forms of the two row passes below (accumulators as float32 pairs,
+// one fma.rn.f32x2 per two rows; the same roundings in the same order), used
+// by the projector.  The spread keeps the scalar forms: its two transmission
+// arrays leave no registers for the broadcast coefficient pairs.
+template <int R, class EmitFn, class KR, class KC>
+__device__ __forceinline__ void rowpass_from_tile_p(const float4* __restrict__ sbuf, int base, EmitFn emit, KR kr, KC kc,
+                                                  int lane, int ny) {
+  constexpr int K = 2 * R + 1;
+  constexpr int NJ = kTXW + 2 * R;
+  Pair4 u[kTXW];
+  const f32x2 zero = pk2(0.f, 0.f);
+#pragma unroll
+  for (int q = 0; q < kTXW; ++q) u[q] = {zero, zero};
+#pragma unroll
+  for (int j = 0; j < NJ; ++j) {
+    const Pair4 r = pair4(sbuf[(base + j) * 32 + lane]);
+#pragma unroll
+    for (int d = 0; d < K; ++d) {
+      const int i = j - d;
+      if (i >= 0 && i < kTXW) {
+        const float k = kr[2 * R - d];
+        axpy4p(u[i], pk2(k, k), r);
+      }
+    }
+    const int i = j - 2 * R;
+    if (i >= 0 && i < kTXW) emit(i, mask_rows(yconv4s<R>(unpair4(u[i]), kc, lane, i & 1), 4 * lane, ny));
+  }
+}
+
 // Row passes of two cameras in one sweep: over the same tile (a camera and
 // its mirror camera in the projector: each tile column is read once and feeds
 // both sliding windows) or over two tiles (the mirror-unit spread); output i
@@ -435,9 +505,49 @@ __device__ __forceinline__ void rowpass2_from_tiles(const float4* __restrict__ s
 }
 
 template <int R, class EmitA, class EmitB, class KRA, class KCA, class KRB, class KCB>
+__device__ __forceinline__ void rowpass2_from_tiles_p(const float4* __restrict__ sa, const float4* __restrict__ sbt,
+                                                    int base, EmitA emit_a, KRA kra, KCA kca, EmitB emit_b, KRB krb,
+                                                    KCB kcb, int lane, int ny) {
+  constexpr int NJ = kTXW + 2 * R;
+  Pair4 ua[kTXW], ub[kTXW];
+  const f32x2 zero = pk2(0.f, 0.f);
+#pragma unroll
+  for (int q = 0; q < kTXW; ++q) {
+    ua[q] = {zero, zero};
+    ub[q] = {zero, zero};
+  }
+#pragma unroll
+  for (int j = 0; j < NJ; ++j) {
+    const float4 rf = sa[(base + j) * 32 + lane];
+    const Pair4 r = pair4(rf);
+    const Pair4 rb = sbt == sa ? r : pair4(sbt[(base + j) * 32 + lane]);
+#pragma unroll
+    for (int d = 0; d <= 2 * R; ++d) {
+      const int i = j - d;
+      if (i >= 0 && i < kTXW) {
+        const float ka = kra[2 * R - d], kb = krb[2 * R - d];
+        axpy4p(ua[i], pk2(ka, ka), r);
+        axpy4p(ub[i], pk2(kb, kb), rb);
+      }
+    }
+    const int i = j - 2 * R;
+    if (i >= 0 && i < kTXW) {
+      emit_b(i, mask_rows(yconv4s<R>(unpair4(ub[i]), kcb, lane, 0), 4 * lane, ny));
+      emit_a(i, mask_rows(yconv4s<R>(unpair4(ua[i]), kca, lane, 1), 4 * lane, ny));
+    }
+  }
+}
+
+template <int R, class EmitA, class EmitB, class KRA, class KCA, class KRB, class KCB>
 __device__ __forceinline__ void rowpass2_from_tile(const float4* __restrict__ sbuf, int base, EmitA emit_a, KRA kra,
                                                    KCA kca, EmitB emit_b, KRB krb, KCB kcb, int lane, int ny) {
   rowpass2_from_tiles<R>(sbuf, sbuf, base, emit_a, kra, kca, emit_b, krb, kcb, lane, ny);
+}
+
+template <int R, class EmitA, class EmitB, class KRA, class KCA, class KRB, class KCB>
+__device__ __forceinline__ void rowpass2_from_tile_p(const float4* __restrict__ sbuf, int base, EmitA emit_a, KRA kra,
+                                                     KCA kca, EmitB emit_b, KRB krb, KCB kcb, int lane, int ny) {
+  rowpass2_from_tiles_p<R>(sbuf, sbuf, base, emit_a, kra, kca, emit_b, krb, kcb, lane, ny);
 }
 
 // Vector reduction of 4 floats into global memory (sm_90+).
@@ -536,20 +646,20 @@ __device__ __forceinline__ void project_item(const YgArgs& a, int cam, int mate,
   auto mate_pass = [&](const float4* sbuf, int z, auto emit_m) {
     if constexpr (PTAB) {
       const float* m = ptab + (a.nz - 1 - z) * 2 * K;
-      rowpass_from_tile<R>(sbuf, warp * kTXW, emit_m, Reversed<R>{m}, m + K, lane, a.ny);
+      rowpass_from_tile_p<R>(sbuf, warp * kTXW, emit_m, Reversed<R>{m}, m + K, lane, a.ny);
     } else {
       const float* m = s_psf_m + z * 2 * K;
-      rowpass_from_tile<R>(sbuf, warp * kTXW, emit_m, m, m + K, lane, a.ny);
+      rowpass_from_tile_p<R>(sbuf, warp * kTXW, emit_m, m, m + K, lane, a.ny);
     }
   };
   auto both_pass = [&](const float4* sbuf, int z, auto emit, auto emit_m) {
     const float* kr = (PTAB ? ptab : s_psf) + z * 2 * K;
     if constexpr (PTAB) {
       const float* m = ptab + (a.nz - 1 - z) * 2 * K;
-      rowpass2_from_tile<R>(sbuf, warp * kTXW, emit, kr, kr + K, emit_m, Reversed<R>{m}, m + K, lane, a.ny);
+      rowpass2_from_tile_p<R>(sbuf, warp * kTXW, emit, kr, kr + K, emit_m, Reversed<R>{m}, m + K, lane, a.ny);
     } else {
       const float* m = s_psf_m + z * 2 * K;
-      rowpass2_from_tile<R>(sbuf, warp * kTXW, emit, kr, kr + K, emit_m, m, m + K, lane, a.ny);
+      rowpass2_from_tile_p<R>(sbuf, warp * kTXW, emit, kr, kr + K, emit_m, m, m + K, lane, a.ny);
     }
   };
   const CamRows cr = cam_rows(a.geom[cam].fwd);
@@ -633,7 +743,7 @@ __device__ __forceinline__ void project_item(const YgArgs& a, int cam, int mate,
         both_pass(sbuf, z, emit, emit_m);
       } else {
         const float* kr = (PTAB ? ptab : s_psf) + z * 2 * K;
-        rowpass_from_tile<R>(sbuf, warp * kTXW, emit, kr, kr + K, lane, a.ny);
+        rowpass_from_tile_p<R>(sbuf, warp * kTXW, emit, kr, kr + K, lane, a.ny);
       }
     } else {
 #pragma unroll

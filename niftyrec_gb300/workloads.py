@@ -1,8 +1,11 @@
 """Named workloads of the projector/backprojector, runnable from the command
 line (e.g. under a profiler) through the device-pointer C-ABI:
 
-    python -m niftyrec_gb300.workloads pair --n 128 --ncam 120 --psf 11 --reps 2
+    python -m niftyrec_gb300.workloads pair --n 128 --ncam 120 --psf 11 --reps 2   # one-call pair
+    python -m niftyrec_gb300.workloads pair2 --n 128 --ncam 120 --reps 2           # two separate calls
     python -m niftyrec_gb300.workloads project --n 64 --ncam 60 --psf 0 --no-att
+    python -m niftyrec_gb300.workloads dmu --reps 1       # exact d/dmu (autograd's attenuation gradient)
+    python -m niftyrec_gb300.workloads fisher --reps 1    # Fisher information of a 64-point grid
     python -m niftyrec_gb300.workloads osem --subsets 8 --reps 1     # plan OSEM iterations
     python -m niftyrec_gb300.workloads batch --volumes 8 --reps 1    # batched OSEM steps
     python -m niftyrec_gb300.workloads gradient --ncam 40 --reps 1   # et_array_gradient_attenuation
@@ -26,7 +29,8 @@ def main(argv=None):
     from . import synthetic as S
 
     ap = argparse.ArgumentParser()
-    ap.add_argument("op", choices=["project", "backproject", "pair", "osem", "batch", "gradient"])
+    ap.add_argument("op", choices=["project", "backproject", "pair", "pair2", "osem", "batch", "gradient", "dmu",
+                                   "fisher"])
     ap.add_argument("--subsets", type=int, default=8, help="osem: interleaved subsets")
     ap.add_argument("--volumes", type=int, default=8, help="batch: volumes of the batched workload")
     ap.add_argument("--n", type=int, default=128)
@@ -107,17 +111,45 @@ def main(argv=None):
                                                     psize, 0.0, 0.0, 0, vp(stream.cuda_stream))
             assert st == 0, st
         run = run_gradient
+    elif a.op == "dmu":  # d/dmu of sum(g * project(act, mu)), the fused recomputed-scan kernel
+        if a.bf16 or t_mu is None:
+            raise SystemExit("dmu: float32 activity and mu required")
+        g = torch.from_numpy(np.random.default_rng(3).uniform(0.5, 1.5, (a.ncam, n, n)).astype(np.float32)).to(dev)
+
+        def run_dmu():
+            st = L.nrgb_attenuation_grad_device(vp(g.data_ptr()), vp(t_act.data_ptr()), mu_p, size,
+                                                vp(t_bk.data_ptr()), cams.ctypes.data_as(vp), csize, psf_p, psize,
+                                                0.0, 0.0, vp(stream.cuda_stream))
+            assert st == 0, st
+        run = run_dmu
+    elif a.op == "fisher":  # et_array_fisher_grid of 64 grid points (host buffers)
+        from . import array_api as A
+
+        grid = np.zeros((n, n, n), np.float32)
+        pts = np.random.default_rng(5).choice(n ** 3, size=64, replace=False)
+        grid.flat[pts] = np.arange(1, 65, dtype=np.float32)
+        psf_f = psf if psf is not None else S.gaussian_psf(3, n)
+
+        def run_fisher():
+            A.fisher_grid(act, S.cameras_about_y(a.ncam), psf_f, grid, 64, mu if not a.no_att else None)
+        run = run_fisher
     else:
         run = None
 
     def run_pair():
         sp = vp(stream.cuda_stream)
-        if a.op in ("project", "pair"):
+        if a.op == "pair" and not a.bf16:
+            st = L.nrgb_project_backproject_device(vp(t_act.data_ptr()), mu_p, size, vp(t_sino.data_ptr()), None,
+                                                   vp(t_bk.data_ptr()), cams.ctypes.data_as(vp), csize, psf_p, psize,
+                                                   0.0, 0.0, 1, a.mode, sp)
+            assert st == 0, st
+            return
+        if a.op in ("project", "pair", "pair2"):
             fn = L.nrgb_project_device_bf16 if a.bf16 else L.nrgb_project_device
             st = fn(vp(t_act.data_ptr()), mu_p, size, vp(t_sino.data_ptr()), cams.ctypes.data_as(vp), csize, psf_p,
                     psize, 0.0, 0.0, 1, sp)
             assert st == 0, st
-        if a.op in ("backproject", "pair"):
+        if a.op in ("backproject", "pair", "pair2"):
             fn = L.nrgb_backproject_device_bf16 if a.bf16 else L.nrgb_backproject_device
             st = fn(vp(t_sino.data_ptr()), mu_p, size, vp(t_bk.data_ptr()), cams.ctypes.data_as(vp), csize, psf_p,
                     psize, 0.0, 0.0, 1, a.mode, sp)
