@@ -283,6 +283,12 @@ int nrgb_osem_ratio_device(const float *d_counts, float *d_projection, long long
 int nrgb_osem_update_device(float *d_activity, const float *d_numerator, const float *d_denominator, long long n,
                             float epsilon, void *stream);
 
+/* Host-side fault injection (no counterpart in the reference): the next n
+ * device work-space allocations that would grow the library's arena fail with
+ * status 4 (allocgpu) before any CUDA call is made, so callers' error paths
+ * can be tested without a GPU fault.  n = 0 clears it. */
+int nrgb_debug_fail_allocations(int n);
+
 /* Diagnostics: 1 if the calling thread's last call ran the fused y-gantry
  * kernels, 2 if it ran the general-orientation kernels, 0 before any call. */
 int nrgb_last_path(void);

@@ -15,6 +15,7 @@
 
 #include "et_array_interface.h"
 #include "et_engine.h"
+#include "et_trace.h"
 #include "et_kernels.h"
 
 using namespace nrgb;
@@ -31,6 +32,18 @@ size_t fbytes(size_t n) { return n * sizeof(float); }
 }  // namespace
 
 void nrgb::set_last_path(int path) { g_last_path = path; }
+
+bool nrgb::log_enabled() {
+  static const bool on = [] {
+    const char* v = std::getenv("NIFTYREC_LOG");
+    return v && *v && std::strcmp(v, "0") != 0;
+  }();
+  return on;
+}
+
+void nrgb::log_call(const char* name, double host_ms) {
+  std::fprintf(stderr, "{\"niftyrec\": \"%s\", \"host_ms\": %.3f, \"path\": %d}\n", name, host_ms, g_last_path);
+}
 
 namespace {
 
@@ -426,6 +439,7 @@ char* niftyrec_error_msg(int status) {
 // --------------------------------------------------------------- devices
 // emission-lib/_et_array_interface.cpp:269-272 returns 0; here 1 when a GPU is usable.
 int et_array_isinstalled() {
+  NRGB_API("et_array_isinstalled");
   int n = 0;
   if (cudaGetDeviceCount(&n) != cudaSuccess) {
     cudaGetLastError();
@@ -437,6 +451,7 @@ int et_array_isinstalled() {
 // emission-lib/_et.cpp:1988-2022: five ints per device
 // {id, SMs * clock_kHz, SMs, clock_kHz, global memory in MB}.
 int et_array_list_gpus(int* gpu_count, int* gpus_info_array) {
+  NRGB_API("et_array_list_gpus");
   int n = 0;
   if (cudaGetDeviceCount(&n) != cudaSuccess) {
     cudaGetLastError();
@@ -463,6 +478,7 @@ int et_array_list_gpus(int* gpu_count, int* gpus_info_array) {
 
 // emission-lib/_et.cpp:2029-2044
 int et_array_set_gpu(int id) {
+  NRGB_API("et_array_set_gpu");
   int n = 0;
   if (cudaGetDeviceCount(&n) != cudaSuccess || id < 0 || id >= n) {
     cudaGetLastError();
@@ -475,7 +491,15 @@ int et_array_set_gpu_pointer(int* id) { return et_array_set_gpu(id[0]); }
 
 // emission-lib/_et.cpp:2445-2451.  Frees this library's work space on the
 // current device; the CUDA context itself is left to its other users.
+// Fault injection for tests of callers' error handling (no counterpart in
+// the reference): the next n work-space allocations fail with status 4.
+int nrgb_debug_fail_allocations(int n) {
+  fail_next_allocations(n);
+  return kOk;
+}
+
 int et_array_reset_gpu() {
+  NRGB_API("et_array_reset_gpu");
   int s;
   DeviceState& ds = current_device_state(&s);
   if (s != kOk) return s;
@@ -498,6 +522,7 @@ int SPECT_project_parallelholes(float* activity, int* activity_size, float* sino
                                 float* cameras, int* cameras_size, float* psf, int* psf_size, float* attenuation,
                                 int* attenuation_size, float* Background, float* Background_attenuation, int* Gpu,
                                 int* Truncate_negative_values) {
+  NRGB_API("SPECT_project_parallelholes");
   (void)Gpu;
   return spect_project(activity, activity_size, sinogram, sinogram_size, cameras, cameras_size, psf, psf_size,
                        attenuation, attenuation_size, *Background, *Background_attenuation,
@@ -508,6 +533,7 @@ int SPECT_project_parallelholes(float* activity, int* activity_size, float* sino
 int et_array_project(float* activity, int* activity_size, float* sinogram, int* sinogram_size, float* cameras,
                      int* cameras_size, float* psf, int* psf_size, float* attenuation, int* attenuation_size,
                      float background, float background_attenuation, int gpu, int truncate_negative_values) {
+  NRGB_API("et_array_project");
   (void)gpu;
   return spect_project(activity, activity_size, sinogram, sinogram_size, cameras, cameras_size, psf, psf_size,
                        attenuation, attenuation_size, background, background_attenuation, truncate_negative_values);
@@ -519,6 +545,7 @@ int SPECT_backproject_parallelholes(float* sino, int* sino_size, float* bkpr, in
                                     int* cameras_size, float* psf, int* psf_size, float* attenuation,
                                     int* attenuation_size, float* Background, float* Background_attenuation,
                                     int* Gpu, int* Truncate_negative_values) {
+  NRGB_API("SPECT_backproject_parallelholes");
   (void)Gpu;
   return spect_backproject(sino, sino_size, bkpr, bkpr_size, cameras, cameras_size, psf, psf_size, attenuation,
                            attenuation_size, *Background, *Background_attenuation, *Truncate_negative_values);
@@ -528,6 +555,7 @@ int SPECT_backproject_parallelholes(float* sino, int* sino_size, float* bkpr, in
 int et_array_backproject(float* sino, int* sino_size, float* bkpr, int* bkpr_size, float* cameras, int* cameras_size,
                          float* psf, int* psf_size, float* attenuation, int* attenuation_size, float background,
                          float background_attenuation, int gpu, int truncate_negative_values) {
+  NRGB_API("et_array_backproject");
   (void)gpu;
   return spect_backproject(sino, sino_size, bkpr, bkpr_size, cameras, cameras_size, psf, psf_size, attenuation,
                            attenuation_size, background, background_attenuation, truncate_negative_values);
@@ -540,6 +568,7 @@ int et_array_gradient_attenuation(float* sino, int* sino_size, float* activity, 
                                   int* gradient_size, float* cameras, int* cameras_size, float* psf, int* psf_size,
                                   float* attenuation, int* attenuation_size, float background,
                                   float background_attenuation, int GPU, int truncate_negative_values) {
+  NRGB_API("et_array_gradient_attenuation");
   (void)GPU;
   (void)attenuation_size;
   if (!sino_size || !activity_size || !gradient_size || !cameras_size || !psf_size) return kErrParameters;
@@ -565,6 +594,7 @@ int et_array_attenuation_gradient(float* sino, int* sino_size, float* activity, 
                                   int* gradient_size, float* cameras, int* cameras_size, float* psf, int* psf_size,
                                   float* attenuation, int* attenuation_size, float background,
                                   float background_attenuation, int GPU, int truncate_negative_values) {
+  NRGB_API("et_array_attenuation_gradient");
   return et_array_gradient_attenuation(sino, sino_size, activity, activity_size, gradient, gradient_size, cameras,
                                        cameras_size, psf, psf_size, attenuation, attenuation_size, background,
                                        background_attenuation, GPU, truncate_negative_values);
@@ -575,6 +605,7 @@ int et_array_attenuation_gradient(float* sino, int* sino_size, float* activity, 
 // fixed 5 x 5 stub filled with ones; kept as is for drop-in behaviour.
 int et_array_calculate_size_psf(unsigned int* psf_size_x, unsigned int* psf_size_y, float, float, float, float,
                                 float, float) {
+  NRGB_API("et_array_calculate_size_psf");
   *psf_size_x = 5;
   *psf_size_y = 5;
   return 0;
@@ -582,6 +613,7 @@ int et_array_calculate_size_psf(unsigned int* psf_size_x, unsigned int* psf_size
 
 int et_array_make_psf(float* psf_data, unsigned int psf_size_x, unsigned int psf_size_y, float, float, float, float,
                       float, float, unsigned int N_psf_planes) {
+  NRGB_API("et_array_make_psf");
   if (psf_size_x != 5 || psf_size_y != 5) {
     std::fprintf(stderr, "et_array_make_psf: PSF size mismatch. \n");
     return 1;
@@ -594,6 +626,7 @@ int et_array_make_psf(float* psf_data, unsigned int psf_size_x, unsigned int psf
 // camera gets the first angle (the reference divides by n-1 = 0 there).
 int et_array_make_cameras(float* cameras_data, float firstcamera_deg, float lastcamera_deg, unsigned int n_cameras,
                           unsigned int rotation_axis) {
+  NRGB_API("et_array_make_cameras");
   const float kPi = 3.141592653589793f;
   for (unsigned cam = 0; cam < n_cameras; ++cam) {
     float angle;
@@ -612,6 +645,7 @@ int et_array_make_cameras(float* cameras_data, float firstcamera_deg, float last
 // emission-lib/_et_array_interface.cpp:112-156: rotate a volume about a centre.
 int et_array_rotate(float* image, int* size, float* rotated_image, float* angles, float* centers, float background,
                     int axis_order, int GPU) {
+  NRGB_API("et_array_rotate");
   (void)GPU;
   if (!size || size[0] <= 0 || size[1] <= 0 || size[2] <= 0) return kErrParameters;
   int s;
@@ -640,6 +674,7 @@ int et_array_osem_step(float* activity_data, int size_x, int size_y, unsigned in
                        int n_cameras, float* cameras_data, int use_attenuation, float* attenuation_data, int use_psf,
                        float* psf_data, unsigned int psf_size_x, unsigned int psf_size_y, float background,
                        float background_attenuation, float epsilon, int use_gpu) {
+  NRGB_API("et_array_osem_step");
   (void)use_gpu;
   if (subset_order == 0 || n_cameras <= 0) return kErrParameters;
   const int nsub = n_cameras / static_cast<int>(subset_order);
@@ -662,6 +697,7 @@ int et_array_osem_step_subset(float* activity_data, int size_x, int size_y, floa
                               float* cameras_data, const int* camera_indexes, int n_subset, int use_attenuation,
                               float* attenuation_data, int use_psf, float* psf_data, unsigned int psf_size_x,
                               unsigned int psf_size_y, float background, float background_attenuation, float epsilon) {
+  NRGB_API("et_array_osem_step_subset");
   if (!camera_indexes || n_subset <= 0) return kErrParameters;
   std::vector<int> idx(camera_indexes, camera_indexes + n_subset);
   return subset_step(activity_data, size_x, size_y, sinogram_data, n_cameras, cameras_data, idx, use_attenuation,
@@ -678,6 +714,7 @@ int et_array_project_partial(float* activity, int* activity_size, float* sinogra
                              int* psf_size, float* attenuation, int* attenuation_size, float background,
                              float* background_image, float background_attenuation, int GPU,
                              int truncate_negative_values, int do_rotate_partial) {
+  NRGB_API("et_array_project_partial");
   (void)GPU;
   if (!activity_size || !cameras_size || !psf_size || !attenuation_size || !sinogram || !partialsum ||
       !partialsum_size)
@@ -719,6 +756,7 @@ int et_array_fisher_grid(float* activity_ptr, int* activity_size, float* cameras
                          int* psf_size, float* grid_ptr, float* fisher_ptr, float* fisher_prior_ptr, int* fisher_size,
                          float* attenuation, int* attenuation_size, float epsilon, float background,
                          float background_attenuation, int GPU) {
+  NRGB_API("et_array_fisher_grid");
   (void)epsilon;
   (void)GPU;
   if (!activity_ptr || !activity_size || !cameras || !cameras_size || !psf || !psf_size || !grid_ptr ||
@@ -769,6 +807,7 @@ int et_array_fisher_grid_projection(float* sinogram_ptr, int* sinogram_size, int
                                     float* fisher_prior_ptr, int* fisher_size, float* attenuation,
                                     int* attenuation_size, float epsilon, float background,
                                     float background_attenuation, int GPU) {
+  NRGB_API("et_array_fisher_grid_projection");
   (void)epsilon;
   (void)GPU;
   (void)attenuation;
@@ -812,6 +851,7 @@ int et_array_mlem_step(float* activity_data, int size_x, int size_y, float* sino
                        float* cameras_data, int use_attenuation, float* attenuation_data, int use_psf,
                        float* psf_data, unsigned int psf_size_x, unsigned int psf_size_y, float background,
                        float background_attenuation, float epsilon, int use_gpu) {
+  NRGB_API("et_array_mlem_step");
   (void)use_gpu;
   if (n_cameras <= 0) return kErrParameters;
   std::vector<int> idx(n_cameras);
@@ -827,6 +867,7 @@ int et_array_osem(float* activity_data, unsigned int size_x, unsigned int size_y
                   int iterations, int use_attenuation, float* attenuation_data, int use_psf, float* psf_data,
                   unsigned int psf_size_x, unsigned int psf_size_y, float background, float background_attenuation,
                   float epsilon, int use_gpu) {
+  NRGB_API("et_array_osem");
   const size_t n = static_cast<size_t>(size_x) * size_y * size_x;
   for (size_t i = 0; i < n; ++i) activity_data[i] = 1.0f;
   std::vector<float> cams(3 * static_cast<size_t>(n_cameras));
@@ -844,6 +885,7 @@ int et_array_mlem(float* activity_data, unsigned int size_x, unsigned int size_y
                   float* attenuation_data, int use_psf, float* psf_data, unsigned int psf_size_x,
                   unsigned int psf_size_y, float background, float background_attenuation, float epsilon,
                   int use_gpu) {
+  NRGB_API("et_array_mlem");
   const size_t n = static_cast<size_t>(size_x) * size_y * size_x;
   for (size_t i = 0; i < n; ++i) activity_data[i] = 1.0f;
   std::vector<float> cams(3 * static_cast<size_t>(n_cameras));
@@ -967,6 +1009,7 @@ int nrgb_project_backproject_device(const float* d_activity, const float* d_atte
                                     const float* cameras, const int* cameras_size, const float* psf,
                                     const int* psf_size, float background, float background_attenuation,
                                     int truncate, int mode, void* stream) {
+  NRGB_API("nrgb_project_backproject_device");
   return pair_device_call(d_activity, d_attenuation, size, d_sinogram, d_backproject_input, d_backprojection,
                           cameras, cameras_size, psf, psf_size, background, background_attenuation, truncate, mode,
                           stream);
@@ -975,6 +1018,7 @@ int nrgb_project_backproject_device(const float* d_activity, const float* d_atte
 int nrgb_project_device(const float* d_activity, const float* d_attenuation, const int* size, float* d_sinogram,
                         const float* cameras, const int* cameras_size, const float* psf, const int* psf_size,
                         float background, float background_attenuation, int truncate, void* stream) {
+  NRGB_API("nrgb_project_device");
   return project_device_call(d_activity, d_attenuation, size, d_sinogram, cameras, cameras_size, psf, psf_size,
                              background, background_attenuation, truncate, false, stream);
 }
@@ -984,6 +1028,7 @@ int nrgb_project_device(const float* d_activity, const float* d_attenuation, con
 int nrgb_backproject_device(const float* d_sinogram, const float* d_attenuation, const int* size, float* d_out,
                             const float* cameras, const int* cameras_size, const float* psf, const int* psf_size,
                             float background, float background_attenuation, int truncate, int mode, void* stream) {
+  NRGB_API("nrgb_backproject_device");
   return backproject_device_call(d_sinogram, d_attenuation, size, d_out, cameras, cameras_size, psf, psf_size,
                                  background, background_attenuation, truncate, mode, false, stream);
 }
@@ -993,6 +1038,7 @@ int nrgb_backproject_device(const float* d_sinogram, const float* d_attenuation,
 int nrgb_project_device_bf16(const void* d_activity, const void* d_attenuation, const int* size, float* d_sinogram,
                              const float* cameras, const int* cameras_size, const float* psf, const int* psf_size,
                              float background, float background_attenuation, int truncate, void* stream) {
+  NRGB_API("nrgb_project_device_bf16");
   return project_device_call(static_cast<const float*>(d_activity), static_cast<const float*>(d_attenuation), size,
                              d_sinogram, cameras, cameras_size, psf, psf_size, background, background_attenuation,
                              truncate, true, stream);
@@ -1002,6 +1048,7 @@ int nrgb_backproject_device_bf16(const float* d_sinogram, const void* d_attenuat
                                  const float* cameras, const int* cameras_size, const float* psf, const int* psf_size,
                                  float background, float background_attenuation, int truncate, int mode,
                                  void* stream) {
+  NRGB_API("nrgb_backproject_device_bf16");
   return backproject_device_call(d_sinogram, static_cast<const float*>(d_attenuation), size, d_out, cameras,
                                  cameras_size, psf, psf_size, background, background_attenuation, truncate, mode, true,
                                  stream);
@@ -1013,6 +1060,7 @@ int nrgb_project_device_f64(const double* d_activity, const double* d_attenuatio
                             double* d_sinogram, const float* cameras, const int* cameras_size, const float* psf,
                             const int* psf_size, double background, double background_attenuation, int truncate,
                             void* stream) {
+  NRGB_API("nrgb_project_device_f64");
   if (!size || !cameras || !cameras_size || (!d_activity && !d_attenuation) || !d_sinogram) return kErrParameters;
   Cameras cc;
   int s = expand_cameras(cameras, cameras_size[0], cameras_size[1], size, &cc);
@@ -1037,6 +1085,7 @@ int nrgb_backproject_device_f64(const double* d_sinogram, const double* d_attenu
                                 double* d_out, const float* cameras, const int* cameras_size, const float* psf,
                                 const int* psf_size, double background, double background_attenuation, int truncate,
                                 void* stream) {
+  NRGB_API("nrgb_backproject_device_f64");
   if (!size || !cameras || !cameras_size || !d_sinogram || !d_out) return kErrParameters;
   Cameras cc;
   const int csz[3] = {size[0], size[1], size[0]};
@@ -1060,6 +1109,7 @@ int nrgb_backproject_device_f64(const double* d_sinogram, const double* d_attenu
 
 int nrgb_osem_ratio_device_f64(const double* d_counts, double* d_projection, long long n, double epsilon,
                                void* stream) {
+  NRGB_API("nrgb_osem_ratio_device_f64");
   if (!d_counts || !d_projection || n < 0) return kErrParameters;
   if (n == 0) return kOk;
   return osem_ratio64(d_counts, d_projection, static_cast<size_t>(n), epsilon, static_cast<cudaStream_t>(stream));
@@ -1067,6 +1117,7 @@ int nrgb_osem_ratio_device_f64(const double* d_counts, double* d_projection, lon
 
 int nrgb_osem_update_device_f64(double* d_activity, const double* d_numerator, const double* d_denominator,
                                 long long n, double epsilon, void* stream) {
+  NRGB_API("nrgb_osem_update_device_f64");
   if (!d_activity || !d_numerator || !d_denominator || n < 0) return kErrParameters;
   if (n == 0) return kOk;
   return osem_update64(d_activity, d_numerator, d_denominator, static_cast<size_t>(n), epsilon,
@@ -1079,6 +1130,7 @@ int nrgb_attenuation_grad_device(const float* d_grad_sinogram, const float* d_ac
                                  const int* size, float* d_out, const float* cameras, const int* cameras_size,
                                  const float* psf, const int* psf_size, float background,
                                  float background_attenuation, void* stream) {
+  NRGB_API("nrgb_attenuation_grad_device");
   if (!size || !cameras || !cameras_size || !d_grad_sinogram || !d_activity || !d_attenuation || !d_out)
     return kErrParameters;
   Cameras cc;
@@ -1106,6 +1158,7 @@ int nrgb_gradient_attenuation_device(const float* d_sinogram, const float* d_act
                                      const int* size, float* d_out, const float* cameras, const int* cameras_size,
                                      const float* psf, const int* psf_size, float background,
                                      float background_attenuation, int truncate, void* stream) {
+  NRGB_API("nrgb_gradient_attenuation_device");
   if (!size || !cameras || !cameras_size || !d_sinogram || !d_activity || !d_attenuation || !d_out)
     return kErrParameters;
   Cameras cc;
@@ -1134,6 +1187,7 @@ int nrgb_gradient_attenuation_device(const float* d_sinogram, const float* d_act
 // projection with y / p (y / eps where p < eps); update (:1036-1044) does
 // x *= num / max(den, eps).
 int nrgb_osem_ratio_device(const float* d_counts, float* d_projection, long long n, float epsilon, void* stream) {
+  NRGB_API("nrgb_osem_ratio_device");
   if (!d_counts || !d_projection || n < 0) return kErrParameters;
   if (n == 0) return kOk;
   return osem_ratio(d_counts, d_projection, static_cast<size_t>(n), epsilon, static_cast<cudaStream_t>(stream));
@@ -1141,6 +1195,7 @@ int nrgb_osem_ratio_device(const float* d_counts, float* d_projection, long long
 
 int nrgb_osem_update_device(float* d_activity, const float* d_numerator, const float* d_denominator, long long n,
                             float epsilon, void* stream) {
+  NRGB_API("nrgb_osem_update_device");
   if (!d_activity || !d_numerator || !d_denominator || n < 0) return kErrParameters;
   if (n == 0) return kOk;
   return osem_update(d_activity, d_numerator, d_denominator, static_cast<size_t>(n), epsilon,
@@ -1150,6 +1205,7 @@ int nrgb_osem_update_device(float* d_activity, const float* d_numerator, const f
 // Tuning table of the fused backprojector: cameras per scratch group for the
 // shape (nx, ny, nz, n_cameras); an all-zero shape sets the default.
 int nrgb_set_backproject_group(int nx, int ny, int nz, int ncam, int group) {
+  NRGB_API("nrgb_set_backproject_group");
   if (group < 0 || group > 64) return kErrParameters;
   set_tuned_group(nx, ny, nz, ncam, group);
   return kOk;
@@ -1160,6 +1216,7 @@ int nrgb_get_backproject_group(int nx, int ny, int nz, int ncam) { return tuned_
 // Tuning table of the fused projector: depth slabs (cluster size 2, 4, 8,
 // 16; 0 removes the entry) for the shape (nx, ny, nz, n_cameras).
 int nrgb_set_project_slabs(int nx, int ny, int nz, int ncam, int slabs) {
+  NRGB_API("nrgb_set_project_slabs");
   if (slabs != 0 && slabs != 2 && slabs != 4 && slabs != 8 && slabs != 16) return kErrParameters;
   set_tuned_project_slabs(nx, ny, nz, ncam, slabs);
   return kOk;
@@ -1171,6 +1228,7 @@ int nrgb_get_project_slabs(int nx, int ny, int nz, int ncam) { return tuned_proj
 // grid centre from the same bilinear samples; 0 computes every camera from
 // its own matrix.  Applies to calls made afterwards.
 int nrgb_set_mirror_pairs(int on) {
+  NRGB_API("nrgb_set_mirror_pairs");
   set_mirror_pairs(on);
   return kOk;
 }
@@ -1184,6 +1242,7 @@ int nrgb_get_mirror_pairs(void) { return mirror_pairs(); }
 // or nrgb_set_mirror_pairs(0)).
 int nrgb_mirror_units(const float* cameras, const int* cameras_size, const int* size, int* out_units, int max_units,
                       int* n_units) {
+  NRGB_API("nrgb_mirror_units");
   if (!cameras || !cameras_size || !size || !n_units || max_units < 0 || (max_units > 0 && !out_units))
     return kErrParameters;
   Cameras cc;
@@ -1203,6 +1262,7 @@ int nrgb_mirror_units(const float* cameras, const int* cameras_size, const int* 
 // none), host only: {first row, rows, first valid row, end of valid rows}
 // per window (valid rows relative to the first row).
 int nrgb_row_windows(int ny, int psf_k, int* out, int max_windows, int* n_windows) {
+  NRGB_API("nrgb_row_windows");
   if (ny < 1 || psf_k < 0 || !n_windows || max_windows < 0 || (max_windows > 0 && !out)) return kErrParameters;
   std::vector<int> w(4 * static_cast<size_t>(ny + 1));
   const int n = yg_row_windows(ny, psf_k, w.data(), ny + 1);

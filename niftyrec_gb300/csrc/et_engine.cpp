@@ -887,8 +887,16 @@ DeviceState& current_device_state(int* status) {
   return *p;
 }
 
+namespace {
+std::atomic<int> g_fail_allocs{0};  // host-side fault injection (nrgb_debug_fail_allocations)
+}  // namespace
+
+void fail_next_allocations(int n) { g_fail_allocs.store(n > 0 ? n : 0); }
+
 int ensure_arena(DeviceState& ds, size_t bytes) {
   if (ds.arena_bytes >= bytes) return kOk;
+  for (int n = g_fail_allocs.load(); n > 0; n = g_fail_allocs.load())
+    if (g_fail_allocs.compare_exchange_weak(n, n - 1)) return kErrAllocGpu;  // injected, before any CUDA call
   if (ds.arena) {
     cudaStreamSynchronize(ds.stream);
     cudaDeviceSynchronize();

@@ -90,6 +90,10 @@ struct DeviceState {
   Staging staging;
 };
 
+// Host-side fault injection: the next n work-space allocations that would
+// grow a device arena fail with kErrAllocGpu instead (no CUDA call is made).
+void fail_next_allocations(int n);
+
 // Lock the current device's state (created on first use) for the caller.
 DeviceState& current_device_state(int* status);
 

@@ -13,6 +13,7 @@
 #include <new>
 #include <vector>
 
+#include "et_trace.h"
 #include "et_array_interface.h"
 #include "et_engine.h"
 #include "et_kernels.h"
@@ -213,6 +214,7 @@ extern "C" {
 int nrgb_plan_create(void** out_plan, const int* size, const float* cameras, const int* cameras_size,
                      const float* psf, const int* psf_size, const float* d_attenuation, float background,
                      float background_attenuation, const int* subset_of_camera, int n_subsets, void* stream) {
+  NRGB_API("nrgb_plan_create");
   if (!out_plan || !size || !cameras || !cameras_size || n_subsets < 1) return kErrParameters;
   *out_plan = nullptr;
   const int nx = size[0], ny = size[1], nz = size[2], ncam = cameras_size[0], ncols = cameras_size[1];
@@ -368,6 +370,7 @@ int nrgb_plan_create(void** out_plan, const int* size, const float* cameras, con
 }
 
 int nrgb_plan_destroy(void* plan) {
+  NRGB_API("nrgb_plan_destroy");
   Plan* p = static_cast<Plan*>(plan);
   if (!p) return kErrParameters;
   cudaDeviceSynchronize();
@@ -379,6 +382,7 @@ int nrgb_plan_destroy(void* plan) {
 
 // out[0..6] = {nx, ny, nz, cy, n_cameras, n_subsets, fused}
 int nrgb_plan_shape(void* plan, int* out) {
+  NRGB_API("nrgb_plan_shape");
   Plan* p = static_cast<Plan*>(plan);
   if (!p || !out) return kErrParameters;
   out[0] = p->proj.nx;
@@ -394,6 +398,7 @@ int nrgb_plan_shape(void* plan, int* out) {
 // Original camera indexes of a subset, in the order its sinogram planes use;
 // returns the subset size (subset -1: all cameras).
 int nrgb_plan_subset_cameras(void* plan, int subset, int* idx_out) {
+  NRGB_API("nrgb_plan_subset_cameras");
   Plan* p = static_cast<Plan*>(plan);
   if (!p || subset < -1 || subset >= p->n_subsets) return -1;
   int b, e;
@@ -407,6 +412,7 @@ int nrgb_plan_subset_cameras(void* plan, int subset, int* idx_out) {
 // ([n_subset][ny][nx] nifti or [n_subset][nx][cy] column layout).
 int nrgb_plan_project(void* plan, int subset, const float* d_activity, float* d_sinogram, int layout, int truncate,
                       void* stream) {
+  NRGB_API("nrgb_plan_project");
   Plan* p = static_cast<Plan*>(plan);
   if (!p || subset < -1 || subset >= p->n_subsets || !d_activity || !d_sinogram) return kErrParameters;
   return plan_project(*p, subset, d_activity, d_sinogram, layout, truncate, static_cast<cudaStream_t>(stream));
@@ -415,6 +421,7 @@ int nrgb_plan_project(void* plan, int subset, const float* d_activity, float* d_
 // Backproject d_sinogram (cameras of `subset`) into d_out (reference semantics).
 int nrgb_plan_backproject(void* plan, int subset, const float* d_sinogram, float* d_out, int layout, int truncate,
                           void* stream) {
+  NRGB_API("nrgb_plan_backproject");
   Plan* p = static_cast<Plan*>(plan);
   if (!p || subset < -1 || subset >= p->n_subsets || !d_sinogram || !d_out) return kErrParameters;
   return plan_backproject(*p, subset, d_sinogram, d_out, layout, truncate, static_cast<cudaStream_t>(stream));
@@ -424,6 +431,7 @@ int nrgb_plan_backproject(void* plan, int subset, const float* d_sinogram, float
 // sensitivity image (backprojection of ones, truncated; floored at epsilon in
 // the update) once.  Call before capturing OSEM steps in a graph.
 int nrgb_plan_osem_prepare(void* plan, int layout, void* stream) {
+  NRGB_API("nrgb_plan_osem_prepare");
   Plan* p = static_cast<Plan*>(plan);
   if (!p || (layout != kLayoutNifti && layout != kLayoutColumn)) return kErrParameters;
   if (layout == kLayoutColumn && !p->fused) return kErrParameters;
@@ -473,6 +481,7 @@ int nrgb_plan_osem_prepare(void* plan, int layout, void* stream) {
 // d_counts holds the subset's planes in nrgb_plan_subset_cameras order.
 int nrgb_plan_osem_step(void* plan, int subset, float* d_activity, const float* d_counts, float epsilon,
                         void* stream) {
+  NRGB_API("nrgb_plan_osem_step");
   Plan* p = static_cast<Plan*>(plan);
   if (!p || subset < 0 || subset >= p->n_subsets || !d_activity || !d_counts || p->osem_layout < 0)
     return kErrParameters;
@@ -494,6 +503,7 @@ int nrgb_plan_osem_step(void* plan, int subset, float* d_activity, const float* 
 // OSL ratio rule.  Same layouts as nrgb_plan_osem_step.
 int nrgb_plan_osmapem_step(void* plan, int subset, float* d_activity, const float* d_counts, float beta,
                            float epsilon, void* stream) {
+  NRGB_API("nrgb_plan_osmapem_step");
   Plan* p = static_cast<Plan*>(plan);
   if (!p || subset < 0 || subset >= p->n_subsets || !d_activity || !d_counts || p->osem_layout < 0)
     return kErrParameters;
@@ -516,6 +526,7 @@ int nrgb_plan_osmapem_step(void* plan, int subset, float* d_activity, const floa
 
 // Quadratic MRF prior gradient of a device volume in nifti order (nx fastest).
 int nrgb_mrf_gradient_device(const float* d_activity, float* d_gradient, const int* size, void* stream) {
+  NRGB_API("nrgb_mrf_gradient_device");
   if (!d_activity || !d_gradient || !size || size[0] <= 0 || size[1] <= 0 || size[2] <= 0) return kErrParameters;
   return mrf_gradient(d_activity, d_gradient, size[0], size[1], size[2], static_cast<cudaStream_t>(stream));
 }
@@ -525,6 +536,7 @@ int nrgb_mrf_gradient_device(const float* d_activity, float* d_gradient, const i
 // direction 1: column -> nifti (truncate: clamp negatives to 0).
 int nrgb_layout_convert(const float* src, float* dst, int nx, int ny, int planes, int direction, int truncate,
                         void* stream) {
+  NRGB_API("nrgb_layout_convert");
   if (!src || !dst || nx <= 0 || ny <= 0 || planes <= 0) return kErrParameters;
   cudaStream_t st = static_cast<cudaStream_t>(stream);
   const int cy = round_up(ny, 4);
@@ -565,6 +577,7 @@ extern "C" {
 // Build a batch over fused plans prepared for OSEM in column layout
 // (nrgb_plan_osem_prepare(plan, 1, ...)).  At most 64 plans, one device.
 int nrgb_batch_create(void** out_batch, void* const* plans, int n_plans, void* stream) {
+  NRGB_API("nrgb_batch_create");
   if (!out_batch || !plans || n_plans < 1 || n_plans > kMaxBatch) return kErrParameters;
   *out_batch = nullptr;
   Batch* b = new (std::nothrow) Batch();
@@ -652,6 +665,7 @@ int nrgb_batch_create(void** out_batch, void* const* plans, int n_plans, void* s
 }
 
 int nrgb_batch_destroy(void* batch) {
+  NRGB_API("nrgb_batch_destroy");
   Batch* b = static_cast<Batch*>(batch);
   if (!b) return kErrParameters;
   cudaDeviceSynchronize();
@@ -662,6 +676,7 @@ int nrgb_batch_destroy(void* batch) {
 
 // Counts of volume v: device (n_cameras, ny, nx) nifti, original camera order.
 int nrgb_batch_set_counts(void* batch, int v, const float* d_counts, void* stream) {
+  NRGB_API("nrgb_batch_set_counts");
   Batch* b = static_cast<Batch*>(batch);
   if (!b || v < 0 || v >= static_cast<int>(b->plans.size()) || !d_counts) return kErrParameters;
   const Plan& p = *b->plans[v];
@@ -677,6 +692,7 @@ int nrgb_batch_set_counts(void* batch, int v, const float* d_counts, void* strea
 
 // Activity of volume v in and out, device (nz, ny, nx) nifti.
 int nrgb_batch_set_activity(void* batch, int v, const float* d_activity, void* stream) {
+  NRGB_API("nrgb_batch_set_activity");
   Batch* b = static_cast<Batch*>(batch);
   if (!b || v < 0 || v >= static_cast<int>(b->plans.size()) || !d_activity) return kErrParameters;
   const Plan& p = *b->plans[v];
@@ -684,6 +700,7 @@ int nrgb_batch_set_activity(void* batch, int v, const float* d_activity, void* s
 }
 
 int nrgb_batch_get_activity(void* batch, int v, float* d_activity, void* stream) {
+  NRGB_API("nrgb_batch_get_activity");
   Batch* b = static_cast<Batch*>(batch);
   if (!b || v < 0 || v >= static_cast<int>(b->plans.size()) || !d_activity) return kErrParameters;
   const Plan& p = *b->plans[v];
@@ -697,6 +714,7 @@ int nrgb_batch_get_activity(void* batch, int v, float* d_activity, void* stream)
 // subsets (step >= iterations * n_subsets_v) sit the step out, so volumes with
 // different subset counts all end after `iterations` iterations.
 int nrgb_batch_osem_step(void* batch, int step, int iterations, float epsilon, void* stream) {
+  NRGB_API("nrgb_batch_osem_step");
   Batch* b = static_cast<Batch*>(batch);
   if (!b || step < 0) return kErrParameters;
   cudaStream_t st = static_cast<cudaStream_t>(stream);

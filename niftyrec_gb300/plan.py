@@ -68,6 +68,7 @@ class Plan:
             sub = np.ascontiguousarray(np.asarray(subsets, dtype=np.int32))
             self.n_subsets = int(sub.max()) + 1 if n_subsets is None else int(n_subsets)
         self._psf = None if psf is None else np.ascontiguousarray(np.asarray(psf, dtype=np.float32))
+        self._mu_ref = attenuation  # for the checkpoint fingerprint
         self.device = attenuation.device if attenuation is not None else torch.device("cuda", torch.cuda.current_device())
         stream = torch.cuda.current_stream(self.device)
         handle = _vp()
@@ -190,18 +191,55 @@ class Plan:
         if st:
             raise NiftyRecError("nrgb_plan_osmapem_step", st)
 
-    def osem(self, counts, iterations, activity=None, layout="column", epsilon=1e-6, graph=False, beta=None):
+    def fingerprint(self):
+        """Digest of the problem an OSEM state of this plan belongs to."""
+        from .checkpoint import fingerprint
+
+        return fingerprint(self.shape, self.cameras, self.n_subsets, self._psf, self._mu_ref)
+
+    def osem(self, counts, iterations, activity=None, layout="column", epsilon=1e-6, graph=False, beta=None,
+             checkpoint=None, resume=False, every=1):
         """OSEM from full-size counts (n, ny, nx); returns the activity in nifti order.
         beta: run one-step-late MAP-EM with the quadratic MRF prior instead
-        (beta_osl of the reference's et_osmapem_step)."""
+        (beta_osl of the reference's et_osmapem_step).
+        checkpoint: file (.npz) that receives the state (activity, next
+        iteration and subset) after every `every` subset steps and at the end;
+        with resume=True an existing checkpoint of this problem is continued
+        (iterations counts from the start of the run, not of the resume)."""
         torch = self.torch
         lay = _layout(layout)
         if self._osem_layout != lay:
             self.osem_prepare(layout)
         ys = self.split_counts(counts, layout)
         nz, ny, nx = self.shape
+        start = (0, 0)
+        if checkpoint is not None:
+            import os
+
+            from . import checkpoint as CK
+
+            if graph:
+                raise ValueError("checkpointing runs subset by subset; it does not combine with graph=True")
+            fp = self.fingerprint()
+            if resume and os.path.exists(checkpoint):
+                state = CK.load(checkpoint)
+                CK.check(state, fp)
+                activity = torch.from_numpy(state["activity"]).to(counts.device)
+                start = (state["iteration"], state["subset"])
         x = activity if activity is not None else torch.ones((nz, ny, nx), dtype=torch.float32, device=counts.device)
         x = self.to_column(x) if lay == COLUMN else x.clone()
+
+        if checkpoint is not None:
+            steps = list(CK.positions(self.n_subsets, iterations, *start))
+            for i, (it, s) in enumerate(steps):
+                if beta is None:
+                    self.osem_step(x, ys[s], s, epsilon)
+                else:
+                    self.osmapem_step(x, ys[s], s, beta, epsilon)
+                if (i + 1) % every == 0 or i == len(steps) - 1:
+                    nxt = (it, s + 1) if s + 1 < self.n_subsets else (it + 1, 0)
+                    CK.save(checkpoint, self.from_column(x) if lay == COLUMN else x, nxt[0], nxt[1], fp)
+            return self.from_column(x) if lay == COLUMN else x
 
         def one_iteration():
             for s in range(self.n_subsets):

@@ -155,10 +155,22 @@ class ShardedOSEM:
         self.op.update(x, num, self.sens[subset], self.epsilon)
         return x
 
-    def run(self, x, iterations):
-        for _ in range(iterations):
-            for s in range(self.n_subsets):
-                self.step(x, s)
+    def run(self, x, iterations, start_iteration=0, start_subset=0, checkpoint=None, fingerprint="", every=1):
+        """`iterations` passes over the subsets from (start_iteration,
+        start_subset); with `checkpoint`, rank 0 saves the state (see
+        niftyrec_gb300.checkpoint) after every `every` subset steps and at the
+        end, and a run resumed from it continues exactly where it stopped."""
+        from . import checkpoint as CK
+
+        k = 0
+        steps = list(CK.positions(self.n_subsets, iterations, start_iteration, start_subset))
+        for i, (it, s) in enumerate(steps):
+            self.step(x, s)
+            k += 1
+            if checkpoint and self.rank == 0 and (k % every == 0 or i == len(steps) - 1):
+                nxt = (it, s + 1) if s + 1 < self.n_subsets else (it + 1, 0)
+                self.sync()
+                CK.save(checkpoint, x, nxt[0], nxt[1], fingerprint)
         return x
 
 

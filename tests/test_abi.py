@@ -246,3 +246,22 @@ def test_autotune_cache_round_trip(lib, tmp_path):
     (tmp_path / "bad.json").write_text("{not json")
     assert AT.load_cache(str(tmp_path / "bad.json")) == {}
     assert AT.load_cache(str(tmp_path / "missing.json")) == {}
+
+
+def test_niftyrec_log_one_json_line_per_call():
+    """NIFTYREC_LOG=1: every C-ABI call writes one JSON line on stderr (entry
+    point, host time, path); unset, nothing is written."""
+    import json
+    import subprocess
+    import sys
+
+    code = ("import sys; sys.path.insert(0, %r); from niftyrec_gb300 import array_api as A; "
+            "A.make_cameras(0.0, 90.0, 4, 1); A.make_cameras(0.0, 180.0, 3, 0)") % ROOT
+    for env_val, expect in (("1", 2), ("0", 0)):
+        env = dict(os.environ, NIFTYREC_LOG=env_val)
+        r = subprocess.run([sys.executable, "-c", code], capture_output=True, text=True, env=env, timeout=120)
+        assert r.returncode == 0, r.stderr
+        lines = [json.loads(x) for x in r.stderr.splitlines() if x.startswith('{"niftyrec"')]
+        assert len(lines) == expect
+        for rec in lines:
+            assert rec["niftyrec"] == "et_array_make_cameras" and rec["host_ms"] >= 0

@@ -87,3 +87,27 @@ def test_plans_on_their_own_streams():
         for s, b in got[i]:
             np.testing.assert_array_equal(s.cpu().numpy(), want[i][0])
             np.testing.assert_array_equal(b.cpu().numpy(), want[i][1])
+
+
+def test_injected_allocation_failure_is_a_status_not_a_fault():
+    """Host-side fault injection: with the arena released, an injected
+    allocation failure makes the next call return status 4 (allocgpu); the
+    call after it succeeds and matches the result before the failure."""
+    from niftyrec_gb300 import _lib
+    from niftyrec_gb300 import array_api as A
+    from niftyrec_gb300 import synthetic as S
+
+    L = _lib.load()
+    shape = (24, 24, 24)
+    act = S.ellipsoid_phantom(shape, seed=2)
+    cams = S.cameras_about_y(6)
+    ref = A.project(act, cams)
+    assert L.et_array_reset_gpu() == 0
+    L.nrgb_debug_fail_allocations(1)
+    from niftyrec_gb300._lib import NiftyRecError
+
+    with pytest.raises(NiftyRecError) as e:
+        A.project(act, cams)
+    assert e.value.status == 4
+    np.testing.assert_array_equal(A.project(act, cams), ref)
+    L.nrgb_debug_fail_allocations(0)
