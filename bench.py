@@ -912,13 +912,26 @@ def batch_compare(dev, n_volumes=24, reps=5):
         b.step(0)
     batch_graph = dev_ms(g_batch.replay)
     n_angles = sum(len(range(0, c["ncam"], c["subsets"])) for c, *_ in vols)
+    # algorithmic bytes of the step: per angle the projector's 8 B and the
+    # backprojector's 12 B per voxel plus 4 B per plane each; the ratio's 12 B
+    # per sinogram element, the update's 16 B per voxel
+    step_bytes = 0
+    for c, *_ in vols:
+        nz, ny, nx = c["shape"]
+        na = len(range(0, c["ncam"], c["subsets"]))
+        step_bytes += na * (20 * nz * ny * nx + 8 * ny * nx) + 12 * na * ny * nx + 16 * nz * ny * nx
+    peak, peak_kind = measured_peak()
+    ach = step_bytes / (batch_graph / 1e3) / 1e9
     return {"workload": f"one OSEM subset step of {n_volumes} volumes (64^3, 96x96x80, 128^3, 160x160x128; "
                         f"60/90/120/180 angles; 4-16 subsets; PSF 11x11; mu), {n_angles} angles in the step",
             "per_call_ms": round(per_call_ms, 3), "plan_eager_ms": round(plan_eager, 3),
             "plan_graph_ms": round(plan_graph, 3), "batch_eager_ms": round(batch_eager, 3),
             "batch_graph_ms": round(batch_graph, 3),
             "speedup_batch_graph_vs_per_call": round(per_call_ms / batch_graph, 2),
-            "speedup_batch_graph_vs_plan_graph": round(plan_graph / batch_graph, 3)}
+            "speedup_batch_graph_vs_plan_graph": round(plan_graph / batch_graph, 3),
+            "roofline": {"bound": "hbm", "achieved": round(ach, 1), "peak": peak, "unit": "GB/s",
+                         "frac": round(ach / peak, 4), "peak_source": peak_kind, "bytes_per_step": step_bytes,
+                         "note": "batch graph step; algorithmic bytes summed over the volumes"}}
 
 
 # ----------------------------------------------------------- CPU baselines

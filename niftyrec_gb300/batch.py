@@ -8,7 +8,10 @@ set, PSF, mu map and subset count).  One batched subset step runs
   x-tile) work items from a queue until none are left, so small volumes fill
   the SMs that one of them alone would leave idle;
 * one ratio launch over all volumes' projections;
-* each plan's reference backprojection;
+* the volumes' reference backprojections, concurrently on four side streams
+  (largest volumes first, each to the least loaded stream; each volume's
+  spread and gather on its own scratch), forked from and joined back into the
+  caller's stream with events;
 * one update launch over all volumes.
 
 Nothing in a step allocates or copies from the host, so a step -- or a whole

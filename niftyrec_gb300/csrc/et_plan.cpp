@@ -139,7 +139,7 @@ int plan_project(Plan& p, int subset, const float* d_act, float* d_sino, int lay
 }
 
 int plan_backproject(Plan& p, int subset, const float* d_sino, float* d_out, int layout, int truncate,
-                     cudaStream_t st) {
+                     cudaStream_t st, int pipelined = 1) {
   int b, e;
   range(p, subset, &b, &e);
   const int n = e - b;
@@ -171,6 +171,7 @@ int plan_backproject(Plan& p, int subset, const float* d_sino, float* d_out, int
     a.group = std::min(pb.group, tuned_group(pb.nx, pb.ny, pb.nz, n));  // by the subset's camera count
     a.work = p.work;
     a.carry = p.carry ? p.carry + static_cast<size_t>(b) * yg_carry_slabs() * pb.nx * p.cy : nullptr;
+    a.pipelined = pipelined;
     int s = yg_backproject(a, st);
     if (s != kOk) return s;
     if (layout == kLayoutNifti) return from_column(p.out_c, d_out, pb.nx, pb.ny, p.cy, pb.nz, truncate, st);
@@ -549,15 +550,23 @@ int nrgb_layout_convert(const float* src, float* dst, int nx, int ny, int planes
 // ------------------------------------------------------------------ batches
 // A batch runs one OSEM subset step of many plans at once: one persistent
 // projector launch over every volume's subset cameras (per PSF width and
-// attenuation kind), one ratio launch, each plan's reference backprojection,
-// one update launch.  The batch owns each volume's activity and counts in
+// attenuation kind), one ratio launch, the plans' reference backprojections
+// concurrently on side streams, one update launch.  The batch owns each volume's activity and counts in
 // column layout; its descriptors are built once, so a step allocates nothing,
 // copies nothing from the host and can be captured in a CUDA graph.
 namespace nrgb {
 namespace {
 
+// Side streams of a batch step: the volumes' backprojections run
+// concurrently on them (each volume on its own scratch), forked from and
+// joined back into the caller's stream with events (capturable in a CUDA
+// graph).
+constexpr int kBatchStreams = 4;
+
 struct Batch {
   int device = 0;
+  cudaStream_t side[kBatchStreams] = {};
+  cudaEvent_t fork = nullptr, join[kBatchStreams] = {};
   std::vector<Plan*> plans;
   std::vector<int> order;      // volumes by decreasing work per item (large first)
   char* mem = nullptr;
@@ -568,6 +577,15 @@ struct Batch {
   BatchStepDesc* d_desc = nullptr;
   int* d_counter = nullptr;    // one per projector launch of a step
 };
+
+void destroy_batch_streams(Batch* b) {
+  if (b->fork) cudaEventDestroy(b->fork);
+  for (int k = 0; k < kBatchStreams; ++k) {
+    if (b->join[k]) cudaEventDestroy(b->join[k]);
+    if (b->side[k]) cudaStreamDestroy(b->side[k]);
+  }
+  b->fork = nullptr;
+}
 
 }  // namespace
 }  // namespace nrgb
@@ -583,11 +601,22 @@ int nrgb_batch_create(void** out_batch, void* const* plans, int n_plans, void* s
   Batch* b = new (std::nothrow) Batch();
   if (!b) return kErrAllocCpu;
   cudaGetDevice(&b->device);
+  bool ok = cudaEventCreateWithFlags(&b->fork, cudaEventDisableTiming) == cudaSuccess;
+  for (int k = 0; k < kBatchStreams && ok; ++k)
+    ok = cudaStreamCreateWithFlags(&b->side[k], cudaStreamNonBlocking) == cudaSuccess &&
+         cudaEventCreateWithFlags(&b->join[k], cudaEventDisableTiming) == cudaSuccess;
+  if (!ok) {
+    cudaGetLastError();
+    destroy_batch_streams(b);
+    delete b;
+    return kErrUnspecified;
+  }
   size_t bytes = al(sizeof(int) * kMaxBatch);
   int ndesc = 0;
   for (int v = 0; v < n_plans; ++v) {
     Plan* p = static_cast<Plan*>(plans[v]);
     if (!p || !p->fused || p->osem_layout != kLayoutColumn || p->device != b->device) {
+      destroy_batch_streams(b);
       delete b;
       return kErrParameters;
     }
@@ -601,6 +630,7 @@ int nrgb_batch_create(void** out_batch, void* const* plans, int n_plans, void* s
   bytes += al(sizeof(BatchStepDesc) * ndesc);
   if (cudaMalloc(&b->mem, bytes) != cudaSuccess) {
     cudaGetLastError();
+    destroy_batch_streams(b);
     delete b;
     return kErrAllocGpu;
   }
@@ -632,6 +662,7 @@ int nrgb_batch_create(void** out_batch, void* const* plans, int n_plans, void* s
       d.nwin = yg_row_windows(pb.ny, pb.psf_k, &d.win[0][0], kMaxWindows);
       if (d.nwin < 0) {
         cudaFree(b->mem);
+        destroy_batch_streams(b);
         delete b;
         return kErrParameters;
       }
@@ -648,6 +679,7 @@ int nrgb_batch_create(void** out_batch, void* const* plans, int n_plans, void* s
   if (cudaMemcpyAsync(b->d_desc, b->h_desc.data(), sizeof(BatchStepDesc) * ndesc, cudaMemcpyHostToDevice, st) !=
       cudaSuccess) {
     cudaFree(b->mem);
+    destroy_batch_streams(b);
     delete b;
     return kErrTransferGpu;
   }
@@ -669,6 +701,7 @@ int nrgb_batch_destroy(void* batch) {
   Batch* b = static_cast<Batch*>(batch);
   if (!b) return kErrParameters;
   cudaDeviceSynchronize();
+  destroy_batch_streams(b);
   cudaFree(b->mem);
   delete b;
   return kOk;
@@ -757,10 +790,22 @@ int nrgb_batch_osem_step(void* batch, int step, int iterations, float epsilon, v
     if (s != kOk) return s;
   }
   int s = osem_ratio_batch(b->d_desc, ratio_e, epsilon, st);
-  for (size_t v = 0; v < b->plans.size() && s == kOk; ++v) {
-    if (sub[v] < 0) continue;
+  if (s != kOk) return s;
+  // the backprojections, volume by volume (largest first) on the least loaded
+  // side stream, each spread and gather in sequence on its stream
+  if (cudaEventRecord(b->fork, st) != cudaSuccess) return kErrKernel;
+  for (int k = 0; k < kBatchStreams; ++k) cudaStreamWaitEvent(b->side[k], b->fork, 0);
+  double load[kBatchStreams] = {};
+  for (int v : b->order) {
+    if (sub[v] < 0 || s != kOk) continue;
     Plan& p = *b->plans[v];
-    s = plan_backproject(p, sub[v], p.osem_p, p.osem_num, kLayoutColumn, 1, st);
+    const int k = static_cast<int>(std::min_element(load, load + kBatchStreams) - load);
+    load[k] += static_cast<double>(p.back.nz) * p.back.nx * p.cy * (p.sub_begin[sub[v] + 1] - p.sub_begin[sub[v]]);
+    s = plan_backproject(p, sub[v], p.osem_p, p.osem_num, kLayoutColumn, 1, b->side[k], 0);
+  }
+  for (int k = 0; k < kBatchStreams; ++k) {
+    cudaEventRecord(b->join[k], b->side[k]);
+    cudaStreamWaitEvent(st, b->join[k], 0);
   }
   if (s == kOk) s = osem_update_batch(b->d_desc, vol_e, epsilon, st);
   return s;
