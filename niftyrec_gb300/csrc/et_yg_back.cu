@@ -209,16 +209,32 @@ __global__ void __launch_bounds__(32 * kW, CTAS)
 // mate: row kernel forward, column kernel reversed) and, summed, are
 // scattered with c's bilinear weights into the accumulator a.out (the mate's
 // footprint of its mirrored column is c's).
-template <int R, bool PSF, bool ATT, bool ADJ, bool PTAB>
+//
+// V = bfloat16 (mu stored in bfloat16): the forward transmission is summed
+// with Kahan compensation (the compensation of each sampled column in shared
+// memory), the mate's transmission is the column total minus the compensated
+// forward sum (no second running sum), and the tiles are single-buffered (a
+// second barrier per plane) so that two CTAs per SM still fit.
+template <int R, class V>
+__host__ __device__ constexpr size_t spread_pair_fixed_smem() {
+  using TS = TileShape<R>;
+  constexpr bool KAHAN = StorageTraits<V>::kKahan;
+  return (KAHAN ? 1 : 2) * TS::kSbBytes + TS::kTapBytes + (KAHAN ? sizeof(float4) * TS::kOwn * 32 * kW : 0);
+}
+
+template <int R, bool PSF, bool ATT, bool ADJ, bool PTAB, class V = float>
 __device__ __forceinline__ void spread_pair_body(const YgArgs& a, int u0, const float* ptab) {
   using TS = TileShape<R>;
+  constexpr bool KAHAN = StorageTraits<V>::kKahan;
+  constexpr int NB = KAHAN ? 1 : 2;  // tile buffers
   constexpr int NS = TS::NS;
   constexpr int K = 2 * R + 1;
-  const float* __restrict__ mu = a.mu + a.row0;
+  const V* __restrict__ mu = reinterpret_cast<const V*>(a.mu) + a.row0;
   extern __shared__ __align__(16) unsigned char smem[];
-  float4* sb = reinterpret_cast<float4*>(smem);                              // [2 stages][2][NS][32]
-  Tap* taps = reinterpret_cast<Tap*>(smem + 2 * TS::kSbBytes);                // [2][kTapSlots]
-  float* s_psf = reinterpret_cast<float*>(smem + 2 * TS::kSbBytes + TS::kTapBytes);  // [zper][2K], mate's next
+  float4* sb = reinterpret_cast<float4*>(smem);                              // [NB stages][2][NS][32]
+  Tap* taps = reinterpret_cast<Tap*>(smem + NB * TS::kSbBytes);               // [2][kTapSlots]
+  float4* scomp = reinterpret_cast<float4*>(smem + NB * TS::kSbBytes + TS::kTapBytes);  // [kOwn][256] (KAHAN)
+  float* s_psf = reinterpret_cast<float*>(smem + spread_pair_fixed_smem<R, V>());  // [zper][2K], mate's next
 
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int ntile = (a.nx + kTXC - 1) / kTXC;
@@ -256,19 +272,21 @@ __device__ __forceinline__ void spread_pair_body(const YgArgs& a, int u0, const 
   const float* __restrict__ mrow = a.sino + static_cast<size_t>(paired ? mate : cam) * a.nx * a.cy + a.row0;
 
   // transmissions per sampled column: forward (from the slab carry) and, for
-  // the mate, from the far end (column total minus the carry)
+  // the mate, from the far end (column total minus the carry; with KAHAN Tr
+  // holds the column total)
   float4 Tc[TS::kOwn], Tr[TS::kOwn];
 #pragma unroll
   for (int k = 0; k < TS::kOwn; ++k) {
     Tc[k] = make_float4(0.f, 0.f, 0.f, 0.f);
     Tr[k] = make_float4(0.f, 0.f, 0.f, 0.f);
+    if (KAHAN) scomp[k * 32 * kW + threadIdx.x] = make_float4(0.f, 0.f, 0.f, 0.f);
     const int xp = x0 - R + warp + kW * k;
     if (ATT && warp + kW * k < NS && xp >= 0 && xp < a.nx && yok) {
       const float* cp = a.slab_T + ((static_cast<size_t>(cam) * slots + slab) * a.nx + xp) * a.cy + a.row0 + yb;
       Tc[k] = ldg4(cp);
       if (paired) {
         const float4 tot = ldg4(cp + static_cast<size_t>(nsl - slab) * a.nx * a.cy);
-        Tr[k] = make_float4(tot.x - Tc[k].x, tot.y - Tc[k].y, tot.z - Tc[k].z, tot.w - Tc[k].w);
+        Tr[k] = KAHAN ? tot : make_float4(tot.x - Tc[k].x, tot.y - Tc[k].y, tot.z - Tc[k].z, tot.w - Tc[k].w);
       }
     }
   }
@@ -277,7 +295,7 @@ __device__ __forceinline__ void spread_pair_body(const YgArgs& a, int u0, const 
 
   for (int z = zbeg; z < zend; ++z) {
     const int b = z & 1;
-    float4* sc = sb + b * 2 * NS * 32;
+    float4* sc = sb + (NB == 2 ? b : 0) * 2 * NS * 32;
     float4* sm = sc + NS * 32;
     Tap* tb = taps + b * TS::kTapSlots;
     if ((ATT || ADJ) && lane < TS::kOwn) {
@@ -300,11 +318,22 @@ __device__ __forceinline__ void spread_pair_body(const YgArgs& a, int u0, const 
         if (paired && ok) q = ldg4(mrow + static_cast<size_t>(a.nx - 1 - xp) * a.cy + yb);
         if (ATT) {
           const float4 m = sample4(mu, tb[tap_slot<R>(c)], yb, yok);
-          add4(Tc[k], m);
-          s = mul4(s, exp_neg4(Tc[k]));
-          if (paired) {
-            q = mul4(q, exp_neg4(Tr[k]));
-            Tr[k] = make_float4(Tr[k].x - m.x, Tr[k].y - m.y, Tr[k].z - m.z, Tr[k].w - m.w);
+          if constexpr (KAHAN) {
+            float4 cc = scomp[k * 32 * kW + threadIdx.x];
+            kahan_add4(Tc[k], cc, m);
+            scomp[k * 32 * kW + threadIdx.x] = cc;
+            const float4 tv = kahan_value4(Tc[k], cc);
+            s = mul4(s, exp_neg4(tv));
+            if (paired)  // sum from the far end, inclusive: total - forward sum + this plane
+              q = mul4(q, exp_neg4(make_float4(Tr[k].x - tv.x + m.x, Tr[k].y - tv.y + m.y, Tr[k].z - tv.z + m.z,
+                                               Tr[k].w - tv.w + m.w)));
+          } else {
+            add4(Tc[k], m);
+            s = mul4(s, exp_neg4(Tc[k]));
+            if (paired) {
+              q = mul4(q, exp_neg4(Tr[k]));
+              Tr[k] = make_float4(Tr[k].x - m.x, Tr[k].y - m.y, Tr[k].z - m.z, Tr[k].w - m.w);
+            }
           }
         }
         sc[c * 32 + lane] = s;
@@ -356,18 +385,19 @@ __device__ __forceinline__ void spread_pair_body(const YgArgs& a, int u0, const 
         write(i, v);
       }
     }
+    if (NB == 1) __syncthreads();  // the single tile buffer is rewritten next plane
   }
 }
 
-template <int R, bool PSF, bool ATT, bool ADJ>
+template <int R, bool PSF, bool ATT, bool ADJ, class V = float>
 __global__ void __launch_bounds__(32 * kW, 2) k_spread_pair_yg(const YgArgs a, int u0) {
-  spread_pair_body<R, PSF, ATT, ADJ, false>(a, u0, nullptr);
+  spread_pair_body<R, PSF, ATT, ADJ, false, V>(a, u0, nullptr);
 }
 
-template <int R, bool ATT, bool ADJ>
+template <int R, bool ATT, bool ADJ, class V = float>
 __global__ void __launch_bounds__(32 * kW, 2)
     k_spread_pair_ptab_yg(const YgArgs a, int u0, const __grid_constant__ PsfTable t) {
-  spread_pair_body<R, true, ATT, ADJ, true>(a, u0, t.c);
+  spread_pair_body<R, true, ATT, ADJ, true, V>(a, u0, t.c);
 }
 
 // ------------------------------------ backprojector: inverse-rotation gather
@@ -490,8 +520,10 @@ int launch_spread_pair_R(const YgArgs& a, int u0, int gcount, cudaStream_t st) {
   const bool psf = a.psf != nullptr;
   const int zper = (a.nz + a.bslabs - 1) / a.bslabs;
   const PsfTable* tab = psf_table<R>(a);
-  const size_t smem =
-      2 * TS::kSbBytes + TS::kTapBytes + (psf && !tab ? sizeof(float) * 2 * zper * 2 * (2 * R + 1) : 0);
+  // bfloat16 mu: the Kahan form (reference mode only)
+  const bool bf16 = a.storage == kStorageBF16 && a.mu && !ADJ;
+  const size_t smem = (bf16 ? spread_pair_fixed_smem<R, __nv_bfloat16>() : spread_pair_fixed_smem<R, float>()) +
+                      (psf && !tab ? sizeof(float) * 2 * zper * 2 * (2 * R + 1) : 0);
   auto go = [&](auto k) {
     cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
     NRGB_LAUNCH_SCOPE(ADJ ? "k_adjoint_pair_yg" : "k_spread_pair_yg", st);
@@ -502,6 +534,14 @@ int launch_spread_pair_R(const YgArgs& a, int u0, int gcount, cudaStream_t st) {
     NRGB_LAUNCH_SCOPE(ADJ ? "k_adjoint_pair_yg" : "k_spread_pair_yg", st);
     k<<<grid, block, smem, st>>>(a, u0, *tab);
   };
+  if constexpr (!ADJ) {
+    if (bf16) {
+      if (psf && tab) go_tab(k_spread_pair_ptab_yg<R, true, false, __nv_bfloat16>);
+      else if (psf) go(k_spread_pair_yg<R, true, true, false, __nv_bfloat16>);
+      else go(k_spread_pair_yg<0, false, true, false, __nv_bfloat16>);
+      return cudaGetLastError() == cudaSuccess ? kOk : kErrKernel;
+    }
+  }
   if (psf && tab) {
     if (a.mu) go_tab(k_spread_pair_ptab_yg<R, true, ADJ>);
     else go_tab(k_spread_pair_ptab_yg<R, false, ADJ>);
@@ -628,8 +668,9 @@ int yg_backproject(const YgArgs& a_in, cudaStream_t st) {
   YgArgs a = a_in;
   if (a.bslabs < 1 || a.bslabs > kSlabsB) return kErrParameters;
   const int R = a.psf ? (a.psf_k - 1) / 2 : 0;
-  // mirror units: float32 mu
-  const bool pair = !a.gradient && a.units && a.nunits > 0 && a.storage != kStorageBF16;
+  // mirror units: float32 mu, or bfloat16 mu in reference mode
+  const bool pair = !a.gradient && a.units && a.nunits > 0 &&
+                    (a.storage != kStorageBF16 || a.back_mode != kBackAdjoint);
   if (!pair) {
     a.units = nullptr;
     a.nunits = 0;

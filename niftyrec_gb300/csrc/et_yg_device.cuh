@@ -396,6 +396,10 @@ struct TileShape {
     return sizeof(float4) * 32 * (2 * steps * NS > (pair ? 3 : 2) * kTXC ? 2 * steps * NS : (pair ? 3 : 2) * kTXC);
   }
   __host__ __device__ static constexpr size_t tap_bytes(int steps = 1) { return sizeof(Tap) * 2 * steps * kTapSlots; }
+  // Projector serving mirror cameras from bfloat16 storage: the Kahan
+  // compensations of T, P and the mate's Q, one float4 per thread and output
+  // column each, in shared memory ([3][kTXC][32]) -- registers hold the sums.
+  __host__ __device__ static constexpr size_t comp_bytes(bool on) { return on ? sizeof(float4) * 3 * kTXC * 32 : 0; }
 };
 
 // Footprint slot of sampled column c in the tap buffer: the columns one warp
@@ -412,6 +416,13 @@ template <int R>
 __host__ __device__ constexpr size_t tile_smem_bytes(int nz, bool pair = false, int steps = 1) {
   return TileShape<R>::sb_bytes(pair, steps) + TileShape<R>::tap_bytes(steps) +
          sizeof(float) * static_cast<size_t>(nz) * 2 * (2 * R + 1) * (pair ? 2 : 1);
+}
+
+// The projector's: the tile above plus, for mirror cameras from bfloat16
+// storage, the shared-memory Kahan compensations.
+template <int R>
+__host__ __device__ constexpr size_t project_smem_bytes(int nz, bool pair, bool kahan, int steps = 1) {
+  return tile_smem_bytes<R>(nz, pair, steps) + TileShape<R>::comp_bytes(pair && kahan);
 }
 
 // Row pass from the shared tile: outputs i = 0..kTXW-1 of this warp use tile
@@ -611,7 +622,8 @@ __device__ __forceinline__ void project_item(const YgArgs& a, int cam, int mate,
                                              const float* ptab = nullptr) {
   using TS = TileShape<R>;
   constexpr bool KAHAN = StorageTraits<V>::kKahan;
-  static_assert(!(PAIR && KAHAN), "mirror cameras are served by the float32 projector");
+  // mirror cameras from bfloat16 storage: compensations in shared memory
+  constexpr bool SCOMP = PAIR && KAHAN;
   const V* __restrict__ act = reinterpret_cast<const V*>(a.act) + a.row0;
   const V* __restrict__ mu = reinterpret_cast<const V*>(a.mu) + a.row0;
   constexpr int NS = TS::NS;
@@ -619,7 +631,8 @@ __device__ __forceinline__ void project_item(const YgArgs& a, int cam, int mate,
   constexpr size_t kSb = TS::sb_bytes(PAIR, STEPS);
   float4* sb = reinterpret_cast<float4*>(smem);                    // [2 * STEPS][NS][32]
   Tap* taps = reinterpret_cast<Tap*>(smem + kSb);                   // [2 * STEPS][kTapSlots]
-  float* s_psf = reinterpret_cast<float*>(smem + kSb + TS::tap_bytes(STEPS));  // [nz][2K]
+  float4* scomp = reinterpret_cast<float4*>(smem + kSb + TS::tap_bytes(STEPS));  // [3][kTXC][32] (SCOMP)
+  float* s_psf = reinterpret_cast<float*>(smem + kSb + TS::tap_bytes(STEPS) + TS::comp_bytes(SCOMP));  // [nz][2K]
   float* s_psf_m = s_psf + static_cast<size_t>(a.nz) * 2 * K;       // [nz][2K] (mate)
 
   cg::cluster_group cluster = cg::this_cluster();
@@ -664,15 +677,41 @@ __device__ __forceinline__ void project_item(const YgArgs& a, int cam, int mate,
   };
   const CamRows cr = cam_rows(a.geom[cam].fwd);
 
-  float4 T[kTXW], P[kTXW], cT[kTXW], cP[kTXW];  // c*: Kahan compensations (KAHAN only)
-  float4 Q[PAIR ? kTXW : 1];                    // mate's slab partial
+  constexpr int NC = SCOMP ? 1 : kTXW;
+  float4 T[kTXW], P[kTXW], cT[NC], cP[NC];  // c*: Kahan compensations (KAHAN without SCOMP)
+  float4 Q[PAIR ? kTXW : 1];                // mate's slab partial
+  // compensation slot of quantity q (0 T, 1 P, 2 Q) of output i (SCOMP)
+  auto cslot = [&](int q, int i) { return scomp + (q * kTXC + warp * kTXW + i) * 32 + lane; };
+  // s += v, Kahan-compensated (KAHAN) or plain; value of a compensated sum
+  auto kadd = [&](float4& s, float4* creg, int q, int i, const float4& v) {
+    if constexpr (SCOMP) {
+      float4 c = *cslot(q, i);
+      kahan_add4(s, c, v);
+      *cslot(q, i) = c;
+    } else if constexpr (KAHAN) {
+      kahan_add4(s, *creg, v);
+    } else {
+      add4(s, v);
+    }
+  };
+  auto kval = [&](const float4& s, const float4* creg, int q, int i) -> float4 {
+    if constexpr (SCOMP) return kahan_value4(s, *cslot(q, i));
+    else if constexpr (KAHAN) return kahan_value4(s, *creg);
+    else return s;
+  };
+  auto kclear = [&](int q, int i) {
+    if constexpr (SCOMP) *cslot(q, i) = make_float4(0.f, 0.f, 0.f, 0.f);
+  };
 #pragma unroll
   for (int i = 0; i < kTXW; ++i) {
     T[i] = make_float4(0.f, 0.f, 0.f, 0.f);
     P[i] = make_float4(0.f, 0.f, 0.f, 0.f);
-    cT[i] = make_float4(0.f, 0.f, 0.f, 0.f);
-    cP[i] = make_float4(0.f, 0.f, 0.f, 0.f);
+    if (!SCOMP) {
+      cT[SCOMP ? 0 : i] = make_float4(0.f, 0.f, 0.f, 0.f);
+      cP[SCOMP ? 0 : i] = make_float4(0.f, 0.f, 0.f, 0.f);
+    }
     if (PAIR) Q[i] = make_float4(0.f, 0.f, 0.f, 0.f);
+    for (int q = 0; q < 3; ++q) kclear(q, i);
   }
   ybuf_zero_pads();
   __syncthreads();
@@ -707,12 +746,24 @@ __device__ __forceinline__ void project_item(const YgArgs& a, int cam, int mate,
     const Tap* tb = taps + b * TS::kTapSlots;
     auto emit_m = [&](int i, const float4& v) {
       if (!ATT) {
-        add4(Q[i], v);
+        if (KAHAN) kadd(Q[i], nullptr, 2, i, v);
+        else add4(Q[i], v);
       } else if (MODE == 0) {  // weight exp(E_z): T holds the sum before plane z
-        fma4(Q[i], v, exp_neg4(make_float4(-T[i].x, -T[i].y, -T[i].z, -T[i].w)));
+        if (KAHAN) {
+          const float4 e = kval(T[i], &cT[SCOMP ? 0 : i], 0, i);
+          kadd(Q[i], nullptr, 2, i, mul4(v, exp_neg4(make_float4(-e.x, -e.y, -e.z, -e.w))));
+        } else {
+          fma4(Q[i], v, exp_neg4(make_float4(-T[i].x, -T[i].y, -T[i].z, -T[i].w)));
+        }
       } else {  // T runs from the slab's far end, inclusive
-        add4(T[i], sample4(mu, tb[tap_slot<R>(warp * kTXW + i + R)], yb, yok));
-        fma4(Q[i], v, exp_neg4(T[i]));
+        const float4 m = sample4(mu, tb[tap_slot<R>(warp * kTXW + i + R)], yb, yok);
+        if (KAHAN) {
+          kadd(T[i], &cT[SCOMP ? 0 : i], 0, i, m);
+          kadd(Q[i], nullptr, 2, i, mul4(v, exp_neg4(kval(T[i], &cT[SCOMP ? 0 : i], 0, i))));
+        } else {
+          add4(T[i], m);
+          fma4(Q[i], v, exp_neg4(T[i]));
+        }
       }
     };
     if (MODE == 1) {
@@ -728,14 +779,14 @@ __device__ __forceinline__ void project_item(const YgArgs& a, int cam, int mate,
       if (ATT) {
         const float4 m = sample4(mu, tb[tap_slot<R>(warp * kTXW + i + R)], yb, yok);
         if (KAHAN) {
-          kahan_add4(T[i], cT[i], m);
-          kahan_add4(P[i], cP[i], mul4(v, exp_neg4(kahan_value4(T[i], cT[i]))));
+          kadd(T[i], &cT[SCOMP ? 0 : i], 0, i, m);
+          kadd(P[i], &cP[SCOMP ? 0 : i], 1, i, mul4(v, exp_neg4(kval(T[i], &cT[SCOMP ? 0 : i], 0, i))));
         } else {
           add4(T[i], m);
           fma4(P[i], v, exp_neg4(T[i]));
         }
       } else {
-        depth_add4<KAHAN>(P[i], cP[i], v);
+        kadd(P[i], &cP[SCOMP ? 0 : i], 1, i, v);
       }
     };
     if (PSF) {
@@ -785,11 +836,17 @@ __device__ __forceinline__ void project_item(const YgArgs& a, int cam, int mate,
       for (int i = 0; i < kTXW; ++i) {
         Q[i] = make_float4(0.f, 0.f, 0.f, 0.f);
         T[i] = make_float4(0.f, 0.f, 0.f, 0.f);  // ends at the slab sum again
+        if (KAHAN) cT[SCOMP ? 0 : i] = make_float4(0.f, 0.f, 0.f, 0.f);
+        kclear(0, i);
+        kclear(2, i);
       }
       walk(std::integral_constant<int, 1>());
     } else {
 #pragma unroll
-      for (int i = 0; i < kTXW; ++i) Q[i] = mul4(Q[i], exp_neg4(T[i]));
+      for (int i = 0; i < kTXW; ++i) {
+        Q[i] = mul4(kval(Q[i], nullptr, 2, i), exp_neg4(kval(T[i], &cT[SCOMP ? 0 : i], 0, i)));
+        kclear(2, i);
+      }
     }
   }
 
@@ -800,9 +857,9 @@ __device__ __forceinline__ void project_item(const YgArgs& a, int cam, int mate,
   float4* sQ = sb + 2 * kTXC * 32;  // [kTXC][32] (PAIR)
 #pragma unroll
   for (int i = 0; i < kTXW; ++i) {
-    sT[(warp * kTXW + i) * 32 + lane] = depth_value4<KAHAN>(T[i], cT[i]);
-    sP[(warp * kTXW + i) * 32 + lane] = depth_value4<KAHAN>(P[i], cP[i]);
-    if (PAIR && paired) sQ[(warp * kTXW + i) * 32 + lane] = Q[i];
+    sT[(warp * kTXW + i) * 32 + lane] = kval(T[i], &cT[SCOMP ? 0 : i], 0, i);
+    sP[(warp * kTXW + i) * 32 + lane] = kval(P[i], &cP[SCOMP ? 0 : i], 1, i);
+    if (PAIR && paired) sQ[(warp * kTXW + i) * 32 + lane] = kval(Q[i], nullptr, 2, i);
   }
   cluster.sync();
   const int per_rank = kTXC / nslabs;  // outputs merged by each CTA of the cluster

@@ -52,12 +52,17 @@ int launch_project_R(const YgArgs& a_in, cudaStream_t st, int* slabs_used) {
   const int ntile = (a.nx + kTXC - 1) / kTXC;
   const bool psf = a.psf != nullptr;
   const bool bf16 = a.storage == kStorageBF16;
-  // mirror cameras are served by the float32 kernels only
-  const bool pair = a.units != nullptr && a.nunits > 0 && !bf16;
-  const int nunits = pair ? a.nunits : a.ncam;
   // the PSF in the kernel parameters when the host copy is given and fits
   const bool ptab = psf && a.psf_host && static_cast<size_t>(a.nz) * 2 * (2 * R + 1) <= kPsfTableFloats;
-  const size_t smem = tile_smem_bytes<R>(psf && !ptab ? a.nz : 0, pair);
+  // mirror cameras: float32 always; bfloat16 (Kahan compensations in shared
+  // memory) where two CTAs per SM still fit
+  bool pair = a.units != nullptr && a.nunits > 0;
+  size_t smem = project_smem_bytes<R>(psf && !ptab ? a.nz : 0, pair, bf16);
+  if (pair && bf16 && 2 * (smem + kYBufBytes + 1024) > 228 * 1024) {
+    pair = false;
+    smem = project_smem_bytes<R>(psf && !ptab ? a.nz : 0, false, true);
+  }
+  const int nunits = pair ? a.nunits : a.ncam;
   // three CTAs per SM need three tiles (plus 1 KB reserved each) in the 228 KB
   const bool three = 3 * (smem + kYBufBytes + 1024) <= 228 * 1024;
   if (a.pslabs != 2 && a.pslabs != 4 && a.pslabs != 8 && a.pslabs != 16)
@@ -117,7 +122,9 @@ int launch_project_R(const YgArgs& a_in, cudaStream_t st, int* slabs_used) {
   using Off = std::false_type;
   using On = std::true_type;
   // the mirror-camera item needs the 128-register budget of two CTAs per SM
-  if (bf16)
+  if (bf16 && pair)
+    pick(__nv_bfloat16(), std::integral_constant<int, 2>(), On());
+  else if (bf16)
     pick(__nv_bfloat16(), std::integral_constant<int, 2>(), Off());
   else if (pair)
     pick(0.0f, std::integral_constant<int, 2>(), On());

@@ -69,15 +69,17 @@ def test_float32_within_1e5_of_float64():
     assert P.rel_error(b32, b64)[0] < 1e-5
 
 
-@pytest.mark.parametrize("shape", [SHAPE, (16, 140, 16)])
-def test_bfloat16_storage(shape):
-    """shape 2 has ny > 128: row windows of the bfloat16 kernels."""
+@pytest.mark.parametrize("shape,ncam", [(SHAPE, 8), ((16, 140, 16), 8), ((64, 64, 64), 60), ((48, 48, 48), 7)])
+def test_bfloat16_storage(shape, ncam):
+    """Opposite cameras form mirror units in the bfloat16 kernels too (8 and
+    60 cameras; 7 cameras have no opposite pairs); shape 2 has ny > 128: row
+    windows of the bfloat16 kernels."""
     from niftyrec_gb300 import precision as P
 
     act = S.ellipsoid_phantom(shape, seed=53)
     mu = S.mu_map(shape, seed=53)
     psf = S.gaussian_psf(7, shape[2], 0.5, 0.05)
-    cams = S.cameras_about_y(8, 3.0)
+    cams = S.cameras_about_y(ncam, 3.0)
     a16, m16 = dev(act, torch.bfloat16), dev(mu, torch.bfloat16)
     p16 = P.project(a16, m16, cams, psf)
     assert p16.dtype == torch.float32
