@@ -167,6 +167,52 @@ __device__ __forceinline__ void axpy4p(Pair4& acc, f32x2 kk, const Pair4& v) {
   ffma2(acc.hi, v.hi, kk);
 }
 
+// Elementwise float4 operations as two packed pair instructions each (the
+// same roundings as the scalar forms, lane by lane): the projector's depth
+// sums and their Kahan steps.
+__device__ __forceinline__ f32x2 add2(f32x2 a, f32x2 b) {
+  f32x2 r;
+  asm("add.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b));
+  return r;
+}
+__device__ __forceinline__ f32x2 sub2(f32x2 a, f32x2 b) {
+  f32x2 r;
+  asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b));
+  return r;
+}
+__device__ __forceinline__ f32x2 mul2(f32x2 a, f32x2 b) {
+  f32x2 r;
+  asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b));
+  return r;
+}
+__device__ __forceinline__ void add4p(float4& a, const float4& b) {
+  const Pair4 x = pair4(a), y = pair4(b);
+  a = unpair4({add2(x.lo, y.lo), add2(x.hi, y.hi)});
+}
+__device__ __forceinline__ float4 mul4p(const float4& a, const float4& b) {
+  const Pair4 x = pair4(a), y = pair4(b);
+  return unpair4({mul2(x.lo, y.lo), mul2(x.hi, y.hi)});
+}
+__device__ __forceinline__ void fma4p(float4& acc, const float4& a, const float4& b) {
+  Pair4 c = pair4(acc);
+  const Pair4 x = pair4(a), y = pair4(b);
+  ffma2(c.lo, x.lo, y.lo);
+  ffma2(c.hi, x.hi, y.hi);
+  acc = unpair4(c);
+}
+// Kahan step (kahan_add below) on pairs: y = v - c; t = s + y; c = (t - s) - y; s = t
+__device__ __forceinline__ void kahan_add4p(float4& s, float4& c, const float4& v) {
+  const Pair4 S = pair4(s), C = pair4(c), V = pair4(v);
+  const f32x2 ylo = sub2(V.lo, C.lo), yhi = sub2(V.hi, C.hi);
+  const f32x2 tlo = add2(S.lo, ylo), thi = add2(S.hi, yhi);
+  c = unpair4({sub2(sub2(tlo, S.lo), ylo), sub2(sub2(thi, S.hi), yhi)});
+  s = unpair4({tlo, thi});
+}
+__device__ __forceinline__ float4 kahan_value4p(const float4& s, const float4& c) {
+  const Pair4 S = pair4(s), C = pair4(c);
+  return unpair4({sub2(S.lo, C.lo), sub2(S.hi, C.hi)});
+}
+
 __device__ __forceinline__ void axpy4(float4& acc, float k, const float4& v) {
   acc.x = fmaf(k, v.x, acc.x);
   acc.y = fmaf(k, v.y, acc.y);
@@ -686,17 +732,17 @@ __device__ __forceinline__ void project_item(const YgArgs& a, int cam, int mate,
   auto kadd = [&](float4& s, float4* creg, int q, int i, const float4& v) {
     if constexpr (SCOMP) {
       float4 c = *cslot(q, i);
-      kahan_add4(s, c, v);
+      kahan_add4p(s, c, v);
       *cslot(q, i) = c;
     } else if constexpr (KAHAN) {
-      kahan_add4(s, *creg, v);
+      kahan_add4p(s, *creg, v);
     } else {
-      add4(s, v);
+      add4p(s, v);
     }
   };
   auto kval = [&](const float4& s, const float4* creg, int q, int i) -> float4 {
-    if constexpr (SCOMP) return kahan_value4(s, *cslot(q, i));
-    else if constexpr (KAHAN) return kahan_value4(s, *creg);
+    if constexpr (SCOMP) return kahan_value4p(s, *cslot(q, i));
+    else if constexpr (KAHAN) return kahan_value4p(s, *creg);
     else return s;
   };
   auto kclear = [&](int q, int i) {
@@ -751,18 +797,18 @@ __device__ __forceinline__ void project_item(const YgArgs& a, int cam, int mate,
       } else if (MODE == 0) {  // weight exp(E_z): T holds the sum before plane z
         if (KAHAN) {
           const float4 e = kval(T[i], &cT[SCOMP ? 0 : i], 0, i);
-          kadd(Q[i], nullptr, 2, i, mul4(v, exp_neg4(make_float4(-e.x, -e.y, -e.z, -e.w))));
+          kadd(Q[i], nullptr, 2, i, mul4p(v, exp_neg4(make_float4(-e.x, -e.y, -e.z, -e.w))));
         } else {
-          fma4(Q[i], v, exp_neg4(make_float4(-T[i].x, -T[i].y, -T[i].z, -T[i].w)));
+          fma4p(Q[i], v, exp_neg4(make_float4(-T[i].x, -T[i].y, -T[i].z, -T[i].w)));
         }
       } else {  // T runs from the slab's far end, inclusive
         const float4 m = sample4(mu, tb[tap_slot<R>(warp * kTXW + i + R)], yb, yok);
         if (KAHAN) {
           kadd(T[i], &cT[SCOMP ? 0 : i], 0, i, m);
-          kadd(Q[i], nullptr, 2, i, mul4(v, exp_neg4(kval(T[i], &cT[SCOMP ? 0 : i], 0, i))));
+          kadd(Q[i], nullptr, 2, i, mul4p(v, exp_neg4(kval(T[i], &cT[SCOMP ? 0 : i], 0, i))));
         } else {
-          add4(T[i], m);
-          fma4(Q[i], v, exp_neg4(T[i]));
+          add4p(T[i], m);
+          fma4p(Q[i], v, exp_neg4(T[i]));
         }
       }
     };
@@ -780,10 +826,10 @@ __device__ __forceinline__ void project_item(const YgArgs& a, int cam, int mate,
         const float4 m = sample4(mu, tb[tap_slot<R>(warp * kTXW + i + R)], yb, yok);
         if (KAHAN) {
           kadd(T[i], &cT[SCOMP ? 0 : i], 0, i, m);
-          kadd(P[i], &cP[SCOMP ? 0 : i], 1, i, mul4(v, exp_neg4(kval(T[i], &cT[SCOMP ? 0 : i], 0, i))));
+          kadd(P[i], &cP[SCOMP ? 0 : i], 1, i, mul4p(v, exp_neg4(kval(T[i], &cT[SCOMP ? 0 : i], 0, i))));
         } else {
-          add4(T[i], m);
-          fma4(P[i], v, exp_neg4(T[i]));
+          add4p(T[i], m);
+          fma4p(P[i], v, exp_neg4(T[i]));
         }
       } else {
         kadd(P[i], &cP[SCOMP ? 0 : i], 1, i, v);
@@ -870,7 +916,16 @@ __device__ __forceinline__ void project_item(const YgArgs& a, int cam, int mate,
       Pt.z = fmaxf(Pt.z, 0.f);
       Pt.w = fmaxf(Pt.w, 0.f);
     }
-    *reinterpret_cast<float4*>(a.out + (static_cast<size_t>(c) * a.nx + x) * a.cy + a.row0 + yb) = Pt;
+    const size_t idx = (static_cast<size_t>(c) * a.nx + x) * a.cy + a.row0 + yb;
+    if (a.ratio_y) {  // the OSEM ratio (emission-lib/_et_array_interface.cpp:1022-1028)
+      const float4 y = ldg4(a.ratio_y + idx);
+      const float e = a.ratio_eps;
+      Pt.x = Pt.x < e ? __fdiv_rn(y.x, e) : __fdiv_rn(y.x, Pt.x);
+      Pt.y = Pt.y < e ? __fdiv_rn(y.y, e) : __fdiv_rn(y.y, Pt.y);
+      Pt.z = Pt.z < e ? __fdiv_rn(y.z, e) : __fdiv_rn(y.z, Pt.z);
+      Pt.w = Pt.w < e ? __fdiv_rn(y.w, e) : __fdiv_rn(y.w, Pt.w);
+    }
+    *reinterpret_cast<float4*>(a.out + idx) = Pt;
   };
   // transmission carries for the backprojector (a.carry_out): the exclusive
   // prefix of the slab sums at every slab, then the column total
