@@ -320,19 +320,21 @@ __device__ __forceinline__ void spread_pair_body(const YgArgs& a, int u0, const 
           const float4 m = sample4(mu, tb[tap_slot<R>(c)], yb, yok);
           if constexpr (KAHAN) {
             float4 cc = scomp[k * 32 * kW + threadIdx.x];
-            kahan_add4(Tc[k], cc, m);
+            kahan_add4p(Tc[k], cc, m);
             scomp[k * 32 * kW + threadIdx.x] = cc;
-            const float4 tv = kahan_value4(Tc[k], cc);
-            s = mul4(s, exp_neg4(tv));
-            if (paired)  // sum from the far end, inclusive: total - forward sum + this plane
-              q = mul4(q, exp_neg4(make_float4(Tr[k].x - tv.x + m.x, Tr[k].y - tv.y + m.y, Tr[k].z - tv.z + m.z,
-                                               Tr[k].w - tv.w + m.w)));
+            const float4 tv = kahan_value4p(Tc[k], cc);
+            s = mul4p(s, exp_neg4(tv));
+            if (paired) {  // sum from the far end, inclusive: total - forward sum + this plane
+              const Pair4 tot = pair4(Tr[k]), v = pair4(tv), mm = pair4(m);
+              q = mul4p(q, exp_neg4(unpair4({add2(sub2(tot.lo, v.lo), mm.lo), add2(sub2(tot.hi, v.hi), mm.hi)})));
+            }
           } else {
-            add4(Tc[k], m);
-            s = mul4(s, exp_neg4(Tc[k]));
+            add4p(Tc[k], m);
+            s = mul4p(s, exp_neg4(Tc[k]));
             if (paired) {
-              q = mul4(q, exp_neg4(Tr[k]));
-              Tr[k] = make_float4(Tr[k].x - m.x, Tr[k].y - m.y, Tr[k].z - m.z, Tr[k].w - m.w);
+              q = mul4p(q, exp_neg4(Tr[k]));
+              const Pair4 tr = pair4(Tr[k]), mm = pair4(m);
+              Tr[k] = unpair4({sub2(tr.lo, mm.lo), sub2(tr.hi, mm.hi)});
             }
           }
         }
@@ -354,7 +356,7 @@ __device__ __forceinline__ void spread_pair_body(const YgArgs& a, int u0, const 
     float4 pend;  // the mate's term of the output being written
     auto keep = [&](int i, const float4& v) { pend = v; };
     auto write_sum = [&](int i, float4 v) {
-      add4(v, pend);
+      add4p(v, pend);
       write(i, v);
     };
     if (PSF) {
