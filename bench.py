@@ -60,8 +60,10 @@ def algorithmic_bytes(kernel: str, launches: int, ncam_total: int) -> float:
         return ncam_total * P_ANGLE
     if kernel in ("k_spread_yg", "k_spread_pair_yg"):  # reads mu and the projection plane per angle
         return ncam_total * (N ** 3 * 4 + N ** 2 * 4)
-    if kernel == "k_gather_yg":  # accumulator read-modify-write per angle
-        return ncam_total * (N ** 3 * 8)
+    # k_gather_yg reads the scratch the spread wrote and gathers once per camera
+    # group (a mirror unit serves two angles), overlapping the next spread on a
+    # second stream: it has no per-angle algorithmic-byte model and no
+    # isolated duration here (its ncu summary gives both)
     return float("nan")
 
 
@@ -372,8 +374,9 @@ def run_ours(args):
                      "frac_of_peak": round(PAIR_BYTES * value / world / 1e9 / peak, 4), "peak_source": peak_kind},
         "roofline": roof,
         "rooflines": rooflines,
-        "rooflines_note": "algorithmic bytes per camera angle as the reference moves them; a mirror unit serves "
-                          "two angles from one pass, so the gather can read above its physical rate",
+        "rooflines_note": "algorithmic bytes per camera angle as the reference moves them (a mirror unit serves "
+                          "two angles from one pass); the gather, an intermediate that overlaps the spread, is "
+                          "left out (its one-kernel ncu summary is under profiles/)",
         "kernels": kernels,
         "kernels_pass": {"ms_per_step": round(sum(ms_prof) / len(ms_prof), 4),
                          "note": "separate pass with CUDA events around every launch"},

@@ -98,6 +98,11 @@ struct YgArgs {
   // depth slabs ([ncam][pslabs + 1][nx][cy], the layout above with bslabs =
   // the projector's slab count; with units, at each unit's first camera).
   float* carry_out = nullptr;
+  // Projector with carry_out: 1 -> also record the transmission at the middle
+  // of every depth slab, so the carries serve twice as many backprojector
+  // slabs (the launcher applies it where the halves line up and the result
+  // has at most 8 slabs; slabs_used reports the carries' slab count).
+  int carry_split = 0;
   // 1: spread on the caller's stream, gather on a second stream, two scratch
   // slots; 0: both on the caller's stream with one slot (creates no stream
   // or event).
@@ -126,8 +131,14 @@ bool yg_supported(int nx, int ny, int nz, int psf_k);
 // Bytes of work space yg_backproject needs (slab carries + `slots` camera-group
 // scratch volumes of `group` cameras each).
 size_t yg_backproject_workspace(int nx, int ny, int nz, int ncam, int group, int slots = 2);
-// slabs_used (if non-null): the projector's depth slabs (the slab count of
-// the carries written to a.carry_out).
+// Camera-group size the backprojector uses for n units and a requested group
+// (groups as even as possible, at most `group` units each).
+int yg_even_group(int n, int group);
+// Depth slabs the per-call projector chooses for nunits mirror units (or
+// cameras) of an nx-wide volume with nz planes, two CTAs per SM.
+int yg_pair_project_slabs(int nunits, int nx, int nz);
+// slabs_used (if non-null): the slab count of the carries written to
+// a.carry_out (the projector's depth slabs, twice that with a carry split).
 int yg_project(const YgArgs& a, cudaStream_t st, int* slabs_used = nullptr);
 // Gradient of sum(g * project(act, mu)) with respect to mu for gantry cameras
 // (column layouts: a.act, a.mu; a.sino = g [ncam][nx][cy]; a.out = the

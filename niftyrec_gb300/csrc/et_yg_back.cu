@@ -615,6 +615,12 @@ int spread_by_radius(int R, const YgArgs& a, int c0, int gcount, cudaStream_t st
 
 }  // namespace
 
+int yg_even_group(int n, int group) {
+  group = std::max(1, std::min(group, n));
+  const int ngroups = (n + group - 1) / group;
+  return (n + ngroups - 1) / ngroups;
+}
+
 size_t yg_backproject_workspace(int nx, int ny, int nz, int ncam, int group, int slots) {
   const size_t cy = round_up(ny, 4);
   const size_t vol = static_cast<size_t>(nz) * nx * scratch_rows(ny);  // one window's scratch volume
@@ -703,9 +709,7 @@ int yg_backproject(const YgArgs& a_in, cudaStream_t st) {
   }
   const int nunits = pair ? a.nunits : a.ncam;  // scratch volumes to spread and gather
   // even groups of at most a.group units
-  int group = std::max(1, std::min(a.group, nunits));
-  const int ngroups = (nunits + group - 1) / group;
-  group = (nunits + ngroups - 1) / ngroups;
+  int group = yg_even_group(nunits, a.group);
   const std::vector<Window> wins = row_windows(a.ny, R);
   // work space: slab carries first (unless given), then the scratch slot(s)
   const size_t vol = static_cast<size_t>(a.nz) * a.nx * scratch_rows(a.ny);

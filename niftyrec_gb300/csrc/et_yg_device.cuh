@@ -55,6 +55,8 @@ constexpr int kGatherWarps = 4;   // warps per CTA of the inverse-rotation gathe
 constexpr int kGatherCols = 2;    // accumulator columns per warp in the gather
 constexpr unsigned kFull = 0xffffffffu;
 
+__host__ __device__ constexpr size_t round_up16(size_t b) { return (b + 15) / 16 * 16; }
+
 __device__ __forceinline__ float fm(float a, float b) { return __fmul_rn(a, b); }
 __device__ __forceinline__ float fa(float a, float b) { return __fadd_rn(a, b); }
 
@@ -680,6 +682,10 @@ __device__ __forceinline__ void project_item(const YgArgs& a, int cam, int mate,
   float4* scomp = reinterpret_cast<float4*>(smem + kSb + TS::tap_bytes(STEPS));  // [3][kTXC][32] (SCOMP)
   float* s_psf = reinterpret_cast<float*>(smem + kSb + TS::tap_bytes(STEPS) + TS::comp_bytes(SCOMP));  // [nz][2K]
   float* s_psf_m = s_psf + static_cast<size_t>(a.nz) * 2 * K;       // [nz][2K] (mate)
+  // carry split: each output column's transmission at the middle of the slab
+  float4* smid = reinterpret_cast<float4*>(
+      reinterpret_cast<unsigned char*>(s_psf) +
+      round_up16(PSF && !PTAB ? sizeof(float) * static_cast<size_t>(a.nz) * 2 * K * (PAIR ? 2 : 1) : 0));  // [kTXC][32]
 
   cg::cluster_group cluster = cg::this_cluster();
   const int slab = static_cast<int>(cluster.block_rank());
@@ -854,6 +860,14 @@ __device__ __forceinline__ void project_item(const YgArgs& a, int cam, int mate,
 
   // walk: STEPS planes per barrier; iteration j uses buffers (j & 1) * STEPS + s,
   // rewritten at iteration j + 2 after the barrier of iteration j + 1
+  // carry split: planes of the slab's first half (the backprojector's slab
+  // of twice the count that starts at zbeg)
+  const bool split = ATT && a.carry_out && a.carry_split;
+  const int zhalf = (a.nz + 2 * nslabs - 1) / (2 * nslabs);
+  auto stash_mid = [&]() {
+#pragma unroll
+    for (int i = 0; i < kTXW; ++i) smid[(warp * kTXW + i) * 32 + lane] = kval(T[i], &cT[SCOMP ? 0 : i], 0, i);
+  };
   auto walk = [&](auto mode) {
     constexpr int MODE = decltype(mode)::value;
     const int n = zend - zbeg;
@@ -864,9 +878,12 @@ __device__ __forceinline__ void project_item(const YgArgs& a, int cam, int mate,
         if (k + s < n) produce(MODE == 0 ? zbeg + k + s : zend - 1 - k - s, base + s);
       __syncthreads();
 #pragma unroll
-      for (int s = 0; s < STEPS; ++s)
+      for (int s = 0; s < STEPS; ++s) {
         if (k + s < n) consume(MODE == 0 ? zbeg + k + s : zend - 1 - k - s, base + s, mode);
+        if (MODE == 0 && split && k + s + 1 == zhalf) stash_mid();
+      }
     }
+    if (MODE == 0 && split && n < zhalf) stash_mid();  // the half ends past the volume
   };
   walk(std::integral_constant<int, 0>());
 
@@ -937,20 +954,28 @@ __device__ __forceinline__ void project_item(const YgArgs& a, int cam, int mate,
     const int x = x0 + o;
     if (o / per_rank != slab || x >= a.nx || !yok || !lane_writes(a, yb)) continue;
     float4 Pt = make_float4(0.f, 0.f, 0.f, 0.f), Tt = make_float4(0.f, 0.f, 0.f, 0.f);
-    float* cdst = carry ? carry + (static_cast<size_t>(cam) * (nslabs + 1) * a.nx + x) * a.cy : nullptr;
+    const int cslabs = split ? 2 * nslabs : nslabs;  // slabs of the carries
+    float* cdst = carry ? carry + (static_cast<size_t>(cam) * (cslabs + 1) * a.nx + x) * a.cy : nullptr;
     for (int s = 0; s < nslabs; ++s) {
       const float4* rT = cluster.map_shared_rank(sT, s);
       const float4* rP = cluster.map_shared_rank(sP, s);
       const float4 ps = rP[o * 32 + lane];
       if (ATT) {
-        if (cdst) *reinterpret_cast<float4*>(cdst + s * cstride) = Tt;
+        if (cdst) {
+          *reinterpret_cast<float4*>(cdst + (split ? 2 * s : s) * cstride) = Tt;
+          if (split) {
+            float4 mid = Tt;
+            add4(mid, cluster.map_shared_rank(smid, s)[o * 32 + lane]);
+            *reinterpret_cast<float4*>(cdst + (2 * s + 1) * cstride) = mid;
+          }
+        }
         fma4(Pt, exp_neg4(Tt), ps);
         add4(Tt, rT[o * 32 + lane]);
       } else {
         add4(Pt, ps);
       }
     }
-    if (cdst) *reinterpret_cast<float4*>(cdst + nslabs * cstride) = Tt;
+    if (cdst) *reinterpret_cast<float4*>(cdst + cslabs * cstride) = Tt;
     store(cam, x, Pt);
     if (PAIR && paired) {  // the mate's slabs from the far end: its column nx-1-x
       Pt = make_float4(0.f, 0.f, 0.f, 0.f);

@@ -9,17 +9,22 @@ int launch_project_R(const YgArgs& a, cudaStream_t st, int* slabs_used);  // et_
 
 // ------------------------------------------------------------- dispatch
 // Depth slabs (cluster size) of the projector: the fewest of 2, 4, 8 (16
-// with at least 8 planes per slab) that give at least four waves of CTAs
+// with at least 8 planes per slab) that give at least three waves of CTAs
 // (fewer slabs merge less; more slabs fill the GPU for small problems, e.g.
 // the 15-camera subsets of an OSEM step).  Measured on GB300 without mirror
 // units: 128^3 x 120 cameras 4 (0.84 ms; 2: 0.87, 8: 0.87), 256^3 x 180: 2
-// (15.9 ms; 4: 16.7), 64^3 x 60: 8 (0.149 ms; 4: 0.158).
+// (15.9 ms; 4: 16.7), 64^3 x 60: 8 (0.149 ms; 4: 0.158); with mirror units
+// (60 units at 128^3 x 120): 4 (0.612 ms; 8: 0.640, 16: 0.858).
 int project_slabs(int items, int ctas_per_sm, int nz) {
   const int slots = sm_count() * ctas_per_sm;
   const int most = nz >= 128 ? 16 : 8;
   for (int s = 2; s < most; s *= 2)
-    if (items * s >= 4 * slots) return s;
+    if (items * s >= 3 * slots) return s;
   return most;
+}
+
+int yg_pair_project_slabs(int nunits, int nx, int nz) {
+  return project_slabs(nunits * ((nx + kTXC - 1) / kTXC), 2, nz);
 }
 
 namespace {
