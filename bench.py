@@ -680,16 +680,14 @@ def config5_leg(dev, flush, stream, args, cpu=True):
     bk = torch.empty((n, n, n), dtype=torch.float32, device=dev)
 
     def pair(bf16):
+        """One pair through nrgb_project_backproject_device(_bf16), as the headline."""
         sp = vp(stream.cuda_stream)
-        fp = L.nrgb_project_device_bf16 if bf16 else L.nrgb_project_device
-        fb = L.nrgb_backproject_device_bf16 if bf16 else L.nrgb_backproject_device
+        fn = L.nrgb_project_backproject_device_bf16 if bf16 else L.nrgb_project_backproject_device
         a, m = (a16, m16) if bf16 else (a32, m32)
-        st = fp(vp(a.data_ptr()), vp(m.data_ptr()), size, vp(sino.data_ptr()), cp.ctypes.data_as(vp), csize,
-                pp.ctypes.data_as(vp), psize, 0.0, 0.0, 1, sp)
-        st2 = fb(vp(sino.data_ptr()), vp(m.data_ptr()), size, vp(bk.data_ptr()), cp.ctypes.data_as(vp), csize,
-                 pp.ctypes.data_as(vp), psize, 0.0, 0.0, 1, 0, sp)
-        if st or st2:
-            raise RuntimeError(f"config-5 pair status {st} {st2}")
+        st = fn(vp(a.data_ptr()), vp(m.data_ptr()), size, vp(sino.data_ptr()), None, vp(bk.data_ptr()),
+                cp.ctypes.data_as(vp), csize, pp.ctypes.data_as(vp), psize, 0.0, 0.0, 1, 0, sp)
+        if st:
+            raise RuntimeError(f"config-5 pair status {st}")
 
     peak, peak_kind = measured_peak()
     reps = max(3, args.steps // 3)
@@ -718,7 +716,7 @@ def config5_leg(dev, flush, stream, args, cpu=True):
     del p64, b64, s32
     out = {"workload": "256^3 activity + mu (seeded ellipsoid phantom, mu map), PSF 15x15 sigma=0.5+0.015*z, "
                        "180 angles x 2 deg, project + reference backproject; float32 vs bfloat16 storage",
-           "unit": "pairs/s", **res,
+           "unit": "pairs/s", "api": "nrgb_project_backproject_device(_bf16), device buffers", **res,
            "bf16_speedup": round(res["bfloat16"]["pairs_per_s"] / res["float32"]["pairs_per_s"], 3)}
     if cpu:
         out["cpu_baseline"] = cpu_pair_sample("config5", 16)

@@ -245,6 +245,15 @@ int nrgb_project_backproject_device(const float *d_activity, const float *d_atte
                                     const int *psf_size, float background, float background_attenuation,
                                     int truncate, int mode, void *stream);
 
+/* The same with bfloat16 activity and mu (nifti order; float32 sinograms and
+ * backprojection), as nrgb_project_device_bf16 / nrgb_backproject_device_bf16
+ * (addition; no counterpart in the reference). */
+int nrgb_project_backproject_device_bf16(const void *d_activity, const void *d_attenuation, const int *size,
+                                         float *d_sinogram, const float *d_backproject_input, float *d_backprojection,
+                                         const float *cameras, const int *cameras_size, const float *psf,
+                                         const int *psf_size, float background, float background_attenuation,
+                                         int truncate, int mode, void *stream);
+
 /* Backprojection that allocates nothing.  No counterpart in the reference.
  * For callers that cannot call cudaMalloc: a plug-in inside a host
  * application whose framework allocator already holds the GPU's memory (a

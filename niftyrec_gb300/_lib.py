@@ -60,6 +60,7 @@ PROTOTYPES = {
     "nrgb_backproject_device": (_I, [_P, _P, _PI, _P, _P, _PI, _P, _PI, _F, _F, _I, _I, _P]),
     "nrgb_debug_fail_allocations": (_I, [_I]),
     "nrgb_project_backproject_device": (_I, [_P, _P, _PI, _P, _P, _P, _P, _PI, _P, _PI, _F, _F, _I, _I, _P]),
+    "nrgb_project_backproject_device_bf16": (_I, [_P, _P, _PI, _P, _P, _P, _P, _PI, _P, _PI, _F, _F, _I, _I, _P]),
     "nrgb_project_device_bf16": (_I, [_P, _P, _PI, _P, _P, _PI, _P, _PI, _F, _F, _I, _P]),
     "nrgb_backproject_device_bf16": (_I, [_P, _P, _PI, _P, _P, _PI, _P, _PI, _F, _F, _I, _I, _P]),
     "nrgb_backproject_device_noalloc":(_I, [_P, _P, _PI, _P, _P, _PI, _P, _PI, _F, _F, _I, _P]),

@@ -967,7 +967,7 @@ int backproject_device_call(const float* d_sinogram, const float* d_attenuation,
 int pair_device_call(const float* d_activity, const float* d_attenuation, const int* size, float* d_sinogram,
                      const float* d_backproject_input, float* d_backprojection, const float* cameras,
                      const int* cameras_size, const float* psf, const int* psf_size, float background,
-                     float background_attenuation, int truncate, int mode, void* stream) {
+                     float background_attenuation, int truncate, int mode, bool bf16, void* stream) {
   if (!size || !cameras || !cameras_size || !d_activity || !d_sinogram || !d_backprojection ||
       (mode != kBackReference && mode != kBackAdjoint))
     return kErrParameters;
@@ -984,6 +984,10 @@ int pair_device_call(const float* d_activity, const float* d_attenuation, const 
   s = make_problem(size[0], size[1], size[2], cb, psf, psf_size, background, background_attenuation, truncate, &pbb);
   if (s != kOk) return s;
   pb.back_mode = pbb.back_mode = mode;
+  if (bf16) {
+    pb.storage = pbb.storage = kStorageBF16;
+    pb.input_bf16 = pbb.input_bf16 = true;
+  }
   DeviceState& ds = current_device_state(&s);
   if (s != kOk) return s;
   std::lock_guard<std::mutex> lk(ds.mu);
@@ -1012,7 +1016,19 @@ int nrgb_project_backproject_device(const float* d_activity, const float* d_atte
   NRGB_API("nrgb_project_backproject_device");
   return pair_device_call(d_activity, d_attenuation, size, d_sinogram, d_backproject_input, d_backprojection,
                           cameras, cameras_size, psf, psf_size, background, background_attenuation, truncate, mode,
-                          stream);
+                          false, stream);
+}
+
+// The same with bfloat16 activity / mu (see the header).
+int nrgb_project_backproject_device_bf16(const void* d_activity, const void* d_attenuation, const int* size,
+                                         float* d_sinogram, const float* d_backproject_input, float* d_backprojection,
+                                         const float* cameras, const int* cameras_size, const float* psf,
+                                         const int* psf_size, float background, float background_attenuation,
+                                         int truncate, int mode, void* stream) {
+  NRGB_API("nrgb_project_backproject_device_bf16");
+  return pair_device_call(static_cast<const float*>(d_activity), static_cast<const float*>(d_attenuation), size,
+                          d_sinogram, d_backproject_input, d_backprojection, cameras, cameras_size, psf, psf_size,
+                          background, background_attenuation, truncate, mode, true, stream);
 }
 
 int nrgb_project_device(const float* d_activity, const float* d_attenuation, const int* size, float* d_sinogram,

@@ -682,11 +682,6 @@ __device__ __forceinline__ void project_item(const YgArgs& a, int cam, int mate,
   float4* scomp = reinterpret_cast<float4*>(smem + kSb + TS::tap_bytes(STEPS));  // [3][kTXC][32] (SCOMP)
   float* s_psf = reinterpret_cast<float*>(smem + kSb + TS::tap_bytes(STEPS) + TS::comp_bytes(SCOMP));  // [nz][2K]
   float* s_psf_m = s_psf + static_cast<size_t>(a.nz) * 2 * K;       // [nz][2K] (mate)
-  // carry split: each output column's transmission at the middle of the slab
-  float4* smid = reinterpret_cast<float4*>(
-      reinterpret_cast<unsigned char*>(s_psf) +
-      round_up16(PSF && !PTAB ? sizeof(float) * static_cast<size_t>(a.nz) * 2 * K * (PAIR ? 2 : 1) : 0));  // [kTXC][32]
-
   cg::cluster_group cluster = cg::this_cluster();
   const int slab = static_cast<int>(cluster.block_rank());
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -861,12 +856,25 @@ __device__ __forceinline__ void project_item(const YgArgs& a, int cam, int mate,
   // walk: STEPS planes per barrier; iteration j uses buffers (j & 1) * STEPS + s,
   // rewritten at iteration j + 2 after the barrier of iteration j + 1
   // carry split: planes of the slab's first half (the backprojector's slab
-  // of twice the count that starts at zbeg)
+  // of twice the count that starts at zbeg); the slab-local transmission at
+  // the middle goes straight into its carry slot, where the merge adds the
+  // transmission of the slabs before (after the cluster barrier, which
+  // orders these writes before the merge's reads)
   const bool split = ATT && a.carry_out && a.carry_split;
   const int zhalf = (a.nz + 2 * nslabs - 1) / (2 * nslabs);
+  const int cslabs = split ? 2 * nslabs : nslabs;  // slabs of the carries
+  const size_t cstride = static_cast<size_t>(a.nx) * a.cy;
+  auto carry_at = [&](int o, int slot) {  // carry of output column o in `slot`
+    return a.carry_out + a.row0 + yb + (static_cast<size_t>(cam) * (cslabs + 1) * a.nx + x0 + o) * a.cy +
+           static_cast<size_t>(slot) * cstride;
+  };
   auto stash_mid = [&]() {
 #pragma unroll
-    for (int i = 0; i < kTXW; ++i) smid[(warp * kTXW + i) * 32 + lane] = kval(T[i], &cT[SCOMP ? 0 : i], 0, i);
+    for (int i = 0; i < kTXW; ++i) {
+      const int o = warp * kTXW + i;
+      if (x0 + o < a.nx && yok && lane_writes(a, yb))
+        *reinterpret_cast<float4*>(carry_at(o, 2 * slab + 1)) = kval(T[i], &cT[SCOMP ? 0 : i], 0, i);
+    }
   };
   auto walk = [&](auto mode) {
     constexpr int MODE = decltype(mode)::value;
@@ -946,27 +954,25 @@ __device__ __forceinline__ void project_item(const YgArgs& a, int cam, int mate,
   };
   // transmission carries for the backprojector (a.carry_out): the exclusive
   // prefix of the slab sums at every slab, then the column total
-  float* carry = ATT && a.carry_out ? a.carry_out + a.row0 + yb : nullptr;
-  const size_t cstride = static_cast<size_t>(a.nx) * a.cy;
+  const bool carry = ATT && a.carry_out;
 #pragma unroll
   for (int i = 0; i < kTXW; ++i) {
     const int o = warp * kTXW + i;
     const int x = x0 + o;
     if (o / per_rank != slab || x >= a.nx || !yok || !lane_writes(a, yb)) continue;
     float4 Pt = make_float4(0.f, 0.f, 0.f, 0.f), Tt = make_float4(0.f, 0.f, 0.f, 0.f);
-    const int cslabs = split ? 2 * nslabs : nslabs;  // slabs of the carries
-    float* cdst = carry ? carry + (static_cast<size_t>(cam) * (cslabs + 1) * a.nx + x) * a.cy : nullptr;
     for (int s = 0; s < nslabs; ++s) {
       const float4* rT = cluster.map_shared_rank(sT, s);
       const float4* rP = cluster.map_shared_rank(sP, s);
       const float4 ps = rP[o * 32 + lane];
       if (ATT) {
-        if (cdst) {
-          *reinterpret_cast<float4*>(cdst + (split ? 2 * s : s) * cstride) = Tt;
-          if (split) {
+        if (carry) {
+          *reinterpret_cast<float4*>(carry_at(o, split ? 2 * s : s)) = Tt;
+          if (split) {  // slab s's mid-slab transmission, from its CTA
+            float4* m = reinterpret_cast<float4*>(carry_at(o, 2 * s + 1));
             float4 mid = Tt;
-            add4(mid, cluster.map_shared_rank(smid, s)[o * 32 + lane]);
-            *reinterpret_cast<float4*>(cdst + (2 * s + 1) * cstride) = mid;
+            add4(mid, __ldcg(m));
+            *m = mid;
           }
         }
         fma4(Pt, exp_neg4(Tt), ps);
@@ -975,7 +981,7 @@ __device__ __forceinline__ void project_item(const YgArgs& a, int cam, int mate,
         add4(Pt, ps);
       }
     }
-    if (cdst) *reinterpret_cast<float4*>(cdst + cslabs * cstride) = Tt;
+    if (carry) *reinterpret_cast<float4*>(carry_at(o, cslabs)) = Tt;
     store(cam, x, Pt);
     if (PAIR && paired) {  // the mate's slabs from the far end: its column nx-1-x
       Pt = make_float4(0.f, 0.f, 0.f, 0.f);

@@ -68,16 +68,12 @@ int launch_project_R(const YgArgs& a_in, cudaStream_t st, int* slabs_used) {
   if (a.pslabs != 2 && a.pslabs != 4 && a.pslabs != 8 && a.pslabs != 16)
     a.pslabs = project_slabs(nunits * ntile, three && !bf16 && !pair ? 3 : 2, a.nz);
   // carry split: the slab's halves must be the backprojector's slabs of twice
-  // the count, with at most 8 of them; the mid-slab transmissions sit after
-  // the tile (16 KB per CTA)
+  // the count, with at most 8 of them
   auto split_ok = [&](int p) {
     return a.carry_out && a.mu && a.carry_split && 2 * p <= 8 &&
            (a.nz + p - 1) / p == 2 * ((a.nz + 2 * p - 1) / (2 * p));
   };
-  const size_t smem_plain = smem;
-  const size_t smem_split = round_up16(smem) + sizeof(float4) * kTXC * 32;
   a.carry_split = split_ok(a.pslabs) ? 1 : 0;
-  if (a.carry_split) smem = smem_split;
   // one cluster of a.pslabs CTAs per (unit, x-tile); 16 is a non-portable
   // cluster size: it falls back to 8 where the kernel cannot be resident so
   bool launch_err = false;
@@ -102,9 +98,6 @@ int launch_project_R(const YgArgs& a_in, cudaStream_t st, int* slabs_used) {
         cudaGetLastError();
         a.pslabs = 8;
         a.carry_split = split_ok(8) ? 1 : 0;
-        smem = a.carry_split ? smem_split : smem_plain;
-        cfg.dynamicSmemBytes = smem;
-        cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
       }
     }
     cfg.gridDim = dim3(nunits * ntile * a.pslabs);

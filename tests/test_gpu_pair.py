@@ -101,3 +101,33 @@ def test_pair_call_rejects_bad_arguments():
                                              0.0, 0.0, 1, 0, None) == 2
     assert L.nrgb_project_backproject_device(p, None, size, p, None, p, cams.ctypes.data_as(vp), csize, None, nopsf,
                                              0.0, 0.0, 1, 7, None) == 2
+
+
+@pytest.mark.parametrize("shape,ncam", [((64, 64, 64), 60), ((48, 40, 48), 9)])
+def test_pair_call_bf16_matches_separate_bf16_calls(shape, ncam):
+    """nrgb_project_backproject_device_bf16 (bfloat16 activity and mu) against
+    nrgb_project_device_bf16 + nrgb_backproject_device_bf16."""
+    L = _lib.load()
+    dev = torch.device("cuda", 0)
+    sp = vp(torch.cuda.current_stream(dev).cuda_stream)
+    nz, ny, nx = shape
+    act = torch.from_numpy(S.ellipsoid_phantom(shape, seed=5)).to(dev).to(torch.bfloat16)
+    mu = torch.from_numpy(S.mu_map(shape, seed=5)).to(dev).to(torch.bfloat16)
+    psf = S.gaussian_psf(7, nz, 0.5, 0.03)
+    cams = np.ascontiguousarray(S.cameras_about_y(ncam, 2.0)[1])
+    size = (ctypes.c_int * 3)(nx, ny, nz)
+    csize = (ctypes.c_int * 2)(ncam, 1)
+    psize = (ctypes.c_int * 3)(*psf.shape[::-1])
+    args = (cams.ctypes.data_as(vp), csize, psf.ctypes.data_as(vp), psize, 0.0, 0.0, 1)
+    s_ref = torch.empty((ncam, ny, nx), dtype=torch.float32, device=dev)
+    b_ref = torch.empty(shape, dtype=torch.float32, device=dev)
+    _call(L, L.nrgb_project_device_bf16, vp(act.data_ptr()), vp(mu.data_ptr()), size, vp(s_ref.data_ptr()), *args, sp)
+    _call(L, L.nrgb_backproject_device_bf16, vp(s_ref.data_ptr()), vp(mu.data_ptr()), size, vp(b_ref.data_ptr()),
+          *args, 0, sp)
+    s = torch.empty_like(s_ref)
+    b = torch.empty_like(b_ref)
+    _call(L, L.nrgb_project_backproject_device_bf16, vp(act.data_ptr()), vp(mu.data_ptr()), size, vp(s.data_ptr()),
+          None, vp(b.data_ptr()), *args, 0, sp)
+    torch.cuda.synchronize(dev)
+    assert _rel(s, s_ref) < TOL
+    assert _rel(b, b_ref) < TOL
