@@ -105,15 +105,17 @@ int project_host(const Problem& pb, const float* act, const float* att, float* s
   char* w = cv.take<char>(ws);
   cudaStream_t st = ds.stream;
   g_last_path = ((use_fused(pb) || use_fused_x(pb)) && act) ? 1 : 2;
-  if (use_fused(pb) && act && host_memory_readable()) {  // the layout kernels read the host arrays
+  const bool direct = use_fused(pb) && act && host_memory_readable();
+  if (direct) {  // the layout kernels read the host arrays and write the host sinogram
     d_act = const_cast<float*>(act);
     d_att = const_cast<float*>(att);
+    d_sino = sino;
   } else {
     if (act && (s = h2d(d_act, act, nvox, st)) != kOk) return finish(ds, s);
     if (att && (s = h2d(d_att, att, nvox, st)) != kOk) return finish(ds, s);
   }
   s = project_device(pb, d_act, d_att, d_sino, w, ws, &ds.staging, st);
-  if (s == kOk) s = d2h(sino, d_sino, nsino, st);
+  if (s == kOk && !direct) s = d2h(sino, d_sino, nsino, st);
   return finish(ds, s);
 }
 
@@ -133,15 +135,17 @@ int backproject_host(const Problem& pb, const float* sino, const float* att, flo
   char* w = cv.take<char>(ws);
   cudaStream_t st = ds.stream;
   g_last_path = (use_fused(pb) || use_fused_x(pb)) ? 1 : 2;
-  if (use_fused(pb) && host_memory_readable()) {  // the layout kernels read the host arrays
+  const bool direct = use_fused(pb) && host_memory_readable();
+  if (direct) {  // the layout kernels read the host arrays and write the host volume
     d_sino = const_cast<float*>(sino);
     d_att = const_cast<float*>(att);
+    d_out = out;
   } else {
     if ((s = h2d(d_sino, sino, nsino, st)) != kOk) return finish(ds, s);
     if (att && (s = h2d(d_att, att, nvox, st)) != kOk) return finish(ds, s);
   }
   s = backproject_device(pb, d_sino, d_att, d_out, w, ws, &ds.staging, st);
-  if (s == kOk) s = d2h(out, d_out, nvox, st);
+  if (s == kOk && !direct) s = d2h(out, d_out, nvox, st);
   return finish(ds, s);
 }
 
