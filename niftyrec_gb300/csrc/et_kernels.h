@@ -83,17 +83,6 @@ struct YgArgs {
   // Backprojector depth slabs (1..16): carries hold bslabs + 1 slots per
   // camera (every slab's exclusive prefix, then the column total).
   int bslabs = 16;
-  // Projector: non-null -> store the OSEM ratio y / p (y / ratio_eps where
-  // p < ratio_eps, after truncation) instead of p; ratio_y has the layout of
-  // the output ([ncam][nx][cy]).
-  const float* ratio_y = nullptr;
-  float ratio_eps = 0.0f;
-  // Backprojector (reference mode): non-null -> the last camera group's
-  // gather also truncates the finished numerator and applies the OSEM update
-  // update_x *= num / max(update_sens, update_eps) ([nz][nx][cy] each).
-  float* update_x = nullptr;
-  const float* update_sens = nullptr;
-  float update_eps = 0.0f;
   // Projector: non-null -> also write the transmission carries of its own
   // depth slabs ([ncam][pslabs + 1][nx][cy], the layout above with bslabs =
   // the projector's slab count; with units, at each unit's first camera).

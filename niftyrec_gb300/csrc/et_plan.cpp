@@ -81,9 +81,7 @@ void subset_units(const Plan& p, int subset, bool back, YgArgs* a) {
   a->nunits = cnt[i];
 }
 
-// ratio_y (column layout, fused plans): store the OSEM ratio y / p instead of p.
-int plan_project(Plan& p, int subset, const float* d_act, float* d_sino, int layout, int truncate, cudaStream_t st,
-                 const float* ratio_y = nullptr, float ratio_eps = 0.0f) {
+int plan_project(Plan& p, int subset, const float* d_act, float* d_sino, int layout, int truncate, cudaStream_t st) {
   int b, e;
   range(p, subset, &b, &e);
   const int n = e - b;
@@ -112,12 +110,6 @@ int plan_project(Plan& p, int subset, const float* d_act, float* d_sino, int lay
     a.psf_host = pb.psf_k ? pb.psf_sep.data() : nullptr;
     a.psf_k = pb.psf_k;
     a.truncate = truncate;
-    if (layout == kLayoutColumn) {
-      a.ratio_y = ratio_y;
-      a.ratio_eps = ratio_eps;
-    } else if (ratio_y) {
-      return kErrParameters;
-    }
     int s = yg_project(a, st);
     if (s != kOk) return s;
     if (layout == kLayoutNifti) return from_column(p.sino_c, d_sino, pb.nx, pb.ny, p.cy, n, 0, st);
@@ -146,11 +138,8 @@ int plan_project(Plan& p, int subset, const float* d_act, float* d_sino, int lay
   return s != kOk ? s : check();
 }
 
-// update_x (column layout, fused plans): the last gather also truncates the
-// numerator and applies the OSEM update to update_x with update_sens.
 int plan_backproject(Plan& p, int subset, const float* d_sino, float* d_out, int layout, int truncate,
-                     cudaStream_t st, int pipelined = 1, float* update_x = nullptr, const float* update_sens = nullptr,
-                     float update_eps = 0.0f) {
+                     cudaStream_t st, int pipelined = 1) {
   int b, e;
   range(p, subset, &b, &e);
   const int n = e - b;
@@ -183,17 +172,10 @@ int plan_backproject(Plan& p, int subset, const float* d_sino, float* d_out, int
     a.work = p.work;
     a.carry = p.carry ? p.carry + static_cast<size_t>(b) * yg_carry_slabs() * pb.nx * p.cy : nullptr;
     a.pipelined = pipelined;
-    const bool fuse_update = update_x && layout == kLayoutColumn && truncate;
-    if (update_x && !fuse_update) return kErrParameters;
-    if (fuse_update) {
-      a.update_x = update_x;
-      a.update_sens = update_sens;
-      a.update_eps = update_eps;
-    }
     int s = yg_backproject(a, st);
     if (s != kOk) return s;
     if (layout == kLayoutNifti) return from_column(p.out_c, d_out, pb.nx, pb.ny, p.cy, pb.nz, truncate, st);
-    if (truncate && !fuse_update) launch_truncate(d_out, static_cast<size_t>(pb.nz) * pb.nx * p.cy, st);
+    if (truncate) launch_truncate(d_out, static_cast<size_t>(pb.nz) * pb.nx * p.cy, st);
     return check();
   }
   if (layout != kLayoutNifti) return kErrParameters;
@@ -508,14 +490,6 @@ int nrgb_plan_osem_step(void* plan, int subset, float* d_activity, const float* 
   const int n = p->sub_begin[subset + 1] - p->sub_begin[subset];
   if (n <= 0) return kOk;
   const float* sens = p->sens + p->vol_elems * subset;
-  if (p->fused && p->osem_layout == kLayoutColumn) {
-    // column layout: the ratio in the projector's store, the update in the
-    // last gather (same roundings as the separate passes)
-    int s = plan_project(*p, subset, d_activity, p->osem_p, kLayoutColumn, 1, st, d_counts, epsilon);
-    if (s == kOk) s = plan_backproject(*p, subset, p->osem_p, p->osem_num, kLayoutColumn, 1, st, 1, d_activity, sens,
-                                       epsilon);
-    return s;
-  }
   int s = plan_project(*p, subset, d_activity, p->osem_p, p->osem_layout, 1, st);
   if (s == kOk) s = osem_ratio(d_counts, p->osem_p, p->plane_elems * n, epsilon, st);
   if (s == kOk) s = plan_backproject(*p, subset, p->osem_p, p->osem_num, p->osem_layout, 1, st);

@@ -406,10 +406,7 @@ __global__ void __launch_bounds__(32 * kW, 2)
 // out[Z][X][y] (+)= sum_g bilinear(temp[g], B_g * (X, y, Z)) with B_g the
 // camera's inverse matrix (ZYX order, -theta), emission-lib/_et.cpp:474-497.
 // With a.units, g runs over units and B_g is the unit's first camera's.
-// last (with a.update_x): the group completes the sum, which is truncated and
-// applied as the OSEM update (emission-lib/_et_array_interface.cpp:1036-1044).
-__global__ void __launch_bounds__(32 * kGatherWarps) k_gather_yg(const YgArgs a, int c0, int gcount, int first,
-                                                                 int last) {
+__global__ void __launch_bounds__(32 * kGatherWarps) k_gather_yg(const YgArgs a, int c0, int gcount, int first) {
   constexpr int C = kGatherCols;
   extern __shared__ Tap s_gtap[];  // [kGatherWarps][C * group]
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -443,28 +440,9 @@ __global__ void __launch_bounds__(32 * kGatherWarps) k_gather_yg(const YgArgs a,
   for (int i = 0; i < C; ++i) {
     const int X = X0 + i;
     if (X >= a.nx) continue;
-    const size_t idx = (static_cast<size_t>(Z) * a.nx + X) * a.cy + a.row0 + yb;
-    float4* dst = reinterpret_cast<float4*>(a.out + idx);
+    float4* dst = reinterpret_cast<float4*>(a.out + (static_cast<size_t>(Z) * a.nx + X) * a.cy + a.row0 + yb);
     if (!first) add4(acc[i], *dst);
-    if (last && a.update_x) {
-      float4 num = acc[i];
-      num.x = fmaxf(num.x, 0.f);
-      num.y = fmaxf(num.y, 0.f);
-      num.z = fmaxf(num.z, 0.f);
-      num.w = fmaxf(num.w, 0.f);
-      *dst = num;
-      float4 d = ldg4(a.update_sens + idx);
-      const float e = a.update_eps;
-      float4* xp = reinterpret_cast<float4*>(a.update_x + idx);
-      float4 x = *xp;
-      x.x = __fmul_rn(x.x, __fdiv_rn(num.x, d.x < e ? e : d.x));
-      x.y = __fmul_rn(x.y, __fdiv_rn(num.y, d.y < e ? e : d.y));
-      x.z = __fmul_rn(x.z, __fdiv_rn(num.z, d.z < e ? e : d.z));
-      x.w = __fmul_rn(x.w, __fdiv_rn(num.w, d.w < e ? e : d.w));
-      *xp = x;
-    } else {
-      *dst = acc[i];
-    }
+    *dst = acc[i];
   }
 }
 
@@ -697,8 +675,6 @@ Pipe* pipe_for_current_device() {
 int yg_backproject(const YgArgs& a_in, cudaStream_t st) {
   YgArgs a = a_in;
   if (a.bslabs < 1 || a.bslabs > kSlabsB) return kErrParameters;
-  // the fused OSEM update rides on the reference mode's last gather
-  if (a.update_x && (a.gradient || a.back_mode == kBackAdjoint || !a.update_sens)) return kErrParameters;
   const int R = a.psf ? (a.psf_k - 1) / 2 : 0;
   // mirror units: float32 mu, or bfloat16 mu in reference mode
   const bool pair = !a.gradient && a.units && a.nunits > 0 &&
@@ -756,8 +732,7 @@ int yg_backproject(const YgArgs& a_in, cudaStream_t st) {
         int st_ = spread(b, c0, gcount);
         if (st_ != kOk) return st_;
         NRGB_LAUNCH_SCOPE("k_gather_yg", st);
-        k_gather_yg<<<gblocks, 32 * kGatherWarps, gsmem, st>>>(b, c0, gcount, c0 == 0 ? 1 : 0,
-                                                               c0 + gcount == nunits ? 1 : 0);
+        k_gather_yg<<<gblocks, 32 * kGatherWarps, gsmem, st>>>(b, c0, gcount, c0 == 0 ? 1 : 0);
       }
     }
     return cudaGetLastError() == cudaSuccess ? kOk : kErrKernel;
@@ -781,8 +756,7 @@ int yg_backproject(const YgArgs& a_in, cudaStream_t st) {
       cudaStreamWaitEvent(pp->aux, pp->spread_done[slot], 0);
       {
         NRGB_LAUNCH_SCOPE("k_gather_yg", pp->aux);
-        k_gather_yg<<<gblocks, 32 * kGatherWarps, gsmem, pp->aux>>>(b, c0, gcount, c0 == 0 ? 1 : 0,
-                                                                    c0 + gcount == nunits ? 1 : 0);
+        k_gather_yg<<<gblocks, 32 * kGatherWarps, gsmem, pp->aux>>>(b, c0, gcount, c0 == 0 ? 1 : 0);
       }
       cudaEventRecord(pp->gather_done[slot], pp->aux);
     }

@@ -941,16 +941,7 @@ __device__ __forceinline__ void project_item(const YgArgs& a, int cam, int mate,
       Pt.z = fmaxf(Pt.z, 0.f);
       Pt.w = fmaxf(Pt.w, 0.f);
     }
-    const size_t idx = (static_cast<size_t>(c) * a.nx + x) * a.cy + a.row0 + yb;
-    if (a.ratio_y) {  // the OSEM ratio (emission-lib/_et_array_interface.cpp:1022-1028)
-      const float4 y = ldg4(a.ratio_y + idx);
-      const float e = a.ratio_eps;
-      Pt.x = Pt.x < e ? __fdiv_rn(y.x, e) : __fdiv_rn(y.x, Pt.x);
-      Pt.y = Pt.y < e ? __fdiv_rn(y.y, e) : __fdiv_rn(y.y, Pt.y);
-      Pt.z = Pt.z < e ? __fdiv_rn(y.z, e) : __fdiv_rn(y.z, Pt.z);
-      Pt.w = Pt.w < e ? __fdiv_rn(y.w, e) : __fdiv_rn(y.w, Pt.w);
-    }
-    *reinterpret_cast<float4*>(a.out + idx) = Pt;
+    *reinterpret_cast<float4*>(a.out + (static_cast<size_t>(c) * a.nx + x) * a.cy + a.row0 + yb) = Pt;
   };
   // transmission carries for the backprojector (a.carry_out): the exclusive
   // prefix of the slab sums at every slab, then the column total

@@ -35,8 +35,10 @@ namespace {
 // is drawn by the cluster's first thread and read by the other CTAs from its
 // shared memory (double-buffered: the slot of item i is rewritten at item i+2,
 // after the barriers of item i+1).
-template <int R, bool PSF, bool ATT>
-__global__ void __cluster_dims__(kSlabsP, 1, 1) __launch_bounds__(32 * kW, 2)
+// CTAS: CTAs per SM the kernel is built for (3: 80 registers and more warps to
+// hide the gathers' latency, where three tiles fit in shared memory; else 2).
+template <int R, bool PSF, bool ATT, int CTAS>
+__global__ void __cluster_dims__(kSlabsP, 1, 1) __launch_bounds__(32 * kW, CTAS)
     k_project_batch_yg(const BatchStepDesc* __restrict__ descs, const BatchSel sel, int* __restrict__ counter) {
   extern __shared__ __align__(16) unsigned char smem[];
   __shared__ int s_item[2];
@@ -81,22 +83,26 @@ int project_by_radius(int R, const YgArgs& a, cudaStream_t st, int* slabs_used) 
   }
 }
 
-// Persistent grid: two CTAs per SM, whole clusters.
-int batch_clusters() { return sm_count() * 2 / kSlabsP; }
+// Persistent grid: `ctas` CTAs per SM, whole clusters.
+int batch_clusters(int ctas) { return sm_count() * ctas / kSlabsP; }
 
 template <int R, bool PSF>
 int launch_project_batch_R(const BatchStepDesc* d, const BatchSel& sel, bool att, int max_nz, int* counter,
                            cudaStream_t st) {
   const size_t smem = tile_smem_bytes<R>(PSF ? max_nz : 0);
-  auto go = [&](auto k) {
+  const bool three = 3 * (smem + kYBufBytes + 1024) <= 228 * 1024;
+  auto go = [&](auto k, int ctas) {
     cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
     NRGB_LAUNCH_SCOPE("k_project_batch_yg", st);
-    k<<<batch_clusters() * kSlabsP, 32 * kW, smem, st>>>(d, sel, counter);
+    k<<<batch_clusters(ctas) * kSlabsP, 32 * kW, smem, st>>>(d, sel, counter);
   };
-  if (att)
-    go(k_project_batch_yg<R, PSF, true>);
-  else
-    go(k_project_batch_yg<R, PSF, false>);
+  if (att) {
+    if (three) go(k_project_batch_yg<R, PSF, true, 3>, 3);
+    else go(k_project_batch_yg<R, PSF, true, 2>, 2);
+  } else {
+    if (three) go(k_project_batch_yg<R, PSF, false, 3>, 3);
+    else go(k_project_batch_yg<R, PSF, false, 2>, 2);
+  }
   return cudaGetLastError() == cudaSuccess ? kOk : kErrKernel;
 }
 
