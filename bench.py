@@ -51,7 +51,7 @@ P_ANGLE = N ** 3 * 8 + N ** 2 * 4
 B_ANGLE = N ** 3 * 12 + N ** 2 * 4
 PAIR_BYTES = NCAM * (P_ANGLE + B_ANGLE)  # 5,048,893,440
 FLUSH_BYTES = 256 << 20  # > 129 MB L2
-DOMINANT = "k_project_yg"  # the pair's largest kernel (per-kernel pass); timed inside the timed region
+DOMINANT = "k_project_yg"  # the pair's largest kernel (serialised ncu launch list); timed inside the timed region
 
 
 def algorithmic_bytes(kernel: str, launches: int, ncam_total: int) -> float:
@@ -335,7 +335,9 @@ def run_ours(args):
 
     # rooflines of the kernels with algorithmic bytes: the projector timed in the
     # timed region, the others in the per-kernel pass; `roofline` is the
-    # dominant kernel's (the largest total of the per-kernel pass)
+    # dominant kernel's: the projector, the largest share of the serialised ncu
+    # launch list (the two camera groups' spreads run concurrently on two
+    # streams, so their event durations include each other's)
     peak, peak_kind = measured_peak()
     rooflines = {}
     for name in (prof or {}):
@@ -352,10 +354,7 @@ def run_ours(args):
                            "bytes_per_launch": per_launch_bytes, "avg_launch_ms": round(avg_s * 1e3, 4),
                            "timed_in": "timed region" if src is prof_dom else "per-kernel pass",
                            "traffic": committed_traffic(name)}
-    roof = None
-    if prof:
-        dom = max(prof, key=lambda k: prof[k][1])
-        roof = rooflines.get(dom)
+    roof = rooflines.get(DOMINANT)
     kernels = {k: {"launches": v[0], "ms_total": round(v[1], 3)} for k, v in (prof or {}).items()}
 
     out = {
@@ -375,8 +374,10 @@ def run_ours(args):
         "roofline": roof,
         "rooflines": rooflines,
         "rooflines_note": "algorithmic bytes per camera angle as the reference moves them (a mirror unit serves "
-                          "two angles from one pass); the gather, an intermediate that overlaps the spread, is "
-                          "left out (its one-kernel ncu summary is under profiles/)",
+                          "two angles from one pass); the spreads of the two camera groups overlap each other "
+                          "(two streams), so their per-kernel-pass durations include the sharing; the gather, an "
+                          "intermediate that overlaps the spread, is left out (its one-kernel ncu summary is under "
+                          "profiles/)",
         "kernels": kernels,
         "kernels_pass": {"ms_per_step": round(sum(ms_prof) / len(ms_prof), 4),
                          "note": "separate pass with CUDA events around every launch"},

@@ -406,6 +406,7 @@ __global__ void __launch_bounds__(32 * kW, 2)
 // out[Z][X][y] (+)= sum_g bilinear(temp[g], B_g * (X, y, Z)) with B_g the
 // camera's inverse matrix (ZYX order, -theta), emission-lib/_et.cpp:474-497.
 // With a.units, g runs over units and B_g is the unit's first camera's.
+template <int U>
 __global__ void __launch_bounds__(32 * kGatherWarps) k_gather_yg(const YgArgs a, int c0, int gcount, int first) {
   constexpr int C = kGatherCols;
   extern __shared__ Tap s_gtap[];  // [kGatherWarps][C * group]
@@ -427,11 +428,25 @@ __global__ void __launch_bounds__(32 * kGatherWarps) k_gather_yg(const YgArgs a,
   if (!lane_rows_ok(a, yb) || !lane_writes(a, yb)) return;
   const size_t vol = static_cast<size_t>(a.nz) * a.nx * a.cs;
   // camera outer, columns inner: neighbouring accumulator columns of one
-  // camera share footprint columns, which then hit in L1
+  // camera share footprint columns, which then hit in L1; U cameras' loads
+  // in flight at once (every footprint offset is inside its volume, see
+  // make_tap), added in camera order
   float4 acc[C];
 #pragma unroll
   for (int i = 0; i < C; ++i) acc[i] = make_float4(0.f, 0.f, 0.f, 0.f);
-  for (int g = 0; g < gcount; ++g) {
+  int g = 0;
+  for (; g + U <= gcount; g += U) {
+    float4 v[U][C];
+#pragma unroll
+    for (int u = 0; u < U; ++u)
+#pragma unroll
+      for (int i = 0; i < C; ++i) v[u][i] = sample4_loaded(a.temp + vol * (g + u), tap[(g + u) * C + i], yb);
+#pragma unroll
+    for (int u = 0; u < U; ++u)
+#pragma unroll
+      for (int i = 0; i < C; ++i) add4(acc[i], v[u][i]);
+  }
+  for (; g < gcount; ++g) {
     const float* src = a.temp + vol * g;
 #pragma unroll
     for (int i = 0; i < C; ++i) add4(acc[i], sample4(src, tap[g * C + i], yb, true));
@@ -444,6 +459,11 @@ __global__ void __launch_bounds__(32 * kGatherWarps) k_gather_yg(const YgArgs a,
     if (!first) add4(acc[i], *dst);
     *dst = acc[i];
   }
+}
+
+void launch_gather(const YgArgs& b, int c0, int gcount, int blocks, size_t smem, cudaStream_t st) {
+  NRGB_LAUNCH_SCOPE("k_gather_yg", st);
+  k_gather_yg<kGatherUnits><<<blocks, 32 * kGatherWarps, smem, st>>>(b, c0, gcount, c0 == 0 ? 1 : 0);
 }
 
 // The separated PSF of a.nz planes as a kernel-parameter table, or null when
@@ -644,7 +664,7 @@ namespace {
 // from several host threads, e.g. plans on their own streams).
 struct Pipe {
   std::mutex mu;
-  cudaStream_t aux = nullptr;
+  cudaStream_t aux = nullptr, aux2 = nullptr;
   cudaEvent_t fork = nullptr, join = nullptr, spread_done[2] = {nullptr, nullptr},
               gather_done[2] = {nullptr, nullptr};
 };
@@ -657,7 +677,9 @@ Pipe* pipe_for_current_device() {
   std::lock_guard<std::mutex> lk(mu);
   Pipe& p = pipes[dev];
   if (!p.aux) {
-    if (cudaStreamCreateWithFlags(&p.aux, cudaStreamNonBlocking) != cudaSuccess) return nullptr;
+    if (cudaStreamCreateWithFlags(&p.aux, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaStreamCreateWithFlags(&p.aux2, cudaStreamNonBlocking) != cudaSuccess)
+      return nullptr;
     cudaEvent_t* evs[] = {&p.fork, &p.join, &p.spread_done[0], &p.spread_done[1], &p.gather_done[0],
                           &p.gather_done[1]};
     for (cudaEvent_t* e : evs)
@@ -668,10 +690,12 @@ Pipe* pipe_for_current_device() {
 
 }  // namespace
 
-// Per row window and camera group: spread on the caller's stream, gather on
-// a second stream; step g (over all windows' groups) uses scratch slot g % 2,
-// so the spread of step g+1 runs while the gather of step g reads the other
-// slot.
+// Per row window and camera group: step g (over all windows' groups) uses
+// scratch slot g % 2 and spreads on the caller's stream (even g) or a second
+// spread stream (odd g), its gather following on a gather stream.  The
+// spread of step g+1 thus starts while step g's last wave of CTAs drains (a
+// 30-unit spread at 128^3 is 3.2 waves on 152 SMs) and runs beside the
+// gather of step g; a slot is spread again only after its gather.
 int yg_backproject(const YgArgs& a_in, cudaStream_t st) {
   YgArgs a = a_in;
   if (a.bslabs < 1 || a.bslabs > kSlabsB) return kErrParameters;
@@ -703,10 +727,11 @@ int yg_backproject(const YgArgs& a_in, cudaStream_t st) {
   }
   if (a.sino_ready) cudaStreamWaitEvent(st, static_cast<cudaEvent_t>(a.sino_ready), 0);
   a.group = group;
-  auto spread = [&](const YgArgs& b, int c0, int gcount) {
-    if (a.gradient) return yg_grad_spread(b, c0, gcount, st);
-    return pair ? spread_pair_by_radius<false>(R, b, c0, gcount, st) : spread_by_radius(R, b, c0, gcount, st);
+  auto spread_on = [&](const YgArgs& b, int c0, int gcount, cudaStream_t ss) {
+    if (a.gradient) return yg_grad_spread(b, c0, gcount, ss);
+    return pair ? spread_pair_by_radius<false>(R, b, c0, gcount, ss) : spread_by_radius(R, b, c0, gcount, ss);
   };
+  auto spread = [&](const YgArgs& b, int c0, int gcount) { return spread_on(b, c0, gcount, st); };
   if (a.back_mode == kBackAdjoint && !a.gradient) {
     // transpose of the projector: one launch per window over all cameras,
     // scattered straight into the zeroed accumulator
@@ -722,7 +747,8 @@ int yg_backproject(const YgArgs& a_in, cudaStream_t st) {
   const int nchunk = (a.nx + kGatherCols - 1) / kGatherCols;
   const int gblocks = (nchunk * a.nz + kGatherWarps - 1) / kGatherWarps;
   const size_t gsmem = sizeof(Tap) * kGatherWarps * kGatherCols * group;
-  cudaFuncSetAttribute(k_gather_yg, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(gsmem));
+  cudaFuncSetAttribute(k_gather_yg<kGatherUnits>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                       static_cast<int>(gsmem));
   if (!a.pipelined) {
     for (const Window& w : wins) {
       YgArgs b = windowed(a, w);
@@ -731,8 +757,7 @@ int yg_backproject(const YgArgs& a_in, cudaStream_t st) {
         const int gcount = std::min(group, nunits - c0);
         int st_ = spread(b, c0, gcount);
         if (st_ != kOk) return st_;
-        NRGB_LAUNCH_SCOPE("k_gather_yg", st);
-        k_gather_yg<<<gblocks, 32 * kGatherWarps, gsmem, st>>>(b, c0, gcount, c0 == 0 ? 1 : 0);
+        launch_gather(b, c0, gcount, gblocks, gsmem, st);
       }
     }
     return cudaGetLastError() == cudaSuccess ? kOk : kErrKernel;
@@ -742,22 +767,21 @@ int yg_backproject(const YgArgs& a_in, cudaStream_t st) {
   std::lock_guard<std::mutex> pipe_lock(pp->mu);
   cudaEventRecord(pp->fork, st);
   cudaStreamWaitEvent(pp->aux, pp->fork, 0);
+  cudaStreamWaitEvent(pp->aux2, pp->fork, 0);
   int gi = 0;
   for (const Window& w : wins) {
     YgArgs b = windowed(a, w);
     for (int c0 = 0; c0 < nunits; c0 += group, ++gi) {
       const int gcount = std::min(group, nunits - c0);
       const int slot = gi & 1;
+      cudaStream_t ss = slot ? pp->aux2 : st;
       b.temp = slot0 + vol * group * slot;
-      if (gi >= 2) cudaStreamWaitEvent(st, pp->gather_done[slot], 0);
-      int st_ = spread(b, c0, gcount);
+      if (gi >= 2) cudaStreamWaitEvent(ss, pp->gather_done[slot], 0);
+      int st_ = spread_on(b, c0, gcount, ss);
       if (st_ != kOk) return st_;
-      cudaEventRecord(pp->spread_done[slot], st);
+      cudaEventRecord(pp->spread_done[slot], ss);
       cudaStreamWaitEvent(pp->aux, pp->spread_done[slot], 0);
-      {
-        NRGB_LAUNCH_SCOPE("k_gather_yg", pp->aux);
-        k_gather_yg<<<gblocks, 32 * kGatherWarps, gsmem, pp->aux>>>(b, c0, gcount, c0 == 0 ? 1 : 0);
-      }
+      launch_gather(b, c0, gcount, gblocks, gsmem, pp->aux);
       cudaEventRecord(pp->gather_done[slot], pp->aux);
     }
   }

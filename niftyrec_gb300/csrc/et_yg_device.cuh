@@ -53,6 +53,7 @@ constexpr int kCarrySlots = kSlabsB + 1;  // carries per camera: slab prefixes, 
 constexpr int kCarryCols = 64 / kSlabsB;  // columns per CTA of the carry pass (32 KB of slab sums)
 constexpr int kGatherWarps = 4;   // warps per CTA of the inverse-rotation gather
 constexpr int kGatherCols = 2;    // accumulator columns per warp in the gather
+constexpr int kGatherUnits = 2;   // scratch volumes whose loads a gather warp has in flight at once
 constexpr unsigned kFull = 0xffffffffu;
 
 __host__ __device__ constexpr size_t round_up16(size_t b) { return (b + 15) / 16 * 16; }
@@ -124,6 +125,22 @@ __device__ __forceinline__ float4 sample4(const V* __restrict__ base, const Tap&
   r.z = fmaf(d.z, t.w11, fmaf(c.z, t.w01, fmaf(b.z, t.w10, a.z * t.w00)));
   r.w = fmaf(d.w, t.w11, fmaf(c.w, t.w01, fmaf(b.w, t.w10, a.w * t.w00)));
   return r;
+}
+
+// sample4 for a lane whose rows are inside the column (yok) without the
+// branch on t.any: the four corner loads are always issued (a footprint's
+// offsets stay inside the volume: clamped corners have zero weight and
+// offset deltas), so loads of several footprints can be in flight together;
+// the value is zero without any valid corner, as in sample4.
+__device__ __forceinline__ float4 sample4_loaded(const float* __restrict__ base, const Tap& t, int yb) {
+  const float* p = base + t.off + yb;
+  const float4 a = ldg4(p), b = ldg4(p + t.dx), c = ldg4(p + t.dz), d = ldg4(p + t.dx + t.dz);
+  float4 r;
+  r.x = fmaf(d.x, t.w11, fmaf(c.x, t.w01, fmaf(b.x, t.w10, a.x * t.w00)));
+  r.y = fmaf(d.y, t.w11, fmaf(c.y, t.w01, fmaf(b.y, t.w10, a.y * t.w00)));
+  r.z = fmaf(d.z, t.w11, fmaf(c.z, t.w01, fmaf(b.z, t.w10, a.z * t.w00)));
+  r.w = fmaf(d.w, t.w11, fmaf(c.w, t.w01, fmaf(b.w, t.w10, a.w * t.w00)));
+  return t.any ? r : make_float4(0.f, 0.f, 0.f, 0.f);
 }
 
 __device__ __forceinline__ float comp(const float4& v, int c) { return c == 0 ? v.x : c == 1 ? v.y : c == 2 ? v.z : v.w; }

@@ -138,10 +138,10 @@ def main(argv=None):
 
     def run_pair():
         sp = vp(stream.cuda_stream)
-        if a.op == "pair" and not a.bf16:
-            st = L.nrgb_project_backproject_device(vp(t_act.data_ptr()), mu_p, size, vp(t_sino.data_ptr()), None,
-                                                   vp(t_bk.data_ptr()), cams.ctypes.data_as(vp), csize, psf_p, psize,
-                                                   0.0, 0.0, 1, a.mode, sp)
+        if a.op == "pair":
+            fn = L.nrgb_project_backproject_device_bf16 if a.bf16 else L.nrgb_project_backproject_device
+            st = fn(vp(t_act.data_ptr()), mu_p, size, vp(t_sino.data_ptr()), None, vp(t_bk.data_ptr()),
+                    cams.ctypes.data_as(vp), csize, psf_p, psize, 0.0, 0.0, 1, a.mode, sp)
             assert st == 0, st
             return
         if a.op in ("project", "pair", "pair2"):
