@@ -311,6 +311,12 @@ def run_ours(args):
     pair(mode=1)
     ms_adj, _, _ = timed(max(3, args.steps // 2), mode=1)
     adjoint = world * 1000.0 / reduce_max(sum(ms_adj) / len(ms_adj), world)
+    # the same in the deterministic form (group scratch + transposed gather)
+    L.nrgb_set_deterministic(1)
+    pair(mode=1)
+    ms_det, _, _ = timed(max(3, args.steps // 2), mode=1)
+    L.nrgb_set_deterministic(0)
+    adjoint_det = world * 1000.0 / reduce_max(sum(ms_det) / len(ms_det), world)
 
     grad = None if args.no_grad else grad_compare(L, t_act, t_mu, t_sino, t_bk, cams, psf, stream, flush, dev)
 
@@ -368,6 +374,7 @@ def run_ours(args):
         "separate_calls_pairs_per_s": round(separate, 3),
         "plain_pairs_per_s": round(plain, 3),
         "adjoint_backprojector_pairs_per_s": round(adjoint, 3),
+        "adjoint_deterministic_pairs_per_s": round(adjoint_det, 3),
         "vs_plain": round(value / plain, 4),
         "pair_hbm": {"bytes_per_pair": PAIR_BYTES, "achieved_gbs": round(PAIR_BYTES * value / world / 1e9, 1),
                      "frac_of_peak": round(PAIR_BYTES * value / world / 1e9 / peak, 4), "peak_source": peak_kind},

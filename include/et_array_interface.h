@@ -386,6 +386,19 @@ int nrgb_get_project_slabs(int nx, int ny, int nz, int ncam);
  * from its own matrix, as the reference.  Applies to calls made afterwards. */
 int nrgb_set_mirror_pairs(int on);
 int nrgb_get_mirror_pairs(void);
+/* Deterministic gradients (no counterpart in the reference).  With on = 1 the
+ * exact-transpose backprojector (back_mode 1) and the exact d/dmu
+ * (nrgb_attenuation_grad_device) on the fused gantry kernels write their
+ * rotated-frame values into camera-group scratch volumes and sum them with a
+ * transposed bilinear gather in a fixed order, so repeated calls give
+ * bit-identical results; 0 (the default) scatters with vector reductions
+ * (faster, summation order varies between runs at the float rounding level).
+ * Cameras off the gantry forms keep the atomic trilinear scatter of the
+ * general path.  The reference-mode backprojector, the projector and the
+ * OSEM/MLEM steps are deterministic either way.  Applies to calls made
+ * afterwards (and to plans made afterwards). */
+int nrgb_set_deterministic(int on);
+int nrgb_get_deterministic(void);
 /* Host-side introspection (no counterpart in the reference; no GPU needed).
  * nrgb_mirror_units: the {camera, mate} pairs (mate -1 when unpaired) the
  * fused kernels form for this camera table and volume size {nx, ny, nz};

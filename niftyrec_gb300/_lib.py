@@ -96,6 +96,8 @@ PROTOTYPES = {
     "nrgb_get_project_slabs": (_I, [_I, _I, _I, _I]),
     "nrgb_set_mirror_pairs": (_I, [_I]),
     "nrgb_get_mirror_pairs": (_I, []),
+    "nrgb_set_deterministic": (_I, [_I]),
+    "nrgb_get_deterministic": (_I, []),
     "nrgb_nifti_info": (_I, [ctypes.c_char_p, _PI]),
     "nrgb_nifti_read": (_I, [ctypes.c_char_p, _P, ctypes.c_longlong]),
     "nrgb_nifti_write": (_I, [ctypes.c_char_p, _P, _PI]),

@@ -9,6 +9,11 @@ projector with depth-dependent PSF and attenuation.  Its backward pass uses
 * d/d(mu): nrgb_attenuation_grad_device, which recomputes the depth scan of
   every ray instead of storing per-angle transmission.
 
+Both sum rotated-frame values into the volume with vector reductions, whose
+order varies between runs; ``set_deterministic(True)`` switches the fused
+gantry kernels to a scratch + transposed-gather form with a fixed order
+(bit-identical gradients from run to run).
+
 Tensors are CUDA float32 in nifti memory order: volumes (nz, ny, nx),
 sinograms (n_cameras, ny, nx).  Cameras and PSF are numpy arrays (see
 niftyrec_gb300.array_api for the conventions).
@@ -22,6 +27,15 @@ import numpy as np
 from ._lib import NiftyRecError, load
 
 _vp = ctypes.c_void_p
+
+
+def set_deterministic(on=True):
+    """Deterministic exact-transpose backprojection and d/dmu (library-wide,
+    for calls made afterwards); returns the previous setting."""
+    L = load()
+    prev = bool(L.nrgb_get_deterministic())
+    L.nrgb_set_deterministic(1 if on else 0)
+    return prev
 
 
 def _cams(cameras):

@@ -944,7 +944,10 @@ int backproject_device_call(const float* d_sinogram, const float* d_attenuation,
   if (!size || !cameras || !cameras_size || !d_sinogram || !d_out || (mode != kBackReference && mode != kBackAdjoint))
     return kErrParameters;
   Cameras cc;
-  const int csz[3] = {size[0], size[1], size[0]};
+  // camera centres: the reference backprojector's {size0, size1, size0} rule;
+  // the exact transpose of the projector takes the projector's (the volume
+  // size), which differ when nz != nx
+  const int csz[3] = {size[0], size[1], mode == kBackAdjoint ? size[2] : size[0]};
   int s = expand_cameras(cameras, cameras_size[0], cameras_size[1], csz, &cc);
   if (s != kOk) return s;
   Problem pb;
@@ -976,9 +979,10 @@ int pair_device_call(const float* d_activity, const float* d_attenuation, const 
       (mode != kBackReference && mode != kBackAdjoint))
     return kErrParameters;
   // camera centres: the projector's from the volume size, the
-  // backprojector's with the reference's {size0, size1, size0} rule
+  // backprojector's with the reference's {size0, size1, size0} rule (the
+  // exact transpose: the projector's)
   Cameras cc, cb;
-  const int csz[3] = {size[0], size[1], size[0]};
+  const int csz[3] = {size[0], size[1], mode == kBackAdjoint ? size[2] : size[0]};
   int s = expand_cameras(cameras, cameras_size[0], cameras_size[1], size, &cc);
   if (s != kOk) return s;
   if ((s = expand_cameras(cameras, cameras_size[0], cameras_size[1], csz, &cb)) != kOk) return s;
@@ -1254,6 +1258,16 @@ int nrgb_set_mirror_pairs(int on) {
 }
 
 int nrgb_get_mirror_pairs(void) { return mirror_pairs(); }
+
+// Deterministic exact-transpose backprojection and d/dmu on the fused kernels
+// (group scratch + transposed gather): 1 on, 0 (default) vector reductions.
+int nrgb_set_deterministic(int on) {
+  NRGB_API("nrgb_set_deterministic");
+  set_deterministic(on);
+  return kOk;
+}
+
+int nrgb_get_deterministic(void) { return deterministic(); }
 
 // The mirror units the fused kernels would form for these cameras and this
 // volume (host only): {camera, mate} pairs, mate -1 when unpaired, in the

@@ -88,10 +88,13 @@ void set_tuned_project_slabs(int nx, int ny, int nz, int ncam, int slabs) {
 
 namespace {
 std::atomic<int> g_mirror_pairs{1};
+std::atomic<int> g_deterministic{0};
 }  // namespace
 
 void set_mirror_pairs(int on) { g_mirror_pairs.store(on ? 1 : 0); }
 int mirror_pairs() { return g_mirror_pairs.load(); }
+void set_deterministic(int on) { g_deterministic.store(on ? 1 : 0); }
+int deterministic() { return g_deterministic.load(); }
 
 int make_problem(int nx, int ny, int nz, const Cameras& cams, const float* psf, const int* psf_size, float bg,
                  float bg_att, int truncate, Problem* out) {
@@ -113,6 +116,7 @@ int make_problem(int nx, int ny, int nz, const Cameras& cams, const float* psf, 
   pb.bg = bg;
   pb.bg_att = bg_att;
   pb.truncate = truncate;
+  pb.det = deterministic();
   pb.group = tuned_group(nx, ny, nz, cams.n);
   pb.pslabs = tuned_project_slabs(nx, ny, nz, cams.n);
   if (psf) {
@@ -438,6 +442,7 @@ int backproject_device(const Problem& pb, const float* d_sino, const float* d_at
     a.sino = d_sino;
     a.out = d_out;
     a.back_mode = pb.back_mode;
+    a.det = pb.det;
     a.group = std::max(1, std::min(pb.group, pb.cams.n));
     a.work = cx.take<float>(yg_backproject_workspace(pb.ny, pb.nx, pb.nz, pb.cams.n, a.group) / sizeof(float));
     if (!a.work) return kErrAllocGpu;
@@ -493,6 +498,7 @@ int backproject_device(const Problem& pb, const float* d_sino, const float* d_at
     a.psf_k = pb.psf_k;
     a.truncate = pb.truncate;
     a.back_mode = pb.back_mode;
+    a.det = pb.det;
     a.group = group;
     a.work = slab;
     if ((s = yg_backproject(a, st)) != kOk) return s;
@@ -593,16 +599,31 @@ int pair_device(const Problem& pb, const Problem& pb_back, const float* d_act, c
   b.sino = in_c;
   b.out = out_c;
   b.back_mode = pb.back_mode;
+  b.det = pb.det;
   b.group = group;
   b.carry = d_att ? work : nullptr;
   b.work = work + (d_att ? carry_n : 0);
   int slabs = 0;
   if ((s = yg_project(a, st, &slabs)) != kOk) return s;
   if (d_att && (slabs < 1 || slabs + 1 > yg_carry_slabs())) return kErrKernel;
-  if ((s = from_column(sino_c, d_sino, pb.nx, pb.ny, cy, pb.cams.n, 0, st)) != kOk) return s;
+  // the caller's projection (nifti order) is written on a side stream while
+  // the backprojector reads the column-layout copy
+  SideStream* side = side_for_current_device();
+  std::unique_lock<std::mutex> side_lock;
+  if (side) {
+    side_lock = std::unique_lock<std::mutex>(side->mu);
+    cudaEventRecord(side->fork, st);
+    cudaStreamWaitEvent(side->stream, side->fork, 0);
+    if ((s = from_column(sino_c, d_sino, pb.nx, pb.ny, cy, pb.cams.n, 0, side->stream)) != kOk) return s;
+    cudaEventRecord(side->done, side->stream);
+  } else if ((s = from_column(sino_c, d_sino, pb.nx, pb.ny, cy, pb.cams.n, 0, st)) != kOk) {
+    return s;
+  }
   if (d_bk_in && (s = to_column(d_bk_in, in_c, pb.nx, pb.ny, cy, pb.cams.n, st)) != kOk) return s;
   b.bslabs = d_att ? slabs : b.bslabs;
-  if ((s = yg_backproject(b, st)) != kOk) return s;
+  s = yg_backproject(b, st);
+  if (side) cudaStreamWaitEvent(st, side->done, 0);
+  if (s != kOk) return s;
   return check(from_column(out_c, d_bk, pb.nx, pb.ny, cy, pb.nz, pb.truncate, st));
 }
 
@@ -638,9 +659,13 @@ int project_partial_device(const Problem& pb, const float* d_act, const float* d
 }
 
 size_t dmu_workspace(const Problem& pb) {
-  if (use_fused_x(pb) && pb.storage == kStorageF32) return general3_workspace(pb);  // fused needs less
+  if (use_fused_x(pb) && pb.storage == kStorageF32)  // the fused form's scratch, or the general path's volumes
+    return std::max(general3_workspace(pb),
+                    common_bytes(pb) + (pb.det ? yg_dmu_det_workspace(pb.ny, pb.nx, pb.nz, pb.cams.n, pb.group) : 0) +
+                        kSlack);
   if (use_fused(pb) && pb.storage == kStorageF32)
-    return common_bytes(pb) + sizeof(float) * (3 * col_n(pb) + sino_col_n(pb)) + 4 * 256;
+    return common_bytes(pb) + sizeof(float) * (3 * col_n(pb) + sino_col_n(pb)) + 4 * 256 +
+           (pb.det ? yg_dmu_det_workspace(pb.nx, pb.ny, pb.nz, pb.cams.n, pb.group) + kSlack : 0);
   return general3_workspace(pb);
 }
 
@@ -659,6 +684,12 @@ int dmu_device(const Problem& pb, const float* d_g, const float* d_act, const fl
     a.mu = d_att;
     a.sino = d_g;
     a.out = d_out;
+    if (pb.det) {
+      a.det = 1;
+      a.group = pb.group;
+      a.work = cx.take<float>(yg_dmu_det_workspace(a.nx, a.ny, a.nz, a.ncam, a.group) / sizeof(float));
+      if (!a.work) return kErrAllocGpu;
+    }
     return check(yg_dmu(a, st));
   }
   Carver cv(ws, ws_bytes);
@@ -690,6 +721,12 @@ int dmu_device(const Problem& pb, const float* d_g, const float* d_act, const fl
     a.psf = d_psf;
     a.psf_host = pb.psf_k ? pb.psf_sep.data() : nullptr;
     a.psf_k = pb.psf_k;
+    if (pb.det) {
+      a.det = 1;
+      a.group = pb.group;
+      a.work = cv.take<float>(yg_dmu_det_workspace(a.nx, a.ny, a.nz, a.ncam, a.group) / sizeof(float));
+      if (!a.work) return kErrAllocGpu;
+    }
     if ((s = yg_dmu(a, st)) != kOk) return s;
     return check(from_column(out_c, d_out, pb.nx, pb.ny, cy, pb.nz, 0, st));
   }

@@ -40,6 +40,10 @@ struct Problem {
   // path widens them to float32 first.
   int storage = kStorageF32;
   bool input_bf16 = false;
+  // Deterministic exact-transpose backprojection and d/dmu on the fused
+  // kernels (scratch + transposed gather instead of vector reductions); set
+  // from the library-wide switch when the problem is made.
+  int det = 0;
 };
 
 // Build a Problem; psf may be null.  psf_size = {kx, ky, planes}.  Returns
@@ -67,6 +71,8 @@ void set_tuned_project_slabs(int nx, int ny, int nz, int ncam, int slabs);
 // samples (1, the default) or every camera from its own matrix (0).
 void set_mirror_pairs(int on);
 int mirror_pairs();
+void set_deterministic(int on);
+int deterministic();
 
 // Pinned, double-buffered staging of the per-call parameters (camera
 // matrices, separated PSF): copies from pinned memory stay asynchronous,

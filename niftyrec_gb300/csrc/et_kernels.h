@@ -108,6 +108,12 @@ struct YgArgs {
   // instead (a.act and a.mu sampled, a.sino the camera planes; no carries,
   // no mirror units), then gathers it like the reference-mode backprojection.
   int gradient = 0;
+  // Non-zero (exact-transpose backprojector, d/dmu): deterministic form --
+  // the rotated-frame values go into the group scratch instead of vector
+  // reductions into a.out, and a transposed gather (fixed order) sums them.
+  int det = 0;
+  // d/dmu: first camera of the launch (scratch volume g = camera - cam0).
+  int cam0 = 0;
 };
 // Carry slots per camera of the backprojector's transmission carries (the
 // exclusive prefix of every depth slab, then the column total).
@@ -133,6 +139,12 @@ int yg_project(const YgArgs& a, cudaStream_t st, int* slabs_used = nullptr);
 // (column layouts: a.act, a.mu; a.sino = g [ncam][nx][cy]; a.out = the
 // gradient [nz][nx][cy], zeroed here); no backgrounds.
 int yg_dmu(const YgArgs& a, cudaStream_t st);
+// Work space of yg_dmu with a.det (one scratch slot of a camera group).
+size_t yg_dmu_det_workspace(int nx, int ny, int nz, int ncam, int group);
+// Deterministic transposed gather of scratch volumes a.temp[0 .. gcount) of
+// units (or cameras) c0 .. c0 + gcount - 1 into a.out (assigned when c0 == 0,
+// else added), rows of the window a describes.
+void yg_tgather(const YgArgs& a, int c0, int gcount, cudaStream_t st);
 int yg_backproject(const YgArgs& a, cudaStream_t st);
 // Spread of the reference attenuation gradient for cameras [c0, c0 + gcount)
 // into the scratch volumes a.temp (one row window: a.row0, a.ny, a.cs).

@@ -73,7 +73,9 @@ __global__ void __launch_bounds__(32 * kSlabsB) k_mu_carry_yg(const YgArgs a, in
 // ADJ: the exact transpose of the projector instead (not in the reference):
 // the PSF taps are flipped (correlation) and each output column is scattered
 // with the projector's own bilinear weights into the accumulator a.out
-// (vector reductions; all cameras in one launch, no scratch).
+// (vector reductions; all cameras in one launch, no scratch), or, with
+// a.det, written to the group scratch like the reference form for the
+// transposed gather k_tgather_yg (a fixed summation order).
 // CTAS: CTAs per SM the kernel is compiled for (3 where three tiles fit in
 // shared memory, for the float32 reference spread; else 2).
 // PTAB: the separated PSF comes from the kernel-parameter table `ptab`
@@ -113,7 +115,8 @@ __device__ __forceinline__ void spread_body(const YgArgs& a, int c0, const float
   }
   const CamRows cr = cam_rows(a.geom[cam].fwd);
   const size_t vol = static_cast<size_t>(a.nz) * a.nx * a.cs;  // one scratch volume
-  float* __restrict__ tmp = ADJ ? a.out + a.row0 : a.temp + vol * g;
+  const bool scatter = ADJ && !a.det;  // uniform over the launch
+  float* __restrict__ tmp = scatter ? a.out + a.row0 : a.temp + vol * g;
   const float* __restrict__ srow = a.sino + static_cast<size_t>(cam) * a.nx * a.cy + a.row0;
 
   float4 Tc[TS::kOwn], cTc[TS::kOwn];  // transmission per sampled column (+ Kahan compensation)
@@ -159,7 +162,7 @@ __device__ __forceinline__ void spread_body(const YgArgs& a, int c0, const float
     auto emit = [&](int i, const float4& v) {
       const int x = x0 + warp * kTXW + i;
       if (x >= a.nx || !yok) return;
-      if (ADJ) {
+      if (scatter) {
         // halo rows lack part of their PSF support: their owner window adds them
         if (lane_writes(a, yb)) scatter4(tmp, tb[tap_slot<R>(warp * kTXW + i + R)], yb, v);
       } else {
@@ -208,7 +211,8 @@ __global__ void __launch_bounds__(32 * kW, CTAS)
 // c's frame go through the transposed PSF (camera: both kernels reversed;
 // mate: row kernel forward, column kernel reversed) and, summed, are
 // scattered with c's bilinear weights into the accumulator a.out (the mate's
-// footprint of its mirrored column is c's).
+// footprint of its mirrored column is c's), or with a.det written to the
+// group scratch for k_tgather_yg.
 //
 // V = bfloat16 (mu stored in bfloat16): the forward transmission is summed
 // with Kahan compensation (the compensation of each sampled column in shared
@@ -267,7 +271,8 @@ __device__ __forceinline__ void spread_pair_body(const YgArgs& a, int u0, const 
   }
   const CamRows cr = cam_rows(a.geom[cam].fwd);
   const size_t vol = static_cast<size_t>(a.nz) * a.nx * a.cs;  // one scratch volume
-  float* __restrict__ tmp = ADJ ? a.out + a.row0 : a.temp + vol * g;
+  const bool scatter = ADJ && !a.det;  // uniform over the launch
+  float* __restrict__ tmp = scatter ? a.out + a.row0 : a.temp + vol * g;
   const float* __restrict__ srow = a.sino + static_cast<size_t>(cam) * a.nx * a.cy + a.row0;
   const float* __restrict__ mrow = a.sino + static_cast<size_t>(paired ? mate : cam) * a.nx * a.cy + a.row0;
 
@@ -346,7 +351,7 @@ __device__ __forceinline__ void spread_pair_body(const YgArgs& a, int u0, const 
     auto write = [&](int i, const float4& v) {
       const int x = x0 + warp * kTXW + i;
       if (x >= a.nx || !yok) return;
-      if (ADJ) {
+      if (scatter) {
         // halo rows lack part of their PSF support: their owner window adds them
         if (lane_writes(a, yb)) scatter4(tmp, tb[tap_slot<R>(warp * kTXW + i + R)], yb, v);
       } else {
@@ -459,6 +464,93 @@ __global__ void __launch_bounds__(32 * kGatherWarps) k_gather_yg(const YgArgs a,
     if (!first) add4(acc[i], *dst);
     *dst = acc[i];
   }
+}
+
+// Forward bilinear weight of corner (X, Z) in the footprint of rotated column
+// (xp, zp) (0 when (X, Z) is not one of its corners): make_tap's position,
+// floor, relative and basis arithmetic, and its product for that corner, so
+// the weight equals the one the scatter of the atomic form applies.
+__device__ __forceinline__ float corner_weight(int xp, int zp, const CamRows& cr, int X, int Z) {
+  const float fx = static_cast<float>(xp), fz = static_cast<float>(zp);
+  const float px = fa(fa(fm(cr.m00, fx), fm(cr.m02, fz)), cr.m03);
+  const float pz = fa(fa(fm(cr.m20, fx), fm(cr.m22, fz)), cr.m23);
+  const int xs = static_cast<int>(floorf(px));
+  const int zs = static_cast<int>(floorf(pz));
+  if ((X != xs && X != xs + 1) || (Z != zs && Z != zs + 1)) return 0.0f;
+  float rx = __fsub_rn(px, static_cast<float>(xs));
+  float rz = __fsub_rn(pz, static_cast<float>(zs));
+  if (rx < 0.0f) rx = 0.0f;
+  if (rz < 0.0f) rz = 0.0f;
+  const float wx = X == xs ? __fsub_rn(1.0f, rx) : rx;
+  const float wz = Z == zs ? __fsub_rn(1.0f, rz) : rz;
+  return wx * wz;
+}
+
+// Deterministic transposed gather: out[Z][X][y] (+)= sum over the group's
+// units g (camera order) and over the rotated columns (x', z') whose forward
+// footprint has (X, Z) as a corner, of that corner's weight times
+// scratch_g[z'][x'][y] -- the transpose of the projector's bilinear sampling
+// without vector reductions.  The forward rows are a rotation, so those
+// columns lie within sqrt(2) of the inverse image of (X, Z): inside the 4 x 4
+// integer box around it.  Lane l evaluates box candidate l % 16 of output
+// column X0 + l / 16; the nonzero weights are then added in lane order.
+__global__ void __launch_bounds__(32 * kGatherWarps) k_tgather_yg(const YgArgs a, int c0, int gcount, int first) {
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int nchunk = (a.nx + 1) / 2;
+  const int item = blockIdx.x * kGatherWarps + warp;
+  if (item >= nchunk * a.nz) return;
+  const int Z = item / nchunk;
+  const int X0 = (item % nchunk) * 2;
+  const int yb = lane * 4;
+  const bool rows = lane_rows_ok(a, yb) && lane_writes(a, yb);
+  const size_t vol = static_cast<size_t>(a.nz) * a.nx * a.cs;
+  const int X = X0 + (lane >> 4);
+  const int bx = (lane & 3) - 1, bz = ((lane >> 2) & 3) - 1;
+  float4 acc[2] = {make_float4(0.f, 0.f, 0.f, 0.f), make_float4(0.f, 0.f, 0.f, 0.f)};
+  for (int g = 0; g < gcount; ++g) {
+    const CamRows cr = cam_rows(a.geom[a.units ? a.units[c0 + g].x : c0 + g].fwd);
+    float w = 0.0f;
+    int off = 0;
+    if (X < a.nx) {
+      const float det = cr.m00 * cr.m22 - cr.m02 * cr.m20;
+      const float dx = static_cast<float>(X) - cr.m03, dz = static_cast<float>(Z) - cr.m23;
+      const int xp = static_cast<int>(floorf((cr.m22 * dx - cr.m02 * dz) / det)) + bx;
+      const int zp = static_cast<int>(floorf((cr.m00 * dz - cr.m20 * dx) / det)) + bz;
+      if (xp >= 0 && xp < a.nx && zp >= 0 && zp < a.nz) {
+        w = corner_weight(xp, zp, cr, X, Z);
+        off = (zp * a.nx + xp) * a.cs;
+      }
+    }
+    const float* src = a.temp + vol * g + yb;
+    for (unsigned m = __ballot_sync(kFull, w != 0.0f); m; m &= m - 1) {
+      const int l = __ffs(m) - 1;
+      const float wl = __shfl_sync(kFull, w, l);
+      const int ol = __shfl_sync(kFull, off, l);
+      if (rows) {
+        const float4 v = ldg4(src + ol);
+        const float4 wv = make_float4(wl * v.x, wl * v.y, wl * v.z, wl * v.w);
+        if (l < 16)  // uniform: l comes from the ballot
+          add4(acc[0], wv);
+        else
+          add4(acc[1], wv);
+      }
+    }
+  }
+  if (!rows) return;
+#pragma unroll
+  for (int i = 0; i < 2; ++i) {
+    const int Xo = X0 + i;
+    if (Xo >= a.nx) continue;
+    float4* dst = reinterpret_cast<float4*>(a.out + (static_cast<size_t>(Z) * a.nx + Xo) * a.cy + a.row0 + yb);
+    if (!first) add4(acc[i], *dst);
+    *dst = acc[i];
+  }
+}
+
+void launch_tgather(const YgArgs& b, int c0, int gcount, cudaStream_t st) {
+  const int blocks = ((b.nx + 1) / 2 * b.nz + kGatherWarps - 1) / kGatherWarps;
+  NRGB_LAUNCH_SCOPE("k_tgather_yg", st);
+  k_tgather_yg<<<blocks, 32 * kGatherWarps, 0, st>>>(b, c0, gcount, c0 == 0 ? 1 : 0);
 }
 
 void launch_gather(const YgArgs& b, int c0, int gcount, int blocks, size_t smem, cudaStream_t st) {
@@ -690,6 +782,8 @@ Pipe* pipe_for_current_device() {
 
 }  // namespace
 
+void yg_tgather(const YgArgs& a, int c0, int gcount, cudaStream_t st) { launch_tgather(a, c0, gcount, st); }
+
 // Per row window and camera group: step g (over all windows' groups) uses
 // scratch slot g % 2 and spreads on the caller's stream (even g) or a second
 // spread stream (odd g), its gather following on a gather stream.  The
@@ -727,12 +821,22 @@ int yg_backproject(const YgArgs& a_in, cudaStream_t st) {
   }
   if (a.sino_ready) cudaStreamWaitEvent(st, static_cast<cudaEvent_t>(a.sino_ready), 0);
   a.group = group;
+  // the exact transpose in its deterministic form: group scratch + transposed gather
+  const bool tgather = a.back_mode == kBackAdjoint && !a.gradient && a.det;
   auto spread_on = [&](const YgArgs& b, int c0, int gcount, cudaStream_t ss) {
     if (a.gradient) return yg_grad_spread(b, c0, gcount, ss);
+    if (tgather)
+      return pair ? spread_pair_by_radius<true>(R, b, c0, gcount, ss) : spread_by_radius_t<true>(R, b, c0, gcount, ss);
     return pair ? spread_pair_by_radius<false>(R, b, c0, gcount, ss) : spread_by_radius(R, b, c0, gcount, ss);
   };
+  auto gather_on = [&](const YgArgs& b, int c0, int gcount, int blocks, size_t smem, cudaStream_t gs) {
+    if (tgather)
+      launch_tgather(b, c0, gcount, gs);
+    else
+      launch_gather(b, c0, gcount, blocks, smem, gs);
+  };
   auto spread = [&](const YgArgs& b, int c0, int gcount) { return spread_on(b, c0, gcount, st); };
-  if (a.back_mode == kBackAdjoint && !a.gradient) {
+  if (a.back_mode == kBackAdjoint && !a.gradient && !a.det) {
     // transpose of the projector: one launch per window over all cameras,
     // scattered straight into the zeroed accumulator
     const size_t full = static_cast<size_t>(a.nz) * a.nx * a.cy;
@@ -757,7 +861,7 @@ int yg_backproject(const YgArgs& a_in, cudaStream_t st) {
         const int gcount = std::min(group, nunits - c0);
         int st_ = spread(b, c0, gcount);
         if (st_ != kOk) return st_;
-        launch_gather(b, c0, gcount, gblocks, gsmem, st);
+        gather_on(b, c0, gcount, gblocks, gsmem, st);
       }
     }
     return cudaGetLastError() == cudaSuccess ? kOk : kErrKernel;
@@ -781,7 +885,7 @@ int yg_backproject(const YgArgs& a_in, cudaStream_t st) {
       if (st_ != kOk) return st_;
       cudaEventRecord(pp->spread_done[slot], ss);
       cudaStreamWaitEvent(pp->aux, pp->spread_done[slot], 0);
-      launch_gather(b, c0, gcount, gblocks, gsmem, pp->aux);
+      gather_on(b, c0, gcount, gblocks, gsmem, pp->aux);
       cudaEventRecord(pp->gather_done[slot], pp->aux);
     }
   }

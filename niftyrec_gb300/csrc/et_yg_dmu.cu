@@ -11,7 +11,9 @@
 // Walk 1 forms each slab's local transmission and partial; the cluster
 // exchanges them (slab s needs exp(-T before s) and the weighted partials of
 // the slabs after it); walk 2 recomputes the samples and row / column passes
-// (nothing per depth is stored) and scatters -g S(z) with vector reductions.
+// (nothing per depth is stored) and scatters -g S(z) with vector reductions,
+// or with a.det writes it to the rotated-frame scratch of its camera (volume
+// camera - a.cam0 at a.temp) for the transposed gather (fixed summation order).
 #include "et_yg_device.cuh"
 
 namespace nrgb {
@@ -23,6 +25,7 @@ __device__ __forceinline__ void dmu_item(const YgArgs& a, int cam, int x0, unsig
   const float* __restrict__ act = a.act + a.row0;
   const float* __restrict__ mu = a.mu + a.row0;
   float* __restrict__ out = a.out + a.row0;
+  float* __restrict__ scratch = a.det ? a.temp + static_cast<size_t>(cam - a.cam0) * a.nz * a.nx * a.cs : nullptr;
   constexpr int NS = TS::NS;
   constexpr int K = 2 * R + 1;
   constexpr size_t kSb = TS::sb_bytes(false);
@@ -140,7 +143,12 @@ __device__ __forceinline__ void dmu_item(const YgArgs& a, int cam, int x0, unsig
       add4(T[i], sample4(mu, t, yb, yok));
       const float4 d = make_float4(fmaf(Bq[i].x, P[i].x, A[i].x), fmaf(Bq[i].y, P[i].y, A[i].y),
                                    fmaf(Bq[i].z, P[i].z, A[i].z), fmaf(Bq[i].w, P[i].w, A[i].w));
-      if (x0 + warp * kTXW + i < a.nx && yok && lane_writes(a, yb)) scatter4(out, t, yb, d);
+      const int x = x0 + warp * kTXW + i;
+      if (a.det) {  // uniform over the launch
+        if (x < a.nx && yok) *reinterpret_cast<float4*>(scratch + (static_cast<size_t>(z) * a.nx + x) * a.cs + yb) = d;
+      } else if (x < a.nx && yok && lane_writes(a, yb)) {
+        scatter4(out, t, yb, d);
+      }
       fma4(P[i], v, exp_neg4(T[i]));
     });
   });
@@ -151,7 +159,7 @@ __global__ void __launch_bounds__(32 * kW, 2) k_dmu_yg(const YgArgs a) {
   extern __shared__ __align__(16) unsigned char smem[];
   const int ntile = (a.nx + kTXC - 1) / kTXC;
   const int item = blockIdx.x / a.pslabs;
-  dmu_item<R, PSF, false>(a, item / ntile, (item % ntile) * kTXC, smem, nullptr);
+  dmu_item<R, PSF, false>(a, a.cam0 + item / ntile, (item % ntile) * kTXC, smem, nullptr);
 }
 
 template <int R>
@@ -159,7 +167,7 @@ __global__ void __launch_bounds__(32 * kW, 2) k_dmu_ptab_yg(const YgArgs a, cons
   extern __shared__ __align__(16) unsigned char smem[];
   const int ntile = (a.nx + kTXC - 1) / kTXC;
   const int item = blockIdx.x / a.pslabs;
-  dmu_item<R, true, true>(a, item / ntile, (item % ntile) * kTXC, smem, t.c);
+  dmu_item<R, true, true>(a, a.cam0 + item / ntile, (item % ntile) * kTXC, smem, t.c);
 }
 
 template <int R>
@@ -226,14 +234,38 @@ int dmu_by_radius(int R, const YgArgs& a, cudaStream_t st) {
 
 int yg_dmu(const YgArgs& a, cudaStream_t st) {
   if (!a.mu || !a.act || !a.sino || !a.out) return kErrParameters;
+  const int R = a.psf ? (a.psf_k - 1) / 2 : 0;
+  if (a.det) {
+    // camera groups into the scratch (a.work, yg_dmu_det_workspace bytes),
+    // each followed by the transposed gather on the same stream
+    if (!a.work) return kErrParameters;
+    const int group = yg_even_group(a.ncam, a.group);
+    for (const Window& w : row_windows(a.ny, R)) {
+      YgArgs b = windowed(a, w);
+      b.temp = a.work;
+      b.units = nullptr;
+      for (int c0 = 0; c0 < a.ncam; c0 += group) {
+        YgArgs d = b;
+        d.cam0 = c0;
+        d.ncam = std::min(group, a.ncam - c0);
+        const int s = dmu_by_radius(R, d, st);
+        if (s != kOk) return s;
+        yg_tgather(b, c0, d.ncam, st);
+      }
+    }
+    return cudaGetLastError() == cudaSuccess ? kOk : kErrKernel;
+  }
   const size_t full = static_cast<size_t>(a.nz) * a.nx * a.cy;
   if (cudaMemsetAsync(a.out, 0, sizeof(float) * full, st) != cudaSuccess) return kErrKernel;
-  const int R = a.psf ? (a.psf_k - 1) / 2 : 0;
   for (const Window& w : row_windows(a.ny, R)) {
     const int s = dmu_by_radius(R, windowed(a, w), st);
     if (s != kOk) return s;
   }
   return kOk;
+}
+
+size_t yg_dmu_det_workspace(int nx, int ny, int nz, int ncam, int group) {
+  return yg_gradient_workspace(nx, ny, nz, ncam, yg_even_group(ncam, group), 1);
 }
 
 }  // namespace nrgb

@@ -717,7 +717,9 @@ int ORC(spect_fisher_grid)(const REAL *act, const int act_size[3], const REAL *c
 }
 
 /* SPECT_backproject_parallelholes, emission-lib/_et_array_interface.cpp:547-710:
- * the centre comes from (sino0, sino1, sino0), the volume grid from bkpr_size. */
+ * the centre comes from (sino0, sino1, sino0), the volume grid from bkpr_size.
+ * The exact adjoint (not in the reference) is the transpose of the projector
+ * and takes the projector's centre, from (sino0, sino1, bkpr2). */
 int ORC(spect_backproject)(const REAL *sino, const int sino_size[3], REAL *bkpr, const int bkpr_size[3],
                            const REAL *cameras, const int cam_size[2], const REAL *psf, const int psf_size[3],
                            const REAL *att, const int att_size[3], REAL bg, REAL bg_att, int truncate, int adjoint)
@@ -727,7 +729,7 @@ int ORC(spect_backproject)(const REAL *sino, const int sino_size[3], REAL *bkpr,
     int ncam = cam_size[0], ncols = cam_size[1];
     if (sino_size[2] != ncam) return ORC_ERR_PARAMETERS;
     if (!no_psf && (psf_size[0] % 2 != 1 || psf_size[1] % 2 != 1 || psf_size[2] != sino_size[0])) return ORC_ERR_PARAMETERS;
-    int csz[3] = {sino_size[0], sino_size[1], sino_size[0]};
+    int csz[3] = {sino_size[0], sino_size[1], adjoint ? bkpr_size[2] : sino_size[0]};
     REAL *angles = (REAL *)malloc(sizeof(REAL) * 3 * ncam);
     REAL *centers = (REAL *)malloc(sizeof(REAL) * 3 * ncam);
     int st = expand_cameras(cameras, ncam, ncols, csz, angles, centers);

@@ -195,3 +195,22 @@ def test_fisher_grid_restatement_matches_golden(golden):
     np.testing.assert_array_equal(f, g["fisher"])
     np.testing.assert_array_equal(pr, g["prior"])
     assert np.allclose(f, f.T) and (np.diag(f) > 0).any()
+
+
+@pytest.mark.parametrize("shape", [(12, 10, 16), (16, 10, 12), (10, 10, 10)])
+def test_adjoint_is_transpose_of_projector(o64, shape):
+    """The exact-adjoint backprojection (not in the reference) is the transpose
+    of the projector, also when nz != nx (it takes the projector's rotation
+    centre, not the reference backprojector's): <A x, y> = <x, A^T y>."""
+    nz, ny, nx = shape
+    rng = np.random.default_rng(nz * 7 + nx)
+    cams = S.cameras_about_y(5, 11.0)
+    # the reference takes a PSF of nx planes (indexed by depth z < nz)
+    psf = S.gaussian_psf(3, nx, 0.6, 0.05) if nx >= nz else None
+    mu = S.mu_map(shape, seed=2).astype(np.float64)
+    x = rng.random(shape)
+    y = rng.random((5, ny, nx))
+    ax = o64.project(x, cams, psf, mu, truncate=0)
+    aty = o64.backproject(y, cams, psf, mu, truncate=0, adjoint=True, nz=nz)
+    lhs, rhs = float(np.sum(ax * y)), float(np.sum(x * aty))
+    assert abs(lhs - rhs) <= 1e-10 * abs(lhs), (lhs, rhs)
