@@ -5,6 +5,7 @@ line (e.g. under a profiler) through the device-pointer C-ABI:
     python -m niftyrec_gb300.workloads pair2 --n 128 --ncam 120 --reps 2           # two separate calls
     python -m niftyrec_gb300.workloads project --n 64 --ncam 60 --psf 0 --no-att
     python -m niftyrec_gb300.workloads dmu --reps 1       # exact d/dmu (autograd's attenuation gradient)
+    python -m niftyrec_gb300.workloads pair --mode 1 --det   # exact transpose, deterministic form
     python -m niftyrec_gb300.workloads fisher --reps 1    # Fisher information of a 64-point grid
     python -m niftyrec_gb300.workloads osem --subsets 8 --reps 1     # plan OSEM iterations
     python -m niftyrec_gb300.workloads batch --volumes 8 --reps 1    # batched OSEM steps
@@ -44,6 +45,8 @@ def main(argv=None):
     ap.add_argument("--group", type=int, default=0, help="backprojector cameras per scratch group (0: tuned)")
     ap.add_argument("--slabs", type=int, default=0, help="projector depth slabs 2/4/8 (0: tuned)")
     ap.add_argument("--no-mirror", action="store_true", help="every camera from its own matrix")
+    ap.add_argument("--det", action="store_true",
+                    help="deterministic exact-transpose backprojection and d/dmu (nrgb_set_deterministic)")
     a = ap.parse_args(argv)
 
     L = _lib.load()
@@ -52,6 +55,7 @@ def main(argv=None):
     if a.slabs:
         L.nrgb_set_project_slabs(a.n, a.n, a.n, a.ncam, a.slabs)
     L.nrgb_set_mirror_pairs(0 if a.no_mirror else 1)
+    L.nrgb_set_deterministic(1 if a.det else 0)
     n = a.n
     act = S.ellipsoid_phantom((n, n, n), seed=0)
     mu = S.mu_map((n, n, n), seed=0)
