@@ -447,7 +447,8 @@ int backproject_device(const Problem& pb, const float* d_sino, const float* d_at
     a.work = cx.take<float>(yg_backproject_workspace(pb.ny, pb.nx, pb.nz, pb.cams.n, a.group) / sizeof(float));
     if (!a.work) return kErrAllocGpu;
     if ((s = yg_backproject(a, st)) != kOk) return s;
-    if (pb.truncate) launch_truncate(d_out, vol_n(pb), st);
+    // the gathers clamp as they store; the vector-reduction transpose does not
+    if (pb.truncate && pb.back_mode == kBackAdjoint && !pb.det) launch_truncate(d_out, vol_n(pb), st);
     return check(kOk);
   }
   Carver cv(ws, ws_bytes);
@@ -770,9 +771,7 @@ int gradient_device(const Problem& pb, const float* d_sino, const float* d_act, 
     a.group = grad_group(pb);
     a.work = cx.take<float>(yg_gradient_workspace(pb.ny, pb.nx, pb.nz, pb.cams.n, a.group) / sizeof(float));
     if (!a.work) return kErrAllocGpu;
-    if ((s = yg_backproject(a, st)) != kOk) return s;
-    if (pb.truncate) launch_truncate(d_out, vol_n(pb), st);
-    return check(kOk);
+    return check(yg_backproject(a, st));  // the last gathers clamp when truncating
   }
   Carver cv(ws, ws_bytes);
   CamGeom* d_geom;

@@ -104,6 +104,8 @@ struct YgArgs {
   // (yg_mu_carry) for exactly these cameras; the backprojector then skips
   // that pass and the work space holds only the scratch slot(s).
   const float* carry = nullptr;
+  // yg_backproject (reference form, deterministic transpose): the window's
+  // last gather stores max(result, 0) when a.truncate is set.
   // Non-zero: yg_backproject spreads the reference's attenuation gradient
   // instead (a.act and a.mu sampled, a.sino the camera planes; no carries,
   // no mirror units), then gathers it like the reference-mode backprojection.
@@ -143,8 +145,9 @@ int yg_dmu(const YgArgs& a, cudaStream_t st);
 size_t yg_dmu_det_workspace(int nx, int ny, int nz, int ncam, int group);
 // Deterministic transposed gather of scratch volumes a.temp[0 .. gcount) of
 // units (or cameras) c0 .. c0 + gcount - 1 into a.out (assigned when c0 == 0,
-// else added), rows of the window a describes.
-void yg_tgather(const YgArgs& a, int c0, int gcount, cudaStream_t st);
+// else added; clamp: negative results stored as zero), rows of the window a
+// describes.
+void yg_tgather(const YgArgs& a, int c0, int gcount, int clamp, cudaStream_t st);
 int yg_backproject(const YgArgs& a, cudaStream_t st);
 // Spread of the reference attenuation gradient for cameras [c0, c0 + gcount)
 // into the scratch volumes a.temp (one row window: a.row0, a.ny, a.cs).

@@ -174,8 +174,8 @@ int plan_backproject(Plan& p, int subset, const float* d_sino, float* d_out, int
     a.pipelined = pipelined;
     int s = yg_backproject(a, st);
     if (s != kOk) return s;
+    // the last gather of every row window already stored max(result, 0) when truncating
     if (layout == kLayoutNifti) return from_column(p.out_c, d_out, pb.nx, pb.ny, p.cy, pb.nz, truncate, st);
-    if (truncate) launch_truncate(d_out, static_cast<size_t>(pb.nz) * pb.nx * p.cy, st);
     return check();
   }
   if (layout != kLayoutNifti) return kErrParameters;

@@ -411,8 +411,11 @@ __global__ void __launch_bounds__(32 * kW, 2)
 // out[Z][X][y] (+)= sum_g bilinear(temp[g], B_g * (X, y, Z)) with B_g the
 // camera's inverse matrix (ZYX order, -theta), emission-lib/_et.cpp:474-497.
 // With a.units, g runs over units and B_g is the unit's first camera's.
+// first: assign instead of adding to a.out; clamp: the last group of the
+// window with a.truncate -- negative sums become zero as they are stored.
 template <int U>
-__global__ void __launch_bounds__(32 * kGatherWarps) k_gather_yg(const YgArgs a, int c0, int gcount, int first) {
+__global__ void __launch_bounds__(32 * kGatherWarps) k_gather_yg(const YgArgs a, int c0, int gcount, int first,
+                                                                int clamp) {
   constexpr int C = kGatherCols;
   extern __shared__ Tap s_gtap[];  // [kGatherWarps][C * group]
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -462,6 +465,7 @@ __global__ void __launch_bounds__(32 * kGatherWarps) k_gather_yg(const YgArgs a,
     if (X >= a.nx) continue;
     float4* dst = reinterpret_cast<float4*>(a.out + (static_cast<size_t>(Z) * a.nx + X) * a.cy + a.row0 + yb);
     if (!first) add4(acc[i], *dst);
+    if (clamp) acc[i] = clamp0(acc[i]);
     *dst = acc[i];
   }
 }
@@ -494,7 +498,8 @@ __device__ __forceinline__ float corner_weight(int xp, int zp, const CamRows& cr
 // columns lie within sqrt(2) of the inverse image of (X, Z): inside the 4 x 4
 // integer box around it.  Lane l evaluates box candidate l % 16 of output
 // column X0 + l / 16; the nonzero weights are then added in lane order.
-__global__ void __launch_bounds__(32 * kGatherWarps) k_tgather_yg(const YgArgs a, int c0, int gcount, int first) {
+__global__ void __launch_bounds__(32 * kGatherWarps) k_tgather_yg(const YgArgs a, int c0, int gcount, int first,
+                                                                  int clamp) {
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int nchunk = (a.nx + 1) / 2;
   const int item = blockIdx.x * kGatherWarps + warp;
@@ -543,19 +548,21 @@ __global__ void __launch_bounds__(32 * kGatherWarps) k_tgather_yg(const YgArgs a
     if (Xo >= a.nx) continue;
     float4* dst = reinterpret_cast<float4*>(a.out + (static_cast<size_t>(Z) * a.nx + Xo) * a.cy + a.row0 + yb);
     if (!first) add4(acc[i], *dst);
+    if (clamp) acc[i] = clamp0(acc[i]);
     *dst = acc[i];
   }
 }
 
-void launch_tgather(const YgArgs& b, int c0, int gcount, cudaStream_t st) {
+// clamp: this is the window's last group and the result is truncated
+void launch_tgather(const YgArgs& b, int c0, int gcount, int clamp, cudaStream_t st) {
   const int blocks = ((b.nx + 1) / 2 * b.nz + kGatherWarps - 1) / kGatherWarps;
   NRGB_LAUNCH_SCOPE("k_tgather_yg", st);
-  k_tgather_yg<<<blocks, 32 * kGatherWarps, 0, st>>>(b, c0, gcount, c0 == 0 ? 1 : 0);
+  k_tgather_yg<<<blocks, 32 * kGatherWarps, 0, st>>>(b, c0, gcount, c0 == 0 ? 1 : 0, clamp);
 }
 
-void launch_gather(const YgArgs& b, int c0, int gcount, int blocks, size_t smem, cudaStream_t st) {
+void launch_gather(const YgArgs& b, int c0, int gcount, int clamp, int blocks, size_t smem, cudaStream_t st) {
   NRGB_LAUNCH_SCOPE("k_gather_yg", st);
-  k_gather_yg<kGatherUnits><<<blocks, 32 * kGatherWarps, smem, st>>>(b, c0, gcount, c0 == 0 ? 1 : 0);
+  k_gather_yg<kGatherUnits><<<blocks, 32 * kGatherWarps, smem, st>>>(b, c0, gcount, c0 == 0 ? 1 : 0, clamp);
 }
 
 // The separated PSF of a.nz planes as a kernel-parameter table, or null when
@@ -782,7 +789,9 @@ Pipe* pipe_for_current_device() {
 
 }  // namespace
 
-void yg_tgather(const YgArgs& a, int c0, int gcount, cudaStream_t st) { launch_tgather(a, c0, gcount, st); }
+void yg_tgather(const YgArgs& a, int c0, int gcount, int clamp, cudaStream_t st) {
+  launch_tgather(a, c0, gcount, clamp, st);
+}
 
 // Per row window and camera group: step g (over all windows' groups) uses
 // scratch slot g % 2 and spreads on the caller's stream (even g) or a second
@@ -829,11 +838,13 @@ int yg_backproject(const YgArgs& a_in, cudaStream_t st) {
       return pair ? spread_pair_by_radius<true>(R, b, c0, gcount, ss) : spread_by_radius_t<true>(R, b, c0, gcount, ss);
     return pair ? spread_pair_by_radius<false>(R, b, c0, gcount, ss) : spread_by_radius(R, b, c0, gcount, ss);
   };
+  // with a.truncate the window's last group clamps the result as it stores it
   auto gather_on = [&](const YgArgs& b, int c0, int gcount, int blocks, size_t smem, cudaStream_t gs) {
+    const int clamp = a.truncate && c0 + gcount == nunits ? 1 : 0;
     if (tgather)
-      launch_tgather(b, c0, gcount, gs);
+      launch_tgather(b, c0, gcount, clamp, gs);
     else
-      launch_gather(b, c0, gcount, blocks, smem, gs);
+      launch_gather(b, c0, gcount, clamp, blocks, smem, gs);
   };
   auto spread = [&](const YgArgs& b, int c0, int gcount) { return spread_on(b, c0, gcount, st); };
   if (a.back_mode == kBackAdjoint && !a.gradient && !a.det) {

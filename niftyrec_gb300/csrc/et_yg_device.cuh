@@ -143,6 +143,15 @@ __device__ __forceinline__ float4 sample4_loaded(const float* __restrict__ base,
   return t.any ? r : make_float4(0.f, 0.f, 0.f, 0.f);
 }
 
+// Negative values to zero (NaN kept), as the truncation of the reference.
+__device__ __forceinline__ float4 clamp0(float4 v) {
+  v.x = v.x < 0.0f ? 0.0f : v.x;
+  v.y = v.y < 0.0f ? 0.0f : v.y;
+  v.z = v.z < 0.0f ? 0.0f : v.z;
+  v.w = v.w < 0.0f ? 0.0f : v.w;
+  return v;
+}
+
 __device__ __forceinline__ float comp(const float4& v, int c) { return c == 0 ? v.x : c == 1 ? v.y : c == 2 ? v.z : v.w; }
 
 // Packed float32 pairs (sm_100 and later): two lanes in one 64-bit register

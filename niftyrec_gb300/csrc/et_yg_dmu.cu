@@ -250,7 +250,7 @@ int yg_dmu(const YgArgs& a, cudaStream_t st) {
         d.ncam = std::min(group, a.ncam - c0);
         const int s = dmu_by_radius(R, d, st);
         if (s != kOk) return s;
-        yg_tgather(b, c0, d.ncam, st);
+        yg_tgather(b, c0, d.ncam, 0, st);
       }
     }
     return cudaGetLastError() == cudaSuccess ? kOk : kErrKernel;

@@ -255,3 +255,34 @@ def test_plan_osem_checkpoint_resume_bit_exact(tmp_path):
     assert (st["iteration"], st["subset"]) == (3, 0)
     with pytest.raises(ValueError):
         Plan(shape, cams[:6].copy(), psf, mu, subsets=3).osem(y[:6], 3, checkpoint=ck, resume=True)
+
+
+def test_truncated_backprojection_of_signed_data(data):
+    """Backprojections of a sinogram with negative entries, truncated (the
+    last gather of each row window stores max(value, 0)) and not, against the
+    oracle: the plan in both layouts, the host-buffer call, and cameras about
+    x (the gantry kernels on the caller's arrays)."""
+    from oracle.oracle import Restated
+
+    o = Restated("f32")
+    act, mu, psf, cams, y = data
+    ys = np.random.default_rng(12).uniform(-1.0, 1.0, y.shape).astype(np.float32)
+    for trunc in (1, 0):
+        bo = o.backproject(ys, cams, psf, mu, truncate=trunc, nz=SHAPE[0])
+        if trunc:
+            assert (bo == 0).any() and (bo > 0).any()
+        b = A.backproject(ys, cams, psf, mu, truncate_negative_values=trunc)
+        assert A.last_path() == 1
+        assert rel_l2(b, bo) < RTOL
+        p = make_plan(data, subsets=None)
+        order = p.subset_cameras(-1)
+        bn = p.backproject(cuda(ys[order]), truncate=bool(trunc)).cpu().numpy()
+        assert rel_l2(bn, bo) < RTOL
+        bc = p.from_column(p.backproject(p.to_column(cuda(ys)), layout="column", truncate=bool(trunc))).cpu().numpy()
+        assert rel_l2(bc, bo) < RTOL
+    cx = np.zeros((3, 10), np.float32)
+    cx[0] = np.deg2rad(5.0 + 36.0 * np.arange(10))
+    yx = np.random.default_rng(13).uniform(-1.0, 1.0, (10,) + SHAPE[1:]).astype(np.float32)
+    bx = A.backproject(yx, cx, psf, mu, truncate_negative_values=1)
+    assert A.last_path() == 1
+    assert rel_l2(bx, o.backproject(yx, cx, psf, mu, truncate=1, nz=SHAPE[0])) < RTOL
