@@ -118,6 +118,22 @@ int et_array_make_psf(float *psf_data, unsigned int psf_size_x, unsigned int psf
 int et_array_make_cameras(float *cameras_data, float firstcamera_deg, float lastcamera_deg, unsigned int n_cameras,
                           unsigned int rotation_axis);
 
+/* Affine transformation of a volume -- emission-lib/_et_array_interface.h:31.
+ * out(x) = trilinear(image, A x), `background` outside; A = affine_ptr, 4 x 4
+ * in column-major order (affine_size {4, 4}); the output has image_size.  The
+ * reference ignores affine_ptr (a zeroed matrix, FIXME in its source); this
+ * applies it, as documented. */
+int et_array_affine(float *image_ptr, int *image_size, float *transformed_image_ptr, int *transformed_image_size,
+                    float *affine_ptr, int *affine_size, float background, int GPU);
+
+/* Per-slice 2D convolution -- emission-lib/_et_array_interface.h:33.
+ * image [nx, ny, nz] (x fastest), kernel slices psf [kx, ky, nz] (odd kx, ky),
+ * out(x, y, z) = sum_{i,j} psf(i, j, z) image(x + (kx-1)/2 - i, y + (ky-1)/2 - j, z)
+ * with the image clamped to its border, as the reference's FFT path intends
+ * (its CPU path is a stub returning 1, its GPU path shifts the size array);
+ * out has the image's size. */
+int et_array_convolve(float *image, int *image_size, float *out, int *out_size, float *psf, int *psf_size, int GPU);
+
 /* Rotation of a volume -- emission-lib/_et_array_interface.h:32. */
 int et_array_rotate(float *image, int *size, float *rotated_image, float *angles, float *centers, float background,
                     int axis_order, int GPU);

@@ -51,6 +51,8 @@ PROTOTYPES = {
     "et_array_make_psf": (_I, [_P, _U, _U, _F, _F, _F, _F, _F, _F, _U]),
     "et_array_make_cameras": (_I, [_P, _F, _F, _U, _U]),
     "et_array_rotate": (_I, [_P, _PI, _P, _P, _P, _F, _I, _I]),
+    "et_array_affine": (_I, [_P, _PI, _P, _PI, _P, _PI, _F, _I]),
+    "et_array_convolve": (_I, [_P, _PI, _P, _PI, _P, _PI, _I]),
     "et_array_osem_step": (_I, [_P, _I, _I, _U, _P, _I, _P, _I, _P, _I, _P, _U, _U, _F, _F, _F, _I]),
     "et_array_osem_step_subset": (_I, [_P, _I, _I, _P, _I, _P, _PI, _I, _I, _P, _I, _P, _U, _U, _F, _F, _F]),
     "et_array_mlem_step": (_I, [_P, _I, _I, _P, _I, _P, _I, _P, _I, _P, _U, _U, _F, _F, _F, _I]),

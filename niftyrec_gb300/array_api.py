@@ -206,6 +206,35 @@ def rotate(volume, angles, center, background=0.0, axis_order=0):
     return out
 
 
+def affine(volume, matrix, background=0.0):
+    """et_array_affine: out(x) = trilinear(volume, matrix @ x) in voxel
+    coordinates (x, y, z, 1), `background` outside; volume (nz, ny, nx)."""
+    L = load()
+    vol = _f32(volume)
+    nz, ny, nx = vol.shape
+    out = np.zeros_like(vol)
+    a = np.asfortranarray(np.asarray(matrix, dtype=np.float32).reshape(4, 4)).ravel(order="F")
+    size = _ints([nx, ny, nz])
+    st = L.et_array_affine(_p(vol), _pi(size), _p(out), _pi(size), _p(a), _pi(_ints([4, 4])), background, 1)
+    _check("et_array_affine", st)
+    return out
+
+
+def convolve(volume, kernels):
+    """et_array_convolve: per-slice 2D convolution; volume (nz, ny, nx),
+    kernels (nz, ky, kx) with odd kx, ky; the image is clamped at its border."""
+    L = load()
+    vol = _f32(volume)
+    k = _f32(kernels)
+    nz, ny, nx = vol.shape
+    out = np.zeros_like(vol)
+    size = _ints([nx, ny, nz])
+    st = L.et_array_convolve(_p(vol), _pi(size), _p(out), _pi(size), _p(k), _pi(_ints([k.shape[2], k.shape[1], k.shape[0]])),
+                             1)
+    _check("et_array_convolve", st)
+    return out
+
+
 def make_cameras(first_deg, last_deg, n, axis=1):
     """et_array_make_cameras -> [3, n]."""
     L = load()

@@ -669,6 +669,75 @@ int et_array_rotate(float* image, int* size, float* rotated_image, float* angles
   return finish(ds, s);
 }
 
+// emission-lib/_et_array_interface.cpp:58-108: affine transformation of a
+// volume, out(x) = trilinear(image, A x) with `background` outside, A the 4 x 4
+// matrix affine_ptr in the interface's column-major order (affine_size {4, 4};
+// the Matlab caller _et_affine_mex.cpp:110-118 passes it so).  The output has
+// the image's size (the reference sizes it from the source and does not read
+// transformed_image_size).  The reference itself never reads affine_ptr (a
+// zeroed mat44 marked FIXME, so every voxel took the value of voxel 0); this
+// applies the matrix, as its documentation states, with the same resampler as
+// et_array_rotate.
+int et_array_affine(float* image_ptr, int* image_size, float* transformed_image_ptr, int* transformed_image_size,
+                    float* affine_ptr, int* affine_size, float background, int GPU) {
+  NRGB_API("et_array_affine");
+  (void)GPU;
+  (void)transformed_image_size;
+  if (!image_ptr || !image_size || !transformed_image_ptr || !affine_ptr || !affine_size) return kErrParameters;
+  if (image_size[0] <= 0 || image_size[1] <= 0 || image_size[2] <= 0) return kErrParameters;
+  if (affine_size[0] != 4 || affine_size[1] != 4) return kErrParameters;
+  int s;
+  DeviceState& ds = current_device_state(&s);
+  if (s != kOk) return s;
+  std::lock_guard<std::mutex> lk(ds.mu);
+  const size_t nvox = static_cast<size_t>(image_size[0]) * image_size[1] * image_size[2];
+  if ((s = ensure_arena(ds, fbytes(2 * nvox) + 512)) != kOk) return s;
+  Carver cv(ds.arena, ds.arena_bytes);
+  float* d_in = cv.take<float>(nvox);
+  float* d_out = cv.take<float>(nvox);
+  float M[16];
+  for (int i = 0; i < 4; ++i)
+    for (int j = 0; j < 4; ++j) M[4 * i + j] = affine_ptr[i + 4 * j];
+  if ((s = h2d(d_in, image_ptr, nvox, ds.stream)) != kOk) return finish(ds, s);
+  s = general_rotate(d_in, d_out, image_size[0], image_size[1], image_size[2], M, background, ds.stream);
+  if (s == kOk) s = d2h(transformed_image_ptr, d_out, nvox, ds.stream);
+  return finish(ds, s);
+}
+
+// emission-lib/_et_array_interface.cpp:161-226: per-slice 2D convolution of
+// an image [nx, ny, nz] with kernel slices [kx, ky, nz] (kx, ky odd), as the
+// reference's GPU path computes it by FFT (emission-lib_gpu/
+// _et_convolveFFT2D_gpu.cu:43-113: kernel centred at ((kx-1)/2, (ky-1)/2),
+// image clamped to its border); here summed directly.  The output has the
+// image's size (out_size is not read, as in the reference).  The reference's
+// CPU path is a stub that returns 1 (_et.cpp:776-780) and its GPU path passes
+// the nifti dim array shifted by one (dim[0] = 3 taken as the height).
+int et_array_convolve(float* image, int* image_size, float* out, int* out_size, float* psf, int* psf_size, int GPU) {
+  NRGB_API("et_array_convolve");
+  (void)GPU;
+  (void)out_size;
+  if (!image || !image_size || !out || !psf || !psf_size) return kErrParameters;
+  const int nx = image_size[0], ny = image_size[1], nz = image_size[2];
+  const int kx = psf_size[0], ky = psf_size[1];
+  if (nx <= 0 || ny <= 0 || nz <= 0 || kx <= 0 || ky <= 0 || kx % 2 != 1 || ky % 2 != 1 || psf_size[2] != nz)
+    return kErrParameters;
+  int s;
+  DeviceState& ds = current_device_state(&s);
+  if (s != kOk) return s;
+  std::lock_guard<std::mutex> lk(ds.mu);
+  const size_t nvox = static_cast<size_t>(nx) * ny * nz, nk = static_cast<size_t>(kx) * ky * nz;
+  if ((s = ensure_arena(ds, fbytes(2 * nvox + nk) + 768)) != kOk) return s;
+  Carver cv(ds.arena, ds.arena_bytes);
+  float* d_in = cv.take<float>(nvox);
+  float* d_out = cv.take<float>(nvox);
+  float* d_k = cv.take<float>(nk);
+  if ((s = h2d(d_in, image, nvox, ds.stream)) != kOk) return finish(ds, s);
+  if ((s = h2d(d_k, psf, nk, ds.stream)) != kOk) return finish(ds, s);
+  s = general_convolve2d(d_in, d_out, nx, ny, nz, d_k, kx, ky, ds.stream);
+  if (s == kOk) s = d2h(out, d_out, nvox, ds.stream);
+  return finish(ds, s);
+}
+
 // ---------------------------------------------------------- OSEM / MLEM
 // emission-lib/_et_array_interface.cpp:972-1054.  Subset of n_cameras /
 // subset_order cameras drawn with rand() as the reference does; an index that

@@ -492,6 +492,41 @@ int general_gradient(const GeneralArgs& a, cudaStream_t st) {
   return cudaGetLastError() == cudaSuccess ? kOk : kErrKernel;
 }
 
+namespace {
+
+// Per-slice 2D true convolution with kernel slice z (centre ((kx-1)/2,
+// (ky-1)/2)), the image clamped to its border outside; terms in (j, i) order,
+// multiply and add rounded separately (the oracle's order and rounding).
+__global__ void k_convolve2d(const float* __restrict__ src, float* __restrict__ dst, int nx, int ny,
+                             const float* __restrict__ psf, int kx, int ky) {
+  const int x = blockIdx.x * blockDim.x + threadIdx.x;
+  const int y = blockIdx.y * blockDim.y + threadIdx.y;
+  const int z = blockIdx.z;
+  if (x >= nx || y >= ny) return;
+  const int cx = (kx - 1) / 2, cy = (ky - 1) / 2;
+  const float* k = psf + static_cast<size_t>(z) * kx * ky;
+  const float* img = src + static_cast<size_t>(z) * nx * ny;
+  float acc = 0.0f;
+  for (int j = 0; j < ky; ++j) {
+    const int yy = min(max(y + cy - j, 0), ny - 1);
+    const float* row = img + static_cast<size_t>(yy) * nx;
+    for (int i = 0; i < kx; ++i) {
+      const int xx = min(max(x + cx - i, 0), nx - 1);
+      acc = __fadd_rn(acc, __fmul_rn(__ldg(k + i + kx * j), __ldg(row + xx)));
+    }
+  }
+  dst[(static_cast<size_t>(z) * ny + y) * nx + x] = acc;
+}
+
+}  // namespace
+
+int general_convolve2d(const float* src, float* dst, int nx, int ny, int nz, const float* psf, int kx, int ky,
+                       cudaStream_t st) {
+  const dim3 block(32, 8), grid((nx + 31) / 32, (ny + 7) / 8, nz);
+  { NRGB_LAUNCH_SCOPE("k_convolve2d", st); k_convolve2d<<<grid, block, 0, st>>>(src, dst, nx, ny, psf, kx, ky); }
+  return cudaGetLastError() == cudaSuccess ? kOk : kErrKernel;
+}
+
 int general_rotate(const float* src, float* dst, int nx, int ny, int nz, const float* m12, float bg, cudaStream_t st) {
   const size_t nvox = static_cast<size_t>(nx) * ny * nz;
   { NRGB_LAUNCH_SCOPE("k_resample", st); k_resample<false><<<grid_for(nvox, 256), 256, 0, st>>>(src, dst, nx, ny, nz, affine_of(m12), bg); }

@@ -45,6 +45,10 @@ int general_adjoint(const GeneralArgs& a, cudaStream_t st);
 // d/dmu of sum(g * project(act, mu)); a.sino = g (sinogram), a.out = gradient.
 int general_dmu(const GeneralArgs& a, cudaStream_t st);
 int general_rotate(const float* src, float* dst, int nx, int ny, int nz, const float* m12, float bg, cudaStream_t st);
+// Per-slice 2D convolution of nz slices (nx x ny, x fastest) with kernel slices
+// [nz][ky][kx], centre ((kx-1)/2, (ky-1)/2), image clamped at its border.
+int general_convolve2d(const float* src, float* dst, int nx, int ny, int nz, const float* psf, int kx, int ky,
+                       cudaStream_t st);
 
 // ---- y-gantry fused path (column layout) ----
 // Callers describe whole volumes (ny rows, column stride cy = round_up(ny, 4));

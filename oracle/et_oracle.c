@@ -818,3 +818,34 @@ void ORC(make_cameras)(REAL *cams, REAL first_deg, REAL last_deg, int n, int axi
         for (int a = 0; a < 3; a++) cams[c + a * n] = (a == axis) ? angle : (REAL)0;
     }
 }
+
+/* et_array_convolve, emission-lib/_et_array_interface.cpp:161-226 (per-slice
+ * FFT convolution on the reference's GPU path, emission-lib_gpu/
+ * _et_convolveFFT2D_gpu.cu:43-113; its CPU path is a stub, _et.cpp:776-780):
+ * restated as the direct sum the FFT computes -- per slice z, a true 2D
+ * convolution with kernel slice z, kernel centre ((kx-1)/2, (ky-1)/2), the
+ * image clamped to its border outside (padDataClampToBorder).  Nifti order,
+ * x fastest; kernel [kx][ky][nz] with kx fastest.  Terms in (j, i) order. */
+void ORC(convolve2d)(const REAL *img, REAL *out, int nx, int ny, int nz, const REAL *psf, int kx, int ky)
+{
+    int cx = (kx - 1) / 2, cy = (ky - 1) / 2;
+    for (int z = 0; z < nz; z++) {
+        const REAL *k = psf + (size_t)z * kx * ky;
+        const REAL *src = img + (size_t)z * nx * ny;
+        for (int y = 0; y < ny; y++)
+            for (int x = 0; x < nx; x++) {
+                REAL acc = 0;
+                for (int j = 0; j < ky; j++) {
+                    int yy = y + cy - j;
+                    yy = yy < 0 ? 0 : (yy >= ny ? ny - 1 : yy);
+                    for (int i = 0; i < kx; i++) {
+                        int xx = x + cx - i;
+                        xx = xx < 0 ? 0 : (xx >= nx ? nx - 1 : xx);
+                        REAL t = k[i + (size_t)kx * j] * src[xx + (size_t)nx * yy];
+                        acc = acc + t;
+                    }
+                }
+                out[x + (size_t)nx * (y + (size_t)ny * z)] = acc;
+            }
+    }
+}

@@ -101,6 +101,19 @@ class Restated:
         fn(_ptr(vol), _ptr(out), _I(nx), _I(ny), _I(nz), _ptr(A), self.real(bg))
         return out
 
+    def convolve2d(self, vol, psf):
+        """Per-slice 2D convolution (et_array_convolve): vol (nz, ny, nx), psf
+        (nz, ky, kx); clamp-to-border."""
+        vol = self._arr(vol)
+        psf = self._arr(psf)
+        nz, ny, nx = vol.shape
+        _, ky, kx = psf.shape
+        out = np.zeros_like(vol)
+        fn = getattr(self.lib, f"orc_convolve2d_{self.precision}")
+        fn.restype = None
+        fn(_ptr(vol), _ptr(out), _I(nx), _I(ny), _I(nz), _ptr(psf), _I(kx), _I(ky))
+        return out
+
     def project(self, act, cameras, psf=None, att=None, bg=0.0, bg_att=0.0, truncate=1):
         act = self._arr(act)
         att = self._arr(att)

@@ -90,6 +90,61 @@ def test_golden_rotate(golden):
     assert rel_l2(r, g["rot_zyx"]) < 1e-6
 
 
+@pytest.mark.parametrize("shape", [(12, 14, 16), (33, 20, 27)])
+def test_affine_matches_oracle_resampler(o32, shape):
+    """et_array_affine applies its 4 x 4 matrix (column-major in the interface)
+    with the reference's trilinear resampler: equal to the oracle's
+    restatement of reg_affine_positionField + reg_resampleSourceImage
+    (reg-lib/_reg_resampling.cpp:305-450) to 1e-6 (the rotation test's bound);
+    the identity returns the input exactly; a rotation matrix gives
+    et_array_rotate's result."""
+    rng = np.random.default_rng(sum(shape))
+    vol = rng.random(shape).astype(np.float32)
+    M = np.array([[0.9, 0.2, -0.1, 1.5], [-0.15, 1.05, 0.05, -0.7], [0.1, -0.05, 0.95, 0.4], [0, 0, 0, 1]],
+                 np.float32)
+    out = A.affine(vol, M, background=0.25)
+    ref = o32.affine_resample(vol, M, bg=0.25)
+    assert (out == 0.25).any() and rel_l2(out, ref) < 1e-6
+    assert np.array_equal(A.affine(vol, np.eye(4, dtype=np.float32)), vol)
+    R = o32.rotation_matrix([0.3, -0.2, 0.5], [5.5, 6.5, 4.5], 0)
+    assert rel_l2(A.affine(vol, R), A.rotate(vol, [0.3, -0.2, 0.5], [5.5, 6.5, 4.5], 0.0, 0)) < 1e-6
+
+
+def test_affine_rejects_bad_matrix_size():
+    import ctypes
+
+    from niftyrec_gb300 import _lib
+
+    L = _lib.load()
+    vol = np.zeros((4, 4, 4), np.float32)
+    out = np.zeros_like(vol)
+    a = np.eye(4, dtype=np.float32)
+    p = lambda x: x.ctypes.data_as(ctypes.c_void_p)
+    size = (ctypes.c_int * 3)(4, 4, 4)
+    assert L.et_array_affine(p(vol), size, p(out), size, p(a), (ctypes.c_int * 2)(3, 4), 0.0, 1) == 2
+    assert L.et_array_affine(p(vol), size, p(out), size, p(a), None, 0.0, 1) == 2
+
+
+@pytest.mark.parametrize("shape,k", [((6, 20, 20), (7, 5)), ((3, 17, 29), (3, 9)), ((1, 32, 24), (11, 11))])
+def test_convolve_matches_oracle(o32, shape, k):
+    """et_array_convolve (per-slice 2D convolution, image clamped at its
+    border) against the oracle's direct restatement, bit for bit (same term
+    order, separate rounding); a centred delta kernel returns the image."""
+    rng = np.random.default_rng(sum(shape))
+    vol = rng.random(shape).astype(np.float32)
+    ker = rng.random((shape[0],) + k).astype(np.float32)
+    out = A.convolve(vol, ker)
+    assert np.array_equal(out, o32.convolve2d(vol, ker))
+    delta = np.zeros_like(ker)
+    delta[:, (k[0] - 1) // 2, (k[1] - 1) // 2] = 1.0
+    assert np.array_equal(A.convolve(vol, delta), vol)
+
+
+def test_convolve_rejects_even_kernel():
+    with pytest.raises(Exception):
+        A.convolve(np.zeros((2, 8, 8), np.float32), np.zeros((2, 4, 3), np.float32))
+
+
 # (nz, ny, nx): the PSF has nx planes (the reference's rule) and plane z serves
 # depth z, so nz <= nx.
 @pytest.mark.parametrize("shape,k,ncam", [((64, 64, 64), 11, 12), ((36, 52, 40), 7, 9), ((30, 18, 32), 15, 5),

@@ -214,3 +214,20 @@ def test_adjoint_is_transpose_of_projector(o64, shape):
     aty = o64.backproject(y, cams, psf, mu, truncate=0, adjoint=True, nz=nz)
     lhs, rhs = float(np.sum(ax * y)), float(np.sum(x * aty))
     assert abs(lhs - rhs) <= 1e-10 * abs(lhs), (lhs, rhs)
+
+
+def test_convolve2d_restatement_known_answers(o32):
+    """The oracle's per-slice convolution: a constant image stays constant
+    times the kernel sum (border clamping), a delta image returns the kernel
+    centred on the delta (the impulse response of a true convolution), per
+    slice."""
+    rng = np.random.default_rng(3)
+    ker = rng.random((2, 5, 3)).astype(np.float32)
+    const = np.full((2, 9, 11), 2.0, np.float32)
+    out = o32.convolve2d(const, ker)
+    np.testing.assert_allclose(out, np.broadcast_to(2.0 * ker.sum(axis=(1, 2))[:, None, None], out.shape), rtol=1e-6)
+    delta = np.zeros((2, 9, 11), np.float32)
+    delta[:, 4, 5] = 1.0
+    out = o32.convolve2d(delta, ker)
+    for z in range(2):
+        np.testing.assert_array_equal(out[z, 2:7, 4:7], ker[z])
