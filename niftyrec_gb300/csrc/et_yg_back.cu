@@ -526,15 +526,27 @@ __global__ void __launch_bounds__(32 * kGatherWarps) k_tgather_yg(const YgArgs a
         off = (zp * a.nx + xp) * a.cs;
       }
     }
-    const float* src = a.temp + vol * g + yb;
-    for (unsigned m = __ballot_sync(kFull, w != 0.0f); m; m &= m - 1) {
-      const int l = __ffs(m) - 1;
-      const float wl = __shfl_sync(kFull, w, l);
-      const int ol = __shfl_sync(kFull, off, l);
-      if (rows) {
-        const float4 v = ldg4(src + ol);
-        const float4 wv = make_float4(wl * v.x, wl * v.y, wl * v.z, wl * v.w);
-        if (l < 16)  // uniform: l comes from the ballot
+    const float* src = a.temp + vol * g + (rows ? yb : 0);
+    // the nonzero weights four at a time: their loads in flight together,
+    // then the terms added in lane order
+    for (unsigned m = __ballot_sync(kFull, w != 0.0f); m;) {
+      int l[4];
+      float wl[4];
+      float4 v[4];
+#pragma unroll
+      for (int q = 0; q < 4; ++q) {
+        l[q] = m ? __ffs(m) - 1 : -1;  // uniform: from the ballot
+        m &= m ? m - 1 : 0u;
+        const int src_lane = l[q] < 0 ? 0 : l[q];
+        wl[q] = __shfl_sync(kFull, w, src_lane);
+        const int ol = __shfl_sync(kFull, off, src_lane);  // an offset inside the volume
+        v[q] = ldg4(src + ol);
+      }
+#pragma unroll
+      for (int q = 0; q < 4; ++q) {
+        if (l[q] < 0) break;
+        const float4 wv = make_float4(wl[q] * v[q].x, wl[q] * v[q].y, wl[q] * v[q].z, wl[q] * v[q].w);
+        if (l[q] < 16)
           add4(acc[0], wv);
         else
           add4(acc[1], wv);

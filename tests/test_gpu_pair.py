@@ -131,3 +131,52 @@ def test_pair_call_bf16_matches_separate_bf16_calls(shape, ncam):
     torch.cuda.synchronize(dev)
     assert _rel(s, s_ref) < TOL
     assert _rel(b, b_ref) < TOL
+
+
+@pytest.mark.parametrize("group", [3, 5, 7])
+def test_many_camera_groups_reuse_scratch_slots(group):
+    """Small camera groups (group 0, 2, 4, ... spread on the caller's stream,
+    1, 3, 5, ... on the second spread stream, each slot spread again only after
+    its gather): reference and exact-transpose backprojections, separate and
+    one-call, against the default grouping (only the float32 order of the group
+    sums differs) at 48^3 x 40 cameras with PSF and mu."""
+    L = _lib.load()
+    dev = torch.device("cuda", 0)
+    sp = vp(torch.cuda.current_stream(dev).cuda_stream)
+    shape = (48, 48, 48)
+    nz, ny, nx = shape
+    ncam = 40
+    act = torch.from_numpy(S.ellipsoid_phantom(shape, seed=21)).to(dev)
+    mu = torch.from_numpy(S.mu_map(shape, seed=21)).to(dev)
+    psf = S.gaussian_psf(5, nz, 0.5, 0.03)
+    cams = np.ascontiguousarray(S.cameras_about_y(ncam, 1.0)[1])
+    size = (ctypes.c_int * 3)(nx, ny, nz)
+    csize = (ctypes.c_int * 2)(ncam, 1)
+    psize = (ctypes.c_int * 3)(*psf.shape[::-1])
+    args = (cams.ctypes.data_as(vp), csize, psf.ctypes.data_as(vp), psize, 0.0, 0.0, 1)
+    y = torch.from_numpy(np.random.default_rng(5).uniform(0.5, 1.5, (ncam, ny, nx)).astype(np.float32)).to(dev)
+
+    def run():
+        out = {}
+        for mode in (0, 1):
+            b = torch.empty(shape, dtype=torch.float32, device=dev)
+            _call(L, L.nrgb_backproject_device, vp(y.data_ptr()), vp(mu.data_ptr()), size, vp(b.data_ptr()), *args,
+                  mode, sp)
+            s = torch.empty((ncam, ny, nx), dtype=torch.float32, device=dev)
+            bp = torch.empty(shape, dtype=torch.float32, device=dev)
+            _call(L, L.nrgb_project_backproject_device, vp(act.data_ptr()), vp(mu.data_ptr()), size, vp(s.data_ptr()),
+                  None, vp(bp.data_ptr()), *args, mode, sp)
+            out[mode] = (b, bp)
+        torch.cuda.synchronize(dev)
+        return out
+
+    ref = run()
+    try:
+        assert L.nrgb_set_backproject_group(nx, ny, nz, ncam, group) == 0
+        got = run()
+    finally:
+        L.nrgb_set_backproject_group(nx, ny, nz, ncam, 0)
+    for mode in (0, 1):
+        for r, g in zip(ref[mode], got[mode]):
+            assert torch.isfinite(g).all()
+            assert _rel(g, r) < TOL
