@@ -130,3 +130,37 @@ def test_autograd_gradients_bit_identical(det):
         grads.append((xa.grad.clone(), ma.grad.clone()))
     assert torch.equal(grads[0][0], grads[1][0])
     assert torch.equal(grads[0][1], grads[1][1])
+
+
+def test_pair_call_exact_transpose_deterministic(det):
+    """nrgb_project_backproject_device in mode 1 with the switch on: repeated
+    calls are bit-identical and equal the separate deterministic calls to 1e-6
+    (the pair takes its carries from the projector)."""
+    import ctypes
+
+    vp = ctypes.c_void_p
+    L = _lib.load()
+    dev = torch.device("cuda", 0)
+    sp = vp(torch.cuda.current_stream(dev).cuda_stream)
+    shape = (64, 64, 64)
+    nz, ny, nx = shape
+    act = cuda(S.ellipsoid_phantom(shape, seed=9))
+    mu = cuda(S.mu_map(shape, seed=9))
+    psf = S.gaussian_psf(7, nz, 0.5, 0.03)
+    cams = np.ascontiguousarray(S.cameras_about_y(40, 1.0)[1])
+    size = (ctypes.c_int * 3)(nx, ny, nz)
+    csize = (ctypes.c_int * 2)(40, 1)
+    psize = (ctypes.c_int * 3)(*psf.shape[::-1])
+    args = (cams.ctypes.data_as(vp), csize, psf.ctypes.data_as(vp), psize, 0.0, 0.0, 0, 1, sp)
+    outs = []
+    for _ in range(2):
+        s = torch.empty((40, ny, nx), dtype=torch.float32, device=dev)
+        b = torch.empty(shape, dtype=torch.float32, device=dev)
+        assert L.nrgb_project_backproject_device(vp(act.data_ptr()), vp(mu.data_ptr()), size, vp(s.data_ptr()), None,
+                                                 vp(b.data_ptr()), *args) == 0
+        outs.append((s, b))
+    bs = torch.empty(shape, dtype=torch.float32, device=dev)
+    assert L.nrgb_backproject_device(vp(outs[0][0].data_ptr()), vp(mu.data_ptr()), size, vp(bs.data_ptr()), *args) == 0
+    torch.cuda.synchronize(dev)
+    assert torch.equal(outs[0][1], outs[1][1])
+    assert _rel(outs[0][1], bs) < 1e-6
