@@ -351,8 +351,12 @@ int project_device(const Problem& pb, const float* d_act, const float* d_att, fl
     float* sino_c = cv.take<float>(sino_col_n(pb));
     if (!act_c || !sino_c || (d_att && !mu_c)) return kErrAllocGpu;
     const int cy = round_up(pb.ny, 4);
-    if ((s = stage_column(pb, d_act, act_c, cy, pb.nz, st)) != kOk) return s;
-    if (d_att && (s = stage_column(pb, d_att, mu_c, cy, pb.nz, st)) != kOk) return s;
+    if (pb.storage == kStorageF32 && d_att) {  // activity and mu in one launch
+      if ((s = to_column2(d_act, act_c, d_att, mu_c, pb.nx, pb.ny, cy, pb.nz, st)) != kOk) return s;
+    } else {
+      if ((s = stage_column(pb, d_act, act_c, cy, pb.nz, st)) != kOk) return s;
+      if (d_att && (s = stage_column(pb, d_att, mu_c, cy, pb.nz, st)) != kOk) return s;
+    }
     YgArgs a;
     a.storage = pb.storage;
     a.pslabs = pb.pslabs;
@@ -569,8 +573,12 @@ int pair_device(const Problem& pb, const Problem& pb_back, const float* d_act, c
   float* work = cv.take<float>(yg_backproject_workspace(pb.nx, pb.ny, pb.nz, pb.cams.n, group) / sizeof(float));
   if (!act_c || !sino_c || !in_c || !out_c || !work || (d_att && !mu_c)) return kErrAllocGpu;
   const size_t carry_n = static_cast<size_t>(pb.cams.n) * yg_carry_slabs() * pb.nx * cy;
-  if ((s = stage_column(pb, d_act, act_c, cy, pb.nz, st)) != kOk) return s;
-  if (d_att && (s = stage_column(pb, d_att, mu_c, cy, pb.nz, st)) != kOk) return s;
+  if (pb.storage == kStorageF32 && d_att) {  // activity and mu in one launch
+    if ((s = to_column2(d_act, act_c, d_att, mu_c, pb.nx, pb.ny, cy, pb.nz, st)) != kOk) return s;
+  } else {
+    if ((s = stage_column(pb, d_act, act_c, cy, pb.nz, st)) != kOk) return s;
+    if (d_att && (s = stage_column(pb, d_att, mu_c, cy, pb.nz, st)) != kOk) return s;
+  }
   YgArgs a;
   a.storage = pb.storage;
   a.pslabs = pb.pslabs;

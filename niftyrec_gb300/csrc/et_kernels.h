@@ -216,6 +216,10 @@ int fisher_pairs(const float* proj, int npx, int npy, const int* coords, const i
 // ---- layout conversion and elementwise helpers ----
 // planes x [ny][nx] (nifti) <-> planes x [nx][cy] (column), zero pads.
 int to_column(const float* src, float* dst, int nx, int ny, int cy, int planes, cudaStream_t st);
+// Two volumes of the same shape laid out in one launch (two launches where
+// the 16-byte form does not apply).
+int to_column2(const float* src_a, float* dst_a, const float* src_b, float* dst_b, int nx, int ny, int cy, int planes,
+               cudaStream_t st);
 int from_column(const float* src, float* dst, int nx, int ny, int cy, int planes, int truncate, cudaStream_t st);
 // Row windows: dst column [planes][nx][cy] <- src nifti rows [row0, row0+rows)
 // (planes of ny_src rows); and nifti rows [row0+r_begin, row0+r_end) of dst

@@ -30,10 +30,18 @@ __global__ void k_to_col(const float* __restrict__ src, float* __restrict__ dst,
 // src is host memory read over NVLink-C2C this reaches the link's read rate
 // (the 32 x 32 form with 4-byte reads stays about 20% below it); on device
 // memory both forms run at the same speed.
+// With src2 (a second volume of the same shape) the planes past `planes`
+// lay out src2 into dst2: two volumes in one launch.
 __global__ void __launch_bounds__(256) k_to_col4(const float* __restrict__ src, float* __restrict__ dst, int nx,
-                                                 int ny_src, int row0, int rows, int cy) {
+                                                 int ny_src, int row0, int rows, int cy, const float* __restrict__ src2,
+                                                 float* __restrict__ dst2, int planes) {
   __shared__ float tile[32][129];
-  const int p = blockIdx.z;
+  int p = blockIdx.z;
+  if (p >= planes) {  // uniform over the CTA
+    p -= planes;
+    src = src2;
+    dst = dst2;
+  }
   const int xb = blockIdx.x * 128, yb = blockIdx.y * 32;
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
   float4 v[4];
@@ -185,7 +193,7 @@ int to_column_rows(const float* src, float* dst, int nx, int ny_src, int row0, i
   if (wide_rows(src, nx)) {
     const dim3 grid((nx + 127) / 128, (cy + 31) / 32, planes);
     NRGB_LAUNCH_SCOPE("k_to_col4", st);
-    k_to_col4<<<grid, 256, 0, st>>>(src, dst, nx, ny_src, row0, rows, cy);
+    k_to_col4<<<grid, 256, 0, st>>>(src, dst, nx, ny_src, row0, rows, cy, nullptr, nullptr, planes);
   } else {
     const dim3 grid((nx + 31) / 32, (cy + 31) / 32, planes), block(32, 8);
     NRGB_LAUNCH_SCOPE("k_to_col", st);
@@ -240,6 +248,18 @@ int from_bf16(const void* src, float* dst, size_t n, cudaStream_t st) {
 
 int to_column(const float* src, float* dst, int nx, int ny, int cy, int planes, cudaStream_t st) {
   return to_column_rows(src, dst, nx, ny, 0, ny, cy, planes, st);
+}
+
+int to_column2(const float* src_a, float* dst_a, const float* src_b, float* dst_b, int nx, int ny, int cy, int planes,
+               cudaStream_t st) {
+  if (!wide_rows(src_a, nx) || !wide_rows(src_b, nx) || 2 * static_cast<long long>(planes) > 65535) {
+    const int s = to_column(src_a, dst_a, nx, ny, cy, planes, st);
+    return s != kOk ? s : to_column(src_b, dst_b, nx, ny, cy, planes, st);
+  }
+  const dim3 grid((nx + 127) / 128, (cy + 31) / 32, 2 * planes);
+  NRGB_LAUNCH_SCOPE("k_to_col4", st);
+  k_to_col4<<<grid, 256, 0, st>>>(src_a, dst_a, nx, ny, 0, ny, cy, src_b, dst_b, planes);
+  return cudaGetLastError() == cudaSuccess ? kOk : kErrKernel;
 }
 
 int from_column(const float* src, float* dst, int nx, int ny, int cy, int planes, int truncate, cudaStream_t st) {
