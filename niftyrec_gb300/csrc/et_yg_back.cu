@@ -436,9 +436,9 @@ __global__ void __launch_bounds__(32 * kGatherWarps) k_gather_yg(const YgArgs a,
   if (!lane_rows_ok(a, yb) || !lane_writes(a, yb)) return;
   const size_t vol = static_cast<size_t>(a.nz) * a.nx * a.cs;
   // camera outer, columns inner: neighbouring accumulator columns of one
-  // camera share footprint columns, which then hit in L1; U cameras' loads
-  // in flight at once (every footprint offset is inside its volume, see
-  // make_tap), added in camera order
+  // camera share footprint columns, which then hit in L1; the loads of U
+  // units' volumes in flight at once (every footprint offset is inside its
+  // volume, see make_tap), added in unit order
   float4 acc[C];
 #pragma unroll
   for (int i = 0; i < C; ++i) acc[i] = make_float4(0.f, 0.f, 0.f, 0.f);
