@@ -265,3 +265,34 @@ def test_niftyrec_log_one_json_line_per_call():
         assert len(lines) == expect
         for rec in lines:
             assert rec["niftyrec"] == "et_array_make_cameras" and rec["host_ms"] >= 0
+
+
+def test_deterministic_switch_round_trip(lib):
+    """nrgb_set_deterministic / nrgb_get_deterministic (a library-wide switch,
+    host only; 0 by default)."""
+    prev = lib.nrgb_get_deterministic()
+    try:
+        assert lib.nrgb_set_deterministic(1) == 0
+        assert lib.nrgb_get_deterministic() == 1
+        assert lib.nrgb_set_deterministic(0) == 0
+        assert lib.nrgb_get_deterministic() == 0
+    finally:
+        lib.nrgb_set_deterministic(prev)
+
+
+def test_affine_and_convolve_reject_bad_arguments(lib):
+    """Argument checks that come before any GPU work: a matrix size other than
+    {4, 4}, missing arrays, even or mismatched kernels -> status 2."""
+    p = lambda a: a.ctypes.data_as(ctypes.c_void_p)
+    vol = np.zeros((4, 5, 6), np.float32)
+    out = np.zeros_like(vol)
+    size = (ctypes.c_int * 3)(6, 5, 4)
+    eye = np.eye(4, dtype=np.float32)
+    assert lib.et_array_affine(p(vol), size, p(out), size, p(eye), (ctypes.c_int * 2)(4, 3), 0.0, 1) == 2
+    assert lib.et_array_affine(p(vol), size, p(out), size, None, (ctypes.c_int * 2)(4, 4), 0.0, 1) == 2
+    assert lib.et_array_affine(p(vol), (ctypes.c_int * 3)(6, 5, 0), p(out), size, p(eye), (ctypes.c_int * 2)(4, 4),
+                               0.0, 1) == 2
+    ker = np.zeros((4, 3, 3), np.float32)
+    assert lib.et_array_convolve(p(vol), size, p(out), size, p(ker), (ctypes.c_int * 3)(4, 3, 4), 1) == 2
+    assert lib.et_array_convolve(p(vol), size, p(out), size, p(ker), (ctypes.c_int * 3)(3, 3, 3), 1) == 2
+    assert lib.et_array_convolve(p(vol), size, None, size, p(ker), (ctypes.c_int * 3)(3, 3, 4), 1) == 2
