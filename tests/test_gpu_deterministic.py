@@ -164,3 +164,40 @@ def test_pair_call_exact_transpose_deterministic(det):
     torch.cuda.synchronize(dev)
     assert torch.equal(outs[0][1], outs[1][1])
     assert _rel(outs[0][1], bs) < 1e-6
+
+
+def test_bf16_exact_transpose_deterministic():
+    """bfloat16 mu (the non-mirror bfloat16 spread): the deterministic exact
+    transpose repeats bit for bit and equals the vector-reduction form to 1e-6."""
+    import ctypes
+
+    vp = ctypes.c_void_p
+    L = _lib.load()
+    dev = torch.device("cuda", 0)
+    sp = vp(torch.cuda.current_stream(dev).cuda_stream)
+    shape = (48, 48, 48)
+    nz, ny, nx = shape
+    mu = torch.from_numpy(S.mu_map(shape, seed=4)).to(dev).to(torch.bfloat16)
+    psf = S.gaussian_psf(5, nz, 0.5, 0.03)
+    cams = np.ascontiguousarray(S.cameras_about_y(24, 1.0)[1])
+    size = (ctypes.c_int * 3)(nx, ny, nz)
+    csize = (ctypes.c_int * 2)(24, 1)
+    psize = (ctypes.c_int * 3)(*psf.shape[::-1])
+    y = torch.from_numpy(np.random.default_rng(3).uniform(0.5, 1.5, (24, ny, nx)).astype(np.float32)).to(dev)
+    args = (cams.ctypes.data_as(vp), csize, psf.ctypes.data_as(vp), psize, 0.0, 0.0, 0, 1, sp)
+    prev = L.nrgb_get_deterministic()
+    outs = []
+    try:
+        for det in (0, 1, 1):
+            L.nrgb_set_deterministic(det)
+            b = torch.empty(shape, dtype=torch.float32, device=dev)
+            assert L.nrgb_backproject_device_bf16(vp(y.data_ptr()), vp(mu.data_ptr()), size, vp(b.data_ptr()),
+                                                  *args) == 0
+            outs.append(b)
+        torch.cuda.synchronize(dev)
+    finally:
+        L.nrgb_set_deterministic(prev)
+    ref, d1, d2 = (o.double() for o in outs)
+    assert torch.isfinite(d1).all()
+    assert torch.equal(outs[1], outs[2])
+    assert float((d1 - ref).norm() / ref.norm()) < 1e-6
